@@ -1,0 +1,302 @@
+"""Host-side mirror of the CFD-Lite hot-path interface over libcfdgpu's C-ABI.
+
+The reference drives one SIMPLE outer iteration from Fortran
+(src/main.f90:50-63): ``update_boundaries`` (src/modules/mod_physics.f90:38),
+``solve_uvwp`` (src/equations/mod_uvwp.f90:95) and, every ``ncoef`` outer
+iterations, ``update_time`` (mod_physics.f90:101).  ``Solver`` exposes the
+same routines, plus the individual routines solve_uvwp calls, on a case that
+stays resident in GPU memory.  Arrays cross the boundary in the reference's
+layouts (1-based index values, xyz-interleaved gradients).
+
+There is no CPU fallback: constructing a ``Solver`` without the CUDA library
+or without a GPU raises ``CfdlError``.
+"""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcfdgpu.so")
+
+CFDL_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "non-finite value in a solve",
+          4: "inner solve reached its iteration cap", 5: "CUDA runtime error", 6: "mesh connectivity error",
+          7: "no CUDA device", 8: "unknown array name"}
+BC_WALL, BC_SYMMETRY = 1, 2
+HEXA_8, TETRA_4, QUAD_4, TRI_3 = 17, 10, 7, 5
+
+
+class CfdlError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__("%s: %s (status %d)" % (what, STATUS.get(status, "unknown"), status))
+
+
+class Config(C.Structure):
+    """cfdl_config: physics constants and inner-solve controls."""
+    _fields_ = [("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double),
+                ("alpha_u", C.c_double), ("alpha_p", C.c_double), ("nit", C.c_int),
+                ("solve_mode", C.c_int), ("rtol_u", C.c_double), ("rtol_p", C.c_double),
+                ("tight_rtol", C.c_double), ("tight_maxit", C.c_int), ("precision", C.c_int),
+                ("precond", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("it_u", C.c_int), ("it_v", C.c_int), ("it_w", C.c_int), ("it_p", C.c_int),
+                ("res_i", C.c_double * 4), ("res_f", C.c_double * 4),
+                ("mass_imbalance", C.c_double), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {"it": [self.it_u, self.it_v, self.it_w, self.it_p], "res_i": list(self.res_i),
+                "res_f": list(self.res_f), "mass_imbalance": self.mass_imbalance, "status": self.status}
+
+
+class Mesh(C.Structure):
+    _fields_ = [("ne", C.c_int), ("nf", C.c_int), ("nbf", C.c_int),
+                ("ef2nb1", C.c_void_p), ("ef2nb2", C.c_void_p), ("ef2nb_idx", C.c_void_p),
+                ("s2g", C.c_void_p), ("bs", C.c_void_p), ("aip", C.c_void_p), ("rip", C.c_void_p),
+                ("xc", C.c_void_p), ("yc", C.c_void_p), ("zc", C.c_void_p), ("vol", C.c_void_p),
+                ("nbc", C.c_int), ("bc_esec", C.c_void_p), ("bc_kind", C.c_void_p), ("bc_vel", C.c_void_p)]
+
+
+class Fields(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("u", "v", "w", "p", "u0", "v0", "w0", "gu", "gv", "gw",
+                                          "gp", "gpc", "mip", "mip0")]
+
+
+_lib = None
+
+
+def lib():
+    """Load libcfdgpu.so (building it if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise CfdlError(5, "libcfdgpu.so is not built (run __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.cfdl_box_zone_sizes.argtypes = [C.c_int, C.c_int, ip, ip, ip, ip]
+    L.cfdl_box_zone_fill.argtypes = [C.c_int, C.c_int, C.c_double, C.c_uint64, vp, vp, vp, vp, vp, vp, C.c_char_p]
+    L.cfdl_setup_create.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_char_p, vp, vp, C.c_int, vp, C.POINTER(vp)]
+    L.cfdl_setup_sizes.argtypes = [vp, vp]
+    L.cfdl_setup_mesh.argtypes = [vp, C.c_double, C.POINTER(Mesh)]
+    L.cfdl_setup_get_int.argtypes = [vp, C.c_char_p, vp]
+    L.cfdl_setup_get_dbl.argtypes = [vp, C.c_char_p, vp]
+    L.cfdl_setup_destroy.argtypes = [vp]
+    L.cfdl_config_default.argtypes = [C.POINTER(Config)]
+    L.cfdl_config_default.restype = None
+    L.cfdl_ctx_create.argtypes = [C.POINTER(Mesh), C.POINTER(Config), C.POINTER(vp)]
+    L.cfdl_set_config.argtypes = [vp, C.POINTER(Config)]
+    L.cfdl_upload_fields.argtypes = [vp, C.POINTER(Fields)]
+    L.cfdl_download_fields.argtypes = [vp, C.POINTER(Fields)]
+    L.cfdl_ctx_destroy.argtypes = [vp]
+    for n in ("cfdl_update_boundaries", "cfdl_update_time", "cfdl_calc_coef_uvw", "cfdl_calc_coef_p",
+              "cfdl_adjust_pc", "cfdl_update_uvwp"):
+        getattr(L, n).argtypes = [vp]
+    for n in ("cfdl_solve_uvwp", "cfdl_solve_momentum", "cfdl_solve_pc"):
+        getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
+    L.cfdl_step.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Stats)]
+    L.cfdl_solve_uvwp_host.argtypes = [vp, C.POINTER(Fields), C.POINTER(Stats)]
+    L.cfdl_calc_grad.argtypes = [vp, C.c_int]
+    L.cfdl_calc_mip.argtypes = [vp, C.c_int]
+    L.cfdl_get_array.argtypes = [vp, C.c_char_p, vp]
+    L.cfdl_set_array.argtypes = [vp, C.c_char_p, vp]
+    L.cfdl_launch_count.argtypes = [vp]
+    L.cfdl_launch_count.restype = C.c_int64
+    L.cfdl_status_string.argtypes = [C.c_int]
+    L.cfdl_status_string.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _check(st, what):
+    if st != CFDL_OK:
+        raise CfdlError(st, what)
+
+
+class Zone:
+    """CGNS-shaped zone of the synthetic cavity (what cell_input reads)."""
+
+    def __init__(self, n, tet=False, jitter=0.0, seed=0):
+        L = lib()
+        nvx, nelem, nsec, m = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(L.cfdl_box_zone_sizes(n, int(tet), C.byref(nvx), C.byref(nelem), C.byref(nsec), C.byref(m)), "zone sizes")
+        self.n, self.tet, self.jitter, self.seed = n, bool(tet), jitter, seed
+        self.nvx, self.nelem, self.nsec, self.ne2vxmax = nvx.value, nelem.value, nsec.value, m.value
+        self.x = np.zeros(self.nvx); self.y = np.zeros(self.nvx); self.z = np.zeros(self.nvx)
+        self.e2vx = np.zeros(self.ne2vxmax * self.nelem, np.int32)
+        self.etype = np.zeros(self.nsec, np.int32)
+        self.esec = np.zeros(2 * self.nsec, np.int32)
+        self.names = C.create_string_buffer(33 * self.nsec)
+        _check(L.cfdl_box_zone_fill(n, int(tet), float(jitter), int(seed), _p(self.x), _p(self.y), _p(self.z),
+                                    _p(self.e2vx), _p(self.etype), _p(self.esec), self.names), "zone fill")
+
+    def section_names(self):
+        raw = self.names.raw
+        return [raw[33 * s:33 * s + 32].split(b"\0")[0].decode() for s in range(self.nsec)]
+
+
+class Setup:
+    """Connectivity and geometry of a zone, in the reference's arrays."""
+
+    def __init__(self, zone):
+        L = lib()
+        self._h = C.c_void_p()
+        _check(L.cfdl_setup_create(zone.nvx, _p(zone.x), _p(zone.y), _p(zone.z), zone.nsec, zone.names,
+                                   _p(zone.etype), _p(zone.esec), zone.ne2vxmax, _p(zone.e2vx), C.byref(self._h)),
+               "mesh set-up")
+        sz = np.zeros(5, np.int32)
+        L.cfdl_setup_sizes(self._h, _p(sz))
+        self.ne, self.nf, self.nbf, self.nsec, self.nred = (int(v) for v in sz)
+        self.H = 2 * self.nf - self.nbf
+
+    def get_int(self, name):
+        n = {"ef2nb1": self.H, "ef2nb2": self.H, "ef2nb_idx": self.ne + 1, "s2g": self.nf, "bs": self.nbf,
+             "esec": 2 * self.nsec, "etype": self.nsec, "red": self.ne}[name]
+        out = np.zeros(n, np.int32)
+        _check(lib().cfdl_setup_get_int(self._h, name.encode(), _p(out)), name)
+        return out
+
+    def get_dbl(self, name):
+        n = {"aip": 3 * self.nf, "rip": 3 * self.nf, "xc": self.ne + self.nbf, "yc": self.ne + self.nbf,
+             "zc": self.ne + self.nbf, "vol": self.ne}[name]
+        out = np.zeros(n)
+        _check(lib().cfdl_setup_get_dbl(self._h, name.encode(), _p(out)), name)
+        return out
+
+    def mesh(self, u_lid=1.0):
+        m = Mesh()
+        _check(lib().cfdl_setup_mesh(self._h, float(u_lid), C.byref(m)), "mesh")
+        return m
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.cfdl_setup_destroy(self._h)
+            self._h = None
+
+
+def default_config(**kw):
+    cfg = Config()
+    lib().cfdl_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v)
+    return cfg
+
+
+def steady(**kw):
+    """The steady under-relaxed SIMPLE form (dt = inf, alpha_u, alpha_p)."""
+    base = dict(rho=1.0, mu=0.01, dt=math.inf, alpha_u=0.7, alpha_p=0.3)
+    base.update(kw)
+    return default_config(**base)
+
+
+class Solver:
+    """One case resident on the GPU, driven like the reference's phys_t."""
+
+    def __init__(self, setup, config=None, u_lid=1.0):
+        self.setup = setup
+        self.mesh = setup.mesh(u_lid)
+        self.config = config if config is not None else default_config()
+        self.ne, self.nf, self.nbf, self.H = setup.ne, setup.nf, setup.nbf, setup.H
+        self._h = C.c_void_p()
+        _check(lib().cfdl_ctx_create(C.byref(self.mesh), C.byref(self.config), C.byref(self._h)), "ctx_create")
+        self.last_stats = Stats()
+
+    # -- reference routines ------------------------------------------------
+    def update_boundaries(self):
+        _check(lib().cfdl_update_boundaries(self._h), "update_boundaries")
+
+    def solve_uvwp(self):
+        st = Stats()
+        _check(lib().cfdl_solve_uvwp(self._h, C.byref(st)), "solve_uvwp")
+        self.last_stats = st
+        return st
+
+    def update_time(self):
+        _check(lib().cfdl_update_time(self._h), "update_time")
+
+    def step(self, n_outer, ncoef=3):
+        st = Stats()
+        _check(lib().cfdl_step(self._h, int(n_outer), int(ncoef), C.byref(st)), "step")
+        self.last_stats = st
+        return st
+
+    def calc_coef_uvw(self):
+        _check(lib().cfdl_calc_coef_uvw(self._h), "calc_coef_uvw")
+
+    def solve_momentum(self):
+        st = Stats()
+        _check(lib().cfdl_solve_momentum(self._h, C.byref(st)), "solve_momentum")
+        return st
+
+    def calc_grad(self, field):
+        idx = {"u": 0, "v": 1, "w": 2, "phic": 3, "pc": 3, "uvw": 4}[field]
+        _check(lib().cfdl_calc_grad(self._h, idx), "calc_grad")
+
+    def calc_mip(self, rhie_chow=True):
+        _check(lib().cfdl_calc_mip(self._h, int(bool(rhie_chow))), "calc_mip")
+
+    def calc_coef_p(self):
+        _check(lib().cfdl_calc_coef_p(self._h), "calc_coef_p")
+
+    def solve_pc(self):
+        st = Stats()
+        _check(lib().cfdl_solve_pc(self._h, C.byref(st)), "solve_pc")
+        return st
+
+    def adjust_pc(self):
+        _check(lib().cfdl_adjust_pc(self._h), "adjust_pc")
+
+    def update_uvwp(self):
+        _check(lib().cfdl_update_uvwp(self._h), "update_uvwp")
+
+    def set_config(self, cfg):
+        _check(lib().cfdl_set_config(self._h, C.byref(cfg)), "set_config")
+        self.config = cfg
+
+    # -- arrays ------------------------------------------------------------
+    def _len(self, name):
+        nc = self.ne + self.nbf
+        if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic"):
+            return nc
+        if name in ("gu", "gv", "gw", "gp", "gpc"):
+            return 3 * nc
+        if name in ("mip", "mip0"):
+            return self.nf
+        if name == "anb":
+            return self.H
+        return self.ne
+
+    def get(self, name):
+        out = np.zeros(self._len(name))
+        _check(lib().cfdl_get_array(self._h, name.encode(), _p(out)), "get " + name)
+        return out
+
+    def set(self, name, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        if a.size != self._len(name):
+            raise ValueError("%s needs %d values" % (name, self._len(name)))
+        _check(lib().cfdl_set_array(self._h, name.encode(), _p(a)), "set " + name)
+
+    def launch_count(self):
+        return int(lib().cfdl_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cfdl_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

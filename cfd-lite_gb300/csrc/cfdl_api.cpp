@@ -1,0 +1,341 @@
+// cfdl_api.cpp -- the C-ABI of libcfdgpu (declared in include/cfdl.h).
+//
+// The entry points mirror the reference's Fortran routines one for one; see
+// the header for the citation of each.  All work is queued on the context's
+// stream; entry points that return results to the host synchronise it.
+#include "cfdl_internal.h"
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+using namespace cfdl;
+
+namespace {
+
+int check_ctx(const cfdl_ctx *ctx) { return ctx && !ctx->cases.empty() ? CFDL_OK : CFDL_ERR_INVALID; }
+
+int validate_config(const cfdl_config *c) {
+    if (!c) return CFDL_ERR_INVALID;
+    if (!(c->rho > 0) || !(c->mu >= 0) || !(c->dt > 0) || !(c->alpha_u > 0 && c->alpha_u <= 1) ||
+        !(c->alpha_p > 0 && c->alpha_p <= 1) || c->nit < 0 || c->tight_maxit < 0 ||
+        (c->solve_mode != 0 && c->solve_mode != 1) || (c->precision != 0 && c->precision != 1) ||
+        !(c->rtol_u > 0) || !(c->rtol_p > 0) || !(c->tight_rtol > 0) || (c->precond != 0 && c->precond != 1))
+        return CFDL_ERR_INVALID;
+    return CFDL_OK;
+}
+
+struct Named { double *ptr; size_t n; bool ell; };
+
+Named lookup(HostCase *hc, const char *name) {
+    CaseDev &d = hc->dev;
+    const size_t nc = (size_t)hc->ne + hc->nbf, ne = hc->ne, nf = hc->nf;
+    std::string s(name ? name : "");
+    struct E { const char *nm; double *p; size_t n; };
+    const E tab[] = {
+        {"u", d.u, nc}, {"v", d.v, nc}, {"w", d.w, nc}, {"p", d.p, nc},
+        {"u0", d.u0, nc}, {"v0", d.v0, nc}, {"w0", d.w0, nc}, {"phic", d.phic, nc},
+        {"gu", d.gu, 3 * nc}, {"gv", d.gv, 3 * nc}, {"gw", d.gw, 3 * nc}, {"gp", d.gp, 3 * nc}, {"gpc", d.gpc, 3 * nc},
+        {"mip", d.mip, nf}, {"mip0", d.mip0, nf},
+        {"ap", d.ap, ne}, {"b", d.b, ne}, {"bu", d.bu, ne}, {"bv", d.bv, ne}, {"bw", d.bw, ne},
+        {"d", d.d, ne}, {"dc", d.dc, ne}, {"rho", d.rho, ne}, {"mu", d.mu, ne},
+    };
+    for (const E &e : tab) if (s == e.nm) return {e.p, e.n, false};
+    if (s == "anb") return {d.anb, (size_t)hc->H, true};
+    return {nullptr, 0, false};
+}
+
+int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool to_host) {
+    Named nm = lookup(hc, name);
+    if (!nm.ptr) return CFDL_ERR_NAME;
+    if (!host) return CFDL_ERR_INVALID;
+    cudaError_t e;
+    if (!nm.ell) {
+        e = cudaMemcpyAsync(to_host ? (void *)host : (void *)nm.ptr, to_host ? (const void *)nm.ptr : (const void *)host,
+                            nm.n * sizeof(double), to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        return cuda_status(e);
+    }
+    // anb: ELL [W][ne] <-> reference CSR half-face order
+    const int ne = hc->ne, W = hc->W;
+    std::vector<double> ell((size_t)W * ne, 0.0);
+    if (to_host) {
+        e = cudaMemcpyAsync(ell.data(), nm.ptr, ell.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        for (int c = 0; c < ne; c++)
+            for (int idx = hc->ef2nb_idx[c]; idx < hc->ef2nb_idx[c + 1]; idx++)
+                host[idx - 1] = ell[(size_t)(idx - hc->ef2nb_idx[c]) * ne + c];
+        return CFDL_OK;
+    }
+    for (int c = 0; c < ne; c++)
+        for (int idx = hc->ef2nb_idx[c]; idx < hc->ef2nb_idx[c + 1]; idx++)
+            ell[(size_t)(idx - hc->ef2nb_idx[c]) * ne + c] = host[idx - 1];
+    e = cudaMemcpyAsync(nm.ptr, ell.data(), ell.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return cuda_status(e);
+}
+
+int transfer_fields(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f, bool to_host) {
+    if (!f) return CFDL_ERR_INVALID;
+    CaseDev &d = hc->dev;
+    const size_t nc = (size_t)hc->ne + hc->nbf, nf = hc->nf;
+    struct P { double *h; double *dv; size_t n; };
+    const P list[] = {
+        {f->u, d.u, nc}, {f->v, d.v, nc}, {f->w, d.w, nc}, {f->p, d.p, nc},
+        {f->u0, d.u0, nc}, {f->v0, d.v0, nc}, {f->w0, d.w0, nc},
+        {f->gu, d.gu, 3 * nc}, {f->gv, d.gv, 3 * nc}, {f->gw, d.gw, 3 * nc}, {f->gp, d.gp, 3 * nc}, {f->gpc, d.gpc, 3 * nc},
+        {f->mip, d.mip, nf}, {f->mip0, d.mip0, nf},
+    };
+    for (const P &p : list) {
+        if (!p.h) continue;
+        cudaError_t e = to_host ? cudaMemcpyAsync(p.h, p.dv, p.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream)
+                                : cudaMemcpyAsync(p.dv, p.h, p.n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    return CFDL_OK;
+}
+
+int finish(cfdl_ctx *ctx, cfdl_stats *st) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
+    if (st) {
+        int s = read_stats(ctx, 0, st);
+        if (s) return s;
+        return st->status == CFDL_ERR_NONFINITE || st->status == CFDL_ERR_ITER_CAP ? st->status : CFDL_OK;
+    }
+    return CFDL_OK;
+}
+
+}  // namespace
+
+namespace cfdl {
+int solve_uvwp_all(cfdl_ctx *ctx) {
+    // solve_uvwp, src/equations/mod_uvwp.f90:95-134
+    launch_coef_uvw(ctx);
+    int st = solve_momentum(ctx);
+    if (st) return st;
+    launch_grad(ctx, 4);
+    launch_calc_mip(ctx, 1);
+    launch_coef_p(ctx);
+    st = solve_pressure(ctx);
+    if (st) return st;
+    launch_adjust_pc(ctx);
+    launch_grad(ctx, 3);
+    launch_update_uvwp(ctx);
+    return cuda_status(cudaGetLastError());
+}
+}  // namespace cfdl
+
+extern "C" {
+
+void cfdl_config_default(cfdl_config *c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    // reference defaults: mod_physics.f90:15-19, mod_properties.f90:86-87
+    c->rho = 5.0; c->mu = 0.01; c->dt = 0.01;
+    c->alpha_u = 1.0; c->alpha_p = 1.0;
+    c->nit = 100; c->solve_mode = 0; c->rtol_u = 0.1; c->rtol_p = 0.1;
+    c->tight_rtol = 1e-13; c->tight_maxit = 20000;
+    c->precision = 0; c->precond = 0;
+}
+
+const char *cfdl_status_string(int s) {
+    switch (s) {
+    case CFDL_OK: return "ok";
+    case CFDL_ERR_INVALID: return "invalid argument";
+    case CFDL_ERR_OOM: return "out of memory";
+    case CFDL_ERR_NONFINITE: return "non-finite value in a solve";
+    case CFDL_ERR_ITER_CAP: return "inner solve reached its iteration cap";
+    case CFDL_ERR_CUDA: return "CUDA runtime error";
+    case CFDL_ERR_MESH: return "mesh connectivity error";
+    case CFDL_ERR_NO_DEVICE: return "no CUDA device";
+    case CFDL_ERR_NAME: return "unknown array name";
+    default: return "unknown status";
+    }
+}
+
+int cfdl_ctx_create(const cfdl_mesh *mesh, const cfdl_config *cfg, cfdl_ctx **out) {
+    if (!out) return CFDL_ERR_INVALID;
+    *out = nullptr;
+    int st = validate_config(cfg);
+    if (st) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return CFDL_ERR_NO_DEVICE; }
+    cfdl_ctx *ctx = new (std::nothrow) cfdl_ctx;
+    if (!ctx) return CFDL_ERR_OOM;
+    cudaGetDevice(&ctx->device);
+    if ((st = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)))) { delete ctx; return st; }
+    HostCase *hc = nullptr;
+    if ((st = create_case(ctx, mesh, cfg, &hc))) { cfdl_ctx_destroy(ctx); return st; }
+    ctx->cases.push_back(hc);
+    if ((st = rebuild_worklists(ctx))) { cfdl_ctx_destroy(ctx); return st; }
+    // construct_uvwp: mip = calc_mip(.false.) from the zero fields, mip0 = mip
+    launch_calc_mip(ctx, 0);
+    launch_set_mip0(ctx);
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) { cfdl_ctx_destroy(ctx); return st; }
+    *out = ctx;
+    return CFDL_OK;
+}
+
+int cfdl_set_config(cfdl_ctx *ctx, const cfdl_config *cfg) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = validate_config(cfg))) return st;
+    for (HostCase *hc : ctx->cases) {
+        if (hc->cfg.rho != cfg->rho || hc->cfg.mu != cfg->mu) {
+            std::vector<double> rho(hc->ne, cfg->rho), mu(hc->ne, cfg->mu);
+            if ((st = cuda_status(cudaMemcpy(hc->dev.rho, rho.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
+            if ((st = cuda_status(cudaMemcpy(hc->dev.mu, mu.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
+        }
+        apply_config(hc, cfg);
+    }
+    return upload_case_table(ctx);
+}
+
+int cfdl_upload_fields(cfdl_ctx *ctx, const cfdl_fields *f) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = transfer_fields(ctx, ctx->cases[0], f, false))) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_download_fields(cfdl_ctx *ctx, cfdl_fields *f) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = transfer_fields(ctx, ctx->cases[0], f, true))) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_ctx_destroy(cfdl_ctx *ctx) {
+    if (!ctx) return CFDL_ERR_INVALID;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (HostCase *hc : ctx->cases) destroy_case(hc);
+    WorkList *wls[3] = {&ctx->cells, &ctx->faces, &ctx->halos};
+    for (WorkList *wl : wls) { cudaFree(wl->d_tiles); cudaFree(wl->d_case_first); cudaFree(wl->d_case_ntiles); }
+    cudaFree(ctx->d_cases);
+    cudaFree(ctx->d_partials);
+    cudaFree(ctx->d_flags);
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CFDL_OK;
+}
+
+int cfdl_update_boundaries(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_bc(ctx);
+    return cuda_status(cudaGetLastError());
+}
+
+int cfdl_solve_uvwp(cfdl_ctx *ctx, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = solve_uvwp_all(ctx))) return st;
+    return finish(ctx, stats);
+}
+
+int cfdl_update_time(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_update_time(ctx);
+    return cuda_status(cudaGetLastError());
+}
+
+int cfdl_step(cfdl_ctx *ctx, int n_outer, int ncoef, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (n_outer < 0) return CFDL_ERR_INVALID;
+    for (int k = 1; k <= n_outer; k++) {
+        launch_bc(ctx);
+        if ((st = solve_uvwp_all(ctx))) return st;
+        if (ncoef > 0 && k % ncoef == 0) launch_update_time(ctx);
+    }
+    return finish(ctx, stats);
+}
+
+int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    HostCase *hc = ctx->cases[0];
+    if ((st = transfer_fields(ctx, hc, f, false))) return st;
+    if ((st = solve_uvwp_all(ctx))) return st;
+    if ((st = transfer_fields(ctx, hc, f, true))) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    return finish(ctx, stats);
+}
+
+int cfdl_calc_coef_uvw(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_coef_uvw(ctx);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_solve_momentum(cfdl_ctx *ctx, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = solve_momentum(ctx))) return st;
+    return finish(ctx, stats);
+}
+
+int cfdl_calc_grad(cfdl_ctx *ctx, int field) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (field < 0 || field > 4) return CFDL_ERR_INVALID;
+    launch_grad(ctx, field);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_calc_mip(cfdl_ctx *ctx, int rhie_chow) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_calc_mip(ctx, rhie_chow ? 1 : 0);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_calc_coef_p(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_coef_p(ctx);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_solve_pc(cfdl_ctx *ctx, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = solve_pressure(ctx))) return st;
+    return finish(ctx, stats);
+}
+
+int cfdl_adjust_pc(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_adjust_pc(ctx);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_update_uvwp(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    launch_update_uvwp(ctx);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_get_array(cfdl_ctx *ctx, const char *name, double *host) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    return copy_named(ctx, ctx->cases[0], name, host, true);
+}
+
+int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    return copy_named(ctx, ctx->cases[0], name, const_cast<double *>(host), false);
+}
+
+int64_t cfdl_launch_count(const cfdl_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

@@ -1,0 +1,356 @@
+// cfdl_case.cpp -- host side of a case: validation of the reference-layout
+// mesh arrays, conversion to the device layout (ELL half-faces, face
+// geometry planes, halo tables), geometry precomputation, and the tile work
+// lists.  Compiled without floating-point contraction.
+//
+// The precomputed face quantities are the sub-expressions the reference
+// evaluates per half-face in calc_coef_uvw, calc_coef_p, calc_mip and
+// update_uvwp (src/equations/mod_uvwp.f90:161-436): area, unit normal, wt
+// (vec_weight, src/modules/mod_util.f90:729-743), dr, ds, the projected
+// distance dr_p/ds_p, and dr.n.  They depend only on the mesh, so the device
+// never recomputes a square root or a division for them.  The least-squares
+// gradient of calc_grad (src/modules/mod_solver.f90:40-81) is folded into a
+// per-half-face stencil A^-1 * (dr/|dr|^2), with A inverted by matinv3
+// (mod_solver.f90:8-38) including its trace fallback.
+#include "cfdl_internal.h"
+#include <algorithm>
+#include <cmath>
+#include <cfloat>
+#include <cstring>
+#include <new>
+
+namespace cfdl {
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return CFDL_OK;
+    if (e == cudaErrorMemoryAllocation) return CFDL_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return CFDL_ERR_NO_DEVICE;
+    return CFDL_ERR_CUDA;
+}
+
+int case_alloc(HostCase *hc, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) { *p = nullptr; cudaGetLastError(); return cuda_status(e); }
+    hc->allocs.push_back(*p);
+    return CFDL_OK;
+}
+
+void destroy_case(HostCase *hc) {
+    if (!hc) return;
+    for (void *p : hc->allocs) cudaFree(p);
+    delete hc;
+}
+
+void apply_config(HostCase *hc, const cfdl_config *cfg) {
+    hc->cfg = *cfg;
+    CaseDev &d = hc->dev;
+    d.dt = cfg->dt; d.alpha_u = cfg->alpha_u; d.alpha_p = cfg->alpha_p;
+    d.rtol_u = cfg->rtol_u; d.rtol_p = cfg->rtol_p; d.tight_rtol = cfg->tight_rtol;
+    d.nit = cfg->nit; d.solve_mode = cfg->solve_mode; d.tight_maxit = cfg->tight_maxit;
+    d.precision = cfg->precision;
+}
+
+namespace {
+
+inline void get_idx(int idx, int &g, int &s) { s = (int)((unsigned)idx & 31u); g = (int)((unsigned)idx >> 5); }
+
+// matinv3, src/modules/mod_solver.f90:8-38
+void matinv3(const double A[3][3], double B[3][3]) {
+    double det = (A[0][0]*A[1][1]*A[2][2] - A[0][0]*A[1][2]*A[2][1]
+                - A[0][1]*A[1][0]*A[2][2] + A[0][1]*A[1][2]*A[2][0]
+                + A[0][2]*A[1][0]*A[2][1] - A[0][2]*A[1][1]*A[2][0]);
+    if (std::fabs(det) > DBL_MIN) {
+        double di = 1.0 / det;
+        B[0][0] = +di * (A[1][1]*A[2][2] - A[1][2]*A[2][1]);
+        B[1][0] = -di * (A[1][0]*A[2][2] - A[1][2]*A[2][0]);
+        B[2][0] = +di * (A[1][0]*A[2][1] - A[1][1]*A[2][0]);
+        B[0][1] = -di * (A[0][1]*A[2][2] - A[0][2]*A[2][1]);
+        B[1][1] = +di * (A[0][0]*A[2][2] - A[0][2]*A[2][0]);
+        B[2][1] = -di * (A[0][0]*A[2][1] - A[0][1]*A[2][0]);
+        B[0][2] = +di * (A[0][1]*A[1][2] - A[0][2]*A[1][1]);
+        B[1][2] = -di * (A[0][0]*A[1][2] - A[0][2]*A[1][0]);
+        B[2][2] = +di * (A[0][0]*A[1][1] - A[0][1]*A[1][0]);
+    } else {
+        std::memset(B, 0, 9 * sizeof(double));
+        double di = 1.0 / (A[0][0] + A[1][1] + A[2][2]);
+        B[0][0] = di; B[1][1] = di; B[2][2] = di;
+    }
+}
+
+double vec_weight(const double *r0, const double *r1, const double *r2) {
+    double ra[3], rb[3];
+    for (int i = 0; i < 3; i++) { ra[i] = r1[i] - r0[i]; rb[i] = r2[i] - r0[i]; }
+    double la = std::sqrt(ra[0]*ra[0] + ra[1]*ra[1] + ra[2]*ra[2]);
+    double lb = std::sqrt(rb[0]*rb[0] + rb[1]*rb[1] + rb[2]*rb[2]);
+    return la + lb > 0. ? la / (la + lb) : 0.5;
+}
+
+template <class T> int upload(HostCase *hc, T **dptr, const std::vector<T> &h) {
+    int st = case_alloc(hc, (void **)dptr, h.size() * sizeof(T));
+    if (st) return st;
+    return cuda_status(cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+template <class T> int zeros(HostCase *hc, T **dptr, size_t n) {
+    int st = case_alloc(hc, (void **)dptr, n * sizeof(T));
+    if (st) return st;
+    return cuda_status(cudaMemset(*dptr, 0, n * sizeof(T)));
+}
+
+int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_nb, const std::vector<int> &hf_fc,
+               const std::vector<double> &hf_G, const std::vector<int> &f_own, const std::vector<int> &f_nb,
+               const std::vector<double> &fgeo, const std::vector<int> &h_own, const std::vector<int> &h_face,
+               const std::vector<int> &h_kind, const std::vector<double> &h_vel, const std::vector<double> &vol) {
+    CaseDev &d = hc->dev;
+    const int ne = hc->ne, nf = hc->nf, nbf = hc->nbf, W = hc->W, nc = ne + nbf;
+    d.ne = ne; d.nbf = nbf; d.nf = nf; d.W = W;
+    int st;
+    if ((st = upload(hc, (int **)&d.hf_nb, hf_nb))) return st;
+    if ((st = upload(hc, (int **)&d.hf_fc, hf_fc))) return st;
+    if ((st = upload(hc, (double **)&d.hf_G, hf_G))) return st;
+    if ((st = upload(hc, (int **)&d.f_own, f_own))) return st;
+    if ((st = upload(hc, (int **)&d.f_nb, f_nb))) return st;
+    if ((st = upload(hc, (double **)&d.fgeo, fgeo))) return st;
+    if ((st = upload(hc, (int **)&d.h_own, h_own))) return st;
+    if ((st = upload(hc, (int **)&d.h_face, h_face))) return st;
+    if ((st = upload(hc, (int **)&d.h_kind, h_kind))) return st;
+    if ((st = upload(hc, (double **)&d.h_vel, h_vel))) return st;
+    if ((st = upload(hc, (double **)&d.vol, vol))) return st;
+    double **cellf[] = {&d.u, &d.v, &d.w, &d.p, &d.u0, &d.v0, &d.w0, &d.phic};
+    for (double **pp : cellf) if ((st = zeros(hc, pp, (size_t)nc))) return st;
+    double **gradf[] = {&d.gu, &d.gv, &d.gw, &d.gp, &d.gpc};
+    for (double **pp : gradf) if ((st = zeros(hc, pp, 3 * (size_t)nc))) return st;
+    if ((st = zeros(hc, &d.mip, (size_t)nf))) return st;
+    if ((st = zeros(hc, &d.mip0, (size_t)nf))) return st;
+    double **ef[] = {&d.bu, &d.bv, &d.bw, &d.d, &d.dc, &d.rho, &d.mu, &d.ap, &d.b};
+    for (double **pp : ef) if ((st = zeros(hc, pp, (size_t)ne))) return st;
+    if ((st = zeros(hc, &d.anb, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.fdiff, (size_t)nf))) return st;
+    if ((st = zeros(hc, &d.fS, 3 * (size_t)nf))) return st;
+    if ((st = zeros(hc, &d.fD, 3 * (size_t)nf))) return st;
+    double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt, &d.kb};
+    for (double **pp : kv) if ((st = zeros(hc, pp, 3 * (size_t)ne))) return st;
+    float **fv[] = {&d.fr, &d.fz, &d.fp, &d.fq, &d.fx, &d.fdiag};
+    for (float **pp : fv) if ((st = zeros(hc, pp, (size_t)ne))) return st;
+    if ((st = zeros(hc, &d.fanb, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.sc, 1))) return st;
+    if ((st = zeros(hc, &d.counters, 16))) return st;
+    std::vector<double> rho(ne, cfg->rho), mu(ne, cfg->mu);
+    if ((st = cuda_status(cudaMemcpy(d.rho, rho.data(), ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
+    return cuda_status(cudaMemcpy(d.mu, mu.data(), ne * sizeof(double), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostCase **out) {
+    *out = nullptr;
+    if (!m || !cfg) return CFDL_ERR_INVALID;
+    const int ne = m->ne, nf = m->nf, nbf = m->nbf;
+    if (ne <= 0 || nf <= 0 || nbf < 0 || !m->ef2nb1 || !m->ef2nb2 || !m->ef2nb_idx || !m->s2g ||
+        (nbf > 0 && !m->bs) || !m->aip || !m->rip || !m->xc || !m->yc || !m->zc || !m->vol)
+        return CFDL_ERR_INVALID;
+    if ((long long)ne + nbf >= (1LL << 26)) return CFDL_ERR_INVALID;
+    const int H = 2 * nf - nbf;
+    if (H <= 0 || m->ef2nb_idx[0] != 1 || m->ef2nb_idx[ne] != H + 1) return CFDL_ERR_INVALID;
+    const int nc = ne + nbf;
+    HostCase *hc = new (std::nothrow) HostCase;
+    if (!hc) return CFDL_ERR_OOM;
+    int st = CFDL_OK;
+    try {
+        hc->ne = ne; hc->nf = nf; hc->nbf = nbf; hc->H = H;
+        hc->ef2nb_idx.assign(m->ef2nb_idx, m->ef2nb_idx + ne + 1);
+        int W = 0;
+        for (int e = 0; e < ne; e++) {
+            int cnt = m->ef2nb_idx[e + 1] - m->ef2nb_idx[e];
+            if (cnt <= 0 || cnt > kMaxW) { delete hc; return CFDL_ERR_INVALID; }
+            W = std::max(W, cnt);
+        }
+        hc->W = W;
+        // ---- ELL half-faces + validation of every index ----
+        std::vector<int> hf_nb((size_t)W * ne, -1), hf_fc((size_t)W * ne, 0);
+        std::vector<int> f_own(nf, -1), f_nb(nf, -1);
+        for (int e = 0; e < ne; e++) {
+            for (int idx = m->ef2nb_idx[e]; idx < m->ef2nb_idx[e + 1]; idx++) {
+                int k = idx - m->ef2nb_idx[e];
+                int enb, lfnb;
+                get_idx(m->ef2nb1[idx - 1], enb, lfnb);
+                int fg = m->ef2nb2[idx - 1];
+                int fa = fg >= 0 ? fg : -fg;
+                if (enb < 1 || enb > nc || fa < 1 || fa > nf) { delete hc; return CFDL_ERR_INVALID; }
+                if ((lfnb == 0) != (enb > ne)) { delete hc; return CFDL_ERR_INVALID; }
+                hf_nb[(size_t)k * ne + e] = enb - 1;
+                hf_fc[(size_t)k * ne + e] = fg > 0 ? fa - 1 : ~(fa - 1);
+                if (fg > 0) {
+                    if (f_own[fa - 1] != -1) { delete hc; return CFDL_ERR_INVALID; }
+                    f_own[fa - 1] = e; f_nb[fa - 1] = enb - 1;
+                }
+            }
+        }
+        for (int f = 0; f < nf; f++) {
+            if (f_own[f] < 0) { delete hc; return CFDL_ERR_INVALID; }
+            int e, lf;
+            get_idx(m->s2g[f], e, lf);           // s2g names the owner side
+            if (e - 1 != f_own[f]) { delete hc; return CFDL_ERR_INVALID; }
+        }
+        // ---- halos and boundary conditions ----
+        std::vector<int> h_own(std::max(nbf, 1), 0), h_face(std::max(nbf, 1), 0), h_kind(std::max(nbf, 1), 0);
+        std::vector<double> h_vel(3 * (size_t)std::max(nbf, 1), 0.0);
+        for (int h = 0; h < nbf; h++) {
+            int b = m->bs[h] < 0 ? -m->bs[h] : m->bs[h], e, lf;
+            get_idx(b, e, lf);
+            if (e < 1 || e > ne || lf < 1 || lf > m->ef2nb_idx[e] - m->ef2nb_idx[e - 1]) { delete hc; return CFDL_ERR_INVALID; }
+            int fg = m->ef2nb2[m->ef2nb_idx[e - 1] + lf - 1 - 1];
+            if (fg < 1 || f_nb[fg - 1] != ne + h) { delete hc; return CFDL_ERR_INVALID; }
+            h_own[h] = e - 1; h_face[h] = fg - 1;
+        }
+        for (int bc = 0; bc < m->nbc; bc++) {
+            int a = m->bc_esec[2 * bc], z = m->bc_esec[2 * bc + 1];
+            if (a < ne + 1 || z > nc || a > z + 1) { delete hc; return CFDL_ERR_INVALID; }
+            int kind = m->bc_kind[bc];
+            if (kind != CFDL_BC_WALL && kind != CFDL_BC_SYMMETRY) { delete hc; return CFDL_ERR_INVALID; }
+            for (int el = a; el <= z; el++) {
+                int h = el - ne - 1;
+                h_kind[h] = kind;
+                for (int q = 0; q < 3; q++) h_vel[3 * (size_t)h + q] = m->bc_vel[3 * bc + q];
+            }
+        }
+        // ---- face geometry planes ----
+        std::vector<double> fgeo((size_t)FG_N * nf, 0.0);
+        auto G = [&](int plane, int f) -> double & { return fgeo[(size_t)plane * nf + f]; };
+        for (int f = 0; f < nf; f++) {
+            int e = f_own[f], n = f_nb[f];
+            const double *a = &m->aip[3 * (size_t)f], *ri = &m->rip[3 * (size_t)f];
+            double rp[3] = {m->xc[e], m->yc[e], m->zc[e]}, rn[3] = {m->xc[n], m->yc[n], m->zc[n]};
+            double area = std::sqrt(a[0]*a[0] + a[1]*a[1] + a[2]*a[2]);
+            double nrm[3] = {a[0] / area, a[1] / area, a[2] / area};
+            double dr[3] = {rn[0] - rp[0], rn[1] - rp[1], rn[2] - rp[2]};
+            double ds = std::sqrt(dr[0]*dr[0] + dr[1]*dr[1] + dr[2]*dr[2]);
+            G(FG_AX, f) = a[0]; G(FG_AY, f) = a[1]; G(FG_AZ, f) = a[2];
+            G(FG_AREA, f) = area;
+            G(FG_DRX, f) = dr[0]; G(FG_DRY, f) = dr[1]; G(FG_DRZ, f) = dr[2];
+            G(FG_ADS, f) = area / ds;
+            if (n < ne) {
+                G(FG_WT, f) = vec_weight(ri, rp, rn);
+                double dn = dr[0]*nrm[0] + dr[1]*nrm[1] + dr[2]*nrm[2];
+                G(FG_ADN, f) = area / dn;
+                double drip[3], t, rpp[3], rnp[3], drp[3];
+                for (int q = 0; q < 3; q++) drip[q] = ri[q] - rp[q];
+                t = drip[0]*nrm[0] + drip[1]*nrm[1] + drip[2]*nrm[2];
+                for (int q = 0; q < 3; q++) rpp[q] = ri[q] - t * nrm[q];
+                for (int q = 0; q < 3; q++) drip[q] = ri[q] - rn[q];
+                t = drip[0]*nrm[0] + drip[1]*nrm[1] + drip[2]*nrm[2];
+                for (int q = 0; q < 3; q++) rnp[q] = ri[q] - t * nrm[q];
+                for (int q = 0; q < 3; q++) drp[q] = rnp[q] - rpp[q];
+                double dsp = std::sqrt(drp[0]*drp[0] + drp[1]*drp[1] + drp[2]*drp[2]);
+                for (int q = 0; q < 3; q++) {
+                    G(FG_ADRX + q, f) = area * dr[q] / ds;
+                    G(FG_EX + q, f) = area * (drp[q] / dsp - dr[q] / ds);
+                }
+            }
+        }
+        // ---- least-squares gradient stencil ----
+        std::vector<double> hf_G(3 * (size_t)W * ne, 0.0);
+        for (int e = 0; e < ne; e++) {
+            double A[3][3] = {{0}}, Ai[3][3], wdr[kMaxW][3];
+            int cnt = m->ef2nb_idx[e + 1] - m->ef2nb_idx[e];
+            for (int k = 0; k < cnt; k++) {
+                int n = hf_nb[(size_t)k * ne + e];
+                double dr[3] = {m->xc[n] - m->xc[e], m->yc[n] - m->yc[e], m->zc[n] - m->zc[e]};
+                double wt = 1. / (dr[0]*dr[0] + dr[1]*dr[1] + dr[2]*dr[2]);
+                for (int q = 0; q < 3; q++) wdr[k][q] = wt * dr[q];
+                A[0][0] = A[0][0] + wt*dr[0]*dr[0];
+                A[0][1] = A[0][1] + wt*dr[0]*dr[1];
+                A[0][2] = A[0][2] + wt*dr[0]*dr[2];
+                A[1][1] = A[1][1] + wt*dr[1]*dr[1];
+                A[1][2] = A[1][2] + wt*dr[1]*dr[2];
+                A[2][2] = A[2][2] + wt*dr[2]*dr[2];
+            }
+            A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
+            matinv3(A, Ai);
+            for (int k = 0; k < cnt; k++)
+                for (int q = 0; q < 3; q++)
+                    hf_G[((size_t)q * W + k) * ne + e] = Ai[q][0]*wdr[k][0] + Ai[q][1]*wdr[k][1] + Ai[q][2]*wdr[k][2];
+        }
+        // ---- device upload ----
+        st = upload_all(hc, cfg, hf_nb, hf_fc, hf_G, f_own, f_nb, fgeo, h_own, h_face, h_kind, h_vel,
+                        std::vector<double>(m->vol, m->vol + ne));
+        if (st) { destroy_case(hc); return st; }
+        apply_config(hc, cfg);
+    } catch (const std::bad_alloc &) {
+        destroy_case(hc);
+        return CFDL_ERR_OOM;
+    }
+    (void)ctx;
+    *out = hc;
+    return CFDL_OK;
+}
+
+// Tile work lists over every case of the context.
+int rebuild_worklists(cfdl_ctx *ctx) {
+    WorkList *wls[3] = {&ctx->cells, &ctx->faces, &ctx->halos};
+    for (int t = 0; t < 3; t++) {
+        WorkList &wl = *wls[t];
+        wl.h_tiles.clear(); wl.case_first.clear(); wl.case_ntiles.clear();
+        for (size_t c = 0; c < ctx->cases.size(); c++) {
+            const HostCase *hc = ctx->cases[c];
+            int n = t == 0 ? hc->ne : t == 1 ? hc->nf : hc->nbf;
+            wl.case_first.push_back((int)wl.h_tiles.size());
+            int cnt = 0;
+            for (int s = 0; s < n; s += kTile, cnt++) wl.h_tiles.push_back({(int)c, s, std::min(n, s + kTile), 0});
+            wl.case_ntiles.push_back(cnt);
+        }
+        wl.ntiles = (int)wl.h_tiles.size();
+        cudaFree(wl.d_tiles); cudaFree(wl.d_case_first); cudaFree(wl.d_case_ntiles);
+        wl.d_tiles = nullptr; wl.d_case_first = nullptr; wl.d_case_ntiles = nullptr;
+        size_t nt = std::max<size_t>(1, wl.h_tiles.size()), ncs = std::max<size_t>(1, ctx->cases.size());
+        int st;
+        if ((st = cuda_status(cudaMalloc(&wl.d_tiles, nt * sizeof(Tile))))) return st;
+        if ((st = cuda_status(cudaMalloc(&wl.d_case_first, ncs * sizeof(int))))) return st;
+        if ((st = cuda_status(cudaMalloc(&wl.d_case_ntiles, ncs * sizeof(int))))) return st;
+        if (!wl.h_tiles.empty()) {
+            if ((st = cuda_status(cudaMemcpy(wl.d_tiles, wl.h_tiles.data(), wl.h_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice)))) return st;
+            if ((st = cuda_status(cudaMemcpy(wl.d_case_first, wl.case_first.data(), wl.case_first.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
+            if ((st = cuda_status(cudaMemcpy(wl.d_case_ntiles, wl.case_ntiles.data(), wl.case_ntiles.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
+        }
+    }
+    int need = std::max({ctx->cells.ntiles, ctx->faces.ntiles, ctx->halos.ntiles, 1});
+    if (need > ctx->partials_cap) {
+        cudaFree(ctx->d_partials);
+        ctx->d_partials = nullptr;
+        int st = cuda_status(cudaMalloc(&ctx->d_partials, (size_t)need * kNPart * sizeof(double)));
+        if (st) { ctx->partials_cap = 0; return st; }
+        ctx->partials_cap = need;
+    }
+    int ncases = (int)ctx->cases.size();
+    if (ncases > ctx->h_flags_cap) {
+        cudaFreeHost(ctx->h_flags); cudaFree(ctx->d_flags);
+        ctx->h_flags = nullptr; ctx->d_flags = nullptr;
+        int cap = std::max(ncases, 8);
+        int st = cuda_status(cudaMallocHost(&ctx->h_flags, (size_t)cap * 4 * sizeof(int)));
+        if (!st) st = cuda_status(cudaMalloc(&ctx->d_flags, (size_t)cap * 4 * sizeof(int)));
+        if (st) { ctx->h_flags_cap = 0; return st; }
+        ctx->h_flags_cap = cap;
+    }
+    return upload_case_table(ctx);
+}
+
+int upload_case_table(cfdl_ctx *ctx) {
+    int n = (int)ctx->cases.size();
+    if (n > ctx->d_cases_cap) {
+        cudaFree(ctx->d_cases);
+        ctx->d_cases = nullptr;
+        int cap = std::max(n, 8);
+        int st = cuda_status(cudaMalloc(&ctx->d_cases, (size_t)cap * sizeof(CaseDev)));
+        if (st) { ctx->d_cases_cap = 0; return st; }
+        ctx->d_cases_cap = cap;
+    }
+    std::vector<CaseDev> tab(n);
+    for (int c = 0; c < n; c++) tab[c] = ctx->cases[c]->dev;
+    if (n == 0) return CFDL_OK;
+    int st = cuda_status(cudaMemcpyAsync(ctx->d_cases, tab.data(), n * sizeof(CaseDev), cudaMemcpyHostToDevice, ctx->stream));
+    if (st) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace cfdl

@@ -1,0 +1,67 @@
+// cfdl_device.cuh -- device helpers shared by the kernels of libcfdgpu.
+#pragma once
+#include "cfdl_internal.h"
+
+namespace cfdl {
+
+// Deterministic block reduction of K doubles (kTile threads): a fixed
+// shuffle tree per warp, then warp partials summed in warp order by one
+// thread.  The result lands in out[0..K-1].
+template <int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double *out) {
+    __shared__ double sm[K][kTile / 32];
+#pragma unroll
+    for (int k = 0; k < K; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) sm[k][wid] = v[k];
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double s = 0.0;
+        for (int w = 0; w < kTile / 32; w++) s += sm[threadIdx.x][w];
+        out[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// Sum the K partials of tiles [first, first+n) in tile order (whole block),
+// result broadcast in shared memory res[0..K-1].
+template <int K>
+__device__ __forceinline__ void sum_partials(const double *partials, int first, int n, double *res) {
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = 0.0;
+    // thread-strided in fixed order, then the fixed tree
+    for (int i = threadIdx.x; i < n; i += kTile)
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] += __ldcg(&partials[(size_t)(first + i) * kNPart + k]);
+    __shared__ double tmp[K];
+    block_reduce<K>(v, tmp);
+    if (threadIdx.x < K) res[threadIdx.x] = tmp[threadIdx.x];
+    __syncthreads();
+}
+
+// "Last tile of the case finalises": every tile of case c publishes its
+// partials, then increments the case counter; the tile that brings it to
+// ntiles sums all partials (in tile order, so the result does not depend on
+// which tile came last) and resets the counter.
+__device__ __forceinline__ bool last_tile_of_case(int *counter, int ntiles) {
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int prev = atomicAdd(counter, 1);
+        is_last = (prev == ntiles - 1);
+        if (is_last) *counter = 0;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last != 0;
+}
+
+__device__ __forceinline__ int face_of(int fc) { return fc >= 0 ? fc : ~fc; }
+
+}  // namespace cfdl

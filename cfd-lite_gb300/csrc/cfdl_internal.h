@@ -1,0 +1,162 @@
+// cfdl_internal.h -- device data layout and launch plumbing of libcfdgpu.
+//
+// Layout in HBM (per case, all device pointers):
+//   cells      0..ne-1 interior, ne..ne+nbf-1 halos (boundary faces): the
+//              reference numbering shifted to 0-based;
+//   half-faces ELL slots [W][ne] (W = max faces per cell, padding nb = -1),
+//              slot k of cell e = local face k+1 of the reference CSR:
+//              hf_nb = neighbour cell or halo, hf_fc = face id (owner side)
+//              or ~face id (neighbour side), hf_G = least-squares gradient
+//              stencil A^-1 * w * dr, planes [3][W][ne];
+//   faces      reference face order fg-1: f_own, f_nb and precomputed
+//              geometry planes fgeo[FG_*][nf];
+//   halos      h_own (owner cell), h_face, h_kind, h_vel (wall velocity).
+// Fields keep the reference layout (gradients xyz-interleaved) so uploads and
+// downloads are plain copies.
+//
+// Every kernel walks a work list of tiles: tile = (case, first, last) over the
+// cells, faces or halos of one case, one CTA per tile.  A single case is a list
+// of one; the batched and served forms put many cases in one list, so one
+// launch covers all of them.  Reductions write one partial per tile; the last
+// tile of a case to finish sums that case's partials in tile order, so every
+// result is deterministic run to run and needs no extra launch.
+#pragma once
+#include "cfdl.h"
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+namespace cfdl {
+
+constexpr int kTile = 256;        // cells / faces / halos per CTA
+constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
+constexpr int kNPart = 16;        // partial slots per tile
+
+// face geometry planes, precomputed once per mesh (cfdl_case.cpp)
+enum FaceGeo {
+    FG_WT = 0,              // vec_weight(rip, r_own, r_nb)
+    FG_AX, FG_AY, FG_AZ,    // aip (area vector, outward from the owner)
+    FG_AREA,                // |aip|
+    FG_ADN,                 // area / (dr . n)
+    FG_DRX, FG_DRY, FG_DRZ, // dr = r_nb - r_own
+    FG_ADS,                 // area / ds
+    FG_ADRX, FG_ADRY, FG_ADRZ,  // area * dr / ds
+    FG_EX, FG_EY, FG_EZ,        // area * (dr_p/ds_p - dr/ds)
+    FG_N
+};
+
+// Per-case solver state on the device.
+struct SolveScalars {
+    // momentum BiCGStab, one lane per component u, v, w
+    double rho[3], alpha[3], omega[3], beta[3];
+    int half[3];
+    double rnorm[3], r0norm[3], bnorm[3], tol[3];
+    int active[3], iters[3], status[3];
+    // pressure CG
+    double rz, rnorm_p, r0norm_p, tol_p, alpha_p, beta_p, mean_b, pref;
+    int active_p, iters_p, status_p;
+    // mixed-precision refinement
+    double res64, res64_0, tol64;
+    int outer_p;
+    float rz32, tol32, alpha32, beta32, rnorm32;
+    int active32, iters32;
+    double mass_imbalance;
+};
+
+struct CaseDev {
+    int ne, nbf, nf, W;
+    // mesh
+    const int *hf_nb, *hf_fc;
+    const double *hf_G;
+    const int *f_own, *f_nb;
+    const double *fgeo;
+    const int *h_own, *h_face, *h_kind;
+    const double *h_vel;
+    const double *vol;
+    // fields (reference layout)
+    double *u, *v, *w, *p, *u0, *v0, *w0;
+    double *gu, *gv, *gw, *gp, *gpc;
+    double *mip, *mip0;
+    double *bu, *bv, *bw, *d, *dc, *rho, *mu;
+    double *ap, *anb, *b, *phic;          // phys_t scratch: ap[ne], anb ELL [W][ne], b[ne], phic[ne+nbf]
+    // face intermediates of the assemblies
+    double *fdiff, *fS, *fD;              // [nf], [3][nf], [3][nf]
+    // Krylov work vectors, [3][ne] each (pressure uses plane 0)
+    double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt, *kb;
+    // FP32 work vectors for the mixed-precision pressure solve, [ne] each
+    float *fr, *fz, *fp, *fq, *fx, *fdiag, *fanb;   // fanb ELL [W][ne]
+    SolveScalars *sc;
+    int *counters;                        // [16] last-tile counters, zero between launches
+    // parameters
+    double dt, alpha_u, alpha_p, rtol_u, rtol_p, tight_rtol;
+    int nit, solve_mode, tight_maxit, precision;
+};
+
+struct Tile { int c, first, last, pad; };
+
+// One work list per entity type, with each case's tile range for reductions.
+struct WorkList {
+    int ntiles = 0;
+    Tile *d_tiles = nullptr;
+    int *d_case_first = nullptr, *d_case_ntiles = nullptr;
+    std::vector<Tile> h_tiles;
+    std::vector<int> case_first, case_ntiles;
+};
+
+// Host-side record of one case.
+struct HostCase {
+    int ne = 0, nf = 0, nbf = 0, W = 0, H = 0;
+    cfdl_config cfg{};
+    std::vector<int> ef2nb_idx;      // [ne+1], 1-based values
+    std::vector<void *> allocs;      // device allocations owned by the case
+    CaseDev dev{};                   // host mirror of the device struct
+};
+
+}  // namespace cfdl
+
+// A context: one or more cases resident on one device, one stream.
+struct cfdl_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<cfdl::HostCase *> cases;
+    cfdl::CaseDev *d_cases = nullptr;
+    int d_cases_cap = 0;
+    cfdl::WorkList cells, faces, halos;
+    double *d_partials = nullptr;        // [max tiles][kNPart]
+    int partials_cap = 0;                // tiles
+    int64_t launches = 0;
+    void *h_pinned = nullptr;            // pinned staging for host transfers
+    size_t h_pinned_bytes = 0;
+    int *h_flags = nullptr;              // pinned, per-case convergence flags
+    int h_flags_cap = 0;
+    int *d_flags = nullptr;
+};
+
+namespace cfdl {
+int cuda_status(cudaError_t e);
+int case_alloc(HostCase *hc, void **p, size_t bytes);
+int rebuild_worklists(cfdl_ctx *ctx);
+int upload_case_table(cfdl_ctx *ctx);
+int create_case(cfdl_ctx *ctx, const cfdl_mesh *mesh, const cfdl_config *cfg, HostCase **out);
+void destroy_case(HostCase *hc);
+void apply_config(HostCase *hc, const cfdl_config *cfg);
+
+// kernel launchers (cfdl_kernels.cu): asynchronous on ctx->stream, all cases
+void launch_bc(cfdl_ctx *ctx);
+void launch_coef_uvw(cfdl_ctx *ctx);
+void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused
+void launch_calc_mip(cfdl_ctx *ctx, int rhie_chow);
+void launch_coef_p(cfdl_ctx *ctx);
+void launch_adjust_pc(cfdl_ctx *ctx);
+void launch_update_uvwp(cfdl_ctx *ctx);
+void launch_update_time(cfdl_ctx *ctx);
+void launch_set_mip0(cfdl_ctx *ctx);
+
+// solvers (cfdl_solvers.cu)
+int solve_momentum(cfdl_ctx *ctx);
+int solve_pressure(cfdl_ctx *ctx);
+int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st);
+
+// one outer iteration for every case of the context (cfdl_api.cpp)
+int solve_uvwp_all(cfdl_ctx *ctx);
+}  // namespace cfdl

@@ -1,0 +1,385 @@
+// cfdl_kernels.cu -- assembly, gradient, flux and correction kernels of one
+// SIMPLE outer iteration (FP64), one CTA per tile of the work list.
+//
+// Each kernel restates a reference routine (cited per kernel).  Per-face
+// quantities that the reference computes twice (once from each side of a
+// face) are computed once per face here and gathered by the cells, and every
+// mesh-only sub-expression comes from the precomputed face planes; the
+// remaining FP64 arithmetic is what the fields require.  Cell-side sums run in
+// the reference's CSR half-face order, and boundary contributions in the
+// reference's BC-loop order (ascending halo index), so the only differences
+// from the reference are the roundings of the reassociated face terms.
+#include "cfdl_device.cuh"
+
+namespace cfdl {
+namespace {
+
+#define TILE_PROLOGUE(WL)                         \
+    const Tile t = tiles[blockIdx.x];             \
+    const CaseDev &C = cases[t.c];                \
+    const int i = t.first + (int)threadIdx.x;     \
+    (void)C;
+
+// ---------------------------------------------------------------------------
+// update_boundaries -> lid / dirichlet0 / symmetry, mod_physics.f90:38-50,
+// mod_uvwp.f90:493-570.  One thread per halo.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_bc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(halos)
+    if (i >= t.last) return;
+    const int kind = C.h_kind[i];
+    if (kind == 0) return;
+    const int e = C.h_own[i], f = C.h_face[i], h = C.ne + i;
+    if (kind == CFDL_BC_WALL) {
+        C.u[h] = C.h_vel[3 * i];
+        C.v[h] = C.h_vel[3 * i + 1];
+        C.w[h] = C.h_vel[3 * i + 2];
+    } else {  // symmetry: velt - 2*veln of the owner velocity
+        const double *g = C.fgeo;
+        const int nf = C.nf;
+        double area = g[FG_AREA * nf + f];
+        double n0 = g[FG_AX * nf + f] / area, n1 = g[FG_AY * nf + f] / area, n2 = g[FG_AZ * nf + f] / area;
+        double vu = C.u[e], vv = C.v[e], vw = C.w[e];
+        double vn = vu * n0 + vv * n1 + vw * n2;
+        double a0 = vn * n0, a1 = vn * n1, a2 = vn * n2;
+        C.u[h] = (vu - a0) - 2 * a0;
+        C.v[h] = (vv - a1) - 2 * a1;
+        C.w[h] = (vw - a2) - 2 * a2;
+    }
+    C.p[h] = C.p[e];
+    C.mip[f] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// calc_coef_uvw, face part (mod_uvwp.f90:183-226): per interior face the
+// diffusion coefficient muip*area/ds and the secondary-stress (sumss) and
+// deferred non-orthogonal correction (sumdefc) terms, from the owner's side;
+// the neighbour takes them with the opposite sign.  Boundary faces: the wall
+// diffusion mu*area/ds of the BC loop (mod_uvwp.f90:257).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    const double *g = C.fgeo;
+    if (n >= C.ne) {
+        C.fdiff[i] = C.mu[o] * g[FG_ADS * nf + i];
+        return;
+    }
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
+    const double muip = omw * C.mu[o] + wt * C.mu[n];
+    C.fdiff[i] = muip * g[FG_ADS * nf + i];
+    const double A0 = g[FG_ADRX * nf + i], A1 = g[FG_ADRY * nf + i], A2 = g[FG_ADRZ * nf + i];
+    const double E0 = g[FG_EX * nf + i], E1 = g[FG_EY * nf + i], E2 = g[FG_EZ * nf + i];
+    double gi[3][3];   // gi[q][m]: component m of grad(u_q) at the face
+    const double *gq[3] = {C.gu, C.gv, C.gw};
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int m = 0; m < 3; m++) gi[q][m] = omw * gq[q][3 * o + m] + wt * gq[q][3 * n + m];
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+        // sumss(m): gip = (du/dx_m, dv/dx_m, dw/dx_m) . dr
+        C.fS[m * nf + i] = muip * (gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2);
+        // sumdefc(q=m): grad(u_m) . (dr_p/ds_p - dr/ds)
+        C.fD[m * nf + i] = muip * (gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2);
+    }
+}
+
+// calc_coef_uvw, cell part (mod_uvwp.f90:174-284) + implicit relaxation.
+__global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, nf = C.nf, W = C.W;
+    double ap = 0.0, sumf = 0.0, ss0 = 0.0, ss1 = 0.0, ss2 = 0.0, dd0 = 0.0, dd1 = 0.0, dd2 = 0.0;
+    double a[kMaxW];
+    int bslot[kMaxW], nb_cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        a[k] = 0.0;
+        if (k >= W) continue;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb < 0) continue;
+        if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
+        const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
+        const double sg = fc >= 0 ? 1.0 : -1.0;
+        const double fl = -sg * C.mip[f];
+        const double ak = C.fdiff[f] + fmax(fl, 0.0);
+        sumf += fl;
+        a[k] = ak;
+        ap += ak;
+        ss0 += sg * C.fS[f]; ss1 += sg * C.fS[nf + f]; ss2 += sg * C.fS[2 * nf + f];
+        dd0 += sg * C.fD[f]; dd1 += sg * C.fD[nf + f]; dd2 += sg * C.fD[2 * nf + f];
+    }
+    const double vol = C.vol[i];
+    const double ap0 = C.rho[i] * vol / C.dt;
+    ap = ap + ap0;
+    const double ue = C.u[i], ve = C.v[i], we = C.w[i];
+    double bu = ap0 * C.u0[i] + sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
+    double bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
+    double bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+    // boundary conditions in BC-loop order (ascending halo index)
+    for (int q = 1; q < nb_cnt; q++) {
+        int s = bslot[q], j = q - 1;
+        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
+        bslot[j + 1] = s;
+    }
+    for (int q = 0; q < nb_cnt; q++) {
+        const int k = bslot[q], h = C.hf_nb[k * ne + i], f = face_of(C.hf_fc[k * ne + i]);
+        const int kind = C.h_kind[h - ne];
+        if (kind == 0) continue;
+        const double dbc = C.fdiff[f];
+        if (kind == CFDL_BC_WALL) {
+            const double area = C.fgeo[FG_AREA * nf + f];
+            const double n0 = C.fgeo[FG_AX * nf + f] / area, n1 = C.fgeo[FG_AY * nf + f] / area, n2 = C.fgeo[FG_AZ * nf + f] / area;
+            const double tn = ue * n0 + ve * n1 + we * n2;
+            const double r0 = C.u[h] - (ue - tn * n0), r1 = C.v[h] - (ve - tn * n1), r2 = C.w[h] - (we - tn * n2);
+            bu = bu + dbc * r0 - dbc * ue;
+            bv = bv + dbc * r1 - dbc * ve;
+            bw = bw + dbc * r2 - dbc * we;
+        }
+        ap = ap + dbc;
+        a[k] = a[k] + dbc;
+    }
+    if (C.alpha_u != 1.0) {
+        const double apr = ap / C.alpha_u, f1 = (1.0 - C.alpha_u) * apr;
+        bu = bu + f1 * ue; bv = bv + f1 * ve; bw = bw + f1 * we;
+        ap = apr;
+    }
+    C.ap[i] = ap;
+    C.bu[i] = bu; C.bv[i] = bv; C.bw[i] = bw;
+    C.d[i] = vol / ap;
+    double dcs = ap;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k < W) {
+            dcs = dcs - a[k];
+            C.anb[k * ne + i] = a[k];
+        }
+    }
+    C.dc[i] = vol / dcs;
+}
+
+// ---------------------------------------------------------------------------
+// calc_grad, mod_solver.f90:40-81, as the stencil sum grad = sum_k G_k dphi_k.
+// NF fields at once (u,v,w share the stencil loads).
+// ---------------------------------------------------------------------------
+template <int NF>
+__global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int field) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, W = C.W;
+    const double *phi[NF];
+    double *grad[NF];
+    if (NF == 3) { phi[0] = C.u; phi[1 % NF] = C.v; phi[2 % NF] = C.w; grad[0] = C.gu; grad[1 % NF] = C.gv; grad[2 % NF] = C.gw; }
+    else {
+        phi[0] = field == 0 ? C.u : field == 1 ? C.v : field == 2 ? C.w : C.phic;
+        grad[0] = field == 0 ? C.gu : field == 1 ? C.gv : field == 2 ? C.gw : C.gpc;
+    }
+    double pe[NF], g[NF][3];
+#pragma unroll
+    for (int q = 0; q < NF; q++) { pe[q] = phi[q][i]; g[q][0] = g[q][1] = g[q][2] = 0.0; }
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= W) break;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb < 0) break;
+        const double G0 = C.hf_G[(0 * W + k) * ne + i], G1 = C.hf_G[(1 * W + k) * ne + i], G2 = C.hf_G[(2 * W + k) * ne + i];
+#pragma unroll
+        for (int q = 0; q < NF; q++) {
+            const double dphi = phi[q][nb] - pe[q];
+            g[q][0] += G0 * dphi; g[q][1] += G1 * dphi; g[q][2] += G2 * dphi;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NF; q++) { grad[q][3 * i] = g[q][0]; grad[q][3 * i + 1] = g[q][1]; grad[q][3 * i + 2] = g[q][2]; }
+}
+
+// ---------------------------------------------------------------------------
+// calc_mip, mod_uvwp.f90:438-490.  One thread per face; boundary faces keep
+// the value their BC set.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int rc) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= C.ne) return;
+    const double *g = C.fgeo;
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
+    const double A0 = g[FG_AX * nf + i], A1 = g[FG_AY * nf + i], A2 = g[FG_AZ * nf + i];
+    const double vx = omw * C.u[o] + wt * C.u[n], vy = omw * C.v[o] + wt * C.v[n], vz = omw * C.w[o] + wt * C.w[n];
+    const double rhoip = C.rho[o] * omw + C.rho[n] * wt;
+    double mip = (vx * A0 + vy * A1 + vz * A2) * rhoip;
+    if (rc) {
+        const double D0 = g[FG_DRX * nf + i], D1 = g[FG_DRY * nf + i], D2 = g[FG_DRZ * nf + i];
+        const double gx = omw * C.gp[3 * o] + wt * C.gp[3 * n];
+        const double gy = omw * C.gp[3 * o + 1] + wt * C.gp[3 * n + 1];
+        const double gz = omw * C.gp[3 * o + 2] + wt * C.gp[3 * n + 2];
+        const double dip = omw * C.d[o] + wt * C.d[n];
+        const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
+        const double rdip = rhoip * dip;
+        mip = mip - rdip * g[FG_ADN * nf + i] * ((C.p[n] - C.p[o]) - (gx * D0 + gy * D1 + gz * D2))
+                  - rhoip / C.dt * dip * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
+    }
+    C.mip[i] = mip;
+}
+
+// ---------------------------------------------------------------------------
+// calc_coef_p, mod_uvwp.f90:289-368: face coefficient
+// rho_ip * dc_ip * area/(dr.n), symmetric, then per cell ap = sum anb and
+// b = net inflow - boundary mass flux.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= C.ne) { C.fdiff[i] = 0.0; return; }
+    const double wt = C.fgeo[FG_WT * nf + i], omw = 1.0 - wt;
+    const double rhoip = omw * C.rho[o] + wt * C.rho[n];
+    C.fdiff[i] = (omw * C.dc[o] + wt * C.dc[n]) * rhoip * C.fgeo[FG_ADN * nf + i];
+}
+
+__global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, W = C.W;
+    double ap = 0.0, sumf = 0.0;
+    int bslot[kMaxW], nb_cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= W) continue;
+        const int nb = C.hf_nb[k * ne + i];
+        double a = 0.0;
+        if (nb >= ne) bslot[nb_cnt++] = k;
+        else if (nb >= 0) {
+            const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
+            const double sg = fc >= 0 ? 1.0 : -1.0;
+            sumf += -sg * C.mip[f];
+            a = C.fdiff[f];
+            ap += a;
+        }
+        C.anb[k * ne + i] = a;
+    }
+    for (int q = 1; q < nb_cnt; q++) {
+        int s = bslot[q], j = q - 1;
+        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
+        bslot[j + 1] = s;
+    }
+    for (int q = 0; q < nb_cnt; q++) {
+        const int k = bslot[q];
+        if (C.h_kind[C.hf_nb[k * ne + i] - ne] == 0) continue;
+        sumf = sumf - C.mip[face_of(C.hf_fc[k * ne + i])];
+    }
+    C.ap[i] = ap;
+    C.b[i] = sumf;
+}
+
+// ---------------------------------------------------------------------------
+// adjust_pc, mod_uvwp.f90:136-158: pc -= pc(1); halo pc = owner pc.
+// ---------------------------------------------------------------------------
+__global__ void k_save_pref(const CaseDev *__restrict__ cases, int ncases) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncases) cases[c].sc->pref = cases[c].phic[0];
+}
+
+__global__ void __launch_bounds__(kTile) k_adjust_pc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, W = C.W;
+    const double v = C.phic[i] - C.sc->pref;
+    C.phic[i] = v;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= W) break;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb >= ne) C.phic[nb] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// update_uvwp, mod_uvwp.f90:370-436: p += alpha_p*pc, gp += alpha_p*gpc on
+// cells; mip -= rho_ip*A*dc_ip*(pc_nb-pc_P)/(dr.n) on interior faces.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_update_cells(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const double a = C.alpha_p;
+    if (a == 1.0) {
+        C.p[i] = C.p[i] + C.phic[i];
+#pragma unroll
+        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = C.gp[3 * i + q] + C.gpc[3 * i + q];
+    } else {
+        C.p[i] = C.p[i] + a * C.phic[i];
+#pragma unroll
+        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = C.gp[3 * i + q] + a * C.gpc[3 * i + q];
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_update_faces(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= C.ne) return;
+    const double wt = C.fgeo[FG_WT * nf + i], omw = 1.0 - wt;
+    const double dip = omw * C.dc[o] + wt * C.dc[n];
+    const double rhoip = (C.rho[o] + C.rho[n]) / 2.0;
+    C.mip[i] = C.mip[i] - rhoip * C.fgeo[FG_ADN * nf + i] * dip * (C.phic[n] - C.phic[o]);
+}
+
+// update_time, mod_physics.f90:101-112
+__global__ void __launch_bounds__(kTile) k_update_time(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i < t.last) { C.u0[i] = C.u[i]; C.v0[i] = C.v[i]; C.w0[i] = C.w[i]; }
+}
+__global__ void __launch_bounds__(kTile) k_update_time_halo(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(halos)
+    if (i < t.last) { const int h = C.ne + i; C.u0[h] = C.u[h]; C.v0[h] = C.v[h]; C.w0[h] = C.w[h]; }
+}
+__global__ void __launch_bounds__(kTile) k_copy_mip0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i < t.last) C.mip0[i] = C.mip[i];
+}
+
+}  // namespace
+
+#define LAUNCH(kern, WL, ...)                                                                   \
+    do {                                                                                        \
+        if (ctx->WL.ntiles > 0) {                                                               \
+            kern<<<ctx->WL.ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__); \
+            ctx->launches++;                                                                    \
+        }                                                                                       \
+    } while (0)
+
+void launch_bc(cfdl_ctx *ctx) { LAUNCH(k_bc, halos); }
+void launch_coef_uvw(cfdl_ctx *ctx) {
+    LAUNCH(k_coef_uvw_face, faces);
+    LAUNCH(k_coef_uvw_cell, cells);
+}
+void launch_grad(cfdl_ctx *ctx, int field) {
+    if (field == 4) LAUNCH(k_grad<3>, cells, 0);
+    else LAUNCH(k_grad<1>, cells, field);
+}
+void launch_calc_mip(cfdl_ctx *ctx, int rc) { LAUNCH(k_calc_mip, faces, rc); }
+void launch_coef_p(cfdl_ctx *ctx) {
+    LAUNCH(k_coef_p_face, faces);
+    LAUNCH(k_coef_p_cell, cells);
+}
+void launch_adjust_pc(cfdl_ctx *ctx) {
+    int n = (int)ctx->cases.size();
+    if (n == 0) return;
+    k_save_pref<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_cases, n);
+    ctx->launches++;
+    LAUNCH(k_adjust_pc, cells);
+}
+void launch_update_uvwp(cfdl_ctx *ctx) {
+    LAUNCH(k_update_cells, cells);
+    LAUNCH(k_update_faces, faces);
+}
+void launch_update_time(cfdl_ctx *ctx) {
+    LAUNCH(k_update_time, cells);
+    LAUNCH(k_update_time_halo, halos);
+    LAUNCH(k_copy_mip0, faces);
+}
+void launch_set_mip0(cfdl_ctx *ctx) { LAUNCH(k_copy_mip0, faces); }
+
+}  // namespace cfdl

@@ -1,0 +1,448 @@
+// cfdl_solvers.cu -- inner linear solves of solve_uvwp on the device (FP64).
+//
+// The reference solves each momentum component with symmetric Gauss-Seidel
+// (solve_gs, src/modules/mod_solver.f90:255-327) and the pressure correction
+// with 4-block Jacobi / SSOR sweeps (multi_subdomain_solver,
+// mod_solver.f90:124-189), both stopping at a 10x residual drop or nit sweeps.
+// Lexicographic Gauss-Seidel is sequential, so here:
+//   momentum  Jacobi-preconditioned BiCGStab on the three components at once
+//             (one matrix, three right-hand sides, independent scalars);
+//   pressure  Jacobi-preconditioned CG on the singular Neumann system with
+//             its right-hand side projected to zero mean (cfdl_precond.cu adds
+//             the aggregation-AMG preconditioner and cfdl_mixed.cu the mixed-
+//             precision form).
+// Stopping: solve_mode 0 stops a component when ||r||2 <= rtol*||r0||2 (the
+// reference's 10x drop with rtol = 0.1) or after nit iterations; solve_mode 1
+// (tight, parity) stops at ||r||2 <= tight_rtol*||b||2.
+//
+// All scalars live on the device.  Each reduction writes one partial per tile;
+// the last tile of a case to finish sums them in tile order and updates that
+// case's scalars, so the iteration never waits for the host.  A component
+// that has converged is frozen (its kernels return at once), so polling the
+// flags every few iterations gives the same result as checking every one.
+#include "cfdl_device.cuh"
+#include <algorithm>
+
+namespace cfdl {
+namespace {
+
+enum { CNT_M1 = 0, CNT_M2, CNT_M3, CNT_M4, CNT_M5, CNT_P0, CNT_P1, CNT_P2, CNT_P3 };
+
+__device__ __forceinline__ double *comp_field(const CaseDev &C, int q) { return q == 0 ? C.u : q == 1 ? C.v : C.w; }
+__device__ __forceinline__ const double *comp_rhs(const CaseDev &C, int q) { return q == 0 ? C.bu : q == 1 ? C.bv : C.bw; }
+
+// (A x)_i for the interior operator: ap_i x_i - sum_{interior nb} anb x_nb
+__device__ __forceinline__ double amul_row(const CaseDev &C, const double *x, int i) {
+    const int ne = C.ne;
+    double s = C.ap[i] * x[i];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= C.W) break;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb < 0) break;
+        if (nb < ne) s -= C.anb[k * ne + i] * x[nb];
+    }
+    return s;
+}
+
+__device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->active[0] | S->active[1] | S->active[2]) != 0; }
+
+#define TILE_HEAD                                             \
+    const Tile t = tiles[blockIdx.x];                         \
+    const CaseDev &C = cases[t.c];                            \
+    SolveScalars *S = C.sc;                                   \
+    const int i = t.first + (int)threadIdx.x, ne = C.ne;      \
+    const bool in = i < t.last;                               \
+    (void)ne; (void)in;
+
+// ------------------------------ momentum ----------------------------------
+// init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0
+__global__ void __launch_bounds__(kTile) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    if (in) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const double *phi = comp_field(C, q);
+            double bb = comp_rhs(C, q)[i];
+            double s = C.ap[i] * phi[i];
+#pragma unroll
+            for (int k = 0; k < kMaxW; k++) {
+                if (k >= C.W) break;
+                const int nb = C.hf_nb[k * ne + i];
+                if (nb < 0) break;
+                const double a = C.anb[k * ne + i];
+                if (nb >= ne) bb += a * phi[nb];
+                else s -= a * phi[nb];
+            }
+            const double r = bb - s;
+            C.kb[q * ne + i] = bb;
+            C.kr[q * ne + i] = r;
+            C.krh[q * ne + i] = r;
+            C.kp[q * ne + i] = 0.0;
+            C.kv[q * ne + i] = 0.0;
+            v[q] = bb * bb;
+            v[3 + q] = r * r;
+        }
+    }
+    block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M1], cnt[t.c])) {
+        __shared__ double s[6];
+        sum_partials<6>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            for (int q = 0; q < 3; q++) {
+                S->bnorm[q] = sqrt(s[q]);
+                S->r0norm[q] = S->rnorm[q] = sqrt(s[3 + q]);
+                S->rho[q] = s[3 + q];
+                S->alpha[q] = 1.0; S->omega[q] = 1.0; S->beta[q] = 0.0; S->half[q] = 0;
+                S->iters[q] = 0; S->status[q] = 0;
+                S->tol[q] = C.solve_mode == 0 ? C.rtol_u * S->r0norm[q] : C.tight_rtol * S->bnorm[q];
+                S->active[q] = (S->r0norm[q] > S->tol[q]) && cap > 0;
+                if (!isfinite(S->r0norm[q]) || !isfinite(S->bnorm[q])) { S->active[q] = 0; S->status[q] = CFDL_ERR_NONFINITE; }
+            }
+        }
+    }
+}
+
+// p = r + beta (p - omega v); ph = p / ap
+__global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_HEAD
+    if (!any_active(S) || !in) return;
+    const double rap = 1.0 / C.ap[i];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        if (!S->active[q]) continue;
+        const int j = q * ne + i;
+        const double pn = S->iters[q] == 0 ? C.kr[j] : C.kr[j] + S->beta[q] * (C.kp[j] - S->omega[q] * C.kv[j]);
+        C.kp[j] = pn;
+        C.kph[j] = pn * rap;
+    }
+}
+
+// v = A ph; alpha = rho / (rh, v)
+__global__ void __launch_bounds__(kTile) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!any_active(S)) return;
+    double v[3] = {0, 0, 0};
+    if (in) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (!S->active[q]) continue;
+            const double y = amul_row(C, C.kph + q * ne, i);
+            C.kv[q * ne + i] = y;
+            v[q] = C.krh[q * ne + i] * y;
+        }
+    }
+    block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M2], cnt[t.c])) {
+        __shared__ double s[3];
+        sum_partials<3>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < 3; q++) {
+                if (!S->active[q]) continue;
+                const double a = S->rho[q] / s[q];
+                if (s[q] == 0.0 || !isfinite(a)) { S->active[q] = 0; S->status[q] = isfinite(a) || s[q] == 0.0 ? S->status[q] : CFDL_ERR_NONFINITE; continue; }
+                S->alpha[q] = a;
+            }
+    }
+}
+
+// s = r - alpha v; sh = s / ap; early exit when ||s|| <= tol
+__global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!any_active(S)) return;
+    double v[3] = {0, 0, 0};
+    if (in) {
+        const double rap = 1.0 / C.ap[i];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (!S->active[q]) continue;
+            const int j = q * ne + i;
+            const double sv = C.kr[j] - S->alpha[q] * C.kv[j];
+            C.ks[j] = sv;
+            C.ksh[j] = sv * rap;
+            v[q] = sv * sv;
+        }
+    }
+    block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M3], cnt[t.c])) {
+        __shared__ double s[3];
+        sum_partials<3>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < 3; q++) {
+                if (!S->active[q]) continue;
+                S->half[q] = sqrt(s[q]) <= S->tol[q];
+            }
+    }
+}
+
+// t = A sh; omega = (t,s)/(t,t)
+__global__ void __launch_bounds__(kTile) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!any_active(S)) return;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    if (in) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (!S->active[q] || S->half[q]) continue;
+            const int j = q * ne + i;
+            const double y = amul_row(C, C.ksh + q * ne, i);
+            C.kt[j] = y;
+            v[q] = y * C.ks[j];
+            v[3 + q] = y * y;
+        }
+    }
+    block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M4], cnt[t.c])) {
+        __shared__ double s[6];
+        sum_partials<6>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0)
+            for (int q = 0; q < 3; q++) {
+                if (!S->active[q]) continue;
+                S->omega[q] = S->half[q] ? 0.0 : (s[3 + q] > 0.0 ? s[q] / s[3 + q] : 0.0);
+            }
+    }
+}
+
+// x += alpha ph + omega sh; r = s - omega t; rho' = (rh, r); beta
+__global__ void __launch_bounds__(kTile) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!any_active(S)) return;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    if (in) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (!S->active[q]) continue;
+            const int j = q * ne + i;
+            double *x = comp_field(C, q);
+            const double om = S->omega[q];
+            x[i] = x[i] + S->alpha[q] * C.kph[j] + om * C.ksh[j];
+            const double r = om == 0.0 ? C.ks[j] : C.ks[j] - om * C.kt[j];
+            C.kr[j] = r;
+            v[q] = r * r;
+            v[3 + q] = C.krh[j] * r;
+        }
+    }
+    block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M5], cnt[t.c])) {
+        __shared__ double s[6];
+        sum_partials<6>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            for (int q = 0; q < 3; q++) {
+                if (!S->active[q]) continue;
+                const double rn = sqrt(s[q]), rho_new = s[3 + q];
+                S->rnorm[q] = rn;
+                S->iters[q] += 1;
+                const double om = S->omega[q];
+                S->beta[q] = (om != 0.0 && S->rho[q] != 0.0) ? (rho_new / S->rho[q]) * (S->alpha[q] / om) : 0.0;
+                S->rho[q] = rho_new;
+                int act = rn > S->tol[q];
+                if (!isfinite(rn)) { act = 0; S->status[q] = CFDL_ERR_NONFINITE; }
+                else if (act && (om == 0.0 || rho_new == 0.0)) act = 0;           // breakdown: stop here
+                else if (act && S->iters[q] >= cap) { act = 0; if (C.solve_mode == 1) S->status[q] = CFDL_ERR_ITER_CAP; }
+                S->active[q] = act;
+            }
+        }
+    }
+}
+
+// ------------------------------ pressure ----------------------------------
+// mean of b (the singular Neumann system is made consistent)
+__global__ void __launch_bounds__(kTile) k_pc_mean(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    double v[1] = {in ? C.b[i] : 0.0};
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_P0], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) S->mean_b = s[0] / ne;
+    }
+}
+
+// r = b - mean, z = r/ap, p = z, x = 0 (set_a_0(phic))
+__global__ void __launch_bounds__(kTile) k_pc_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    double v[3] = {0, 0, 0};
+    if (in) {
+        const double r = C.b[i] - S->mean_b, z = r / C.ap[i];
+        C.kr[i] = r; C.ks[i] = z; C.kp[i] = z; C.phic[i] = 0.0;
+        v[0] = r * r; v[1] = r * z; v[2] = C.b[i] * C.b[i];
+    }
+    block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_P1], cnt[t.c])) {
+        __shared__ double s[3];
+        sum_partials<3>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            S->r0norm_p = S->rnorm_p = sqrt(s[0]);
+            S->rz = s[1];
+            S->mass_imbalance = sqrt(s[2]);
+            S->iters_p = 0; S->status_p = 0;
+            S->tol_p = (C.solve_mode == 0 ? C.rtol_p : C.tight_rtol) * S->r0norm_p;
+            S->active_p = S->r0norm_p > S->tol_p && cap > 0;
+            if (!isfinite(S->r0norm_p)) { S->active_p = 0; S->status_p = CFDL_ERR_NONFINITE; }
+        }
+    }
+}
+
+// q = A p; alpha = rz / (p, q)
+__global__ void __launch_bounds__(kTile) k_pc_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!S->active_p) return;
+    double v[1] = {0};
+    if (in) {
+        const double q = amul_row(C, C.kp, i);
+        C.kv[i] = q;
+        v[0] = C.kp[i] * q;
+    }
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_P2], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            if (!(s[0] > 0.0) || !isfinite(s[0])) { S->active_p = 0; if (!isfinite(s[0])) S->status_p = CFDL_ERR_NONFINITE; }
+            else S->alpha_p = S->rz / s[0];
+        }
+    }
+}
+
+// x += alpha p; r -= alpha q; z = r/ap; beta = (r,z)'/(r,z)
+__global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    if (!S->active_p) return;
+    double v[2] = {0, 0};
+    if (in) {
+        const double a = S->alpha_p;
+        C.phic[i] = C.phic[i] + a * C.kp[i];
+        const double r = C.kr[i] - a * C.kv[i], z = r / C.ap[i];
+        C.kr[i] = r; C.ks[i] = z;
+        v[0] = r * r; v[1] = r * z;
+    }
+    block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_P3], cnt[t.c])) {
+        __shared__ double s[2];
+        sum_partials<2>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            const double rn = sqrt(s[0]);
+            S->rnorm_p = rn;
+            S->iters_p += 1;
+            S->beta_p = S->rz != 0.0 ? s[1] / S->rz : 0.0;
+            S->rz = s[1];
+            int act = rn > S->tol_p;
+            if (!isfinite(rn)) { act = 0; S->status_p = CFDL_ERR_NONFINITE; }
+            else if (act && S->iters_p >= cap) { act = 0; if (C.solve_mode == 1) S->status_p = CFDL_ERR_ITER_CAP; }
+            S->active_p = act;
+        }
+    }
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kTile) k_pc_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_HEAD
+    if (!S->active_p || !in) return;
+    C.kp[i] = C.ks[i] + S->beta_p * C.kp[i];
+}
+
+// per-case activity flags for the host poll: bit0 momentum, bit1 pressure
+__global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncases) return;
+    const SolveScalars *S = cases[c].sc;
+    flags[c] = (any_active(S) ? 1 : 0) | (S->active_p ? 2 : 0);
+}
+
+}  // namespace
+
+#define SLAUNCH(kern, WL, ...)                                                                           \
+    do {                                                                                                 \
+        kern<<<ctx->WL.ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__);   \
+        ctx->launches++;                                                                                 \
+    } while (0)
+#define RED ctx->cells.d_case_first, ctx->cells.d_case_ntiles, ctx->d_partials
+
+static int poll(cfdl_ctx *ctx, int mask) {
+    const int n = (int)ctx->cases.size();
+    k_poll<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_cases, n, ctx->d_flags);
+    ctx->launches++;
+    cudaError_t e = cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return -1;
+    for (int c = 0; c < n; c++) if (ctx->h_flags[c] & mask) return 1;
+    return 0;
+}
+
+static int max_cap(cfdl_ctx *ctx) {
+    int cap = 0;
+    for (auto *hc : ctx->cases) cap = std::max(cap, hc->cfg.solve_mode == 0 ? hc->cfg.nit : hc->cfg.tight_maxit);
+    return cap;
+}
+
+int solve_momentum(cfdl_ctx *ctx) {
+    if (ctx->cells.ntiles == 0) return CFDL_OK;
+    SLAUNCH(k_mom_init, cells, RED);
+    const int cap = max_cap(ctx);
+    int it = 0, chunk = 2;
+    while (it < cap) {
+        for (int k = 0; k < chunk && it < cap; k++, it++) {
+            SLAUNCH(k_mom_p, cells);
+            SLAUNCH(k_mom_v, cells, RED);
+            SLAUNCH(k_mom_s, cells, RED);
+            SLAUNCH(k_mom_t, cells, RED);
+            SLAUNCH(k_mom_x, cells, RED);
+        }
+        int a = poll(ctx, 1);
+        if (a < 0) return CFDL_ERR_CUDA;
+        if (a == 0) break;
+        chunk = std::min(chunk * 2, 16);
+    }
+    return cuda_status(cudaGetLastError());
+}
+
+int solve_pressure(cfdl_ctx *ctx) {
+    if (ctx->cells.ntiles == 0) return CFDL_OK;
+    SLAUNCH(k_pc_mean, cells, RED);
+    SLAUNCH(k_pc_init, cells, RED);
+    const int cap = max_cap(ctx);
+    int it = 0, chunk = 4;
+    while (it < cap) {
+        for (int k = 0; k < chunk && it < cap; k++, it++) {
+            SLAUNCH(k_pc_q, cells, RED);
+            SLAUNCH(k_pc_x, cells, RED);
+            SLAUNCH(k_pc_p, cells);
+        }
+        int a = poll(ctx, 2);
+        if (a < 0) return CFDL_ERR_CUDA;
+        if (a == 0) break;
+        chunk = std::min(chunk * 2, 64);
+    }
+    return cuda_status(cudaGetLastError());
+}
+
+int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st) {
+    SolveScalars S;
+    cudaError_t e = cudaMemcpyAsync(&S, ctx->cases[c]->dev.sc, sizeof(S), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    st->it_u = S.iters[0]; st->it_v = S.iters[1]; st->it_w = S.iters[2]; st->it_p = S.iters_p;
+    for (int q = 0; q < 3; q++) { st->res_i[q] = S.r0norm[q]; st->res_f[q] = S.rnorm[q]; }
+    st->res_i[3] = S.r0norm_p; st->res_f[3] = S.rnorm_p;
+    st->mass_imbalance = S.mass_imbalance;
+    st->status = 0;
+    for (int q = 0; q < 3; q++) if (S.status[q]) st->status = S.status[q];
+    if (S.status_p) st->status = S.status_p;
+    return CFDL_OK;
+}
+
+}  // namespace cfdl

@@ -1,0 +1,183 @@
+/*
+ * cfdl.h -- C-ABI of libcfdgpu, the GB300 (sm_103a) implementation of the
+ * CFD-Lite SIMPLE outer iteration (solve_uvwp and its callees).
+ *
+ * The boundary mirrors the reference's Fortran interfaces.  Arrays use the
+ * reference layouts (1-based index values, Fortran column order, xyz
+ * interleaving), real = double, integer = int32, and every array is passed as
+ * a plain pointer to its first element, like the reference's existing
+ * bind(C) crossings (src/VTK/mod_vtk.f90:4-29).  The caller keeps ownership
+ * of all host arrays.  Every entry point returns a status code (CFDL_OK = 0).
+ *
+ * Threading: one CUDA stream per context; a context is not thread-safe;
+ * different contexts may be used from different threads.
+ */
+#ifndef CFDL_H
+#define CFDL_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CFDL_OK             0
+#define CFDL_ERR_INVALID    1   /* bad argument or size                     */
+#define CFDL_ERR_OOM        2   /* device or host allocation failed         */
+#define CFDL_ERR_NONFINITE  3   /* NaN/Inf detected in a solve              */
+#define CFDL_ERR_ITER_CAP   4   /* inner solve hit its iteration cap (tight) */
+#define CFDL_ERR_CUDA       5   /* CUDA runtime error                        */
+#define CFDL_ERR_MESH       6   /* connectivity could not be built           */
+#define CFDL_ERR_NO_DEVICE  7   /* no CUDA device                            */
+#define CFDL_ERR_NAME       8   /* unknown array name                        */
+
+/* CGNS element type codes (src/modules/mod_util.f90:18-39) */
+#define CFDL_TRI_3    5
+#define CFDL_QUAD_4   7
+#define CFDL_TETRA_4 10
+#define CFDL_HEXA_8  17
+
+/* Boundary condition kinds, the procedures the reference binds per section
+ * in construct_uvwp (src/equations/mod_uvwp.f90:73-78, 493-570). */
+#define CFDL_BC_WALL      1   /* dirichlet0 / lid: halo velocity = wall velocity, bc_type 'dirichlet' */
+#define CFDL_BC_SYMMETRY  2   /* symmetry: reflected velocity, bc_type 'zero_flux' */
+
+/* ======================================================================
+ * 1. Synthetic CGNS-shaped zone (the input the reference reads with
+ *    cell_input, src/setup/cell_input.f90:36-99).  Unit cube, n^3 hexes
+ *    (HEXA_8) or 6 Kuhn tets per hex (TETRA_4); sections: volume, then
+ *    bottom, top, south, north, west, east (QUAD_4 / TRI_3).  Interior
+ *    vertices are jittered by U(-jitter,jitter)*h per coordinate, drawn from
+ *    SplitMix64(seed) in vertex order.  names: nsec blocks of 33 chars.
+ * ====================================================================== */
+int cfdl_box_zone_sizes(int n, int tet, int *nvx, int *nelem, int *nsec, int *ne2vxmax);
+int cfdl_box_zone_fill(int n, int tet, double jitter, uint64_t seed,
+                       double *x, double *y, double *z, int *e2vx,
+                       int *etype, int *esec, char *names);
+
+/* ======================================================================
+ * 2. Mesh set-up: the connectivity and geometry arrays that the reference's
+ *    cell_input builds (find_element_nb, calc_aip_xyzip_uns,
+ *    calc_vol_cv_centers_uns; src/setup/mod_mg_lvl_uns.f90:283-488,
+ *    src/setup/calc_aip_xyzip.f90:7-74, src/setup/calc_vol_cv_centers.f90:4-61),
+ *    with the same face numbering, orientation and ordering.  A Fortran host
+ *    that already ran cell_input skips this and fills cfdl_mesh from geom.
+ * ====================================================================== */
+typedef struct cfdl_setup cfdl_setup;
+
+typedef struct cfdl_mesh {
+    int ne, nf, nbf;             /* cells, faces, boundary faces (= halos)   */
+    const int *ef2nb1;           /* [2nf-nbf] geom%ef2nb(:,1): enb<<5|lfnb    */
+    const int *ef2nb2;           /* [2nf-nbf] geom%ef2nb(:,2): +-fg           */
+    const int *ef2nb_idx;        /* [ne+1]    geom%ef2nb_idx                  */
+    const int *s2g;              /* [nf]      fine_lvl%s2g: owner<<5|lf       */
+    const int *bs;               /* [nbf]     fine_lvl%bs(ne+1:ne+nbf)        */
+    const double *aip, *rip;     /* [3nf]                                     */
+    const double *xc, *yc, *zc;  /* [ne+nbf]                                  */
+    const double *vol;           /* [ne]                                      */
+    int nbc;                     /* boundary conditions, eqn%bcs order        */
+    const int *bc_esec;          /* [2nbc] halo element range of each bc      */
+    const int *bc_kind;          /* [nbc]  CFDL_BC_*                          */
+    const double *bc_vel;        /* [3nbc] wall velocity (lid: (U,0,0))       */
+} cfdl_mesh;
+
+int cfdl_setup_create(int nvx, const double *x, const double *y, const double *z,
+                      int nsec, const char *names, const int *etype, const int *esec,
+                      int ne2vxmax, const int *e2vx, cfdl_setup **out);
+/* sizes[0..4] = ne, nf, nbf, nsec, nred */
+int cfdl_setup_sizes(const cfdl_setup *s, int *sizes);
+/* Fill a cfdl_mesh whose pointers stay valid until cfdl_setup_destroy.
+ * Boundary conditions are bound by section name as construct_uvwp does:
+ * 'top' -> moving wall (u_lid,0,0), every other 2D section -> wall at rest. */
+int cfdl_setup_mesh(const cfdl_setup *s, double u_lid, cfdl_mesh *mesh);
+/* Copy out named integer arrays: ef2nb1, ef2nb2, ef2nb_idx, s2g, bs, esec,
+ * etype, red (calc_redblack order, src/setup/mod_meshds_uns.f90:134-204). */
+int cfdl_setup_get_int(const cfdl_setup *s, const char *name, int *out);
+/* Copy out named real arrays: aip, rip (3nf), xc, yc, zc (ne+nbf), vol (ne). */
+int cfdl_setup_get_dbl(const cfdl_setup *s, const char *name, double *out);
+int cfdl_setup_destroy(cfdl_setup *s);
+
+/* ======================================================================
+ * 3. Device context: mesh and fields resident in HBM.
+ * ====================================================================== */
+typedef struct cfdl_ctx cfdl_ctx;
+
+typedef struct cfdl_config {
+    double rho, mu;        /* properties (reference: 5, 0.01; mod_properties.f90:86-87) */
+    double dt;             /* time step (reference 0.01; INFINITY = steady)             */
+    double alpha_u;        /* momentum under-relaxation (1 = none, as the reference)    */
+    double alpha_p;        /* pressure under-relaxation (1 = none)                      */
+    int    nit;            /* inner iteration cap (reference phys%nit = 100)            */
+    int    solve_mode;     /* 0: stop each inner solve at a residual drop of rtol_*;
+                              1: tight, ||r||2 <= tight_rtol*||b||2 (parity mode)        */
+    double rtol_u, rtol_p; /* mode 0 residual drop (reference: 0.1)                      */
+    double tight_rtol;     /* mode 1 tolerance                                           */
+    int    tight_maxit;    /* mode 1 iteration cap                                       */
+    int    precision;      /* 0: FP64 throughout; 1: mixed pressure solve (FP32 SpMV,
+                              preconditioner and inner CG, FP64 residual/refinement)    */
+    int    precond;        /* pressure preconditioner: 0 Jacobi, 1 aggregation AMG      */
+} cfdl_config;
+
+typedef struct cfdl_stats {
+    int    it_u, it_v, it_w, it_p;   /* inner iterations of the last solve_uvwp       */
+    double res_i[4], res_f[4];       /* initial/final residual 2-norms (u,v,w,pc)     */
+    double mass_imbalance;           /* ||b||2 of calc_coef_p (net inflow per cell)   */
+    int    status;
+} cfdl_stats;
+
+/* Fields in reference layout (host pointers; NULL members are skipped). */
+typedef struct cfdl_fields {
+    double *u, *v, *w, *p;           /* [ne+nbf]      */
+    double *u0, *v0, *w0;            /* [ne+nbf]      */
+    double *gu, *gv, *gw, *gp, *gpc; /* [3(ne+nbf)]   */
+    double *mip, *mip0;              /* [nf]          */
+} cfdl_fields;
+
+void cfdl_config_default(cfdl_config *cfg);
+/* construct_physics + construct_uvwp (mod_physics.f90:52-75, mod_uvwp.f90:20-84):
+ * upload the mesh, zero the fields, set rho/mu, bind BCs, mip = calc_mip(.false.),
+ * mip0 = mip. */
+int cfdl_ctx_create(const cfdl_mesh *mesh, const cfdl_config *cfg, cfdl_ctx **out);
+int cfdl_set_config(cfdl_ctx *ctx, const cfdl_config *cfg);
+int cfdl_upload_fields(cfdl_ctx *ctx, const cfdl_fields *f);
+int cfdl_download_fields(cfdl_ctx *ctx, cfdl_fields *f);
+int cfdl_ctx_destroy(cfdl_ctx *ctx);
+
+/* ---- the hot path (device-resident state) ---- */
+int cfdl_update_boundaries(cfdl_ctx *ctx);               /* mod_physics.f90:38-50  */
+int cfdl_solve_uvwp(cfdl_ctx *ctx, cfdl_stats *st);      /* mod_uvwp.f90:95-134    */
+int cfdl_update_time(cfdl_ctx *ctx);                     /* mod_physics.f90:101-112 */
+/* n_outer iterations of main.f90:50-63 (update_boundaries + solve_uvwp,
+ * update_time after every ncoef of them). */
+int cfdl_step(cfdl_ctx *ctx, int n_outer, int ncoef, cfdl_stats *st);
+
+/* Drop-in for the Fortran solve_uvwp with host arrays: uploads the fields
+ * solve_uvwp reads, runs it, downloads what it writes. */
+int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *st);
+
+/* ---- individual routines, for per-routine replacement and parity ---- */
+int cfdl_calc_coef_uvw(cfdl_ctx *ctx);                   /* mod_uvwp.f90:161-286   */
+int cfdl_solve_momentum(cfdl_ctx *ctx, cfdl_stats *st);  /* mod_uvwp.f90:114-116 (solve_gs x3) */
+/* field: 0 u, 1 v, 2 w, 3 phic; gradient into gu/gv/gw/gpc (mod_solver.f90:40-81) */
+int cfdl_calc_grad(cfdl_ctx *ctx, int field);
+int cfdl_calc_mip(cfdl_ctx *ctx, int rhie_chow);         /* mod_uvwp.f90:438-490   */
+int cfdl_calc_coef_p(cfdl_ctx *ctx);                     /* mod_uvwp.f90:289-368   */
+int cfdl_solve_pc(cfdl_ctx *ctx, cfdl_stats *st);        /* mod_uvwp.f90:126-127 + mod_solver.f90:329-344 */
+int cfdl_adjust_pc(cfdl_ctx *ctx);                       /* mod_uvwp.f90:136-158   */
+int cfdl_update_uvwp(cfdl_ctx *ctx);                     /* mod_uvwp.f90:370-436   */
+
+/* Copy a named device array to/from a host buffer in reference layout.
+ * Names: u v w p u0 v0 w0 phic (ne+nbf), gu gv gw gp gpc (3(ne+nbf)),
+ * mip mip0 (nf), ap b bu bv bw d dc rho mu (ne), anb (2nf-nbf). */
+int cfdl_get_array(cfdl_ctx *ctx, const char *name, double *host);
+int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host);
+
+/* Number of kernel launches issued by this context since creation. */
+int64_t cfdl_launch_count(const cfdl_ctx *ctx);
+/* Human-readable text for a status code. */
+const char *cfdl_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,198 @@
+"""GPU parity: libcfdgpu (through its C-ABI) against the CPU oracle.
+
+Per routine, both sides start from the same seeded state and the outputs are
+compared with tolerance RTOL_KERNEL relative to each array's scale: the GPU
+computes every face term once per face from precomputed geometry, so values
+differ from the reference's per-half-face arithmetic by a few roundings.
+End to end, both sides run in the tight mode (every inner solve to
+||r|| <= 1e-13 ||b||) and the u, v, w, p fields must agree within 1e-9
+relative L2 after the same number of outer iterations (the target the
+reference comparison is stated in).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cfdl
+import oracle_lib
+
+pytestmark = pytest.mark.gpu
+
+RTOL_KERNEL = 1e-12      # per routine, max-norm relative to the array scale
+RTOL_FIELD = 1e-9        # end to end, relative L2 after the same iteration count
+
+
+def rel_max(a, b):
+    s = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / s
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make_pair(n=6, tet=False, jit=0.2, seed=7, gpu_cfg=None, or_cfg=None):
+    z = cfdl.Zone(n, tet, jit, seed=seed)
+    s = cfdl.Setup(z)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(or_cfg)
+    g = cfdl.Solver(s, gpu_cfg)
+    return z, s, o, g
+
+
+def tight_pair(n=6, tet=False, jit=0.2, steady=True, **kw):
+    if steady:
+        gc = cfdl.steady(solve_mode=1, tight_rtol=1e-13, **kw)
+        oc = oracle_lib.steady(mode=1, tight_rtol=1e-13)
+    else:
+        gc = cfdl.default_config(rho=5.0, solve_mode=1, tight_rtol=1e-13, **kw)
+        oc = oracle_lib.config(rho=5.0, mode=1, tight_rtol=1e-13)
+    return make_pair(n, tet, jit, gpu_cfg=gc, or_cfg=oc)
+
+
+def seed_state(o, g, rng):
+    """Same random state on both sides (reference layouts)."""
+    nc = o.ne + o.nbf
+    vals = {}
+    for f in ("u", "v", "w", "p", "u0", "v0", "w0"):
+        vals[f] = rng.standard_normal(nc)
+    for f in ("gu", "gv", "gw", "gp"):
+        vals[f] = rng.standard_normal(3 * nc)
+    vals["mip"] = 1e-3 * rng.standard_normal(o.nf)
+    vals["mip0"] = 1e-3 * rng.standard_normal(o.nf)
+    for f, v in vals.items():
+        o.set(f, v)
+        g.set(f, v)
+    return vals
+
+
+@pytest.mark.parametrize("n,tet,jit", [(6, False, 0.2), (4, True, 0.0), (3, True, 0.1)])
+def test_routines_match_oracle(need_gpu, n, tet, jit):
+    z, s, o, g = tight_pair(n, tet, jit, steady=False)
+    rng = np.random.default_rng(1234)
+    seed_state(o, g, rng)
+    # update_boundaries
+    o.update_boundaries(); g.update_boundaries()
+    for f in ("u", "v", "w", "p", "mip"):
+        assert np.array_equal(g.get(f), o.get(f)), f
+    # calc_grad (u, v, w fused and single)
+    for f in ("u", "v", "w"):
+        ref = o.calc_grad(o.get(f), o.get("g" + f))
+        o.set("g" + f, ref)
+    g.calc_grad("uvw")
+    for f in ("gu", "gv", "gw"):
+        assert rel_max(g.get(f), o.get(f)) < RTOL_KERNEL, f
+    # calc_coef_uvw
+    o.calc_coef_uvw(); g.calc_coef_uvw()
+    for f in ("ap", "anb", "bu", "bv", "bw", "d", "dc"):
+        assert rel_max(g.get(f), o.get(f)) < RTOL_KERNEL, f
+    # calc_mip with Rhie-Chow
+    o.calc_mip(True); g.calc_mip(True)
+    assert rel_max(g.get("mip"), o.get("mip")) < RTOL_KERNEL
+    # calc_coef_p
+    o.calc_coef_p(); g.calc_coef_p()
+    for f in ("ap", "anb", "b"):
+        assert rel_max(g.get(f), o.get(f)) < RTOL_KERNEL, f
+    # pressure-correction solve (tight), adjust_pc, grad(pc), update_uvwp
+    o.solve_pc(); st = g.solve_pc()
+    assert st.status == 0
+    o.adjust_pc(); g.adjust_pc()
+    assert rel_max(g.get("phic"), o.get("phic")) < 1e-9
+    pc = o.get("phic")
+    o.set("gpc", o.calc_grad(pc, o.get("gpc")))
+    g.calc_grad("pc")
+    assert rel_max(g.get("gpc"), o.get("gpc")) < 1e-9
+    o.update_uvwp(); g.update_uvwp()
+    for f in ("p", "gp", "mip"):
+        assert rel_max(g.get(f), o.get(f)) < 1e-9, f
+
+
+def test_momentum_solve_tight(need_gpu):
+    z, s, o, g = tight_pair(6, False, 0.2, steady=True)
+    rng = np.random.default_rng(5)
+    seed_state(o, g, rng)
+    o.update_boundaries(); g.update_boundaries()
+    o.calc_coef_uvw(); g.calc_coef_uvw()
+    for comp in range(3):
+        o.solve_momentum(comp)
+    st = g.solve_momentum()
+    assert st.status == 0
+    for f in ("u", "v", "w"):
+        assert rel_l2(g.get(f), o.get(f)) < 1e-11, f
+
+
+@pytest.mark.parametrize("n,tet,jit,steady,nout", [
+    (8, False, 0.2, True, 40),     # jittered hex, steady under-relaxed SIMPLE
+    (6, False, 0.0, False, 12),    # reference physics: pseudo-transient, rho=5, dt=0.01
+    (4, True, 0.0, True, 25),      # tet split
+])
+def test_end_to_end_tight_parity(need_gpu, n, tet, jit, steady, nout):
+    z, s, o, g = tight_pair(n, tet, jit, steady=steady)
+    o.run(nout, 3)
+    st = g.step(nout, 3)
+    assert st.status == 0
+    for f in ("u", "v", "w", "p"):
+        a, b = g.get(f)[:o.ne], o.get(f)[:o.ne]
+        assert rel_l2(a, b) < RTOL_FIELD, (f, rel_l2(a, b))
+
+
+def test_config1_cavity_32_tight(need_gpu):
+    """Config 1 (32^3 hex, Re=100, alpha 0.7/0.3) through 15 outer iterations."""
+    z, s, o, g = tight_pair(32, False, 0.0, steady=True)
+    o.run(15, 3)
+    g.step(15, 3)
+    for f in ("u", "v", "w", "p"):
+        assert rel_l2(g.get(f)[:o.ne], o.get(f)[:o.ne]) < RTOL_FIELD, f
+
+
+def test_default_mode_reaches_oracle_steady_state(need_gpu):
+    """The production mode (each inner solve to a 10x residual drop, as the
+    reference) converges to the same discrete steady state as the oracle."""
+    z = cfdl.Zone(6, False, 0.2, seed=7)
+    s = cfdl.Setup(z)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1))
+    o.run(300)
+    g = cfdl.Solver(s, cfdl.steady(solve_mode=0))
+    g.step(300)
+    for f in ("u", "v", "w"):
+        assert rel_l2(g.get(f)[:o.ne], o.get(f)[:o.ne]) < 1e-5, f
+
+
+def test_deterministic_and_launches_counted(need_gpu):
+    z = cfdl.Zone(10, False, 0.2, seed=9)
+    s = cfdl.Setup(z)
+    res = []
+    for _ in range(2):
+        g = cfdl.Solver(s, cfdl.steady())
+        n0 = g.launch_count()
+        g.step(5)
+        assert g.launch_count() > n0
+        res.append([g.get(f) for f in ("u", "v", "w", "p", "mip")])
+        g.close()
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
+
+
+def test_host_dropin_matches_resident(need_gpu):
+    """cfdl_solve_uvwp_host (host arrays in and out) equals the resident path."""
+    import ctypes as C
+    z = cfdl.Zone(6, False, 0.1, seed=2)
+    s = cfdl.Setup(z)
+    g1 = cfdl.Solver(s, cfdl.steady())
+    g2 = cfdl.Solver(s, cfdl.steady())
+    nc, nf = s.ne + s.nbf, s.nf
+    host = {f: np.zeros(nc) for f in ("u", "v", "w", "p", "u0", "v0", "w0")}
+    host.update({f: np.zeros(3 * nc) for f in ("gu", "gv", "gw", "gp", "gpc")})
+    host.update({"mip": g2.get("mip"), "mip0": g2.get("mip0")})
+    fl = cfdl.Fields(**{k: v.ctypes.data_as(C.c_void_p) for k, v in host.items()})
+    for _ in range(3):
+        g1.update_boundaries(); g1.solve_uvwp()
+        g2.update_boundaries()
+        g2_dl = cfdl.lib().cfdl_download_fields(g2._h, C.byref(fl))
+        assert g2_dl == 0
+        st = cfdl.Stats()
+        assert cfdl.lib().cfdl_solve_uvwp_host(g2._h, C.byref(fl), C.byref(st)) == 0
+    for f in ("u", "v", "w", "p", "mip"):
+        assert np.array_equal(g1.get(f), host[f]), f

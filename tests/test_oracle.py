@@ -1,0 +1,111 @@
+"""Self-checks of the CPU oracle: hand-derivable invariants of the reference
+discretisation and the committed golden runs (tests/golden/oracle_runs.json).
+CPU only."""
+import hashlib
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import cfdl
+import oracle_lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("n,tet,jit", [(4, False, 0.0), (5, False, 0.2), (3, True, 0.0)])
+def test_grad_exact_for_linear_fields(n, tet, jit):
+    """calc_grad is exact for linear fields, halos included: halo centres sit
+    on the boundary face centroids (calc_vol_cv_centers.f90:37-42)."""
+    z = cfdl.Zone(n, tet, jit, seed=1)
+    o = oracle_lib.Oracle(z, n_subdomains=1)
+    xc, yc, zc = o.get("xc"), o.get("yc"), o.get("zc")
+    phi = 0.3 + 1.5 * xc - 2.0 * yc + 0.7 * zc
+    g = o.calc_grad(phi).reshape(-1, 3)[:o.ne]
+    assert np.abs(g - np.array([1.5, -2.0, 0.7])).max() < 1e-10
+
+
+def _fresh(n=5, tet=False, jit=0.2, cfg=None, nsub=4):
+    z = cfdl.Zone(n, tet, jit, seed=7)
+    o = oracle_lib.Oracle(z, n_subdomains=nsub)
+    o.physics_init(cfg or oracle_lib.steady(mode=1))
+    return z, o
+
+
+def test_pressure_matrix_symmetric_rows_sum_to_zero():
+    z, o = _fresh()
+    o.run(3)
+    o.update_boundaries()
+    o.calc_coef_uvw()
+    o.calc_coef_p()
+    ap, anb, b = o.get("ap"), o.get("anb"), o.get("b")
+    ef1, ef2, idx = o.get_int("ef2nb1"), o.get_int("ef2nb2"), o.get_int("ef2nb_idx")
+    A = {}
+    for e in range(o.ne):
+        row = 0.0
+        for h in range(idx[e] - 1, idx[e + 1] - 1):
+            enb, lf = ef1[h] >> 5, ef1[h] & 31
+            row += anb[h]
+            if lf:
+                A[(e, enb - 1)] = anb[h]
+            else:
+                assert anb[h] == 0.0            # boundary d = 0 (mod_uvwp.f90:354-363)
+        assert abs(row - ap[e]) <= 1e-15 * ap[e]
+    for (i, j), a in A.items():
+        assert abs(a - A[(j, i)]) <= 1e-13 * abs(a)
+    # b = net inflow: sums to minus the boundary net flux (zero at walls)
+    assert abs(b.sum()) < 1e-14 * np.abs(o.get("mip")).sum()
+
+
+def test_golden_runs():
+    with open(os.path.join(ROOT, "tests", "golden", "oracle_runs.json")) as fh:
+        gold = json.load(fh)["cases"]
+    for key, rec in gold.items():
+        kw = dict(rec["config"])
+        if kw.get("dt") in ("inf", "Infinity"):
+            kw["dt"] = math.inf
+        z = cfdl.Zone(rec["n"], rec["tet"], rec["jitter"], seed=rec["seed"])
+        o = oracle_lib.Oracle(z, n_subdomains=4)
+        o.physics_init(oracle_lib.config(**kw))
+        st = o.run(rec["n_outer"], 3)
+        assert [st.it_u, st.it_v, st.it_w, st.it_p] == rec["iters"], key
+        for f, h in rec["hash"].items():
+            assert sha(o.get(f)) == h, (key, f)
+
+
+def test_reference_pressure_quirk_runs_full_nit():
+    """multi_subdomain_solver never resets res_f_tot (mod_solver.f90:175-178),
+    so for small residuals the 4-block pressure solve runs all nit sweeps."""
+    z, o = _fresh(cfg=oracle_lib.config(rho=5.0, mode=0))
+    o.update_boundaries()
+    st = o.solve_uvwp()
+    assert st.it_p == 100
+
+
+def test_ref_and_tight_reach_the_same_steady_state():
+    """The reference's sweep-based inner solves and the tight Krylov solves are
+    two routes to the same discrete steady state."""
+    runs = {}
+    for mode in (0, 1):
+        z, o = _fresh(n=5, cfg=oracle_lib.steady(mode=mode))
+        o.run(220)
+        runs[mode] = o
+    for f in ("u", "v", "w"):
+        a, b = runs[0].get(f)[:runs[0].ne], runs[1].get(f)[:runs[1].ne]
+        assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b), f
+
+
+def test_mass_conservation_improves():
+    z, o = _fresh(n=6, cfg=oracle_lib.steady(mode=1))
+    o.run(1)
+    o.update_boundaries(); o.calc_coef_uvw(); o.calc_mip(True); o.calc_coef_p()
+    b0 = np.linalg.norm(o.get("b"))
+    o.run(40)
+    o.update_boundaries(); o.calc_coef_uvw(); o.calc_mip(True); o.calc_coef_p()
+    assert np.linalg.norm(o.get("b")) < 0.2 * b0

@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark of the CFD-Lite SIMPLE outer iteration on GB300.
+
+Workload (the reference-cavity configuration the metric is quoted on): the
+lid-driven cavity in the unit cube on n^3 = 128^3 hex cells (2.1M cells),
+interior nodes jittered by a seeded U(-0.2, 0.2) cell spacing, rho = 1,
+mu = 0.01 (Re = 100), SIMPLE with under-relaxation 0.7 (velocity) and 0.3
+(pressure), FP64.  One step = one outer iteration: update_boundaries +
+solve_uvwp (+ update_time every ncoef = 3), with every inner solve stopped,
+as in the reference, at a 10x residual drop or nit = 100 iterations.
+Synthetic mesh: the reference's own sample mesh is not available.
+
+The working set (~3 GB) is far larger than the 129 MB L2, so no L2 flush is
+needed between steps.  Device time is taken with CUDA events on the solver's
+own stream; `e2e` repeats the measurement through the host-array drop-in
+(pinned host buffers uploaded and downloaded every step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cfd-lite_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "SIMPLE cell-iters/s"
+UNIT = "cell-iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--jitter", type=float, default=0.2)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tet", action="store_true")
+    ap.add_argument("--mode", type=int, default=0, help="0: reference stopping rule, 1: tight")
+    ap.add_argument("--precision", type=int, default=0, help="0: FP64, 1: mixed pressure solve")
+    ap.add_argument("--precond", type=int, default=0, help="pressure preconditioner: 0 Jacobi, 1 AMG")
+    ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- distributed
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)])
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)])
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi samples during the timed region (read-only query)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1])); smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for k, nm in enumerate(names):
+                    if f[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic(kernel, n):
+    """DRAM bytes per launch from a committed ncu summary (profiles/ncu_traffic.txt:
+    lines 'kernel n_cells bytes_per_launch'), scaled to n^3 cells when the
+    capture was taken on a smaller mesh; None when absent."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    best = None
+    with open(path) as fh:
+        for line in fh:
+            f = line.split()
+            if len(f) >= 3 and f[0] == kernel and not line.startswith("#"):
+                best = (int(f[1]), float(f[2]))
+    if not best:
+        return None
+    cells, b = best
+    return b * (n ** 3) / cells
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(a, dist):
+    import numpy as np
+    import cfdl
+    from bytes_model import kernel_bytes
+
+    cfdl.select_device(dist.local)
+    zone = cfdl.Zone(a.n, a.tet, a.jitter, seed=a.seed)
+    setup = cfdl.Setup(zone)
+    cfg = cfdl.steady(solve_mode=a.mode, precision=a.precision, precond=a.precond)
+    g = cfdl.Solver(setup, cfg)
+    W = 4 if a.tet else 6
+    ne, nf, nbf = setup.ne, setup.nf, setup.nbf
+    state = {"it": 0}
+
+    def step():
+        g.update_boundaries()
+        g.solve_uvwp(stats=False)
+        state["it"] += 1
+        if state["it"] % 3 == 0:
+            g.update_time()
+
+    for _ in range(a.warmup):
+        step()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    g.timer_begin()
+    clocks.start()
+    l0 = g.launch_count()
+    for _ in range(a.steps):
+        step()
+    ms = g.timer_end()
+    launches = g.launch_count() - l0
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    cells_total = dist.sum(ne * a.steps)
+    value = cells_total / (ms_max / 1e3)
+    st = g.solve_uvwp() if False else g.last_stats
+
+    # roofline: find the dominant kernel, then time its launches alone
+    g.profile_start(None)
+    for _ in range(min(3, a.steps)):
+        step()
+    prof = g.profile_stop()
+    dominant = max(prof.items(), key=lambda kv: kv[1][1])[0]
+    g.profile_start(dominant)
+    for _ in range(a.steps):
+        step()
+    dp = g.profile_stop()[dominant]
+    avg_s = dp[1] / dp[0] / 1e3
+    peaks, peak_kind = measured_peaks()
+    nbytes = kernel_bytes(dominant, ne, nf, nbf, W)
+    achieved = nbytes / avg_s / 1e9 if nbytes else None
+    traffic = ncu_traffic(dominant, a.n)
+    breakdown = {k: {"launches": c, "ms": round(t, 3), "share": round(t / sum(v[1] for v in prof.values()), 4)}
+                 for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    if a.breakdown and dist.rank == 0:
+        sys.stderr.write(json.dumps(breakdown, indent=1) + "\n")
+
+    # inner iteration counts of the last step
+    g.update_boundaries()
+    stl = g.solve_uvwp()
+
+    # end to end through the host-array drop-in
+    e2e = None
+    if not a.no_e2e:
+        import torch
+        nc = ne + nbf
+        sizes = {"u": nc, "v": nc, "w": nc, "p": nc, "u0": nc, "v0": nc, "w0": nc,
+                 "gu": 3 * nc, "gv": 3 * nc, "gw": 3 * nc, "gp": 3 * nc, "gpc": 3 * nc, "mip": nf, "mip0": nf}
+        host = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for k, n in sizes.items()}
+        import ctypes as C
+        fl = cfdl.Fields(**{k: v.ctypes.data_as(C.c_void_p) for k, v in host.items()})
+        L = cfdl.lib()
+        cfdl._check(L.cfdl_download_fields(g._h, C.byref(fl)), "download")
+        bytes_step = sum(v.nbytes for v in host.values())
+
+        def e2e_step():
+            cfdl._check(L.cfdl_upload_fields(g._h, C.byref(fl)), "upload")
+            g.update_boundaries()
+            g.solve_uvwp(stats=False)
+            state["it"] += 1
+            if state["it"] % 3 == 0:
+                g.update_time()
+            cfdl._check(L.cfdl_download_fields(g._h, C.byref(fl)), "download")
+
+        for _ in range(2):
+            e2e_step()
+        dist.barrier()
+        t0 = time.perf_counter()
+        g.timer_begin()
+        for _ in range(a.steps):
+            e2e_step()
+        ms_e = g.timer_end()
+        wall = time.perf_counter() - t0
+        ms_e = max(ms_e, wall * 1e3)
+        ms_e = dist.max(ms_e)
+        e2e = {"value": dist.sum(ne * a.steps) / (ms_e / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step,
+               "api": "cfdl_upload_fields + cfdl_update_boundaries + cfdl_solve_uvwp + cfdl_download_fields"}
+
+    cpu = None
+    if not a.no_cpu and dist.rank == 0 and dist.world == 1:
+        cpu = cpu_baseline(zone, setup, budget_s=20.0)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if a.precision == 0 else "f64+f32 (mixed pressure solve)",
+        "data": "synthetic (seeded jittered unit-cube hex mesh; the reference's sample mesh is unavailable)",
+        "config": {"workload": "lid-driven cavity %d^3 %s, jitter %.2f, Re=100 (rho=1, mu=0.01), SIMPLE "
+                               "alpha_u=0.7 alpha_p=0.3, FP64" % (a.n, "tet-split" if a.tet else "hex", a.jitter),
+                   "cells": ne, "faces": nf, "inner_solve": "10x residual drop / nit=100" if a.mode == 0 else "tight 1e-13",
+                   "pressure_precond": ["jacobi", "amg"][a.precond], "parallelism": "replicas" if dist.world > 1 else "single",
+                   "l2": "working set > L2 (no flush needed)"},
+        "gpu_launches": launches // max(1, 1),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                     "traffic": traffic, "algorithmic_bytes": nbytes, "avg_launch_us": avg_s * 1e6,
+                     "launches": dp[0], "peak_source": peak_kind},
+        "inner_iterations": {"u": stl.it_u, "v": stl.it_v, "w": stl.it_w, "pc": stl.it_p},
+        "kernel_shares": {k: v["share"] for k, v in list(breakdown.items())[:8]},
+    }
+    if clk:
+        out["clocks"] = clk
+    if e2e:
+        out["e2e"] = e2e
+    if cpu:
+        out["cpu_baseline"] = cpu
+    g.close()
+    return out
+
+
+# ---------------------------------------------------------- CPU reference
+def oracle_case(zone, setup):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    o = oracle_lib.Oracle(zone, n_subdomains=4, setup=setup)
+    o.physics_init(oracle_lib.steady(mode=0))
+    return o, oracle_lib
+
+
+def cpu_baseline(zone, setup, budget_s=20.0):
+    """The reference algorithm (CPU oracle, ref mode: Gauss-Seidel / 4-block
+    SSOR inner solves, nsubd = 4), single thread like the serial reference,
+    timed over a bounded number of outer iterations of the same mesh."""
+    o, _ = oracle_case(zone, setup)
+    t0 = time.perf_counter()
+    o.run(1, 3)                       # untimed warm iteration
+    t1 = time.perf_counter() - t0
+    k = max(1, min(4, int(budget_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.run(k, 3)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": o.ne * k / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d outer iteration(s) of the full %d-cell mesh after 1 warm-up iteration, %.1f s" % (k, o.ne, dt)}
+
+
+def run_reference(a, dist):
+    if dist.rank != 0:
+        return None
+    import cfdl
+    zone = cfdl.Zone(a.n, a.tet, a.jitter, seed=a.seed)
+    setup = cfdl.Setup(zone)
+    o, _ = oracle_case(zone, setup)
+    t0 = time.perf_counter()
+    o.run(1, 3)
+    t_it = time.perf_counter() - t0
+    warm = max(0, min(a.warmup, 1) - 1)
+    if warm:
+        o.run(warm, 3)
+    steps = max(1, min(a.steps, int(150.0 / max(t_it, 1e-3))))
+    t0 = time.perf_counter()
+    o.run(steps, 3)
+    dt = time.perf_counter() - t0
+    value = o.ne * steps / dt
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+           "steps": steps, "steps_requested": a.steps, "warmup": 1 + warm, "ms_per_step": dt / steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded jittered unit-cube hex mesh)",
+           "config": {"workload": "lid-driven cavity %d^3 %s, jitter %.2f, Re=100, SIMPLE alpha 0.7/0.3, FP64"
+                                  % (a.n, "tet-split" if a.tet else "hex", a.jitter), "cells": o.ne},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                            "sample": "%d outer iterations of the full mesh (reference algorithm, serial), %.1f s"
+                                      % (steps, dt)},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    o.close()
+    return out
+
+
+def main():
+    a = parse()
+    dist = Dist()
+    try:
+        out = run_reference(a, dist) if a.impl == "reference" else run_ours(a, dist)
+        if out is not None and dist.rank == 0:
+            print(json.dumps(out))
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

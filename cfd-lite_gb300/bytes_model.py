@@ -1,0 +1,62 @@
+"""Algorithmic (compulsory) HBM bytes per launch of each kernel.
+
+Each array a kernel reads or writes is counted once per launch: FP64 = 8 B,
+FP32 = 4 B, int32 = 4 B; a gathered neighbour value is counted once for the
+cell that owns it, not once per gather.  W = faces per cell (6 for hex, 4 for
+tet), ne cells, nf faces (interior + boundary), nbf boundary faces (halos).
+These are the figures behind roofline.achieved in bench.py: bytes / average
+launch duration.
+"""
+
+
+def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
+    nfi = nf - nbf                    # interior faces
+    ell_i = 4 * W * ne                # one int32 ELL plane
+    ell_d = 8 * W * ne                # one FP64 ELL plane
+    m = ncomp_active
+    table = {
+        # update_boundaries: halo tables + halo u,v,w,p writes, owner p, mip
+        "k_bc": nbf * (4 + 4 + 4 + 24 + 32 + 8 + 8),
+        # momentum face terms: own/nb, 8 geometry planes, 7 outputs; mu + 9 gradient comps per cell
+        "k_coef_uvw_face": nfi * (8 + 64 + 56) + nbf * (8 + 8 + 8) + ne * (8 + 72),
+        # momentum cell gather: ELL nb/fc, 8 face doubles, 13 cell doubles in, 6 out, anb ELL out
+        "k_coef_uvw_cell": 2 * ell_i + nf * 64 + ne * (104 + 48) + ell_d + nbf * (24 + 4 + 32),
+        "k_grad3": ell_i + 3 * ell_d + 24 * (ne + nbf) + 72 * ne,
+        "k_grad1": ell_i + 3 * ell_d + 8 * (ne + nbf) + 24 * ne,
+        # Rhie-Chow: own/nb, 8 geometry planes, mip0 in, mip out; 12 cell doubles
+        "k_calc_mip": nfi * (8 + 64 + 16) + ne * 96,
+        "k_coef_p_face": nfi * (8 + 16 + 8) + nbf * 8 + ne * 16,
+        "k_coef_p_cell": 2 * ell_i + nf * 16 + ell_d + ne * 16,
+        "k_adjust_pc": ell_i + ne * 16 + nbf * 8,
+        "k_update_cells": ne * (8 + 8 + 8 + 24 + 24 + 24),
+        "k_update_faces": nfi * (8 + 16 + 16) + ne * 32,
+        "k_update_time": ne * 48,
+        "k_update_time_halo": nbf * 48,
+        "k_copy_mip0": nf * 16,
+        # momentum BiCGStab, m active components
+        "k_mom_init": ne * 8 + ell_d + ell_i + m * ne * (8 + 8 + 40) + m * nbf * 8,
+        "k_mom_p": ne * 8 + m * ne * (24 + 16),
+        "k_mom_v": ne * 8 + ell_d + ell_i + m * ne * (8 + 8 + 8),
+        "k_mom_s": ne * 8 + m * ne * (16 + 16),
+        "k_mom_t": ne * 8 + ell_d + ell_i + m * ne * (8 + 8 + 8),
+        "k_mom_x": m * ne * (16 + 8 + 8 + 8 + 8 + 8 + 8),
+        # pressure CG
+        "k_pc_mean": ne * 8,
+        "k_pc_init": ne * (8 + 8 + 8 * 4),
+        "k_pc_q": ne * (8 + 8 + 8) + ell_d + ell_i,
+        "k_pc_x": ne * (16 + 8 + 16 + 8 + 8 + 8),
+        "k_pc_p": ne * 24,
+    }
+    return table.get(name)
+
+
+def kernel_bytes_f32(name, ne, nf, nbf, W):
+    """Same for the FP32 kernels of the mixed-precision pressure solve."""
+    ell_i = 4 * W * ne
+    ell_f = 4 * W * ne
+    table = {
+        "k_mx_q": ne * (4 + 4 + 4) + ell_f + ell_i,
+        "k_mx_x": ne * 4 * 7,
+        "k_mx_p": ne * 12,
+    }
+    return table.get(name)

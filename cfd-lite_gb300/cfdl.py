@@ -104,6 +104,12 @@ def lib():
     L.cfdl_calc_mip.argtypes = [vp, C.c_int]
     L.cfdl_get_array.argtypes = [vp, C.c_char_p, vp]
     L.cfdl_set_array.argtypes = [vp, C.c_char_p, vp]
+    L.cfdl_select_device.argtypes = [C.c_int]
+    L.cfdl_timer_begin.argtypes = [vp]
+    L.cfdl_timer_end.argtypes = [vp, dp]
+    L.cfdl_profile_start.argtypes = [vp, C.c_char_p]
+    L.cfdl_profile_stop.argtypes = [vp, ip]
+    L.cfdl_profile_get.argtypes = [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int64), dp]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]
@@ -182,6 +188,10 @@ class Setup:
             self._h = None
 
 
+def select_device(device):
+    _check(lib().cfdl_select_device(int(device)), "select_device")
+
+
 def default_config(**kw):
     cfg = Config()
     lib().cfdl_config_default(C.byref(cfg))
@@ -215,7 +225,10 @@ class Solver:
     def update_boundaries(self):
         _check(lib().cfdl_update_boundaries(self._h), "update_boundaries")
 
-    def solve_uvwp(self):
+    def solve_uvwp(self, stats=True):
+        if not stats:
+            _check(lib().cfdl_solve_uvwp(self._h, None), "solve_uvwp")
+            return None
         st = Stats()
         _check(lib().cfdl_solve_uvwp(self._h, C.byref(st)), "solve_uvwp")
         self.last_stats = st
@@ -286,6 +299,30 @@ class Solver:
         if a.size != self._len(name):
             raise ValueError("%s needs %d values" % (name, self._len(name)))
         _check(lib().cfdl_set_array(self._h, name.encode(), _p(a)), "set " + name)
+
+    # -- measurement ---------------------------------------------------------
+    def timer_begin(self):
+        _check(lib().cfdl_timer_begin(self._h), "timer_begin")
+
+    def timer_end(self):
+        ms = C.c_double()
+        _check(lib().cfdl_timer_end(self._h, C.byref(ms)), "timer_end")
+        return ms.value
+
+    def profile_start(self, kernel=None):
+        _check(lib().cfdl_profile_start(self._h, kernel.encode() if kernel else None), "profile_start")
+
+    def profile_stop(self):
+        """Returns {kernel: (launches, total_ms)} for the profiled span."""
+        n = C.c_int()
+        _check(lib().cfdl_profile_stop(self._h, C.byref(n)), "profile_stop")
+        out = {}
+        name = C.create_string_buffer(64)
+        cnt, tot = C.c_int64(), C.c_double()
+        for i in range(n.value):
+            _check(lib().cfdl_profile_get(self._h, i, name, C.byref(cnt), C.byref(tot)), "profile_get")
+            out[name.value.decode()] = (cnt.value, tot.value)
+        return out
 
     def launch_count(self):
         return int(lib().cfdl_launch_count(self._h))

@@ -218,6 +218,7 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     cudaFree(ctx->d_flags);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    prof_destroy(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CFDL_OK;

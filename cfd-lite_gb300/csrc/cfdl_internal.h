@@ -130,6 +130,7 @@ struct cfdl_ctx {
     int *h_flags = nullptr;              // pinned, per-case convergence flags
     int h_flags_cap = 0;
     int *d_flags = nullptr;
+    void *prof = nullptr;                // event profiler state (cfdl_prof.cpp)
 };
 
 namespace cfdl {
@@ -151,6 +152,25 @@ void launch_adjust_pc(cfdl_ctx *ctx);
 void launch_update_uvwp(cfdl_ctx *ctx);
 void launch_update_time(cfdl_ctx *ctx);
 void launch_set_mip0(cfdl_ctx *ctx);
+
+// event profiler (cfdl_prof.cpp)
+bool prof_wants(cfdl_ctx *ctx, const char *name);
+void prof_begin(cfdl_ctx *ctx, const char *name);
+void prof_end(cfdl_ctx *ctx);
+void prof_destroy(cfdl_ctx *ctx);
+
+// Launch a tile kernel over work list WL of the context, with optional
+// event bracketing for the profiler.
+#define CFDL_LAUNCH(name, kern, WL, ...)                                                            \
+    do {                                                                                            \
+        if (ctx->WL.ntiles > 0) {                                                                   \
+            const bool p_ = ctx->prof && cfdl::prof_wants(ctx, name);                               \
+            if (p_) cfdl::prof_begin(ctx, name);                                                    \
+            kern<<<ctx->WL.ntiles, cfdl::kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__); \
+            if (p_) cfdl::prof_end(ctx);                                                            \
+            ctx->launches++;                                                                        \
+        }                                                                                           \
+    } while (0)
 
 // solvers (cfdl_solvers.cu)
 int solve_momentum(cfdl_ctx *ctx);

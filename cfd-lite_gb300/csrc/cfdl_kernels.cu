@@ -342,44 +342,39 @@ __global__ void __launch_bounds__(kTile) k_copy_mip0(const CaseDev *__restrict__
 
 }  // namespace
 
-#define LAUNCH(kern, WL, ...)                                                                   \
-    do {                                                                                        \
-        if (ctx->WL.ntiles > 0) {                                                               \
-            kern<<<ctx->WL.ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__); \
-            ctx->launches++;                                                                    \
-        }                                                                                       \
-    } while (0)
-
-void launch_bc(cfdl_ctx *ctx) { LAUNCH(k_bc, halos); }
+void launch_bc(cfdl_ctx *ctx) { CFDL_LAUNCH("k_bc", k_bc, halos); }
 void launch_coef_uvw(cfdl_ctx *ctx) {
-    LAUNCH(k_coef_uvw_face, faces);
-    LAUNCH(k_coef_uvw_cell, cells);
+    CFDL_LAUNCH("k_coef_uvw_face", k_coef_uvw_face, faces);
+    CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell, cells);
 }
 void launch_grad(cfdl_ctx *ctx, int field) {
-    if (field == 4) LAUNCH(k_grad<3>, cells, 0);
-    else LAUNCH(k_grad<1>, cells, field);
+    if (field == 4) CFDL_LAUNCH("k_grad3", k_grad<3>, cells, 0);
+    else CFDL_LAUNCH("k_grad1", k_grad<1>, cells, field);
 }
-void launch_calc_mip(cfdl_ctx *ctx, int rc) { LAUNCH(k_calc_mip, faces, rc); }
+void launch_calc_mip(cfdl_ctx *ctx, int rc) { CFDL_LAUNCH("k_calc_mip", k_calc_mip, faces, rc); }
 void launch_coef_p(cfdl_ctx *ctx) {
-    LAUNCH(k_coef_p_face, faces);
-    LAUNCH(k_coef_p_cell, cells);
+    CFDL_LAUNCH("k_coef_p_face", k_coef_p_face, faces);
+    CFDL_LAUNCH("k_coef_p_cell", k_coef_p_cell, cells);
 }
 void launch_adjust_pc(cfdl_ctx *ctx) {
     int n = (int)ctx->cases.size();
     if (n == 0) return;
+    const bool p_ = ctx->prof && prof_wants(ctx, "k_save_pref");
+    if (p_) prof_begin(ctx, "k_save_pref");
     k_save_pref<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_cases, n);
+    if (p_) prof_end(ctx);
     ctx->launches++;
-    LAUNCH(k_adjust_pc, cells);
+    CFDL_LAUNCH("k_adjust_pc", k_adjust_pc, cells);
 }
 void launch_update_uvwp(cfdl_ctx *ctx) {
-    LAUNCH(k_update_cells, cells);
-    LAUNCH(k_update_faces, faces);
+    CFDL_LAUNCH("k_update_cells", k_update_cells, cells);
+    CFDL_LAUNCH("k_update_faces", k_update_faces, faces);
 }
 void launch_update_time(cfdl_ctx *ctx) {
-    LAUNCH(k_update_time, cells);
-    LAUNCH(k_update_time_halo, halos);
-    LAUNCH(k_copy_mip0, faces);
+    CFDL_LAUNCH("k_update_time", k_update_time, cells);
+    CFDL_LAUNCH("k_update_time_halo", k_update_time_halo, halos);
+    CFDL_LAUNCH("k_copy_mip0", k_copy_mip0, faces);
 }
-void launch_set_mip0(cfdl_ctx *ctx) { LAUNCH(k_copy_mip0, faces); }
+void launch_set_mip0(cfdl_ctx *ctx) { CFDL_LAUNCH("k_copy_mip0", k_copy_mip0, faces); }
 
 }  // namespace cfdl

@@ -365,11 +365,6 @@ __global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags
 
 }  // namespace
 
-#define SLAUNCH(kern, WL, ...)                                                                           \
-    do {                                                                                                 \
-        kern<<<ctx->WL.ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__);   \
-        ctx->launches++;                                                                                 \
-    } while (0)
 #define RED ctx->cells.d_case_first, ctx->cells.d_case_ntiles, ctx->d_partials
 
 static int poll(cfdl_ctx *ctx, int mask) {
@@ -391,16 +386,16 @@ static int max_cap(cfdl_ctx *ctx) {
 
 int solve_momentum(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    SLAUNCH(k_mom_init, cells, RED);
+    CFDL_LAUNCH("k_mom_init", k_mom_init, cells, RED);
     const int cap = max_cap(ctx);
     int it = 0, chunk = 2;
     while (it < cap) {
         for (int k = 0; k < chunk && it < cap; k++, it++) {
-            SLAUNCH(k_mom_p, cells);
-            SLAUNCH(k_mom_v, cells, RED);
-            SLAUNCH(k_mom_s, cells, RED);
-            SLAUNCH(k_mom_t, cells, RED);
-            SLAUNCH(k_mom_x, cells, RED);
+            CFDL_LAUNCH("k_mom_p", k_mom_p, cells);
+            CFDL_LAUNCH("k_mom_v", k_mom_v, cells, RED);
+            CFDL_LAUNCH("k_mom_s", k_mom_s, cells, RED);
+            CFDL_LAUNCH("k_mom_t", k_mom_t, cells, RED);
+            CFDL_LAUNCH("k_mom_x", k_mom_x, cells, RED);
         }
         int a = poll(ctx, 1);
         if (a < 0) return CFDL_ERR_CUDA;
@@ -412,15 +407,15 @@ int solve_momentum(cfdl_ctx *ctx) {
 
 int solve_pressure(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    SLAUNCH(k_pc_mean, cells, RED);
-    SLAUNCH(k_pc_init, cells, RED);
+    CFDL_LAUNCH("k_pc_mean", k_pc_mean, cells, RED);
+    CFDL_LAUNCH("k_pc_init", k_pc_init, cells, RED);
     const int cap = max_cap(ctx);
     int it = 0, chunk = 4;
     while (it < cap) {
         for (int k = 0; k < chunk && it < cap; k++, it++) {
-            SLAUNCH(k_pc_q, cells, RED);
-            SLAUNCH(k_pc_x, cells, RED);
-            SLAUNCH(k_pc_p, cells);
+            CFDL_LAUNCH("k_pc_q", k_pc_q, cells, RED);
+            CFDL_LAUNCH("k_pc_x", k_pc_x, cells, RED);
+            CFDL_LAUNCH("k_pc_p", k_pc_p, cells);
         }
         int a = poll(ctx, 2);
         if (a < 0) return CFDL_ERR_CUDA;

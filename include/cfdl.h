@@ -172,6 +172,20 @@ int cfdl_update_uvwp(cfdl_ctx *ctx);                     /* mod_uvwp.f90:370-436
 int cfdl_get_array(cfdl_ctx *ctx, const char *name, double *host);
 int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host);
 
+/* ---- measurement (CUDA events on the context's stream) ---- */
+/* Make device `device` current for the contexts created afterwards on this
+ * thread (one process per GPU). */
+int cfdl_select_device(int device);
+int cfdl_timer_begin(cfdl_ctx *ctx);
+int cfdl_timer_end(cfdl_ctx *ctx, double *ms);      /* synchronises */
+/* Bracket every launch (kernel = NULL or "") or the launches of one named
+ * kernel with events until cfdl_profile_stop, which returns the number of
+ * distinct kernels seen; cfdl_profile_get reads kernel i's name (64 chars),
+ * launch count and summed device time. */
+int cfdl_profile_start(cfdl_ctx *ctx, const char *kernel);
+int cfdl_profile_stop(cfdl_ctx *ctx, int *nkernels);
+int cfdl_profile_get(cfdl_ctx *ctx, int i, char *name64, int64_t *launches, double *total_ms);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);
 /* Human-readable text for a status code. */

@@ -55,6 +55,15 @@ typedef struct {
 ocase *or_create(int nvx, const double *x, const double *y, const double *z,
                  int nsec, const char *names, const int *etype, const int *esec,
                  int ne2vxmax, const int *e2vx, int n_subdomains);
+/* Same, from set-up arrays that were already built (what a host that ran
+ * cell_input holds): skips find_element_nb and the geometry, keeps the
+ * oct-tree partition and subdomains.  Arrays are 0-offset copies of the
+ * reference's 1-based-valued arrays; esec/etype/names as in or_create. */
+ocase *or_create_from_arrays(int ne, int nf, int nbf, int nsec, const char *names, const int *etype,
+                             const int *esec, const int *ef2nb1, const int *ef2nb2, const int *ef2nb_idx,
+                             const int *s2g, const int *bs, const double *aip, const double *rip,
+                             const double *xc, const double *yc, const double *zc, const double *vol,
+                             int n_subdomains);
 void or_destroy(ocase *c);
 
 /* sizes: ne, nf, nbf, nvx, nelem, nsec, nred, nsubd, nintf_c2b */

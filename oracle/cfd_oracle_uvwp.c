@@ -108,6 +108,52 @@ ocase *or_create(int nvx, const double *x, const double *y, const double *z,
     return c;
 }
 
+ocase *or_create_from_arrays(int ne, int nf, int nbf, int nsec, const char *names, const int *etype,
+                             const int *esec, const int *ef2nb1, const int *ef2nb2, const int *ef2nb_idx,
+                             const int *s2g, const int *bs, const double *aip, const double *rip,
+                             const double *xc, const double *yc, const double *zc, const double *vol,
+                             int n_subdomains) {
+    ocase *c = o_alloc(1, sizeof(ocase));
+    c->ne = ne; c->nf = nf; c->nbf = nbf; c->nelem = ne + nbf; c->nsec = nsec;
+    c->H = 2 * nf - nbf;
+    c->esec = o_alloc(2 * (size_t)nsec, sizeof(int));
+    c->etype = o_alloc((size_t)nsec + 1, sizeof(int));
+    c->secname = o_alloc((size_t)nsec + 1, 33);
+    c->sec2intf = o_alloc((size_t)nsec + 1, sizeof(int));
+    c->bs_idx = o_alloc((size_t)nsec + 2, sizeof(int));
+    for (int s = 1; s <= nsec; s++) {
+        c->etype[s] = etype[s-1];
+        c->esec[2*(s-1)] = esec[2*(s-1)]; c->esec[2*(s-1)+1] = esec[2*(s-1)+1];
+        memcpy(c->secname[s], names + 33*(s-1), 32);
+        c->secname[s][32] = 0;
+    }
+    /* sections are taken as already ordered (add_meshds); interfaces = 2D sections */
+    c->bs_idx[1] = 1;
+    int n = 0;
+    for (int s = 1; s <= nsec; s++) {
+        c->bs_idx[s+1] = c->esec[2*(s-1)+1] + 1;
+        if (c->etype[s] < 10) { n++; c->sec2intf[s] = n; }
+    }
+    c->nintf_c2b = n;
+    c->intf2sec = o_alloc((size_t)n + 1, sizeof(int));
+    for (int s = 1; s <= nsec; s++) if (c->sec2intf[s] > 0) c->intf2sec[c->sec2intf[s]] = s;
+    const size_t nc = (size_t)ne + nbf;
+#define COPYI(dst, src, cnt) do { dst = o_alloc((size_t)(cnt) + 2, sizeof(int)); memcpy(dst + 1, src, (size_t)(cnt) * sizeof(int)); } while (0)
+#define COPYD(dst, src, cnt) do { dst = o_alloc((size_t)(cnt) + 1, sizeof(double)); memcpy(dst + 1, src, (size_t)(cnt) * sizeof(double)); } while (0)
+    COPYI(c->ef2nb1, ef2nb1, c->H); COPYI(c->ef2nb2, ef2nb2, c->H); COPYI(c->ef2nb_idx, ef2nb_idx, ne + 1);
+    COPYI(c->s2g, s2g, nf);
+    c->bs_store = o_alloc((size_t)nbf + 1, sizeof(int));
+    memcpy(c->bs_store + 1, bs, (size_t)nbf * sizeof(int));
+    COPYD(c->aip, aip, 3 * (size_t)nf); COPYD(c->rip, rip, 3 * (size_t)nf);
+    COPYD(c->xc, xc, nc); COPYD(c->yc, yc, nc); COPYD(c->zc, zc, nc); COPYD(c->vol, vol, ne);
+#undef COPYI
+#undef COPYD
+    c->red = o_alloc((size_t)ne + 2, sizeof(int));
+    c->nsubd = 1;
+    if (n_subdomains > 1 && o_build_partition(c, n_subdomains)) { or_destroy(c); return NULL; }
+    return c;
+}
+
 void or_destroy(ocase *c) {
     if (!c) return;
     free(c->x); free(c->y); free(c->z); free(c->e2vx); free(c->esec); free(c->etype);

@@ -44,6 +44,8 @@ def lib():
         vp = C.c_void_p
         L.or_create.restype = vp
         L.or_create.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_char_p, vp, vp, C.c_int, vp, C.c_int]
+        L.or_create_from_arrays.restype = vp
+        L.or_create_from_arrays.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p] + [vp] * 13 + [C.c_int]
         for n in ("or_destroy", "or_update_boundaries", "or_update_time", "or_calc_coef_uvw", "or_calc_coef_p",
                   "or_adjust_pc", "or_update_uvwp"):
             getattr(L, n).argtypes = [vp]
@@ -93,13 +95,26 @@ class Oracle:
     """One case in the CPU oracle, built from a zone (cfd-lite_gb300 Zone or any
     object with the same CGNS-shaped attributes)."""
 
-    def __init__(self, zone, n_subdomains=4):
+    def __init__(self, zone, n_subdomains=4, setup=None):
+        """Build from the zone with the oracle's own set-up restatement, or,
+        when ``setup`` (a cfdl.Setup of the same zone) is given, from its
+        arrays -- bit-identical to the restatement (tests/test_setup.py) and
+        much faster on large meshes."""
         L = lib()
-        self._h = L.or_create(zone.nvx, _p(zone.x), _p(zone.y), _p(zone.z), zone.nsec, zone.names,
-                              _p(zone.etype), _p(zone.esec), zone.ne2vxmax, _p(zone.e2vx), n_subdomains)
-        if not self._h:
+        if setup is None:
+            h = L.or_create(zone.nvx, _p(zone.x), _p(zone.y), _p(zone.z), zone.nsec, zone.names,
+                            _p(zone.etype), _p(zone.esec), zone.ne2vxmax, _p(zone.e2vx), n_subdomains)
+        else:
+            s = setup
+            arrs = [s.get_int("esec"), s.get_int("etype")]
+            ints = [s.get_int(n) for n in ("ef2nb1", "ef2nb2", "ef2nb_idx", "s2g", "bs")]
+            dbls = [s.get_dbl(n) for n in ("aip", "rip", "xc", "yc", "zc", "vol")]
+            self._keep = arrs + ints + dbls
+            h = L.or_create_from_arrays(s.ne, s.nf, s.nbf, zone.nsec, zone.names, _p(arrs[1]), _p(arrs[0]),
+                                        *[_p(a) for a in ints], *[_p(a) for a in dbls], n_subdomains)
+        if not h:
             raise RuntimeError("oracle mesh set-up failed")
-        self._h = C.c_void_p(self._h)
+        self._h = C.c_void_p(h)
         sz = np.zeros(9, np.int32)
         L.or_sizes(self._h, _p(sz))
         (self.ne, self.nf, self.nbf, self.nvx, self.nelem, self.nsec, self.nred, self.nsubd,

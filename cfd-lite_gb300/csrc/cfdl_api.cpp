@@ -151,6 +151,7 @@ const char *cfdl_status_string(int s) {
     case CFDL_ERR_MESH: return "mesh connectivity error";
     case CFDL_ERR_NO_DEVICE: return "no CUDA device";
     case CFDL_ERR_NAME: return "unknown array name";
+    case CFDL_ERR_TOO_LARGE: return "problem larger than the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
     }
 }

@@ -186,6 +186,35 @@ int cfdl_profile_start(cfdl_ctx *ctx, const char *kernel);
 int cfdl_profile_stop(cfdl_ctx *ctx, int *nkernels);
 int cfdl_profile_get(cfdl_ctx *ctx, int i, char *name64, int64_t *launches, double *total_ms);
 
+/* ---- allocation-free pressure-correction solve --------------------------
+ * No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory themselves or let a library do it: a Fortran host whose device
+ * arrays belong to another runtime or memory pool, a process held to a fixed
+ * device-memory budget, or a time-stepping loop in which allocation is not
+ * allowed.  It solves the pressure-correction system A pc = b (the
+ * Jacobi-preconditioned CG of cfdl_solve_pc, from pc = 0, right-hand side
+ * projected to zero mean, stop at ||r||2 <= rtol*||r0||2 or maxit) on arrays
+ * the caller already holds in device memory, in the reference layout:
+ *   ef2nb1 [nh], ef2nb_idx [ne+1]: geom%ef2nb(:,1) and geom%ef2nb_idx;
+ *   ap [ne], anb [nh], b [ne]: calc_coef_p's coefficients (nh = 2nf-nbf);
+ *   phic [ne]: output, the interior cells of the pressure correction.
+ * It allocates nothing, on the device or the host: its Krylov vectors,
+ * reduction partials and scalars live in one file-scope device array sized
+ * for CFDL_NOALLOC_MAX_CELLS cells (about 4.2 MB), which every GPU that loads
+ * the library holds until the process exits.  Larger systems are rejected
+ * with CFDL_ERR_TOO_LARGE.  The first call on a device looks up that array's
+ * device address with the device current; make that first call before any
+ * stream capture.  Every call shares the one array (the call clears what must
+ * start at zero), so calls that overlap on the GPU -- from several host
+ * threads, or on one device at the same time -- race.  Work is queued on the
+ * legacy default stream and the call returns after synchronising it; iters
+ * and rnorm (optional) receive the CG iterations and the final ||r||2. */
+#define CFDL_ERR_TOO_LARGE      9
+#define CFDL_NOALLOC_MAX_CELLS  131072
+int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_idx, const double *ap,
+                          const double *anb, const double *b, double *phic, double rtol, int maxit,
+                          int *iters, double *rnorm);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);
 /* Human-readable text for a status code. */

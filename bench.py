@@ -225,6 +225,15 @@ def run_ours(a, dist):
     avg_s = dp[1] / dp[0] / 1e3
     peaks, peak_kind = measured_peaks()
     nbytes = kernel_bytes(dominant, ne, nf, nbf, W)
+    if nbytes is None:
+        import ctypes as C
+        from bytes_model import amg_kernel_bytes
+        nl = C.c_int()
+        ns, ws = (C.c_int * 16)(), (C.c_int * 16)()
+        cfdl._check(cfdl.lib().cfdl_amg_info(g._h, 15, C.byref(nl), ns, ws), "amg_info")
+        levels = [(ns[l], ws[l]) for l in range(nl.value + 1)]
+        val = 4 if (a.precision == 1 and (dominant.startswith("k_v_") or dominant.startswith("k_mx_"))) else 8
+        nbytes = amg_kernel_bytes(dominant, levels, val)
     achieved = nbytes / avg_s / 1e9 if nbytes else None
     traffic = ncu_traffic(dominant, a.n)
     breakdown = {k: {"launches": c, "ms": round(t, 3), "share": round(t / sum(v[1] for v in prof.values()), 4)}

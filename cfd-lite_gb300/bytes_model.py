@@ -50,13 +50,45 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
     return table.get(name)
 
 
-def kernel_bytes_f32(name, ne, nf, nbf, W):
-    """Same for the FP32 kernels of the mixed-precision pressure solve."""
+def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
+    """One V-cycle kernel at one level of n cells and ELL width W."""
+    ell_i = 4 * W * n
+    return {
+        "jac0": 3 * s * n,
+        "jac": 5 * s * n + W * s * n + ell_i,
+        "resid": 4 * s * n + W * s * n + ell_i,
+        "prolong": (5 * s + 4) * n + W * s * n + ell_i + n_next * s,
+        "restrict": n_prev * (s + 4) + n * (4 + s),     # into this level from the finer one
+    }[kind]
+
+
+def amg_kernel_bytes(name, levels, s):
+    """Multigrid and CG-around-multigrid kernels.  levels = [(n_l, W_l)] for
+    l = 0 (mesh) .. L (coarsest); s = value size (8 for the FP64 form, 4 for
+    the FP32 inner solve of the mixed form).  Kernels suffixed _f run on the
+    mesh level; _c kernels are averaged over the coarse levels they run on."""
+    ne, W = levels[0]
+    L = len(levels) - 1
     ell_i = 4 * W * ne
-    ell_f = 4 * W * ne
-    table = {
-        "k_mx_q": ne * (4 + 4 + 4) + ell_f + ell_i,
-        "k_mx_x": ne * 4 * 7,
-        "k_mx_p": ne * 12,
+    fixed = {
+        "k_apc_rz": 16 * ne, "k_apc_p": 24 * ne, "k_apc_x": 48 * ne,
+        "k_apc_q": ne * 24 + 8 * W * ne + ell_i,
+        "k_mx_rz": 8 * ne, "k_mx_p": 12 * ne, "k_mx_x": 24 * ne,
+        "k_mx_q": ne * 12 + 4 * W * ne + ell_i,
     }
-    return table.get(name)
+    if name in fixed:
+        return fixed[name]
+    if not name.startswith("k_v_") or L < 1:
+        return None
+    kind, where = name[4:].rsplit("_", 1)
+    if where == "f":
+        if kind == "restrict":
+            return _vcycle_level_bytes(kind, levels[1][0], levels[1][1], s, n_prev=ne)
+        return _vcycle_level_bytes(kind, ne, W, s, n_next=levels[1][0])
+    if kind == "restrict":
+        ls = list(range(2, L + 1))
+        vals = [_vcycle_level_bytes(kind, levels[l][0], levels[l][1], s, n_prev=levels[l - 1][0]) for l in ls]
+    else:
+        ls = list(range(1, L))
+        vals = [_vcycle_level_bytes(kind, levels[l][0], levels[l][1], s, n_next=levels[l + 1][0]) for l in ls]
+    return sum(vals) / len(vals) if vals else None

@@ -112,6 +112,7 @@ def lib():
     L.cfdl_profile_get.argtypes = [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int64), dp]
     L.cfdl_solve_pc_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int,
                                         ip, dp]
+    L.cfdl_amg_info.argtypes = [vp, C.c_int, ip, vp, vp]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]

@@ -1,0 +1,793 @@
+// cfdl_amg.cu -- aggregation-AMG preconditioned CG for the pressure
+// correction (FP64), and the mixed-precision form (FP32 AMG-PCG inner solve,
+// FP64 residual and refinement).
+//
+// The reference solves the pressure correction with 4-block Jacobi / SSOR
+// sweeps (multi_subdomain_solver, src/modules/mod_solver.f90:124-189), whose
+// convergence degrades with the mesh size.  Here CG on the same singular
+// Neumann system (right-hand side projected to zero mean) is preconditioned
+// by one V-cycle of aggregation multigrid:
+//   level l -> l+1   two damped-Jacobi sweeps, residual restricted by summing
+//                    over each aggregate (P^T, P piecewise constant);
+//   coarsest level   dense inverse of (A_L + c 11^T), which is A_L's
+//                    pseudo-inverse on zero-sum right-hand sides;
+//   level l+1 -> l   prolongation (injection) fused into the first of two
+//                    damped-Jacobi sweeps.
+// Pre- and post-smoothing match, so the preconditioner is symmetric and
+// positive semi-definite, as CG requires.  The coarse operators are rebuilt
+// at every pressure solve from the current coefficients (A_c = P^T A P).
+#include "cfdl_amg.h"
+#include "cfdl_device.cuh"
+#include <algorithm>
+
+namespace cfdl {
+namespace {
+
+constexpr double kOmega = 0.8;     // damped Jacobi weight
+constexpr double kOverCorrect = 2.0;   // scaling of the prolongated coarse correction
+enum { CNT_A0 = 9, CNT_A1, CNT_A2, CNT_A3, CNT_A4, CNT_A5 };
+
+template <class T> struct LP {
+    int n, W;
+    const int *nb;
+    const T *a, *dg, *rd;
+    T *r, *z, *t;
+};
+
+template <class T> __device__ __forceinline__ LP<T> level(const CaseDev &C, int l);
+template <> __device__ __forceinline__ LP<double> level<double>(const CaseDev &C, int l) {
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb, C.ap, C.rap, C.kr, C.ks, C.ksh};
+    const AmgLevelDev &L = C.lev[l - 1];
+    return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t};
+}
+template <> __device__ __forceinline__ LP<float> level<float>(const CaseDev &C, int l) {
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb, C.fdiag, C.frap, C.fr, C.fz, C.ft};
+    const AmgLevelDev &L = C.lev[l - 1];
+    return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32};
+}
+
+// (A x)_i at a level; neighbours outside [0, n) (halos, padding) are skipped
+template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x, int i) {
+    T s = P.dg[i] * x[i];
+    for (int k = 0; k < P.W; k++) {
+        const int j = P.nb[k * P.n + i];
+        if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * x[j];
+    }
+    return s;
+}
+
+__device__ __forceinline__ bool pactive(const CaseDev &C) { return C.sc->active_p != 0; }
+__device__ __forceinline__ bool mactive(const CaseDev &C) { return C.sc->active32 != 0; }
+
+// ------------------------------------------------------------ Galerkin
+__global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const int I = t.first + (int)threadIdx.x;
+    if (I >= t.last) return;
+    const AmgLevelDev &L = C.lev[l - 1];
+    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    const double *df = l == 1 ? C.ap : C.lev[l - 2].dg;
+    const bool mixed = C.precision == 1;
+    for (int k = 0; k < L.W; k++) {
+        const int s = k * L.n + I;
+        double v = 0.0;
+        for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
+        L.a[s] = v;
+        if (mixed) L.a32[s] = (float)v;
+    }
+    double dsum = 0.0;
+    for (int m = L.mem_ptr[I]; m < L.mem_ptr[I + 1]; m++) dsum += df[L.mem[m]];
+    for (int q = L.d_ptr[I]; q < L.d_ptr[I + 1]; q++) dsum -= af[L.d_src[q]];
+    L.dg[I] = dsum;
+    L.rd[I] = 1.0 / dsum;
+    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(1.0 / dsum); }
+}
+
+// level-0 diagonal inverse and the FP32 copies the mixed form needs
+__global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const int i = t.first + (int)threadIdx.x;
+    if (i >= t.last) return;
+    const double ap = C.ap[i];
+    C.rap[i] = 1.0 / ap;
+    if (C.precision == 1) {
+        C.fdiag[i] = (float)ap;
+        C.frap[i] = (float)(1.0 / ap);
+        for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = (float)C.anb[k * C.ne + i];
+    }
+}
+
+// Dense inverse of A_L + c 11^T at each case's coarsest level (one CTA per
+// case, Gauss-Jordan in shared memory; the matrix is SPD, no pivoting).
+__global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restrict__ cases, int ncases) {
+    const int c = blockIdx.x;
+    if (c >= ncases) return;
+    const CaseDev &C = cases[c];
+    if (C.precond != 1) return;
+    __shared__ double M[kAmgCoarsest * kAmgCoarsest];
+    __shared__ double piv;
+    const LP<double> P = level<double>(C, C.nlev);
+    const int n = P.n;
+    if (n > kAmgCoarsest) return;   // cannot happen: the builder coarsens to <= kAmgCoarsest
+    double dmax = 0.0;
+    for (int i = 0; i < n; i++) dmax = fmax(dmax, fabs(P.dg[i]));
+    const double cc = dmax > 0.0 ? dmax / n : 1.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        double v = cc + (i == j ? P.dg[i] : 0.0);
+        M[e] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        for (int k = 0; k < P.W; k++) {
+            const int j = P.nb[k * n + e];
+            if (j >= 0 && j < n) M[e * n + j] -= P.a[k * n + e];
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        if (threadIdx.x == 0) piv = M[k * n + k];
+        __syncthreads();
+        const double p = piv;
+        // scale row k
+        for (int j = threadIdx.x; j < n; j += blockDim.x) M[k * n + j] = (j == k ? 1.0 : M[k * n + j]) / p;
+        __syncthreads();
+        // eliminate column k from the other rows
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const int i = e / n, j = e % n;
+            if (i == k) continue;
+            const double f = M[i * n + k];
+            if (j == k) continue;
+            M[e] -= f * M[k * n + j];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            if (i != k) M[i * n + k] = -M[i * n + k] * M[k * n + k];
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        C.cinv[e] = M[e];
+        if (C.precision == 1) C.cinv32[e] = (float)M[e];
+    }
+}
+
+// ------------------------------------------------------------ V-cycle
+// t = w D^-1 r
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int i = tl.first + (int)threadIdx.x;
+    if (i >= tl.last) return;
+    const LP<T> P = level<T>(C, l);
+    P.t[i] = (T)kOmega * P.rd[i] * P.r[i];
+}
+
+// z = t + w D^-1 (r - A t)
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int i = tl.first + (int)threadIdx.x;
+    if (i >= tl.last) return;
+    const LP<T> P = level<T>(C, l);
+    P.z[i] = P.t[i] + (T)kOmega * P.rd[i] * (P.r[i] - amul<T>(P, P.t, i));
+}
+
+// t = r - A z (the smoothed residual, one thread per cell, coalesced)
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int i = tl.first + (int)threadIdx.x;
+    if (i >= tl.last) return;
+    const LP<T> P = level<T>(C, l);
+    P.t[i] = P.r[i] - amul<T>(P, P.z, i);
+}
+
+// r_{l+1}[I] = sum of the residual t_l over the members of aggregate I
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int I = tl.first + (int)threadIdx.x;
+    if (I >= tl.last) return;
+    const AmgLevelDev &L = C.lev[l1 - 1];
+    const LP<T> F = level<T>(C, l1 - 1);
+    T s = 0;
+    for (int m = L.mem_ptr[I]; m < L.mem_ptr[I + 1]; m++) s += F.t[L.mem[m]];
+    T *rc = sizeof(T) == 8 ? (T *)L.r : (T *)L.r32;
+    rc[I] = s;
+}
+
+// coarsest: z_L = Minv r_L (one CTA per case)
+template <class T>
+__global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ cases, int ncases) {
+    const int c = blockIdx.x;
+    if (c >= ncases) return;
+    const CaseDev &C = cases[c];
+    if (C.precond != 1 || (sizeof(T) == 8 ? !pactive(C) : !mactive(C))) return;
+    const LP<T> P = level<T>(C, C.nlev);
+    const T *Mi = sizeof(T) == 8 ? (const T *)C.cinv : (const T *)C.cinv32;
+    const int n = P.n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        T s = 0;
+        for (int j = 0; j < n; j++) s += Mi[i * n + j] * P.r[j];
+        P.z[i] = s;
+    }
+}
+
+// t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly)
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int i = tl.first + (int)threadIdx.x;
+    if (i >= tl.last) return;
+    const LP<T> P = level<T>(C, l);
+    const AmgLevelDev &L = C.lev[l];
+    const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
+    const T sc = (T)kOverCorrect;
+    const T xi = P.z[i] + sc * zc[L.agg[i]];
+    T s = P.dg[i] * xi;
+    for (int k = 0; k < P.W; k++) {
+        const int j = P.nb[k * P.n + i];
+        if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
+    }
+    P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - s);
+}
+
+// ------------------------------------------------------------ CG (FP64)
+// r = b - mean, x = 0; ||r0||
+__global__ void __launch_bounds__(kTile) k_apc_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    double v[2] = {0, 0};
+    FOR_CELLS(t) {
+        const double r = C.b[i] - S->mean_b;
+        C.kr[i] = r; C.phic[i] = 0.0;
+        v[0] += r * r; v[1] += C.b[i] * C.b[i];
+    }
+    block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A0], cnt[t.c])) {
+        __shared__ double s[2];
+        sum_partials<2>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            S->r0norm_p = S->rnorm_p = sqrt(s[0]);
+            S->mass_imbalance = sqrt(s[1]);
+            S->iters_p = 0; S->status_p = 0; S->rz = 0.0;
+            S->tol_p = (C.solve_mode == 0 ? C.rtol_p : C.tight_rtol) * S->r0norm_p;
+            S->active_p = S->r0norm_p > S->tol_p && cap > 0;
+            if (!isfinite(S->r0norm_p)) { S->active_p = 0; S->status_p = CFDL_ERR_NONFINITE; }
+        }
+    }
+}
+
+// beta = (r,z)/(r,z)_old (0 on the first iteration)
+__global__ void __launch_bounds__(kTile) k_apc_rz(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    double v[1] = {0.0};
+    FOR_CELLS(t) v[0] += C.kr[i] * C.ks[i];
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A1], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            S->beta_p = S->iters_p == 0 || S->rz == 0.0 ? 0.0 : s[0] / S->rz;
+            S->rz = s[0];
+            if (!isfinite(s[0])) { S->active_p = 0; S->status_p = CFDL_ERR_NONFINITE; }
+        }
+    }
+}
+
+// p = z + beta p; q = A p needs every p, so it is the next kernel
+__global__ void __launch_bounds__(kTile) k_apc_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    FOR_CELLS(t) C.kp[i] = S->iters_p == 0 ? C.ks[i] : C.ks[i] + S->beta_p * C.kp[i];
+}
+
+// q = A p; alpha = rz / (p, q)
+__global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    double v[1] = {0};
+    FOR_CELLS(t) {
+        const LP<double> P = level<double>(C, 0);
+        const double q = amul<double>(P, C.kp, i);
+        C.kv[i] = q;
+        v[0] += C.kp[i] * q;
+    }
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            if (!(s[0] > 0.0) || !isfinite(s[0])) { S->active_p = 0; if (!isfinite(s[0])) S->status_p = CFDL_ERR_NONFINITE; }
+            else S->alpha_p = S->rz / s[0];
+        }
+    }
+}
+
+// x += alpha p; r -= alpha q; ||r||
+__global__ void __launch_bounds__(kTile) k_apc_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    double v[1] = {0};
+    FOR_CELLS(t) {
+        const double a = S->alpha_p;
+        C.phic[i] = C.phic[i] + a * C.kp[i];
+        const double r = C.kr[i] - a * C.kv[i];
+        C.kr[i] = r;
+        v[0] += r * r;
+    }
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A3], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            const double rn = sqrt(s[0]);
+            S->rnorm_p = rn;
+            S->iters_p += 1;
+            int act = rn > S->tol_p;
+            if (!isfinite(rn)) { act = 0; S->status_p = CFDL_ERR_NONFINITE; }
+            else if (act && S->iters_p >= cap) { act = 0; if (C.solve_mode == 1) S->status_p = CFDL_ERR_ITER_CAP; }
+            S->active_p = act;
+        }
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+namespace {
+
+template <class T> int dupload(HostCase *hc, T **d, const std::vector<T> &h) {
+    size_t bytes = std::max<size_t>(1, h.size()) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)d, bytes);
+    if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+    hc->amg_allocs.push_back(*d);
+    if (h.empty()) return CFDL_OK;
+    return cuda_status(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+template <class T> int dzeros(HostCase *hc, T **d, size_t n) {
+    cudaError_t e = cudaMalloc((void **)d, std::max<size_t>(1, n) * sizeof(T));
+    if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
+    hc->amg_allocs.push_back(*d);
+    return cuda_status(cudaMemset(*d, 0, std::max<size_t>(1, n) * sizeof(T)));
+}
+
+// Build and upload the hierarchy of one case (mesh-only, once).
+int build_case_amg(HostCase *hc) {
+    if (hc->amg) return CFDL_OK;
+    CaseDev &d = hc->dev;
+    const int ne = hc->ne, W = hc->W, nf = hc->nf;
+    // strength = area/(dr.n) per interior slot, read back from the device planes
+    std::vector<int> nb((size_t)W * ne), fc((size_t)W * ne);
+    std::vector<double> adn(nf);
+    int st;
+    if ((st = cuda_status(cudaMemcpy(nb.data(), d.hf_nb, nb.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
+    if ((st = cuda_status(cudaMemcpy(fc.data(), d.hf_fc, fc.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
+    if ((st = cuda_status(cudaMemcpy(adn.data(), d.fgeo + (size_t)FG_ADN * nf, nf * sizeof(double), cudaMemcpyDeviceToHost)))) return st;
+    std::vector<double> strength((size_t)W * ne, 0.0);
+    for (size_t s = 0; s < nb.size(); s++) {
+        if (nb[s] < 0 || nb[s] >= ne) { nb[s] = -1; continue; }
+        int f = fc[s] >= 0 ? fc[s] : ~fc[s];
+        strength[s] = std::fabs(adn[f]);
+    }
+    AmgHierarchy *H = new AmgHierarchy;
+    AmgFineView fv{ne, W, nb.data(), strength.data()};
+    if ((st = build_amg_hierarchy(fv, *H))) { delete H; return st; }
+    hc->amg = H;
+    const int nlev = (int)H->levels.size();
+    std::vector<AmgLevelDev> devl(nlev);
+    for (int l = 0; l < nlev; l++) {
+        const AmgHostLevel &L = H->levels[l];
+        AmgLevelDev &D = devl[l];
+        D.n = L.n; D.W = L.W; D.n_fine = L.n_fine; D.W_fine = L.W_fine;
+        if ((st = dupload(hc, (int **)&D.nb, L.nb))) return st;
+        if ((st = dupload(hc, (int **)&D.agg, L.agg))) return st;
+        if ((st = dupload(hc, (int **)&D.mem_ptr, L.mem_ptr))) return st;
+        if ((st = dupload(hc, (int **)&D.mem, L.mem))) return st;
+        if ((st = dupload(hc, (int **)&D.g_ptr, L.g_ptr))) return st;
+        if ((st = dupload(hc, (int **)&D.g_src, L.g_src))) return st;
+        if ((st = dupload(hc, (int **)&D.d_ptr, L.d_ptr))) return st;
+        if ((st = dupload(hc, (int **)&D.d_src, L.d_src))) return st;
+        if ((st = dzeros(hc, &D.a, (size_t)L.W * L.n))) return st;
+        if ((st = dzeros(hc, &D.a32, (size_t)L.W * L.n))) return st;
+        double **v64[] = {&D.dg, &D.rd, &D.r, &D.z, &D.t};
+        for (double **p : v64) if ((st = dzeros(hc, p, (size_t)L.n))) return st;
+        float **v32[] = {&D.dg32, &D.rd32, &D.r32, &D.z32, &D.t32};
+        for (float **p : v32) if ((st = dzeros(hc, p, (size_t)L.n))) return st;
+    }
+    AmgLevelDev *dlev = nullptr;
+    if ((st = dupload(hc, &dlev, devl))) return st;
+    const int ncoarse = nlev ? H->levels.back().n : ne;
+    if (ncoarse > kAmgCoarsest) return CFDL_ERR_MESH;
+    if ((st = dzeros(hc, &d.cinv, (size_t)ncoarse * ncoarse))) return st;
+    if ((st = dzeros(hc, &d.cinv32, (size_t)ncoarse * ncoarse))) return st;
+    d.nlev = nlev;
+    d.ncoarse = ncoarse;
+    d.lev = dlev;
+    return CFDL_OK;
+}
+
+}  // namespace
+
+int ensure_amg(cfdl_ctx *ctx) {
+    bool changed = false;
+    for (HostCase *hc : ctx->cases) {
+        if (!hc->amg) {
+            int st = build_case_amg(hc);
+            if (st) return st;
+            changed = true;
+        }
+    }
+    if (!changed && ctx->amg_lmax >= 0) return CFDL_OK;
+    int lmax = 0;
+    for (HostCase *hc : ctx->cases) lmax = std::max(lmax, hc->dev.nlev);
+    for (auto &wl : ctx->amg_cells) free_worklist(wl);
+    for (auto &wl : ctx->amg_smooth) free_worklist(wl);
+    ctx->amg_cells.assign(lmax + 1, WorkList());
+    ctx->amg_smooth.assign(lmax + 1, WorkList());
+    for (int l = 0; l <= lmax; l++) {
+        std::vector<int> cells, smooth;
+        for (HostCase *hc : ctx->cases) {
+            int n = l == 0 ? hc->ne : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].n : 0);
+            cells.push_back(l <= hc->dev.nlev ? n : 0);
+            smooth.push_back(l < hc->dev.nlev ? n : 0);
+        }
+        int st;
+        if ((st = build_worklist(ctx, ctx->amg_cells[l], cells))) return st;
+        if ((st = build_worklist(ctx, ctx->amg_smooth[l], smooth))) return st;
+    }
+    ctx->amg_lmax = lmax;
+    return upload_case_table(ctx);
+}
+
+#define ALAUNCH(name, kern, WL, ...)                                                                 \
+    do {                                                                                             \
+        if ((WL).ntiles > 0) {                                                                       \
+            const bool p_ = ctx->prof && prof_wants(ctx, name);                                      \
+            if (p_) prof_begin(ctx, name);                                                           \
+            kern<<<(WL).ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, (WL).d_tiles, ##__VA_ARGS__); \
+            if (p_) prof_end(ctx);                                                                   \
+            ctx->launches++;                                                                         \
+        }                                                                                            \
+    } while (0)
+#define CLAUNCH(name, kern, threads)                                                                 \
+    do {                                                                                             \
+        const int nc_ = (int)ctx->cases.size();                                                      \
+        const bool p_ = ctx->prof && prof_wants(ctx, name);                                          \
+        if (p_) prof_begin(ctx, name);                                                               \
+        kern<<<nc_, threads, 0, ctx->stream>>>(ctx->d_cases, nc_);                                   \
+        if (p_) prof_end(ctx);                                                                       \
+        ctx->launches++;                                                                             \
+    } while (0)
+
+// Coarse operators of every level and the coarsest inverse.
+static void amg_setup_operators(cfdl_ctx *ctx) {
+    ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
+    for (int l = 1; l <= ctx->amg_lmax; l++) ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+    CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, 256);
+}
+
+// One V-cycle z_0 = M^-1 r_0 on every active case.
+template <class T> static void vcycle(cfdl_ctx *ctx) {
+    const int L = ctx->amg_lmax;
+    for (int l = 0; l < L; l++) {
+        ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
+        ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+        ALAUNCH(l ? "k_v_resid_c" : "k_v_resid_f", k_v_resid<T>, ctx->amg_smooth[l], l);
+        ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_cells[l + 1], l + 1);
+    }
+    CLAUNCH("k_v_coarse", k_v_coarse<T>, 256);
+    for (int l = L - 1; l >= 0; l--) {
+        ALAUNCH(l ? "k_v_prolong_c" : "k_v_prolong_f", k_v_prolong<T>, ctx->amg_smooth[l], l);
+        ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+    }
+}
+
+void launch_pc_mean(cfdl_ctx *ctx);
+
+int solve_pressure_amg(cfdl_ctx *ctx) {
+    int st = ensure_amg(ctx);
+    if (st) return st;
+#define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
+    amg_setup_operators(ctx);
+    launch_pc_mean(ctx);
+    ALAUNCH("k_apc_init", k_apc_init, ctx->cellsv, RED);
+    int cap = 0;
+    for (auto *hc : ctx->cases) cap = std::max(cap, hc->cfg.solve_mode == 0 ? hc->cfg.nit : hc->cfg.tight_maxit);
+    int it = 0, maxit = 0;
+    while (it < cap) {
+        const int chunk = poll_chunk(it, ctx->last_iters_p);
+        for (int k = 0; k < chunk && it < cap; k++, it++) {
+            vcycle<double>(ctx);
+            ALAUNCH("k_apc_rz", k_apc_rz, ctx->cellsv, RED);
+            ALAUNCH("k_apc_p", k_apc_p, ctx->cellsv);
+            ALAUNCH("k_apc_q", k_apc_q, ctx->cellsv, RED);
+            ALAUNCH("k_apc_x", k_apc_x, ctx->cellsv, RED);
+        }
+        int a = poll_kind(ctx, 1, &maxit);
+        if (a < 0) return CFDL_ERR_CUDA;
+        if (a == 0) break;
+    }
+    ctx->last_iters_p = maxit;
+#undef RED
+    return cuda_status(cudaGetLastError());
+}
+
+
+// ------------------------------------------------------------------------
+// Mixed precision: FP64 outer residual and refinement around an FP32 inner
+// PCG (FP32 SpMV, preconditioner, vectors and dot-product accumulation).
+// ------------------------------------------------------------------------
+namespace {
+
+enum { CNT_M0 = 15 };   // shares the last counter slot only with itself
+
+// outer start: r64 = b - mean, x = 0
+__global__ void __launch_bounds__(kTile) k_mx_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    double v[2] = {0, 0};
+    FOR_CELLS(t) {
+        const double r = C.b[i] - S->mean_b;
+        C.kr[i] = r; C.phic[i] = 0.0;
+        v[0] += r * r; v[1] += C.b[i] * C.b[i];
+    }
+    block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A0], cnt[t.c])) {
+        __shared__ double s[2];
+        sum_partials<2>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            S->r0norm_p = S->rnorm_p = sqrt(s[0]);
+            S->mass_imbalance = sqrt(s[1]);
+            S->iters_p = 0; S->status_p = 0; S->outer_p = 0;
+            S->tol_p = (C.solve_mode == 0 ? C.rtol_p : C.tight_rtol) * S->r0norm_p;
+            S->active_p = S->r0norm_p > S->tol_p && (C.solve_mode == 0 ? C.nit : C.tight_maxit) > 0;
+            if (!isfinite(S->r0norm_p)) { S->active_p = 0; S->status_p = CFDL_ERR_NONFINITE; }
+        }
+    }
+}
+
+// inner start: fr = (float) r64, fx = 0; ||fr|| in FP32
+__global__ void __launch_bounds__(kTile) k_mx_start(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    float v[1] = {0.f};
+    FOR_CELLS(t) {
+        const float r = (float)C.kr[i];
+        C.fr[i] = r; C.fx[i] = 0.f;
+        v[0] += r * r;
+    }
+    block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A1], cnt[t.c])) {
+        __shared__ float s[1];
+        sum_partials<1, float>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const float rn = sqrtf(s[0]);
+            // inner tolerance: the reference's drop for mode 0, 1e-4 per refinement when tight
+            const float eps = C.solve_mode == 0 ? (float)C.rtol_p : 1e-4f;
+            S->rnorm32 = rn;
+            S->tol32 = eps * rn;
+            S->rz32 = 0.f;
+            S->iters32 = 0;
+            S->active32 = rn > 0.f && isfinite(rn);
+        }
+    }
+}
+
+// z = M^-1 r for the Jacobi preconditioner (the AMG form uses the V-cycle)
+__global__ void __launch_bounds__(kTile) k_mx_jacobi(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    if (!C.sc->active32) return;
+    FOR_CELLS(t) C.fz[i] = C.fr[i] * C.frap[i];
+}
+
+__global__ void __launch_bounds__(kTile) k_mx_rz(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active32) return;
+    float v[1] = {0.f};
+    FOR_CELLS(t) v[0] += C.fr[i] * C.fz[i];
+    block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
+        __shared__ float s[1];
+        sum_partials<1, float>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            S->beta32 = S->iters32 == 0 || S->rz32 == 0.f ? 0.f : s[0] / S->rz32;
+            S->rz32 = s[0];
+            if (!isfinite(s[0])) S->active32 = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_mx_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const SolveScalars *S = C.sc;
+    if (!S->active32) return;
+    FOR_CELLS(t) C.fp[i] = S->iters32 == 0 ? C.fz[i] : C.fz[i] + S->beta32 * C.fp[i];
+}
+
+__global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active32) return;
+    float v[1] = {0.f};
+    FOR_CELLS(t) {
+        const LP<float> P = level<float>(C, 0);
+        const float q = amul<float>(P, C.fp, i);
+        C.fq[i] = q;
+        v[0] += C.fp[i] * q;
+    }
+    block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A3], cnt[t.c])) {
+        __shared__ float s[1];
+        sum_partials<1, float>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            if (!(s[0] > 0.f) || !isfinite(s[0])) S->active32 = 0;
+            else S->alpha32 = S->rz32 / s[0];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTile) k_mx_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active32) return;
+    float v[1] = {0.f};
+    FOR_CELLS(t) {
+        const float a = S->alpha32;
+        C.fx[i] = C.fx[i] + a * C.fp[i];
+        const float r = C.fr[i] - a * C.fq[i];
+        C.fr[i] = r;
+        v[0] += r * r;
+    }
+    block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_A4], cnt[t.c])) {
+        __shared__ float s[1];
+        sum_partials<1, float>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const float rn = sqrtf(s[0]);
+            S->rnorm32 = rn;
+            S->iters32 += 1;
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            S->active32 = rn > S->tol32 && isfinite(rn) && S->iters32 < cap;
+        }
+    }
+}
+
+// x += (double) fx
+__global__ void __launch_bounds__(kTile) k_mx_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    if (!C.sc->active_p) return;
+    FOR_CELLS(t) C.phic[i] = C.phic[i] + (double)C.fx[i];
+}
+
+// FP64 true residual r = (b - mean) - A x and the outer stopping test
+__global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    SolveScalars *S = C.sc;
+    if (!S->active_p) return;
+    double v[1] = {0};
+    FOR_CELLS(t) {
+        const LP<double> P = level<double>(C, 0);
+        const double r = (C.b[i] - S->mean_b) - amul<double>(P, C.phic, i);
+        C.kr[i] = r;
+        v[0] += r * r;
+    }
+    block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M0], cnt[t.c])) {
+        __shared__ double s[1];
+        sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            const double rn = sqrt(s[0]);
+            S->rnorm_p = rn;
+            S->outer_p += 1;
+            S->iters_p += S->iters32;
+            int act = rn > S->tol_p;
+            if (!isfinite(rn)) { act = 0; S->status_p = CFDL_ERR_NONFINITE; }
+            else if (act && S->outer_p >= 60) { act = 0; if (C.solve_mode == 1) S->status_p = CFDL_ERR_ITER_CAP; }
+            S->active_p = act;
+        }
+    }
+}
+
+}  // namespace
+
+int solve_pressure_mixed(cfdl_ctx *ctx) {
+    const bool amg = ctx->cases[0]->cfg.precond == 1;
+    int st;
+    if (amg && (st = ensure_amg(ctx))) return st;
+#define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
+#define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
+    if (amg) amg_setup_operators(ctx);
+    else ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
+    launch_pc_mean(ctx);
+    ALAUNCH("k_mx_init", k_mx_init, ctx->cellsv, RED);
+    int cap = 0;
+    for (auto *hc : ctx->cases) cap = std::max(cap, hc->cfg.solve_mode == 0 ? hc->cfg.nit : hc->cfg.tight_maxit);
+    for (int outer = 0; outer < 60; outer++) {
+        ALAUNCH("k_mx_start", k_mx_start, ctx->cellsv, RED32);
+        int it = 0, maxit = 0;
+        while (it < cap) {
+            const int chunk = poll_chunk(it, ctx->last_iters_p);
+            for (int k = 0; k < chunk && it < cap; k++, it++) {
+                if (amg) vcycle<float>(ctx);
+                else ALAUNCH("k_mx_jacobi", k_mx_jacobi, ctx->cellsv);
+                ALAUNCH("k_mx_rz", k_mx_rz, ctx->cellsv, RED32);
+                ALAUNCH("k_mx_p", k_mx_p, ctx->cellsv);
+                ALAUNCH("k_mx_q", k_mx_q, ctx->cellsv, RED32);
+                ALAUNCH("k_mx_x", k_mx_x, ctx->cellsv, RED32);
+            }
+            int a = poll_kind(ctx, 2, &maxit);
+            if (a < 0) return CFDL_ERR_CUDA;
+            if (a == 0) break;
+        }
+        ctx->last_iters_p = maxit;
+        ALAUNCH("k_mx_apply", k_mx_apply, ctx->cellsv);
+        ALAUNCH("k_mx_res", k_mx_res, ctx->cellsv, RED);
+        int a = poll_kind(ctx, 3, nullptr);
+        if (a < 0) return CFDL_ERR_CUDA;
+        if (a == 0) break;
+    }
+#undef RED
+#undef RED32
+    return cuda_status(cudaGetLastError());
+}
+
+}  // namespace cfdl
+
+extern "C" int cfdl_amg_info(cfdl_ctx *ctx, int maxlev, int *nlev, int *n, int *W) {
+    using namespace cfdl;
+    if (!ctx || ctx->cases.empty() || !nlev || maxlev < 0) return CFDL_ERR_INVALID;
+    const HostCase *hc = ctx->cases[0];
+    const int L = hc->amg ? (int)hc->amg->levels.size() : 0;
+    *nlev = L;
+    for (int l = 0; l <= L && l <= maxlev; l++) {
+        if (n) n[l] = l == 0 ? hc->ne : hc->amg->levels[l - 1].n;
+        if (W) W[l] = l == 0 ? hc->W : hc->amg->levels[l - 1].W;
+    }
+    return CFDL_OK;
+}

@@ -213,7 +213,10 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (HostCase *hc : ctx->cases) destroy_case(hc);
     WorkList *wls[3] = {&ctx->cells, &ctx->faces, &ctx->halos};
-    for (WorkList *wl : wls) { cudaFree(wl->d_tiles); cudaFree(wl->d_case_first); cudaFree(wl->d_case_ntiles); }
+    for (WorkList *wl : wls) free_worklist(*wl);
+    free_worklist(ctx->cellsv);
+    for (auto &wl : ctx->amg_cells) free_worklist(wl);
+    for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     cudaFree(ctx->d_cases);
     cudaFree(ctx->d_partials);
     cudaFree(ctx->d_flags);

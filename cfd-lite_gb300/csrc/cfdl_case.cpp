@@ -13,6 +13,7 @@
 // per-half-face stencil A^-1 * (dr/|dr|^2), with A inverted by matinv3
 // (mod_solver.f90:8-38) including its trace fallback.
 #include "cfdl_internal.h"
+#include "cfdl_amg.h"
 #include <algorithm>
 #include <cmath>
 #include <cfloat>
@@ -20,6 +21,11 @@
 #include <new>
 
 namespace cfdl {
+
+void delete_amg(HostCase *hc) {
+    delete hc->amg;
+    hc->amg = nullptr;
+}
 
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return CFDL_OK;
@@ -40,7 +46,40 @@ int case_alloc(HostCase *hc, void **p, size_t bytes) {
 void destroy_case(HostCase *hc) {
     if (!hc) return;
     for (void *p : hc->allocs) cudaFree(p);
+    for (void *p : hc->amg_allocs) cudaFree(p);
+    delete_amg(hc);
     delete hc;
+}
+
+void free_worklist(WorkList &wl) {
+    cudaFree(wl.d_tiles); cudaFree(wl.d_case_first); cudaFree(wl.d_case_ntiles);
+    wl.d_tiles = nullptr; wl.d_case_first = nullptr; wl.d_case_ntiles = nullptr;
+    wl.ntiles = 0;
+}
+
+// Tile list over per-case entity counts (sizes[c] = 0 leaves case c out).
+int build_worklist(cfdl_ctx *ctx, WorkList &wl, const std::vector<int> &sizes, int tile) {
+    free_worklist(wl);
+    wl.h_tiles.clear(); wl.case_first.clear(); wl.case_ntiles.clear();
+    for (size_t c = 0; c < sizes.size(); c++) {
+        wl.case_first.push_back((int)wl.h_tiles.size());
+        int cnt = 0;
+        for (int s = 0; s < sizes[c]; s += tile, cnt++) wl.h_tiles.push_back({(int)c, s, std::min(sizes[c], s + tile), 0});
+        wl.case_ntiles.push_back(cnt);
+    }
+    wl.ntiles = (int)wl.h_tiles.size();
+    size_t nt = std::max<size_t>(1, wl.h_tiles.size()), ncs = std::max<size_t>(1, sizes.size());
+    int st;
+    if ((st = cuda_status(cudaMalloc(&wl.d_tiles, nt * sizeof(Tile))))) return st;
+    if ((st = cuda_status(cudaMalloc(&wl.d_case_first, ncs * sizeof(int))))) return st;
+    if ((st = cuda_status(cudaMalloc(&wl.d_case_ntiles, ncs * sizeof(int))))) return st;
+    if (!wl.h_tiles.empty()) {
+        if ((st = cuda_status(cudaMemcpy(wl.d_tiles, wl.h_tiles.data(), wl.h_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice)))) return st;
+        if ((st = cuda_status(cudaMemcpy(wl.d_case_first, wl.case_first.data(), wl.case_first.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
+        if ((st = cuda_status(cudaMemcpy(wl.d_case_ntiles, wl.case_ntiles.data(), wl.case_ntiles.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
+    }
+    (void)ctx;
+    return CFDL_OK;
 }
 
 void apply_config(HostCase *hc, const cfdl_config *cfg) {
@@ -50,6 +89,7 @@ void apply_config(HostCase *hc, const cfdl_config *cfg) {
     d.rtol_u = cfg->rtol_u; d.rtol_p = cfg->rtol_p; d.tight_rtol = cfg->tight_rtol;
     d.nit = cfg->nit; d.solve_mode = cfg->solve_mode; d.tight_maxit = cfg->tight_maxit;
     d.precision = cfg->precision;
+    d.precond = cfg->precond;
 }
 
 namespace {
@@ -131,9 +171,10 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
     if ((st = zeros(hc, &d.fD, 3 * (size_t)nf))) return st;
     double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt, &d.kb};
     for (double **pp : kv) if ((st = zeros(hc, pp, 3 * (size_t)ne))) return st;
-    float **fv[] = {&d.fr, &d.fz, &d.fp, &d.fq, &d.fx, &d.fdiag};
+    float **fv[] = {&d.fr, &d.fz, &d.fp, &d.fq, &d.fx, &d.fdiag, &d.ft, &d.frap};
     for (float **pp : fv) if ((st = zeros(hc, pp, (size_t)ne))) return st;
     if ((st = zeros(hc, &d.fanb, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.rap, (size_t)ne))) return st;
     if ((st = zeros(hc, &d.sc, 1))) return st;
     if ((st = zeros(hc, &d.counters, 16))) return st;
     std::vector<double> rho(ne, cfg->rho), mu(ne, cfg->mu);
@@ -288,32 +329,16 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
 
 // Tile work lists over every case of the context.
 int rebuild_worklists(cfdl_ctx *ctx) {
-    WorkList *wls[3] = {&ctx->cells, &ctx->faces, &ctx->halos};
-    for (int t = 0; t < 3; t++) {
-        WorkList &wl = *wls[t];
-        wl.h_tiles.clear(); wl.case_first.clear(); wl.case_ntiles.clear();
-        for (size_t c = 0; c < ctx->cases.size(); c++) {
-            const HostCase *hc = ctx->cases[c];
-            int n = t == 0 ? hc->ne : t == 1 ? hc->nf : hc->nbf;
-            wl.case_first.push_back((int)wl.h_tiles.size());
-            int cnt = 0;
-            for (int s = 0; s < n; s += kTile, cnt++) wl.h_tiles.push_back({(int)c, s, std::min(n, s + kTile), 0});
-            wl.case_ntiles.push_back(cnt);
-        }
-        wl.ntiles = (int)wl.h_tiles.size();
-        cudaFree(wl.d_tiles); cudaFree(wl.d_case_first); cudaFree(wl.d_case_ntiles);
-        wl.d_tiles = nullptr; wl.d_case_first = nullptr; wl.d_case_ntiles = nullptr;
-        size_t nt = std::max<size_t>(1, wl.h_tiles.size()), ncs = std::max<size_t>(1, ctx->cases.size());
-        int st;
-        if ((st = cuda_status(cudaMalloc(&wl.d_tiles, nt * sizeof(Tile))))) return st;
-        if ((st = cuda_status(cudaMalloc(&wl.d_case_first, ncs * sizeof(int))))) return st;
-        if ((st = cuda_status(cudaMalloc(&wl.d_case_ntiles, ncs * sizeof(int))))) return st;
-        if (!wl.h_tiles.empty()) {
-            if ((st = cuda_status(cudaMemcpy(wl.d_tiles, wl.h_tiles.data(), wl.h_tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice)))) return st;
-            if ((st = cuda_status(cudaMemcpy(wl.d_case_first, wl.case_first.data(), wl.case_first.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
-            if ((st = cuda_status(cudaMemcpy(wl.d_case_ntiles, wl.case_ntiles.data(), wl.case_ntiles.size() * sizeof(int), cudaMemcpyHostToDevice)))) return st;
-        }
-    }
+    std::vector<int> nc, nfc, nh;
+    for (const HostCase *hc : ctx->cases) { nc.push_back(hc->ne); nfc.push_back(hc->nf); nh.push_back(hc->nbf); }
+    int st;
+    if ((st = build_worklist(ctx, ctx->cells, nc))) return st;
+    if ((st = build_worklist(ctx, ctx->faces, nfc))) return st;
+    if ((st = build_worklist(ctx, ctx->halos, nh))) return st;
+    if ((st = build_worklist(ctx, ctx->cellsv, nc, kTile * kVec))) return st;
+    for (auto &wl : ctx->amg_cells) free_worklist(wl);
+    for (auto &wl : ctx->amg_smooth) free_worklist(wl);
+    ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_lmax = -1;
     int need = std::max({ctx->cells.ntiles, ctx->faces.ntiles, ctx->halos.ntiles, 1});
     if (need > ctx->partials_cap) {
         cudaFree(ctx->d_partials);

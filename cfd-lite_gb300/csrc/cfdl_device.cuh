@@ -7,9 +7,9 @@ namespace cfdl {
 // Deterministic block reduction of K doubles (kTile threads): a fixed
 // shuffle tree per warp, then warp partials summed in warp order by one
 // thread.  The result lands in out[0..K-1].
-template <int K>
-__device__ __forceinline__ void block_reduce(double (&v)[K], double *out) {
-    __shared__ double sm[K][kTile / 32];
+template <int K, class T = double>
+__device__ __forceinline__ void block_reduce(T (&v)[K], T *out) {
+    __shared__ T sm[K][kTile / 32];
 #pragma unroll
     for (int k = 0; k < K; k++)
 #pragma unroll
@@ -20,7 +20,7 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double *out) {
         for (int k = 0; k < K; k++) sm[k][wid] = v[k];
     __syncthreads();
     if (threadIdx.x < K) {
-        double s = 0.0;
+        T s = 0;
         for (int w = 0; w < kTile / 32; w++) s += sm[threadIdx.x][w];
         out[threadIdx.x] = s;
     }
@@ -29,17 +29,33 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double *out) {
 
 // Sum the K partials of tiles [first, first+n) in tile order (whole block),
 // result broadcast in shared memory res[0..K-1].
-template <int K>
-__device__ __forceinline__ void sum_partials(const double *partials, int first, int n, double *res) {
-    double v[K];
+template <int K, class T = double>
+__device__ __forceinline__ void sum_partials(const T *partials, int first, int n, T *res) {
+    T v[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) v[k] = 0.0;
-    // thread-strided in fixed order, then the fixed tree
-    for (int i = threadIdx.x; i < n; i += kTile)
+    for (int k = 0; k < K; k++) v[k] = 0;
+    // thread-strided in a fixed order with four independent accumulators (so
+    // the loads overlap instead of forming one dependent chain), then the
+    // fixed tree
+    T a1[K], a2[K], a3[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) a1[k] = a2[k] = a3[k] = 0;
+    int i = threadIdx.x;
+    for (; i + 3 * kTile < n; i += 4 * kTile)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            v[k] += __ldcg(&partials[(size_t)(first + i) * kNPart + k]);
+            a1[k] += __ldcg(&partials[(size_t)(first + i + kTile) * kNPart + k]);
+            a2[k] += __ldcg(&partials[(size_t)(first + i + 2 * kTile) * kNPart + k]);
+            a3[k] += __ldcg(&partials[(size_t)(first + i + 3 * kTile) * kNPart + k]);
+        }
+    for (; i < n; i += kTile)
 #pragma unroll
         for (int k = 0; k < K; k++) v[k] += __ldcg(&partials[(size_t)(first + i) * kNPart + k]);
-    __shared__ double tmp[K];
-    block_reduce<K>(v, tmp);
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = (v[k] + a1[k]) + (a2[k] + a3[k]);
+    __shared__ T tmp[K];
+    block_reduce<K, T>(v, tmp);
     if (threadIdx.x < K) res[threadIdx.x] = tmp[threadIdx.x];
     __syncthreads();
 }

@@ -31,6 +31,12 @@ namespace cfdl {
 constexpr int kTile = 256;        // cells / faces / halos per CTA
 constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
 constexpr int kNPart = 16;        // partial slots per tile
+constexpr int kVec = 4;           // cells per thread in the solver kernels (tile = kTile*kVec cells)
+
+// Loop over the cells of a wide solver tile: thread t handles cells
+// first+t, first+t+kTile, ... (coalesced, kVec of them).
+#define FOR_CELLS(t) \
+    for (int j_ = 0, i = (t).first + (int)threadIdx.x; j_ < cfdl::kVec; j_++, i += cfdl::kTile) if (i < (t).last)
 
 // face geometry planes, precomputed once per mesh (cfdl_case.cpp)
 enum FaceGeo {
@@ -44,6 +50,9 @@ enum FaceGeo {
     FG_EX, FG_EY, FG_EZ,        // area * (dr_p/ds_p - dr/ds)
     FG_N
 };
+
+struct AmgLevelDev;
+struct AmgHierarchy;
 
 // Per-case solver state on the device.
 struct SolveScalars {
@@ -85,11 +94,18 @@ struct CaseDev {
     double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt, *kb;
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each
     float *fr, *fz, *fp, *fq, *fx, *fdiag, *fanb;   // fanb ELL [W][ne]
+    float *ft, *frap;
+    // pressure preconditioner: 1/ap of the pressure operator, AMG levels, coarsest inverse
+    double *rap;
+    int nlev, ncoarse;                    // coarse levels; cells of the coarsest level
+    const AmgLevelDev *lev;               // [nlev] device array
+    double *cinv;                         // [ncoarse^2] dense inverse of the coarsest operator
+    float *cinv32;
     SolveScalars *sc;
     int *counters;                        // [16] last-tile counters, zero between launches
     // parameters
     double dt, alpha_u, alpha_p, rtol_u, rtol_p, tight_rtol;
-    int nit, solve_mode, tight_maxit, precision;
+    int nit, solve_mode, tight_maxit, precision, precond;
 };
 
 struct Tile { int c, first, last, pad; };
@@ -110,6 +126,8 @@ struct HostCase {
     std::vector<int> ef2nb_idx;      // [ne+1], 1-based values
     std::vector<void *> allocs;      // device allocations owned by the case
     CaseDev dev{};                   // host mirror of the device struct
+    AmgHierarchy *amg = nullptr;     // host hierarchy, built on first AMG use
+    std::vector<void *> amg_allocs;  // device allocations of the hierarchy
 };
 
 }  // namespace cfdl
@@ -122,6 +140,8 @@ struct cfdl_ctx {
     cfdl::CaseDev *d_cases = nullptr;
     int d_cases_cap = 0;
     cfdl::WorkList cells, faces, halos;
+    cfdl::WorkList cellsv;               // wide tiles (kTile*kVec cells) for the solver kernels
+    int last_iters_m = 0, last_iters_p = 0;   // previous inner iteration counts (poll scheduling)
     double *d_partials = nullptr;        // [max tiles][kNPart]
     int partials_cap = 0;                // tiles
     int64_t launches = 0;
@@ -131,6 +151,10 @@ struct cfdl_ctx {
     int h_flags_cap = 0;
     int *d_flags = nullptr;
     void *prof = nullptr;                // event profiler state (cfdl_prof.cpp)
+    // AMG work lists: amg_cells[l] = level-l cells of cases with nlev >= l,
+    // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
+    std::vector<cfdl::WorkList> amg_cells, amg_smooth;
+    int amg_lmax = -1;
 };
 
 namespace cfdl {
@@ -175,7 +199,15 @@ void prof_destroy(cfdl_ctx *ctx);
 // solvers (cfdl_solvers.cu)
 int solve_momentum(cfdl_ctx *ctx);
 int solve_pressure(cfdl_ctx *ctx);
+// AMG-preconditioned pressure solve (cfdl_amg.cu)
+int ensure_amg(cfdl_ctx *ctx);
+int solve_pressure_amg(cfdl_ctx *ctx);
+int solve_pressure_mixed(cfdl_ctx *ctx);
+void free_worklist(WorkList &wl);
+int build_worklist(cfdl_ctx *ctx, WorkList &wl, const std::vector<int> &sizes, int tile = kTile);
 int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st);
+int poll_kind(cfdl_ctx *ctx, int kind, int *maxit);
+int poll_chunk(int done, int expected);
 
 // one outer iteration for every case of the context (cfdl_api.cpp)
 int solve_uvwp_all(cfdl_ctx *ctx);

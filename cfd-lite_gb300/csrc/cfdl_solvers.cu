@@ -51,9 +51,8 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
     const Tile t = tiles[blockIdx.x];                         \
     const CaseDev &C = cases[t.c];                            \
     SolveScalars *S = C.sc;                                   \
-    const int i = t.first + (int)threadIdx.x, ne = C.ne;      \
-    const bool in = i < t.last;                               \
-    (void)ne; (void)in;
+    const int ne = C.ne;                                      \
+    (void)ne;
 
 // ------------------------------ momentum ----------------------------------
 // init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0
@@ -61,7 +60,7 @@ __global__ void __launch_bounds__(kTile) k_mom_init(const CaseDev *__restrict__ 
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             const double *phi = comp_field(C, q);
@@ -82,8 +81,8 @@ __global__ void __launch_bounds__(kTile) k_mom_init(const CaseDev *__restrict__ 
             C.krh[q * ne + i] = r;
             C.kp[q * ne + i] = 0.0;
             C.kv[q * ne + i] = 0.0;
-            v[q] = bb * bb;
-            v[3 + q] = r * r;
+            v[q] += bb * bb;
+            v[3 + q] += r * r;
         }
     }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -109,15 +108,17 @@ __global__ void __launch_bounds__(kTile) k_mom_init(const CaseDev *__restrict__ 
 // p = r + beta (p - omega v); ph = p / ap
 __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
-    if (!any_active(S) || !in) return;
-    const double rap = 1.0 / C.ap[i];
+    if (!any_active(S)) return;
+    FOR_CELLS(t) {
+        const double rap = 1.0 / C.ap[i];
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-        if (!S->active[q]) continue;
-        const int j = q * ne + i;
-        const double pn = S->iters[q] == 0 ? C.kr[j] : C.kr[j] + S->beta[q] * (C.kp[j] - S->omega[q] * C.kv[j]);
-        C.kp[j] = pn;
-        C.kph[j] = pn * rap;
+        for (int q = 0; q < 3; q++) {
+            if (!S->active[q]) continue;
+            const int j = q * ne + i;
+            const double pn = S->iters[q] == 0 ? C.kr[j] : C.kr[j] + S->beta[q] * (C.kp[j] - S->omega[q] * C.kv[j]);
+            C.kp[j] = pn;
+            C.kph[j] = pn * rap;
+        }
     }
 }
 
@@ -127,13 +128,13 @@ __global__ void __launch_bounds__(kTile) k_mom_v(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[3] = {0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!S->active[q]) continue;
             const double y = amul_row(C, C.kph + q * ne, i);
             C.kv[q * ne + i] = y;
-            v[q] = C.krh[q * ne + i] * y;
+            v[q] += C.krh[q * ne + i] * y;
         }
     }
     block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[3] = {0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
         const double rap = 1.0 / C.ap[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
             const double sv = C.kr[j] - S->alpha[q] * C.kv[j];
             C.ks[j] = sv;
             C.ksh[j] = sv * rap;
-            v[q] = sv * sv;
+            v[q] += sv * sv;
         }
     }
     block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -186,15 +187,15 @@ __global__ void __launch_bounds__(kTile) k_mom_t(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[6] = {0, 0, 0, 0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!S->active[q] || S->half[q]) continue;
             const int j = q * ne + i;
             const double y = amul_row(C, C.ksh + q * ne, i);
             C.kt[j] = y;
-            v[q] = y * C.ks[j];
-            v[3 + q] = y * y;
+            v[q] += y * C.ks[j];
+            v[3 + q] += y * y;
         }
     }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(kTile) k_mom_x(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[6] = {0, 0, 0, 0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!S->active[q]) continue;
@@ -225,8 +226,8 @@ __global__ void __launch_bounds__(kTile) k_mom_x(const CaseDev *__restrict__ cas
             x[i] = x[i] + S->alpha[q] * C.kph[j] + om * C.ksh[j];
             const double r = om == 0.0 ? C.ks[j] : C.ks[j] - om * C.kt[j];
             C.kr[j] = r;
-            v[q] = r * r;
-            v[3 + q] = C.krh[j] * r;
+            v[q] += r * r;
+            v[3 + q] += C.krh[j] * r;
         }
     }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -258,7 +259,8 @@ __global__ void __launch_bounds__(kTile) k_mom_x(const CaseDev *__restrict__ cas
 __global__ void __launch_bounds__(kTile) k_pc_mean(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
-    double v[1] = {in ? C.b[i] : 0.0};
+    double v[1] = {0.0};
+    FOR_CELLS(t) v[0] += C.b[i];
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_P0], cnt[t.c])) {
         __shared__ double s[1];
@@ -272,10 +274,10 @@ __global__ void __launch_bounds__(kTile) k_pc_init(const CaseDev *__restrict__ c
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[3] = {0, 0, 0};
-    if (in) {
+    FOR_CELLS(t) {
         const double r = C.b[i] - S->mean_b, z = r / C.ap[i];
         C.kr[i] = r; C.ks[i] = z; C.kp[i] = z; C.phic[i] = 0.0;
-        v[0] = r * r; v[1] = r * z; v[2] = C.b[i] * C.b[i];
+        v[0] += r * r; v[1] += r * z; v[2] += C.b[i] * C.b[i];
     }
     block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_P1], cnt[t.c])) {
@@ -300,10 +302,10 @@ __global__ void __launch_bounds__(kTile) k_pc_q(const CaseDev *__restrict__ case
     TILE_HEAD
     if (!S->active_p) return;
     double v[1] = {0};
-    if (in) {
+    FOR_CELLS(t) {
         const double q = amul_row(C, C.kp, i);
         C.kv[i] = q;
-        v[0] = C.kp[i] * q;
+        v[0] += C.kp[i] * q;
     }
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_P2], cnt[t.c])) {
@@ -322,12 +324,12 @@ __global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ case
     TILE_HEAD
     if (!S->active_p) return;
     double v[2] = {0, 0};
-    if (in) {
+    FOR_CELLS(t) {
         const double a = S->alpha_p;
         C.phic[i] = C.phic[i] + a * C.kp[i];
         const double r = C.kr[i] - a * C.kv[i], z = r / C.ap[i];
         C.kr[i] = r; C.ks[i] = z;
-        v[0] = r * r; v[1] = r * z;
+        v[0] += r * r; v[1] += r * z;
     }
     block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_P3], cnt[t.c])) {
@@ -351,31 +353,51 @@ __global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ case
 // p = z + beta p
 __global__ void __launch_bounds__(kTile) k_pc_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
-    if (!S->active_p || !in) return;
-    C.kp[i] = C.ks[i] + S->beta_p * C.kp[i];
+    if (!S->active_p) return;
+    FOR_CELLS(t) C.kp[i] = C.ks[i] + S->beta_p * C.kp[i];
 }
 
-// per-case activity flags for the host poll: bit0 momentum, bit1 pressure
-__global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags) {
+// Per-case activity flag and iteration count for the host poll.
+// kind 0 momentum, 1 pressure CG, 2 mixed inner CG, 3 mixed outer refinement.
+__global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags, int kind) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncases) return;
     const SolveScalars *S = cases[c].sc;
-    flags[c] = (any_active(S) ? 1 : 0) | (S->active_p ? 2 : 0);
+    int act = 0, its = 0;
+    if (kind == 0) { act = any_active(S); its = max(S->iters[0], max(S->iters[1], S->iters[2])); }
+    else if (kind == 1) { act = S->active_p; its = S->iters_p; }
+    else if (kind == 2) { act = S->active32; its = S->iters32; }
+    else { act = S->active_p; its = S->outer_p; }
+    flags[2 * c] = act != 0;
+    flags[2 * c + 1] = its;
 }
 
 }  // namespace
 
-#define RED ctx->cells.d_case_first, ctx->cells.d_case_ntiles, ctx->d_partials
+#define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
 
-static int poll(cfdl_ctx *ctx, int mask) {
+// Returns 1 if any case is still active, 0 if none, -1 on error; *maxit =
+// the largest iteration count over the cases.
+int poll_kind(cfdl_ctx *ctx, int kind, int *maxit) {
     const int n = (int)ctx->cases.size();
-    k_poll<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_cases, n, ctx->d_flags);
+    k_poll<<<(n + 127) / 128, 128, 0, ctx->stream>>>(ctx->d_cases, n, ctx->d_flags, kind);
     ctx->launches++;
-    cudaError_t e = cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, 2 * n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return -1;
-    for (int c = 0; c < n; c++) if (ctx->h_flags[c] & mask) return 1;
-    return 0;
+    int any = 0, m = 0;
+    for (int c = 0; c < n; c++) { any |= ctx->h_flags[2 * c]; m = std::max(m, ctx->h_flags[2 * c + 1]); }
+    if (maxit) *maxit = m;
+    return any;
+}
+
+// Iterations to issue before the next poll: first up to just short of the
+// previous solve's count (consecutive outer iterations need similar counts),
+// then one at a time.  Converged cases are frozen on the device, so the
+// schedule changes only the number of idle launches, never the result.
+int poll_chunk(int done, int expected) {
+    if (done == 0) return std::max(1, expected - 1);
+    return 1;
 }
 
 static int max_cap(cfdl_ctx *ctx) {
@@ -386,42 +408,48 @@ static int max_cap(cfdl_ctx *ctx) {
 
 int solve_momentum(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    CFDL_LAUNCH("k_mom_init", k_mom_init, cells, RED);
+    CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED);
     const int cap = max_cap(ctx);
-    int it = 0, chunk = 2;
+    int it = 0, maxit = 0;
     while (it < cap) {
+        const int chunk = poll_chunk(it, ctx->last_iters_m);
         for (int k = 0; k < chunk && it < cap; k++, it++) {
-            CFDL_LAUNCH("k_mom_p", k_mom_p, cells);
-            CFDL_LAUNCH("k_mom_v", k_mom_v, cells, RED);
-            CFDL_LAUNCH("k_mom_s", k_mom_s, cells, RED);
-            CFDL_LAUNCH("k_mom_t", k_mom_t, cells, RED);
-            CFDL_LAUNCH("k_mom_x", k_mom_x, cells, RED);
+            CFDL_LAUNCH("k_mom_p", k_mom_p, cellsv);
+            CFDL_LAUNCH("k_mom_v", k_mom_v, cellsv, RED);
+            CFDL_LAUNCH("k_mom_s", k_mom_s, cellsv, RED);
+            CFDL_LAUNCH("k_mom_t", k_mom_t, cellsv, RED);
+            CFDL_LAUNCH("k_mom_x", k_mom_x, cellsv, RED);
         }
-        int a = poll(ctx, 1);
+        int a = poll_kind(ctx, 0, &maxit);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;
-        chunk = std::min(chunk * 2, 16);
     }
+    ctx->last_iters_m = maxit;
     return cuda_status(cudaGetLastError());
 }
 
+void launch_pc_mean(cfdl_ctx *ctx) { CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv, RED); }
+
 int solve_pressure(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    CFDL_LAUNCH("k_pc_mean", k_pc_mean, cells, RED);
-    CFDL_LAUNCH("k_pc_init", k_pc_init, cells, RED);
+    if (ctx->cases[0]->cfg.precision == 1) return solve_pressure_mixed(ctx);
+    if (ctx->cases[0]->cfg.precond == 1) return solve_pressure_amg(ctx);
+    CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv, RED);
+    CFDL_LAUNCH("k_pc_init", k_pc_init, cellsv, RED);
     const int cap = max_cap(ctx);
-    int it = 0, chunk = 4;
+    int it = 0, maxit = 0;
     while (it < cap) {
+        const int chunk = poll_chunk(it, ctx->last_iters_p);
         for (int k = 0; k < chunk && it < cap; k++, it++) {
-            CFDL_LAUNCH("k_pc_q", k_pc_q, cells, RED);
-            CFDL_LAUNCH("k_pc_x", k_pc_x, cells, RED);
-            CFDL_LAUNCH("k_pc_p", k_pc_p, cells);
+            CFDL_LAUNCH("k_pc_q", k_pc_q, cellsv, RED);
+            CFDL_LAUNCH("k_pc_x", k_pc_x, cellsv, RED);
+            CFDL_LAUNCH("k_pc_p", k_pc_p, cellsv);
         }
-        int a = poll(ctx, 2);
+        int a = poll_kind(ctx, 1, &maxit);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;
-        chunk = std::min(chunk * 2, 64);
     }
+    ctx->last_iters_p = maxit;
     return cuda_status(cudaGetLastError());
 }
 

@@ -215,6 +215,11 @@ int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_id
                           const double *anb, const double *b, double *phic, double rtol, int maxit,
                           int *iters, double *rnorm);
 
+/* Multigrid hierarchy of case 0 (built on the first AMG pressure solve):
+ * *nlev coarse levels; n[0..nlev] cells and W[0..nlev] ELL widths per level
+ * (level 0 = the mesh); at most maxlev+1 entries are written. */
+int cfdl_amg_info(cfdl_ctx *ctx, int maxlev, int *nlev, int *n, int *W);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);
 /* Human-readable text for a status code. */

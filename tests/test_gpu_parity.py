@@ -137,6 +137,35 @@ def test_end_to_end_tight_parity(need_gpu, n, tet, jit, steady, nout):
         assert rel_l2(a, b) < RTOL_FIELD, (f, rel_l2(a, b))
 
 
+@pytest.mark.parametrize("precond,precision", [(1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("n,tet,jit", [(8, False, 0.2), (4, True, 0.0), (4, False, 0.0)])
+def test_pressure_solver_forms_tight_parity(need_gpu, n, tet, jit, precond, precision):
+    """AMG-preconditioned CG and the mixed-precision form (FP32 inner PCG, FP64
+    residual and refinement), tight, against the oracle after 20 iterations."""
+    z, s, o, g = tight_pair(n, tet, jit, steady=True, precond=precond, precision=precision)
+    o.run(20, 3)
+    st = g.step(20, 3)
+    assert st.status == 0
+    for f in ("u", "v", "w", "p"):
+        a, b = g.get(f)[:o.ne], o.get(f)[:o.ne]
+        assert rel_l2(a, b) < RTOL_FIELD, (f, rel_l2(a, b))
+
+
+@pytest.mark.parametrize("precond,precision", [(1, 0), (1, 1)])
+def test_amg_default_mode_reaches_steady_state(need_gpu, precond, precision):
+    """Production stopping rule with the AMG pressure solve, FP64 and mixed:
+    the steady state is the oracle's within 1e-6 relative L2."""
+    z = cfdl.Zone(10, False, 0.2, seed=7)
+    s = cfdl.Setup(z)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1))
+    o.run(400)
+    g = cfdl.Solver(s, cfdl.steady(solve_mode=0, precond=precond, precision=precision))
+    g.step(400)
+    for f in ("u", "v", "w"):
+        assert rel_l2(g.get(f)[:o.ne], o.get(f)[:o.ne]) < 1e-6, f
+
+
 def test_config1_cavity_32_tight(need_gpu):
     """Config 1 (32^3 hex, Re=100, alpha 0.7/0.3) through 15 outer iterations."""
     z, s, o, g = tight_pair(32, False, 0.0, steady=True)

@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--tet", action="store_true")
     ap.add_argument("--mode", type=int, default=0, help="0: reference stopping rule, 1: tight")
     ap.add_argument("--precision", type=int, default=0, help="0: FP64, 1: mixed pressure solve")
-    ap.add_argument("--precond", type=int, default=0, help="pressure preconditioner: 0 Jacobi, 1 AMG")
+    ap.add_argument("--precond", type=int, default=1, help="pressure preconditioner: 0 Jacobi, 1 AMG")
+    ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of the graph")
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -183,6 +184,7 @@ def run_ours(a, dist):
     setup = cfdl.Setup(zone)
     cfg = cfdl.steady(solve_mode=a.mode, precision=a.precision, precond=a.precond)
     g = cfdl.Solver(setup, cfg)
+    g.set_graph_mode(not a.eager)
     W = 4 if a.tet else 6
     ne, nf, nbf = setup.ne, setup.nf, setup.nbf
     state = {"it": 0}

@@ -113,6 +113,7 @@ def lib():
     L.cfdl_solve_pc_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int,
                                         ip, dp]
     L.cfdl_amg_info.argtypes = [vp, C.c_int, ip, vp, vp]
+    L.cfdl_set_graph_mode.argtypes = [vp, C.c_int]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]
@@ -274,6 +275,10 @@ class Solver:
 
     def update_uvwp(self):
         _check(lib().cfdl_update_uvwp(self._h), "update_uvwp")
+
+    def set_graph_mode(self, on):
+        """solve_uvwp as one CUDA graph (True, default) or as individual launches."""
+        _check(lib().cfdl_set_graph_mode(self._h, int(bool(on))), "set_graph_mode")
 
     def set_config(self, cfg):
         _check(lib().cfdl_set_config(self._h, C.byref(cfg)), "set_config")

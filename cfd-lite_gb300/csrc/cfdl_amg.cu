@@ -513,31 +513,40 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
 
 void launch_pc_mean(cfdl_ctx *ctx);
 
-int solve_pressure_amg(cfdl_ctx *ctx) {
-    int st = ensure_amg(ctx);
-    if (st) return st;
 #define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
+#define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
+
+// FP64 AMG-PCG: coarse operators, zero-mean right-hand side, x = 0
+void apc_init(cfdl_ctx *ctx) {
     amg_setup_operators(ctx);
     launch_pc_mean(ctx);
     ALAUNCH("k_apc_init", k_apc_init, ctx->cellsv, RED);
+}
+
+// one preconditioned CG iteration
+void apc_iter(cfdl_ctx *ctx) {
+    vcycle<double>(ctx);
+    ALAUNCH("k_apc_rz", k_apc_rz, ctx->cellsv, RED);
+    ALAUNCH("k_apc_p", k_apc_p, ctx->cellsv);
+    ALAUNCH("k_apc_q", k_apc_q, ctx->cellsv, RED);
+    ALAUNCH("k_apc_x", k_apc_x, ctx->cellsv, RED);
+}
+
+int solve_pressure_amg(cfdl_ctx *ctx) {
+    int st = ensure_amg(ctx);
+    if (st) return st;
+    apc_init(ctx);
     int cap = 0;
     for (auto *hc : ctx->cases) cap = std::max(cap, hc->cfg.solve_mode == 0 ? hc->cfg.nit : hc->cfg.tight_maxit);
     int it = 0, maxit = 0;
     while (it < cap) {
         const int chunk = poll_chunk(it, ctx->last_iters_p);
-        for (int k = 0; k < chunk && it < cap; k++, it++) {
-            vcycle<double>(ctx);
-            ALAUNCH("k_apc_rz", k_apc_rz, ctx->cellsv, RED);
-            ALAUNCH("k_apc_p", k_apc_p, ctx->cellsv);
-            ALAUNCH("k_apc_q", k_apc_q, ctx->cellsv, RED);
-            ALAUNCH("k_apc_x", k_apc_x, ctx->cellsv, RED);
-        }
+        for (int k = 0; k < chunk && it < cap; k++, it++) apc_iter(ctx);
         int a = poll_kind(ctx, 1, &maxit);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;
     }
     ctx->last_iters_p = maxit;
-#undef RED
     return cuda_status(cudaGetLastError());
 }
 
@@ -728,7 +737,7 @@ __global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ ca
             S->iters_p += S->iters32;
             int act = rn > S->tol_p;
             if (!isfinite(rn)) { act = 0; S->status_p = CFDL_ERR_NONFINITE; }
-            else if (act && S->outer_p >= 60) { act = 0; if (C.solve_mode == 1) S->status_p = CFDL_ERR_ITER_CAP; }
+            else if (act && S->outer_p >= kMixedMaxOuter) { act = 0; if (C.solve_mode == 1) S->status_p = CFDL_ERR_ITER_CAP; }
             S->active_p = act;
         }
     }
@@ -736,46 +745,53 @@ __global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ ca
 
 }  // namespace
 
-int solve_pressure_mixed(cfdl_ctx *ctx) {
-    const bool amg = ctx->cases[0]->cfg.precond == 1;
-    int st;
-    if (amg && (st = ensure_amg(ctx))) return st;
-#define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
-#define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
-    if (amg) amg_setup_operators(ctx);
+// mixed form: FP32 operator copies (+ coarse operators), FP64 start
+void mx_init(cfdl_ctx *ctx) {
+    if (ctx->cases[0]->cfg.precond == 1) amg_setup_operators(ctx);
     else ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
     launch_pc_mean(ctx);
     ALAUNCH("k_mx_init", k_mx_init, ctx->cellsv, RED);
+}
+void mx_start(cfdl_ctx *ctx) { ALAUNCH("k_mx_start", k_mx_start, ctx->cellsv, RED32); }
+void mx_inner_iter(cfdl_ctx *ctx) {
+    if (ctx->cases[0]->cfg.precond == 1) vcycle<float>(ctx);
+    else ALAUNCH("k_mx_jacobi", k_mx_jacobi, ctx->cellsv);
+    ALAUNCH("k_mx_rz", k_mx_rz, ctx->cellsv, RED32);
+    ALAUNCH("k_mx_p", k_mx_p, ctx->cellsv);
+    ALAUNCH("k_mx_q", k_mx_q, ctx->cellsv, RED32);
+    ALAUNCH("k_mx_x", k_mx_x, ctx->cellsv, RED32);
+}
+void mx_finish(cfdl_ctx *ctx) {
+    ALAUNCH("k_mx_apply", k_mx_apply, ctx->cellsv);
+    ALAUNCH("k_mx_res", k_mx_res, ctx->cellsv, RED);
+}
+
+int solve_pressure_mixed(cfdl_ctx *ctx) {
+    int st;
+    if (ctx->cases[0]->cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
+    mx_init(ctx);
     int cap = 0;
     for (auto *hc : ctx->cases) cap = std::max(cap, hc->cfg.solve_mode == 0 ? hc->cfg.nit : hc->cfg.tight_maxit);
-    for (int outer = 0; outer < 60; outer++) {
-        ALAUNCH("k_mx_start", k_mx_start, ctx->cellsv, RED32);
+    for (int outer = 0; outer < kMixedMaxOuter; outer++) {
+        mx_start(ctx);
         int it = 0, maxit = 0;
         while (it < cap) {
             const int chunk = poll_chunk(it, ctx->last_iters_p);
-            for (int k = 0; k < chunk && it < cap; k++, it++) {
-                if (amg) vcycle<float>(ctx);
-                else ALAUNCH("k_mx_jacobi", k_mx_jacobi, ctx->cellsv);
-                ALAUNCH("k_mx_rz", k_mx_rz, ctx->cellsv, RED32);
-                ALAUNCH("k_mx_p", k_mx_p, ctx->cellsv);
-                ALAUNCH("k_mx_q", k_mx_q, ctx->cellsv, RED32);
-                ALAUNCH("k_mx_x", k_mx_x, ctx->cellsv, RED32);
-            }
+            for (int k = 0; k < chunk && it < cap; k++, it++) mx_inner_iter(ctx);
             int a = poll_kind(ctx, 2, &maxit);
             if (a < 0) return CFDL_ERR_CUDA;
             if (a == 0) break;
         }
         ctx->last_iters_p = maxit;
-        ALAUNCH("k_mx_apply", k_mx_apply, ctx->cellsv);
-        ALAUNCH("k_mx_res", k_mx_res, ctx->cellsv, RED);
+        mx_finish(ctx);
         int a = poll_kind(ctx, 3, nullptr);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;
     }
-#undef RED
-#undef RED32
     return cuda_status(cudaGetLastError());
 }
+#undef RED
+#undef RED32
 
 }  // namespace cfdl
 

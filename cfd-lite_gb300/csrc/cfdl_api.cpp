@@ -111,7 +111,9 @@ int finish(cfdl_ctx *ctx, cfdl_stats *st) {
 
 namespace cfdl {
 int solve_uvwp_all(cfdl_ctx *ctx) {
-    // solve_uvwp, src/equations/mod_uvwp.f90:95-134
+    // solve_uvwp, src/equations/mod_uvwp.f90:95-134: as one graph launch unless
+    // graphs are off or launches are being profiled one by one
+    if (ctx->use_graph && !prof_active(ctx)) return solve_uvwp_graph(ctx);
     launch_coef_uvw(ctx);
     int st = solve_momentum(ctx);
     if (st) return st;
@@ -137,7 +139,7 @@ void cfdl_config_default(cfdl_config *c) {
     c->alpha_u = 1.0; c->alpha_p = 1.0;
     c->nit = 100; c->solve_mode = 0; c->rtol_u = 0.1; c->rtol_p = 0.1;
     c->tight_rtol = 1e-13; c->tight_maxit = 20000;
-    c->precision = 0; c->precond = 0;
+    c->precision = 0; c->precond = 1;
 }
 
 const char *cfdl_status_string(int s) {
@@ -223,6 +225,8 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     prof_destroy(ctx);
+    destroy_graph(ctx);
+    cudaFree(ctx->d_loop_passes);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CFDL_OK;
@@ -341,6 +345,15 @@ int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host) {
     return copy_named(ctx, ctx->cases[0], name, const_cast<double *>(host), false);
 }
 
-int64_t cfdl_launch_count(const cfdl_ctx *ctx) { return ctx ? ctx->launches : -1; }
+int64_t cfdl_launch_count(const cfdl_ctx *ctx) {
+    if (!ctx) return -1;
+    return ctx->launches + graph_loop_kernels(const_cast<cfdl_ctx *>(ctx));
+}
+
+int cfdl_set_graph_mode(cfdl_ctx *ctx, int on) {
+    if (!ctx) return CFDL_ERR_INVALID;
+    ctx->use_graph = on != 0;
+    return CFDL_OK;
+}
 
 }  // extern "C"

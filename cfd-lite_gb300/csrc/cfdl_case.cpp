@@ -339,6 +339,7 @@ int rebuild_worklists(cfdl_ctx *ctx) {
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_lmax = -1;
+    destroy_graph(ctx);   // captured launch arguments refer to the old lists
     int need = std::max({ctx->cells.ntiles, ctx->faces.ntiles, ctx->halos.ntiles, 1});
     if (need > ctx->partials_cap) {
         cudaFree(ctx->d_partials);

@@ -1,0 +1,236 @@
+// cfdl_graph.cu -- one outer iteration (solve_uvwp) as one CUDA graph.
+//
+// The inner solves of solve_uvwp loop until a residual test passes
+// (solve_gs / multi_subdomain_solver in the reference,
+// src/modules/mod_solver.f90:124-327).  Here each such loop is a graph
+// "while" node whose body is one Krylov iteration followed by a one-thread
+// kernel that sets the loop condition from the per-case activity flags the
+// iteration's reductions left on the device.  The whole outer iteration --
+// momentum assembly, three-component BiCGStab loop, gradients, Rhie-Chow
+// fluxes, pressure assembly, pressure-correction loop (nested loops for the
+// mixed-precision form), correction -- is then a single cudaGraphLaunch with
+// no host round trip.  The graph is built once per context and kernel
+// sequence; coefficients, tolerances and fields are read from device memory
+// at run time, so changing them does not rebuild it.
+#include "cfdl_internal.h"
+#include <cuda_runtime.h>
+
+namespace cfdl {
+
+void mom_init(cfdl_ctx *ctx);
+void mom_iter(cfdl_ctx *ctx);
+void pcj_init(cfdl_ctx *ctx);
+void pcj_iter(cfdl_ctx *ctx);
+void apc_init(cfdl_ctx *ctx);
+void apc_iter(cfdl_ctx *ctx);
+void mx_init(cfdl_ctx *ctx);
+void mx_start(cfdl_ctx *ctx);
+void mx_inner_iter(cfdl_ctx *ctx);
+void mx_finish(cfdl_ctx *ctx);
+
+namespace {
+
+enum { LOOP_MOM = 0, LOOP_P = 1, LOOP_INNER = 2, LOOP_OUTER = 3 };
+
+// Loop condition = any case still active for this loop kind; counts the pass.
+__global__ void k_setcond(const CaseDev *__restrict__ cases, int ncases, cudaGraphConditionalHandle h, int kind,
+                          unsigned long long *loop_passes) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int any = 0;
+    for (int c = 0; c < ncases; c++) {
+        const SolveScalars *S = cases[c].sc;
+        int a;
+        if (kind == LOOP_MOM) a = S->active[0] | S->active[1] | S->active[2];
+        else if (kind == LOOP_INNER) a = S->active32;
+        else a = S->active_p;
+        any |= (a != 0);
+    }
+    cudaGraphSetConditional(h, any ? 1u : 0u);
+    loop_passes[kind] += 1;
+}
+
+__global__ void k_setone(cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, 1u);
+}
+
+struct Builder {
+    cfdl_ctx *ctx;
+    int64_t kernels = 0;
+
+    void setcond(cudaGraphConditionalHandle h, int kind) {
+        k_setcond<<<1, 32, 0, ctx->stream>>>(ctx->d_cases, (int)ctx->cases.size(), h, kind, ctx->d_loop_passes);
+        ctx->launches++;
+    }
+    template <class F> int capture(F f, cudaGraph_t *out, int64_t *count) {
+        const int64_t l0 = ctx->launches;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_status(e);
+        f();
+        e = cudaStreamEndCapture(ctx->stream, out);
+        *count = ctx->launches - l0;
+        ctx->launches = l0;
+        return cuda_status(e);
+    }
+    template <class F> int capture_into(cudaGraph_t body, F f, int64_t *count) {
+        const int64_t l0 = ctx->launches;
+        cudaError_t e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_status(e);
+        f();
+        cudaGraph_t out = nullptr;
+        e = cudaStreamEndCapture(ctx->stream, &out);
+        *count = ctx->launches - l0;
+        ctx->launches = l0;
+        return cuda_status(e);
+    }
+    // append a captured segment as a child-graph node after *prev
+    template <class F> int segment(cudaGraph_t G, cudaGraphNode_t *prev, F f, int64_t *count) {
+        cudaGraph_t child = nullptr;
+        int st = capture(f, &child, count);
+        if (st) return st;
+        cudaGraphNode_t n;
+        cudaError_t e = cudaGraphAddChildGraphNode(&n, G, *prev ? prev : nullptr, *prev ? 1 : 0, child);
+        cudaGraphDestroy(child);
+        if (e != cudaSuccess) return cuda_status(e);
+        *prev = n;
+        return CFDL_OK;
+    }
+    // append a while node; fill(body) builds its body graph
+    template <class F> int loop(cudaGraph_t G, cudaGraphNode_t *prev, cudaGraphConditionalHandle h, F fill) {
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t n;
+        cudaError_t e = cudaGraphAddNode(&n, G, *prev ? prev : nullptr, nullptr, *prev ? 1 : 0, &p);
+        if (e != cudaSuccess) return cuda_status(e);
+        int st = fill(p.conditional.phGraph_out[0]);
+        if (st) return st;
+        *prev = n;
+        return CFDL_OK;
+    }
+};
+
+}  // namespace
+
+void destroy_graph(cfdl_ctx *ctx) {
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->graph_exec = nullptr;
+    ctx->graph = nullptr;
+    ctx->graph_form = -1;
+}
+
+static int graph_form(const cfdl_ctx *ctx) {
+    const cfdl_config &c = ctx->cases[0]->cfg;
+    return c.precision * 2 + c.precond;
+}
+
+int build_graph(cfdl_ctx *ctx) {
+    destroy_graph(ctx);
+    const cfdl_config &cfg = ctx->cases[0]->cfg;
+    int st;
+    if (cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
+    if (!ctx->d_loop_passes) {
+        if ((st = cuda_status(cudaMalloc(&ctx->d_loop_passes, 4 * sizeof(unsigned long long))))) return st;
+        if ((st = cuda_status(cudaMemset(ctx->d_loop_passes, 0, 4 * sizeof(unsigned long long))))) return st;
+    }
+    cudaGraph_t G = nullptr;
+    if ((st = cuda_status(cudaGraphCreate(&G, 0)))) return st;
+    Builder b{ctx};
+    ctx->capturing = true;
+    cudaGraphNode_t prev = nullptr;
+    int64_t k = 0;
+    cudaGraphConditionalHandle hm, hp;
+    int64_t body[4] = {0, 0, 0, 0};
+    auto fail = [&](int s) { ctx->capturing = false; cudaGraphDestroy(G); return s; };
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hm, G, 1, cudaGraphCondAssignDefault)))) return fail(st);
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hp, G, 1, cudaGraphCondAssignDefault)))) return fail(st);
+    // momentum assembly and BiCGStab
+    if ((st = b.segment(G, &prev, [&] { launch_coef_uvw(ctx); mom_init(ctx); }, &k))) return fail(st);
+    b.kernels += k;
+    st = b.loop(G, &prev, hm, [&](cudaGraph_t body_g) {
+        return b.capture_into(body_g, [&] { mom_iter(ctx); b.setcond(hm, LOOP_MOM); }, &body[LOOP_MOM]);
+    });
+    if (st) return fail(st);
+    // gradients, Rhie-Chow fluxes, pressure assembly, pressure-solve start
+    if ((st = b.segment(G, &prev, [&] {
+             launch_grad(ctx, 4);
+             launch_calc_mip(ctx, 1);
+             launch_coef_p(ctx);
+             if (cfg.precision == 1) mx_init(ctx);
+             else if (cfg.precond == 1) apc_init(ctx);
+             else pcj_init(ctx);
+         }, &k)))
+        return fail(st);
+    b.kernels += k;
+    if (cfg.precision == 0) {
+        st = b.loop(G, &prev, hp, [&](cudaGraph_t body_g) {
+            return b.capture_into(body_g, [&] {
+                if (cfg.precond == 1) apc_iter(ctx);
+                else pcj_iter(ctx);
+                b.setcond(hp, LOOP_P);
+            }, &body[LOOP_P]);
+        });
+    } else {
+        // refinement loop around the FP32 inner loop
+        st = b.loop(G, &prev, hp, [&](cudaGraph_t outer) {
+            cudaGraphConditionalHandle hi;
+            int s2 = cuda_status(cudaGraphConditionalHandleCreate(&hi, outer, 1, 0));
+            if (s2) return s2;
+            cudaGraphNode_t op = nullptr;
+            int64_t k1 = 0, k2 = 0;
+            if ((s2 = b.segment(outer, &op, [&] { mx_start(ctx); k_setone<<<1, 32, 0, ctx->stream>>>(hi); ctx->launches++; }, &k1))) return s2;
+            if ((s2 = b.loop(outer, &op, hi, [&](cudaGraph_t inner) {
+                     return b.capture_into(inner, [&] { mx_inner_iter(ctx); b.setcond(hi, LOOP_INNER); }, &body[LOOP_INNER]);
+                 })))
+                return s2;
+            if ((s2 = b.segment(outer, &op, [&] { mx_finish(ctx); b.setcond(hp, LOOP_OUTER); }, &k2))) return s2;
+            body[LOOP_OUTER] = k1 + k2;
+            return CFDL_OK;
+        });
+    }
+    if (st) return fail(st);
+    // correction
+    if ((st = b.segment(G, &prev, [&] {
+             launch_adjust_pc(ctx);
+             launch_grad(ctx, 3);
+             launch_update_uvwp(ctx);
+         }, &k)))
+        return fail(st);
+    b.kernels += k;
+    ctx->capturing = false;
+    cudaGraphExec_t exec = nullptr;
+    if ((st = cuda_status(cudaGraphInstantiate(&exec, G, 0)))) { cudaGraphDestroy(G); return st; }
+    ctx->graph = G;
+    ctx->graph_exec = exec;
+    ctx->graph_form = graph_form(ctx);
+    ctx->graph_static_kernels = b.kernels;
+    for (int i = 0; i < 4; i++) ctx->graph_body_kernels[i] = body[i];
+    return CFDL_OK;
+}
+
+// One solve_uvwp through the graph (built on first use, rebuilt when the
+// kernel sequence changes).  Returns a status; falls back to nothing.
+int solve_uvwp_graph(cfdl_ctx *ctx) {
+    int st;
+    if (!ctx->graph_exec || ctx->graph_form != graph_form(ctx))
+        if ((st = build_graph(ctx))) return st;
+    ctx->launches += ctx->graph_static_kernels;
+    ctx->graph_launches++;
+    return cuda_status(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+}
+
+// Kernels the graph ran inside its loops so far (synchronises).
+int64_t graph_loop_kernels(cfdl_ctx *ctx) {
+    if (!ctx->d_loop_passes) return 0;
+    unsigned long long passes[4] = {0, 0, 0, 0};
+    if (cudaMemcpyAsync(passes, ctx->d_loop_passes, sizeof(passes), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        return 0;
+    int64_t n = 0;
+    for (int i = 0; i < 4; i++) n += (int64_t)passes[i] * ctx->graph_body_kernels[i];
+    return n;
+}
+
+}  // namespace cfdl

@@ -32,6 +32,7 @@ constexpr int kTile = 256;        // cells / faces / halos per CTA
 constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
 constexpr int kNPart = 16;        // partial slots per tile
 constexpr int kVec = 4;           // cells per thread in the solver kernels (tile = kTile*kVec cells)
+constexpr int kMixedMaxOuter = 60;   // FP64 refinement cycles of the mixed pressure solve
 
 // Loop over the cells of a wide solver tile: thread t handles cells
 // first+t, first+t+kTile, ... (coalesced, kVec of them).
@@ -155,6 +156,13 @@ struct cfdl_ctx {
     // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
     std::vector<cfdl::WorkList> amg_cells, amg_smooth;
     int amg_lmax = -1;
+    // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
+    bool use_graph = true, capturing = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_form = -1;
+    int64_t graph_static_kernels = 0, graph_body_kernels[4] = {0, 0, 0, 0}, graph_launches = 0;
+    unsigned long long *d_loop_passes = nullptr;   // passes of each loop kind
 };
 
 namespace cfdl {
@@ -179,6 +187,7 @@ void launch_set_mip0(cfdl_ctx *ctx);
 
 // event profiler (cfdl_prof.cpp)
 bool prof_wants(cfdl_ctx *ctx, const char *name);
+bool prof_active(cfdl_ctx *ctx);
 void prof_begin(cfdl_ctx *ctx, const char *name);
 void prof_end(cfdl_ctx *ctx);
 void prof_destroy(cfdl_ctx *ctx);
@@ -209,6 +218,14 @@ int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st);
 int poll_kind(cfdl_ctx *ctx, int kind, int *maxit);
 int poll_chunk(int done, int expected);
 
+void launch_pc_mean(cfdl_ctx *ctx);
+
 // one outer iteration for every case of the context (cfdl_api.cpp)
 int solve_uvwp_all(cfdl_ctx *ctx);
+
+// graph form of solve_uvwp (cfdl_graph.cu)
+int build_graph(cfdl_ctx *ctx);
+void destroy_graph(cfdl_ctx *ctx);
+int solve_uvwp_graph(cfdl_ctx *ctx);
+int64_t graph_loop_kernels(cfdl_ctx *ctx);
 }  // namespace cfdl

@@ -40,8 +40,13 @@ void prof_destroy(cfdl_ctx *ctx) {
 
 bool prof_wants(cfdl_ctx *ctx, const char *name) {
     Prof *p = static_cast<Prof *>(ctx->prof);
-    if (!p || p->mode == 0) return false;
+    if (!p || p->mode == 0 || ctx->capturing) return false;
     return p->mode == 1 || p->only == name;
+}
+
+bool prof_active(cfdl_ctx *ctx) {
+    Prof *p = static_cast<Prof *>(ctx->prof);
+    return p && p->mode != 0;
 }
 
 void prof_begin(cfdl_ctx *ctx, const char *name) {

@@ -406,20 +406,35 @@ static int max_cap(cfdl_ctx *ctx) {
     return cap;
 }
 
+void mom_init(cfdl_ctx *ctx) { CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED); }
+
+void mom_iter(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_mom_p", k_mom_p, cellsv);
+    CFDL_LAUNCH("k_mom_v", k_mom_v, cellsv, RED);
+    CFDL_LAUNCH("k_mom_s", k_mom_s, cellsv, RED);
+    CFDL_LAUNCH("k_mom_t", k_mom_t, cellsv, RED);
+    CFDL_LAUNCH("k_mom_x", k_mom_x, cellsv, RED);
+}
+
+void pcj_init(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv, RED);
+    CFDL_LAUNCH("k_pc_init", k_pc_init, cellsv, RED);
+}
+
+void pcj_iter(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_pc_q", k_pc_q, cellsv, RED);
+    CFDL_LAUNCH("k_pc_x", k_pc_x, cellsv, RED);
+    CFDL_LAUNCH("k_pc_p", k_pc_p, cellsv);
+}
+
 int solve_momentum(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED);
+    mom_init(ctx);
     const int cap = max_cap(ctx);
     int it = 0, maxit = 0;
     while (it < cap) {
         const int chunk = poll_chunk(it, ctx->last_iters_m);
-        for (int k = 0; k < chunk && it < cap; k++, it++) {
-            CFDL_LAUNCH("k_mom_p", k_mom_p, cellsv);
-            CFDL_LAUNCH("k_mom_v", k_mom_v, cellsv, RED);
-            CFDL_LAUNCH("k_mom_s", k_mom_s, cellsv, RED);
-            CFDL_LAUNCH("k_mom_t", k_mom_t, cellsv, RED);
-            CFDL_LAUNCH("k_mom_x", k_mom_x, cellsv, RED);
-        }
+        for (int k = 0; k < chunk && it < cap; k++, it++) mom_iter(ctx);
         int a = poll_kind(ctx, 0, &maxit);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;
@@ -434,17 +449,12 @@ int solve_pressure(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
     if (ctx->cases[0]->cfg.precision == 1) return solve_pressure_mixed(ctx);
     if (ctx->cases[0]->cfg.precond == 1) return solve_pressure_amg(ctx);
-    CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv, RED);
-    CFDL_LAUNCH("k_pc_init", k_pc_init, cellsv, RED);
+    pcj_init(ctx);
     const int cap = max_cap(ctx);
     int it = 0, maxit = 0;
     while (it < cap) {
         const int chunk = poll_chunk(it, ctx->last_iters_p);
-        for (int k = 0; k < chunk && it < cap; k++, it++) {
-            CFDL_LAUNCH("k_pc_q", k_pc_q, cellsv, RED);
-            CFDL_LAUNCH("k_pc_x", k_pc_x, cellsv, RED);
-            CFDL_LAUNCH("k_pc_p", k_pc_p, cellsv);
-        }
+        for (int k = 0; k < chunk && it < cap; k++, it++) pcj_iter(ctx);
         int a = poll_kind(ctx, 1, &maxit);
         if (a < 0) return CFDL_ERR_CUDA;
         if (a == 0) break;

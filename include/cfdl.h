@@ -215,6 +215,12 @@ int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_id
                           const double *anb, const double *b, double *phic, double rtol, int maxit,
                           int *iters, double *rnorm);
 
+/* solve_uvwp runs as one CUDA graph (inner solve loops as device-side while
+ * nodes) when on (the default), or as individually launched kernels with
+ * host polling of the inner convergence when off; the results are the same.
+ * Per-kernel profiling always uses the second form. */
+int cfdl_set_graph_mode(cfdl_ctx *ctx, int on);
+
 /* Multigrid hierarchy of case 0 (built on the first AMG pressure solve):
  * *nlev coarse levels; n[0..nlev] cells and W[0..nlev] ELL widths per level
  * (level 0 = the mesh); at most maxlev+1 entries are written. */

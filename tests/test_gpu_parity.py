@@ -204,6 +204,25 @@ def test_deterministic_and_launches_counted(need_gpu):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precond,precision,mode", [(0, 0, 0), (1, 0, 0), (1, 1, 0), (1, 0, 1), (1, 1, 1)])
+def test_graph_equals_eager(need_gpu, precond, precision, mode):
+    """solve_uvwp as one CUDA graph with device-side loops runs the same
+    kernels with the same device-side decisions as the host-polled launches,
+    so the fields agree bit for bit."""
+    z = cfdl.Zone(12, False, 0.2, seed=5)
+    s = cfdl.Setup(z)
+    out = []
+    for graph in (True, False):
+        g = cfdl.Solver(s, cfdl.steady(solve_mode=mode, precond=precond, precision=precision))
+        g.set_graph_mode(graph)
+        st = g.step(7, 3)
+        assert st.status == 0
+        out.append([g.get(f) for f in ("u", "v", "w", "p", "mip", "gp")])
+        g.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
 def test_host_dropin_matches_resident(need_gpu):
     """cfdl_solve_uvwp_host (host arrays in and out) equals the resident path."""
     import ctypes as C

@@ -46,11 +46,15 @@ class Config(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("it_u", C.c_int), ("it_v", C.c_int), ("it_w", C.c_int), ("it_p", C.c_int),
                 ("res_i", C.c_double * 4), ("res_f", C.c_double * 4),
-                ("mass_imbalance", C.c_double), ("status", C.c_int)]
+                ("mass_imbalance", C.c_double), ("status", C.c_int),
+                ("outer_done", C.c_int), ("run_left", C.c_int), ("converged", C.c_int),
+                ("mass_ratio", C.c_double)]
 
     def as_dict(self):
         return {"it": [self.it_u, self.it_v, self.it_w, self.it_p], "res_i": list(self.res_i),
-                "res_f": list(self.res_f), "mass_imbalance": self.mass_imbalance, "status": self.status}
+                "res_f": list(self.res_f), "mass_imbalance": self.mass_imbalance, "status": self.status,
+                "outer_done": self.outer_done, "run_left": self.run_left, "converged": self.converged,
+                "mass_ratio": self.mass_ratio}
 
 
 class Mesh(C.Structure):
@@ -114,6 +118,19 @@ def lib():
                                         ip, dp]
     L.cfdl_amg_info.argtypes = [vp, C.c_int, ip, vp, vp]
     L.cfdl_set_graph_mode.argtypes = [vp, C.c_int]
+    L.cfdl_batch_create.argtypes = [C.c_int, vp, vp, C.POINTER(vp)]
+    L.cfdl_case_add.argtypes = [vp, C.POINTER(Mesh), C.POINTER(Config), ip]
+    L.cfdl_case_remove.argtypes = [vp, C.c_int]
+    L.cfdl_case_count.argtypes = [vp]
+    L.cfdl_case_ids.argtypes = [vp, vp]
+    L.cfdl_case_get_array.argtypes = [vp, C.c_int, C.c_char_p, vp]
+    L.cfdl_case_set_array.argtypes = [vp, C.c_int, C.c_char_p, vp]
+    L.cfdl_case_stats.argtypes = [vp, C.c_int, C.POINTER(Stats)]
+    L.cfdl_case_info.argtypes = [vp, C.c_int, ip, C.POINTER(C.c_size_t)]
+    L.cfdl_case_bytes_estimate.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+    L.cfdl_case_bytes_estimate.restype = C.c_size_t
+    L.cfdl_case_set_run.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double]
+    L.cfdl_run.argtypes = [vp, C.c_int, ip]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]
@@ -276,6 +293,17 @@ class Solver:
     def update_uvwp(self):
         _check(lib().cfdl_update_uvwp(self._h), "update_uvwp")
 
+    def set_run(self, n_outer, ncoef=0, conv_tol=0.0, cid=-1):
+        """Give case cid (-1: every case) n_outer outer iterations to run, an
+        update_time cadence and an early-stop tolerance on the mass ratio."""
+        _check(lib().cfdl_case_set_run(self._h, int(cid), int(n_outer), int(ncoef), float(conv_tol)), "case_set_run")
+
+    def run(self, max_outer):
+        """Up to max_outer passes; returns the number of cases with iterations left."""
+        running = C.c_int()
+        _check(lib().cfdl_run(self._h, int(max_outer), C.byref(running)), "run")
+        return running.value
+
     def set_graph_mode(self, on):
         """solve_uvwp as one CUDA graph (True, default) or as individual launches."""
         _check(lib().cfdl_set_graph_mode(self._h, int(bool(on))), "set_graph_mode")
@@ -345,3 +373,82 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def _array_len(name, ne, nf, nbf, H):
+    nc = ne + nbf
+    if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic"):
+        return nc
+    if name in ("gu", "gv", "gw", "gp", "gpc"):
+        return 3 * nc
+    if name in ("mip", "mip0"):
+        return nf
+    if name == "anb":
+        return H
+    return ne
+
+
+class Batch(Solver):
+    """Many independent cases resident in one context and advanced by the same
+    launches.  The context-level routines of Solver act on every case; the
+    case_* methods address one case by id.  All cases share the pressure-solve
+    form (precision, precond)."""
+
+    def __init__(self, setups, configs, u_lids=None):
+        setups = list(setups)
+        configs = list(configs)
+        if not setups or len(setups) != len(configs):
+            raise ValueError("one config per setup")
+        u_lids = list(u_lids) if u_lids is not None else [1.0] * len(setups)
+        self.setup = setups[0]
+        self.config = configs[0]
+        meshes = (Mesh * len(setups))(*[s.mesh(u) for s, u in zip(setups, u_lids)])
+        cfgs = (Config * len(configs))(*configs)
+        self._h = C.c_void_p()
+        _check(lib().cfdl_batch_create(len(setups), C.cast(meshes, C.c_void_p), C.cast(cfgs, C.c_void_p),
+                                       C.byref(self._h)), "batch_create")
+        self._sizes = {i: (s.ne, s.nf, s.nbf, s.H) for i, s in enumerate(setups)}
+        self.ne, self.nf, self.nbf, self.H = self._sizes[0]
+        self.last_stats = Stats()
+
+    def add(self, setup, config, u_lid=1.0):
+        mesh = setup.mesh(u_lid)
+        cid = C.c_int()
+        _check(lib().cfdl_case_add(self._h, C.byref(mesh), C.byref(config), C.byref(cid)), "case_add")
+        self._sizes[cid.value] = (setup.ne, setup.nf, setup.nbf, setup.H)
+        return cid.value
+
+    def remove(self, cid):
+        _check(lib().cfdl_case_remove(self._h, int(cid)), "case_remove")
+        self._sizes.pop(cid, None)
+
+    def ids(self):
+        n = lib().cfdl_case_count(self._h)
+        out = np.zeros(n, dtype=np.int32)
+        _check(lib().cfdl_case_ids(self._h, _p(out)), "case_ids")
+        return [int(i) for i in out]
+
+    def case_get(self, cid, name):
+        out = np.zeros(_array_len(name, *self._sizes[cid]))
+        _check(lib().cfdl_case_get_array(self._h, int(cid), name.encode(), _p(out)), "case_get " + name)
+        return out
+
+    def case_set(self, cid, name, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        if a.size != _array_len(name, *self._sizes[cid]):
+            raise ValueError("%s has the wrong size" % name)
+        _check(lib().cfdl_case_set_array(self._h, int(cid), name.encode(), _p(a)), "case_set " + name)
+
+    def case_stats(self, cid):
+        st = Stats()
+        _check(lib().cfdl_case_stats(self._h, int(cid), C.byref(st)), "case_stats")
+        return st
+
+    def case_info(self, cid):
+        ne, nb = C.c_int(), C.c_size_t()
+        _check(lib().cfdl_case_info(self._h, int(cid), C.byref(ne), C.byref(nb)), "case_info")
+        return ne.value, nb.value
+
+
+def case_bytes_estimate(ne, nf, nbf, W=6):
+    return int(lib().cfdl_case_bytes_estimate(int(ne), int(nf), int(nbf), int(W)))

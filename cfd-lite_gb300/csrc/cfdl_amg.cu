@@ -48,34 +48,40 @@ template <> __device__ __forceinline__ LP<float> level<float>(const CaseDev &C, 
 
 // (A x)_i at a level; neighbours outside [0, n) (halos, padding) are skipped
 template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x, int i) {
-    T s = P.dg[i] * x[i];
-    for (int k = 0; k < P.W; k++) {
-        const int j = P.nb[k * P.n + i];
-        if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * x[j];
-    }
-    return s;
+    T y[1];
+    ell_row<1, T>(P.nb, P.a, P.dg[i], x, 0, P.n, P.W, i, y);
+    return y[0];
 }
 
 __device__ __forceinline__ bool pactive(const CaseDev &C) { return C.sc->active_p != 0; }
 __device__ __forceinline__ bool mactive(const CaseDev &C) { return C.sc->active32 != 0; }
 
 // ------------------------------------------------------------ Galerkin
+// off-diagonal coefficient of one coarse ELL slot s = k*n + I: the sum of the
+// fine coefficients between the two aggregates, in a fixed order
+__global__ void __launch_bounds__(kTile) k_amg_gal_off(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const int s = t.first + (int)threadIdx.x;
+    if (s >= t.last || C.sc->halted) return;
+    const AmgLevelDev &L = C.lev[l - 1];
+    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    double v = 0.0;
+    for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
+    L.a[s] = v;
+    if (C.precision == 1) L.a32[s] = (float)v;
+}
+
+// diagonal of coarse cell I: member diagonals minus the couplings inside I
 __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const int I = t.first + (int)threadIdx.x;
-    if (I >= t.last) return;
+    if (I >= t.last || C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
     const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
     const double *df = l == 1 ? C.ap : C.lev[l - 2].dg;
     const bool mixed = C.precision == 1;
-    for (int k = 0; k < L.W; k++) {
-        const int s = k * L.n + I;
-        double v = 0.0;
-        for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
-        L.a[s] = v;
-        if (mixed) L.a32[s] = (float)v;
-    }
     double dsum = 0.0;
     for (int m = L.mem_ptr[I]; m < L.mem_ptr[I + 1]; m++) dsum += df[L.mem[m]];
     for (int q = L.d_ptr[I]; q < L.d_ptr[I + 1]; q++) dsum -= af[L.d_src[q]];
@@ -89,7 +95,7 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const int i = t.first + (int)threadIdx.x;
-    if (i >= t.last) return;
+    if (i >= t.last || C.sc->halted) return;
     const double ap = C.ap[i];
     C.rap[i] = 1.0 / ap;
     if (C.precision == 1) {
@@ -105,7 +111,7 @@ __global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restric
     const int c = blockIdx.x;
     if (c >= ncases) return;
     const CaseDev &C = cases[c];
-    if (C.precond != 1) return;
+    if (C.precond != 1 || C.sc->halted) return;
     __shared__ double M[kAmgCoarsest * kAmgCoarsest];
     __shared__ double piv;
     const LP<double> P = level<double>(C, C.nlev);
@@ -251,6 +257,7 @@ __global__ void __launch_bounds__(kTile) k_apc_init(const CaseDev *__restrict__ 
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
+    if (S->halted) return;
     double v[2] = {0, 0};
     FOR_CELLS(t) {
         const double r = C.b[i] - S->mean_b;
@@ -370,6 +377,7 @@ template <class T> int dupload(HostCase *hc, T **d, const std::vector<T> &h) {
     cudaError_t e = cudaMalloc((void **)d, bytes);
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
     hc->amg_allocs.push_back(*d);
+    hc->bytes += bytes;
     if (h.empty()) return CFDL_OK;
     return cuda_status(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
 }
@@ -377,6 +385,7 @@ template <class T> int dzeros(HostCase *hc, T **d, size_t n) {
     cudaError_t e = cudaMalloc((void **)d, std::max<size_t>(1, n) * sizeof(T));
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
     hc->amg_allocs.push_back(*d);
+    hc->bytes += std::max<size_t>(1, n) * sizeof(T);
     return cuda_status(cudaMemset(*d, 0, std::max<size_t>(1, n) * sizeof(T)));
 }
 
@@ -451,18 +460,23 @@ int ensure_amg(cfdl_ctx *ctx) {
     for (HostCase *hc : ctx->cases) lmax = std::max(lmax, hc->dev.nlev);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
+    for (auto &wl : ctx->amg_slots) free_worklist(wl);
     ctx->amg_cells.assign(lmax + 1, WorkList());
     ctx->amg_smooth.assign(lmax + 1, WorkList());
+    ctx->amg_slots.assign(lmax + 1, WorkList());
     for (int l = 0; l <= lmax; l++) {
-        std::vector<int> cells, smooth;
+        std::vector<int> cells, smooth, slots;
         for (HostCase *hc : ctx->cases) {
             int n = l == 0 ? hc->ne : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].n : 0);
+            int W = l == 0 ? hc->W : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].W : 0);
             cells.push_back(l <= hc->dev.nlev ? n : 0);
             smooth.push_back(l < hc->dev.nlev ? n : 0);
+            slots.push_back(l <= hc->dev.nlev ? n * W : 0);
         }
         int st;
         if ((st = build_worklist(ctx, ctx->amg_cells[l], cells))) return st;
         if ((st = build_worklist(ctx, ctx->amg_smooth[l], smooth))) return st;
+        if ((st = build_worklist(ctx, ctx->amg_slots[l], slots))) return st;
     }
     ctx->amg_lmax = lmax;
     return upload_case_table(ctx);
@@ -491,7 +505,10 @@ int ensure_amg(cfdl_ctx *ctx) {
 // Coarse operators of every level and the coarsest inverse.
 static void amg_setup_operators(cfdl_ctx *ctx) {
     ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
-    for (int l = 1; l <= ctx->amg_lmax; l++) ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+    for (int l = 1; l <= ctx->amg_lmax; l++) {
+        ALAUNCH("k_amg_gal_off", k_amg_gal_off, ctx->amg_slots[l], l);
+        ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+    }
     CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, 256);
 }
 
@@ -565,6 +582,7 @@ __global__ void __launch_bounds__(kTile) k_mx_init(const CaseDev *__restrict__ c
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
+    if (S->halted) return;
     double v[2] = {0, 0};
     FOR_CELLS(t) {
         const double r = C.b[i] - S->mean_b;

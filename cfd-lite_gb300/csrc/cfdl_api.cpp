@@ -171,6 +171,7 @@ int cfdl_ctx_create(const cfdl_mesh *mesh, const cfdl_config *cfg, cfdl_ctx **ou
     if ((st = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)))) { delete ctx; return st; }
     HostCase *hc = nullptr;
     if ((st = create_case(ctx, mesh, cfg, &hc))) { cfdl_ctx_destroy(ctx); return st; }
+    hc->id = ctx->next_id++;
     ctx->cases.push_back(hc);
     if ((st = rebuild_worklists(ctx))) { cfdl_ctx_destroy(ctx); return st; }
     // construct_uvwp: mip = calc_mip(.false.) from the zero fields, mip0 = mip
@@ -219,6 +220,7 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     free_worklist(ctx->cellsv);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
+    for (auto &wl : ctx->amg_slots) free_worklist(wl);
     cudaFree(ctx->d_cases);
     cudaFree(ctx->d_partials);
     cudaFree(ctx->d_flags);
@@ -227,6 +229,8 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     prof_destroy(ctx);
     destroy_graph(ctx);
     cudaFree(ctx->d_loop_passes);
+    cudaFree(ctx->d_run_ctl);
+    if (ctx->h_run_ctl) cudaFreeHost(ctx->h_run_ctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CFDL_OK;
@@ -348,6 +352,145 @@ int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host) {
 int64_t cfdl_launch_count(const cfdl_ctx *ctx) {
     if (!ctx) return -1;
     return ctx->launches + graph_loop_kernels(const_cast<cfdl_ctx *>(ctx));
+}
+
+// ---------------------------------------------------------------- batches
+static int find_case(const cfdl_ctx *ctx, int id) {
+    for (size_t c = 0; c < ctx->cases.size(); c++) if (ctx->cases[c]->id == id) return (int)c;
+    return -1;
+}
+
+static bool same_form(const cfdl_config *a, const cfdl_config *b) {
+    return a->precision == b->precision && a->precond == b->precond;
+}
+
+int cfdl_batch_create(int ncases, const cfdl_mesh *meshes, const cfdl_config *cfgs, cfdl_ctx **out) {
+    if (!out || ncases <= 0 || !meshes || !cfgs) return CFDL_ERR_INVALID;
+    *out = nullptr;
+    for (int c = 0; c < ncases; c++) {
+        int st = validate_config(&cfgs[c]);
+        if (st) return st;
+        if (!same_form(&cfgs[0], &cfgs[c])) return CFDL_ERR_INVALID;
+    }
+    cfdl_ctx *ctx = nullptr;
+    int st = cfdl_ctx_create(&meshes[0], &cfgs[0], &ctx);
+    if (st) return st;
+    for (int c = 1; c < ncases; c++) {
+        HostCase *hc = nullptr;
+        if ((st = create_case(ctx, &meshes[c], &cfgs[c], &hc))) { cfdl_ctx_destroy(ctx); return st; }
+        hc->id = ctx->next_id++;
+        ctx->cases.push_back(hc);
+    }
+    if ((st = rebuild_worklists(ctx))) { cfdl_ctx_destroy(ctx); return st; }
+    *out = ctx;
+    return CFDL_OK;
+}
+
+int cfdl_case_add(cfdl_ctx *ctx, const cfdl_mesh *mesh, const cfdl_config *cfg, int *id) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = validate_config(cfg))) return st;
+    if (!same_form(&ctx->cases[0]->cfg, cfg)) return CFDL_ERR_INVALID;
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    HostCase *hc = nullptr;
+    if ((st = create_case(ctx, mesh, cfg, &hc))) return st;
+    hc->id = ctx->next_id++;
+    ctx->cases.push_back(hc);
+    // construct_uvwp on zero fields leaves mip = mip0 = 0, as allocated
+    if ((st = rebuild_worklists(ctx))) return st;
+    if (id) *id = hc->id;
+    return CFDL_OK;
+}
+
+int cfdl_case_remove(cfdl_ctx *ctx, int id) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    int c = find_case(ctx, id);
+    if (c < 0) return CFDL_ERR_INVALID;
+    if (ctx->cases.size() == 1) return CFDL_ERR_INVALID;   // a context keeps at least one case
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    destroy_case(ctx->cases[c]);
+    ctx->cases.erase(ctx->cases.begin() + c);
+    return rebuild_worklists(ctx);
+}
+
+int cfdl_case_count(const cfdl_ctx *ctx) { return ctx ? (int)ctx->cases.size() : -1; }
+
+int cfdl_case_ids(const cfdl_ctx *ctx, int *ids) {
+    if (!ctx || !ids) return CFDL_ERR_INVALID;
+    for (size_t c = 0; c < ctx->cases.size(); c++) ids[c] = ctx->cases[c]->id;
+    return CFDL_OK;
+}
+
+int cfdl_case_get_array(cfdl_ctx *ctx, int id, const char *name, double *host) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    int c = find_case(ctx, id);
+    if (c < 0) return CFDL_ERR_INVALID;
+    return copy_named(ctx, ctx->cases[c], name, host, true);
+}
+
+int cfdl_case_set_array(cfdl_ctx *ctx, int id, const char *name, const double *host) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    int c = find_case(ctx, id);
+    if (c < 0) return CFDL_ERR_INVALID;
+    return copy_named(ctx, ctx->cases[c], name, const_cast<double *>(host), false);
+}
+
+int cfdl_case_stats(cfdl_ctx *ctx, int id, cfdl_stats *st_out) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    int c = find_case(ctx, id);
+    if (c < 0 || !st_out) return CFDL_ERR_INVALID;
+    return read_stats(ctx, c, st_out);
+}
+
+int cfdl_case_info(const cfdl_ctx *ctx, int id, int *ne, size_t *device_bytes) {
+    if (!ctx) return CFDL_ERR_INVALID;
+    int c = find_case(ctx, id);
+    if (c < 0) return CFDL_ERR_INVALID;
+    if (ne) *ne = ctx->cases[c]->ne;
+    if (device_bytes) *device_bytes = ctx->cases[c]->bytes;
+    return CFDL_OK;
+}
+
+size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
+    const size_t c = (size_t)ne, f = (size_t)nf, b = (size_t)nbf, nc = c + b, w = (size_t)W;
+    size_t bytes = 0;
+    bytes += 2 * w * c * 4 + 3 * w * c * 8;          // ELL connectivity, gradient stencil
+    bytes += 2 * f * 4 + 16 * f * 8;                 // face tables, geometry planes
+    bytes += 3 * b * 4 + 3 * b * 8 + c * 8;          // halo tables, volume
+    bytes += 8 * nc * 8 + 15 * nc * 8 + 2 * f * 8;   // cell fields, gradients, mip/mip0
+    bytes += 9 * c * 8 + w * c * 8 + 7 * f * 8;      // coefficients, face intermediates
+    bytes += 27 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
+    bytes += 160 * c;                                 // multigrid hierarchy (bound)
+    return bytes;
+}
+
+int cfdl_case_set_run(cfdl_ctx *ctx, int id, int n_outer, int ncoef, double conv_tol) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (n_outer < 0 || ncoef < 0 || !(conv_tol >= 0)) return CFDL_ERR_INVALID;
+    if (id != -1 && find_case(ctx, id) < 0) return CFDL_ERR_INVALID;
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    for (HostCase *hc : ctx->cases) {
+        if (id != -1 && hc->id != id) continue;
+        SolveScalars S;
+        if ((st = cuda_status(cudaMemcpy(&S, hc->dev.sc, sizeof(S), cudaMemcpyDeviceToHost)))) return st;
+        S.run_left = n_outer; S.outer_done = 0; S.ncoef = ncoef; S.halted = 0; S.time_due = 0; S.converged = 0;
+        S.conv_tol = conv_tol; S.mip_abs = 0.0; S.mass_ratio = 0.0;
+        if ((st = cuda_status(cudaMemcpy(hc->dev.sc, &S, sizeof(S), cudaMemcpyHostToDevice)))) return st;
+    }
+    return CFDL_OK;
+}
+
+int cfdl_run(cfdl_ctx *ctx, int max_outer, int *running) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (max_outer < 0) return CFDL_ERR_INVALID;
+    if ((st = run_outer(ctx, max_outer, running))) return st;
+    return cuda_status(cudaGetLastError());
 }
 
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on) {

@@ -40,6 +40,7 @@ int case_alloc(HostCase *hc, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) { *p = nullptr; cudaGetLastError(); return cuda_status(e); }
     hc->allocs.push_back(*p);
+    hc->bytes += bytes;
     return CFDL_OK;
 }
 
@@ -64,7 +65,8 @@ int build_worklist(cfdl_ctx *ctx, WorkList &wl, const std::vector<int> &sizes, i
     for (size_t c = 0; c < sizes.size(); c++) {
         wl.case_first.push_back((int)wl.h_tiles.size());
         int cnt = 0;
-        for (int s = 0; s < sizes[c]; s += tile, cnt++) wl.h_tiles.push_back({(int)c, s, std::min(sizes[c], s + tile), 0});
+        for (int s = 0; s < sizes[c]; s += tile, cnt++)
+            wl.h_tiles.push_back({(int)c, s, std::min(sizes[c], s + tile), (tile + kTile - 1) / kTile});
         wl.case_ntiles.push_back(cnt);
     }
     wl.ntiles = (int)wl.h_tiles.size();
@@ -90,6 +92,9 @@ void apply_config(HostCase *hc, const cfdl_config *cfg) {
     d.nit = cfg->nit; d.solve_mode = cfg->solve_mode; d.tight_maxit = cfg->tight_maxit;
     d.precision = cfg->precision;
     d.precond = cfg->precond;
+    d.steady = std::isinf(cfg->dt) ? 1 : 0;
+    d.rdt = d.steady ? 0.0 : 1.0 / cfg->dt;
+    d.ralpha_u = 1.0 / cfg->alpha_u;
 }
 
 namespace {
@@ -335,10 +340,11 @@ int rebuild_worklists(cfdl_ctx *ctx) {
     if ((st = build_worklist(ctx, ctx->cells, nc))) return st;
     if ((st = build_worklist(ctx, ctx->faces, nfc))) return st;
     if ((st = build_worklist(ctx, ctx->halos, nh))) return st;
-    if ((st = build_worklist(ctx, ctx->cellsv, nc, kTile * kVec))) return st;
+    if ((st = build_worklist(ctx, ctx->cellsv, nc, kTile * ctx->vec))) return st;
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
-    ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_lmax = -1;
+    for (auto &wl : ctx->amg_slots) free_worklist(wl);
+    ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_slots.clear(); ctx->amg_lmax = -1;
     destroy_graph(ctx);   // captured launch arguments refer to the old lists
     int need = std::max({ctx->cells.ntiles, ctx->faces.ntiles, ctx->halos.ntiles, 1});
     if (need > ctx->partials_cap) {

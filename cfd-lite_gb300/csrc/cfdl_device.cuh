@@ -80,4 +80,56 @@ __device__ __forceinline__ bool last_tile_of_case(int *counter, int ntiles) {
 
 __device__ __forceinline__ int face_of(int fc) { return fc >= 0 ? fc : ~fc; }
 
+// Row i of an ELL operator, y_c = diag*x_c[i] - sum_k a[k][i]*x_c[nb[k][i]]
+// for NC vectors x_c = x + c*stride.  Neighbours outside [0, n) (halos,
+// padding) contribute nothing.  W is a compile-time width so the index and
+// coefficient loads of all slots are issued before any arithmetic; invalid
+// slots read x[i] with a zero coefficient instead of branching.
+template <int W, int NC, class T>
+__device__ __forceinline__ void ell_row_w(const int *__restrict__ nb, const T *__restrict__ a, T diag,
+                                          const T *x, int stride, int n, int i, T (&y)[NC]) {
+    int j[W];
+    T c[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const int jj = __ldg(&nb[k * n + i]);
+        const bool ok = (unsigned)jj < (unsigned)n;
+        j[k] = ok ? jj : i;
+        c[k] = ok ? a[k * n + i] : (T)0;
+    }
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        const T *xq = x + q * stride;
+        T s = diag * xq[i];
+#pragma unroll
+        for (int k = 0; k < W; k++) s -= c[k] * xq[j[k]];
+        y[q] = s;
+    }
+}
+
+template <int NC, class T>
+__device__ __forceinline__ void ell_row(const int *__restrict__ nb, const T *__restrict__ a, T diag, const T *x,
+                                        int stride, int n, int W, int i, T (&y)[NC]) {
+    if (W == 6) { ell_row_w<6, NC, T>(nb, a, diag, x, stride, n, i, y); return; }
+    if (W == 4) { ell_row_w<4, NC, T>(nb, a, diag, x, stride, n, i, y); return; }
+#pragma unroll
+    for (int q = 0; q < NC; q++) y[q] = diag * x[q * stride + i];
+    for (int k = 0; k < W; k++) {
+        const int jj = nb[k * n + i];
+        if ((unsigned)jj >= (unsigned)n) continue;
+        const T ak = a[k * n + i];
+#pragma unroll
+        for (int q = 0; q < NC; q++) y[q] -= ak * x[q * stride + jj];
+    }
+}
+
+// -x when neg, else x: a sign-bit flip in the integer pipe (no FP64 op)
+__device__ __forceinline__ double flip_sign(double x, bool neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ ((long long)neg << 63));
+}
+// max(x, 0) for non-NaN x, decided on the bit pattern (no FP64 op); -0 -> 0
+__device__ __forceinline__ double positive_part(double x) {
+    return __double_as_longlong(x) > 0 ? x : 0.0;
+}
+
 }  // namespace cfdl

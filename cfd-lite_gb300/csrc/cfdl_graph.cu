@@ -55,10 +55,14 @@ __global__ void k_setone(cudaGraphConditionalHandle h) {
 
 struct Builder {
     cfdl_ctx *ctx;
-    int64_t kernels = 0;
+    unsigned long long *passes;   // this graph's loop-pass counters
 
     void setcond(cudaGraphConditionalHandle h, int kind) {
-        k_setcond<<<1, 32, 0, ctx->stream>>>(ctx->d_cases, (int)ctx->cases.size(), h, kind, ctx->d_loop_passes);
+        k_setcond<<<1, 32, 0, ctx->stream>>>(ctx->d_cases, (int)ctx->cases.size(), h, kind, passes);
+        ctx->launches++;
+    }
+    void setone(cudaGraphConditionalHandle h) {
+        k_setone<<<1, 32, 0, ctx->stream>>>(h);
         ctx->launches++;
     }
     template <class F> int capture(F f, cudaGraph_t *out, int64_t *count) {
@@ -113,7 +117,7 @@ struct Builder {
 
 }  // namespace
 
-void destroy_graph(cfdl_ctx *ctx) {
+static void drop_uvwp_graph(cfdl_ctx *ctx) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
     ctx->graph_exec = nullptr;
@@ -121,51 +125,78 @@ void destroy_graph(cfdl_ctx *ctx) {
     ctx->graph_form = -1;
 }
 
+static void drop_run_graph(cfdl_ctx *ctx) {
+    if (ctx->run_exec) cudaGraphExecDestroy(ctx->run_exec);
+    if (ctx->run_graph) cudaGraphDestroy(ctx->run_graph);
+    ctx->run_exec = nullptr;
+    ctx->run_graph = nullptr;
+    ctx->run_form = -1;
+}
+
+void destroy_graph(cfdl_ctx *ctx) {
+    drop_uvwp_graph(ctx);
+    drop_run_graph(ctx);
+}
+
 static int graph_form(const cfdl_ctx *ctx) {
     const cfdl_config &c = ctx->cases[0]->cfg;
     return c.precision * 2 + c.precond;
 }
 
-int build_graph(cfdl_ctx *ctx) {
-    destroy_graph(ctx);
+static int ensure_graph_state(cfdl_ctx *ctx) {
+    int st;
+    if (ctx->cases[0]->cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
+    if (!ctx->d_loop_passes) {
+        const size_t bytes = kLoopSlots * sizeof(unsigned long long);
+        if ((st = cuda_status(cudaMalloc(&ctx->d_loop_passes, bytes)))) return st;
+        if ((st = cuda_status(cudaMemset(ctx->d_loop_passes, 0, bytes)))) return st;
+    }
+    return CFDL_OK;
+}
+
+// Appends the nodes of one solve_uvwp to G after *prev.  pre() is captured at
+// the head of the first segment, post() at the tail of the last.  Loop
+// handles are created in G and raised by a kernel before each loop, so the
+// same nodes work at the top level and inside the body of an outer loop.
+// static_k gets the kernels outside the loops, body[0..3] those of each
+// loop's body.
+template <class Pre, class Post>
+static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre, Post post, int64_t *static_k,
+                       int64_t *body) {
+    cfdl_ctx *ctx = b.ctx;
     const cfdl_config &cfg = ctx->cases[0]->cfg;
     int st;
-    if (cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
-    if (!ctx->d_loop_passes) {
-        if ((st = cuda_status(cudaMalloc(&ctx->d_loop_passes, 4 * sizeof(unsigned long long))))) return st;
-        if ((st = cuda_status(cudaMemset(ctx->d_loop_passes, 0, 4 * sizeof(unsigned long long))))) return st;
-    }
-    cudaGraph_t G = nullptr;
-    if ((st = cuda_status(cudaGraphCreate(&G, 0)))) return st;
-    Builder b{ctx};
-    ctx->capturing = true;
-    cudaGraphNode_t prev = nullptr;
     int64_t k = 0;
     cudaGraphConditionalHandle hm, hp;
-    int64_t body[4] = {0, 0, 0, 0};
-    auto fail = [&](int s) { ctx->capturing = false; cudaGraphDestroy(G); return s; };
-    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hm, G, 1, cudaGraphCondAssignDefault)))) return fail(st);
-    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hp, G, 1, cudaGraphCondAssignDefault)))) return fail(st);
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hm, G, 0, 0)))) return st;
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hp, G, 0, 0)))) return st;
     // momentum assembly and BiCGStab
-    if ((st = b.segment(G, &prev, [&] { launch_coef_uvw(ctx); mom_init(ctx); }, &k))) return fail(st);
-    b.kernels += k;
-    st = b.loop(G, &prev, hm, [&](cudaGraph_t body_g) {
+    if ((st = b.segment(G, prev, [&] {
+             pre();
+             launch_coef_uvw(ctx);
+             mom_init(ctx);
+             b.setone(hm);
+         }, &k)))
+        return st;
+    *static_k += k;
+    st = b.loop(G, prev, hm, [&](cudaGraph_t body_g) {
         return b.capture_into(body_g, [&] { mom_iter(ctx); b.setcond(hm, LOOP_MOM); }, &body[LOOP_MOM]);
     });
-    if (st) return fail(st);
+    if (st) return st;
     // gradients, Rhie-Chow fluxes, pressure assembly, pressure-solve start
-    if ((st = b.segment(G, &prev, [&] {
+    if ((st = b.segment(G, prev, [&] {
              launch_grad(ctx, 4);
              launch_calc_mip(ctx, 1);
              launch_coef_p(ctx);
              if (cfg.precision == 1) mx_init(ctx);
              else if (cfg.precond == 1) apc_init(ctx);
              else pcj_init(ctx);
+             b.setone(hp);
          }, &k)))
-        return fail(st);
-    b.kernels += k;
+        return st;
+    *static_k += k;
     if (cfg.precision == 0) {
-        st = b.loop(G, &prev, hp, [&](cudaGraph_t body_g) {
+        st = b.loop(G, prev, hp, [&](cudaGraph_t body_g) {
             return b.capture_into(body_g, [&] {
                 if (cfg.precond == 1) apc_iter(ctx);
                 else pcj_iter(ctx);
@@ -174,13 +205,13 @@ int build_graph(cfdl_ctx *ctx) {
         });
     } else {
         // refinement loop around the FP32 inner loop
-        st = b.loop(G, &prev, hp, [&](cudaGraph_t outer) {
+        st = b.loop(G, prev, hp, [&](cudaGraph_t outer) {
             cudaGraphConditionalHandle hi;
-            int s2 = cuda_status(cudaGraphConditionalHandleCreate(&hi, outer, 1, 0));
+            int s2 = cuda_status(cudaGraphConditionalHandleCreate(&hi, outer, 0, 0));
             if (s2) return s2;
             cudaGraphNode_t op = nullptr;
             int64_t k1 = 0, k2 = 0;
-            if ((s2 = b.segment(outer, &op, [&] { mx_start(ctx); k_setone<<<1, 32, 0, ctx->stream>>>(hi); ctx->launches++; }, &k1))) return s2;
+            if ((s2 = b.segment(outer, &op, [&] { mx_start(ctx); b.setone(hi); }, &k1))) return s2;
             if ((s2 = b.loop(outer, &op, hi, [&](cudaGraph_t inner) {
                      return b.capture_into(inner, [&] { mx_inner_iter(ctx); b.setcond(hi, LOOP_INNER); }, &body[LOOP_INNER]);
                  })))
@@ -190,24 +221,91 @@ int build_graph(cfdl_ctx *ctx) {
             return CFDL_OK;
         });
     }
-    if (st) return fail(st);
+    if (st) return st;
     // correction
-    if ((st = b.segment(G, &prev, [&] {
+    if ((st = b.segment(G, prev, [&] {
              launch_adjust_pc(ctx);
              launch_grad(ctx, 3);
              launch_update_uvwp(ctx);
+             post();
          }, &k)))
-        return fail(st);
-    b.kernels += k;
+        return st;
+    *static_k += k;
+    return CFDL_OK;
+}
+
+int build_graph(cfdl_ctx *ctx) {
+    drop_uvwp_graph(ctx);
+    int st;
+    if ((st = ensure_graph_state(ctx))) return st;
+    cudaGraph_t G = nullptr;
+    if ((st = cuda_status(cudaGraphCreate(&G, 0)))) return st;
+    Builder b{ctx, ctx->d_loop_passes};
+    ctx->capturing = true;
+    cudaGraphNode_t prev = nullptr;
+    int64_t stat = 0, body[4] = {0, 0, 0, 0};
+    st = append_uvwp(b, G, &prev, [] {}, [] {}, &stat, body);
     ctx->capturing = false;
+    if (st) { cudaGraphDestroy(G); return st; }
     cudaGraphExec_t exec = nullptr;
     if ((st = cuda_status(cudaGraphInstantiate(&exec, G, 0)))) { cudaGraphDestroy(G); return st; }
     ctx->graph = G;
     ctx->graph_exec = exec;
     ctx->graph_form = graph_form(ctx);
-    ctx->graph_static_kernels = b.kernels;
+    ctx->graph_static_kernels = stat;
     for (int i = 0; i < 4; i++) ctx->graph_body_kernels[i] = body[i];
     return CFDL_OK;
+}
+
+// The run graph: while (a case has outer iterations left and the launch's
+// budget is not spent) { per-case start; update_boundaries; solve_uvwp;
+// per-case end with the convergence test; gated update_time }.  Cases whose
+// run is over are skipped by every kernel until the host gives them more.
+int build_run_graph(cfdl_ctx *ctx) {
+    drop_run_graph(ctx);
+    int st;
+    if ((st = ensure_graph_state(ctx))) return st;
+    cudaGraph_t G = nullptr;
+    if ((st = cuda_status(cudaGraphCreate(&G, 0)))) return st;
+    Builder b{ctx, ctx->d_loop_passes + 4};
+    ctx->capturing = true;
+    cudaGraphNode_t prev = nullptr;
+    int64_t stat = 0, k = 0, body[5] = {0, 0, 0, 0, 0};
+    cudaGraphConditionalHandle hr;
+    auto fail = [&](int s) { ctx->capturing = false; cudaGraphDestroy(G); return s; };
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hr, G, 0, 0)))) return fail(st);
+    if ((st = b.segment(G, &prev, [&] { launch_run_cond(ctx, hr, 0, nullptr); }, &k))) return fail(st);
+    stat += k;
+    st = b.loop(G, &prev, hr, [&](cudaGraph_t outer) {
+        cudaGraphNode_t op = nullptr;
+        int64_t inner_static = 0;
+        int s2 = append_uvwp(
+            b, outer, &op, [&] { launch_run_begin(ctx); launch_bc(ctx); },
+            [&] { launch_run_end(ctx); launch_run_cond(ctx, hr, 1, ctx->d_loop_passes + 8); }, &inner_static, body);
+        body[4] = inner_static;
+        return s2;
+    });
+    if (st) return fail(st);
+    if ((st = b.segment(G, &prev, [&] { launch_run_finish(ctx); }, &k))) return fail(st);
+    stat += k;
+    ctx->capturing = false;
+    cudaGraphExec_t exec = nullptr;
+    if ((st = cuda_status(cudaGraphInstantiate(&exec, G, 0)))) { cudaGraphDestroy(G); return st; }
+    ctx->run_graph = G;
+    ctx->run_exec = exec;
+    ctx->run_form = graph_form(ctx);
+    ctx->run_static_kernels = stat;
+    for (int i = 0; i < 5; i++) ctx->run_body_kernels[i] = body[i];
+    return CFDL_OK;
+}
+
+int run_graph_launch(cfdl_ctx *ctx) {
+    int st;
+    if (!ctx->run_exec || ctx->run_form != graph_form(ctx))
+        if ((st = build_run_graph(ctx))) return st;
+    ctx->launches += ctx->run_static_kernels;
+    ctx->graph_launches++;
+    return cuda_status(cudaGraphLaunch(ctx->run_exec, ctx->stream));
 }
 
 // One solve_uvwp through the graph (built on first use, rebuilt when the
@@ -224,12 +322,14 @@ int solve_uvwp_graph(cfdl_ctx *ctx) {
 // Kernels the graph ran inside its loops so far (synchronises).
 int64_t graph_loop_kernels(cfdl_ctx *ctx) {
     if (!ctx->d_loop_passes) return 0;
-    unsigned long long passes[4] = {0, 0, 0, 0};
+    unsigned long long passes[kLoopSlots] = {};
     if (cudaMemcpyAsync(passes, ctx->d_loop_passes, sizeof(passes), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         return 0;
     int64_t n = 0;
     for (int i = 0; i < 4; i++) n += (int64_t)passes[i] * ctx->graph_body_kernels[i];
+    for (int i = 0; i < 4; i++) n += (int64_t)passes[4 + i] * ctx->run_body_kernels[i];
+    n += (int64_t)passes[8] * ctx->run_body_kernels[4];
     return n;
 }
 

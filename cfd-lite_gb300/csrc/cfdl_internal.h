@@ -31,13 +31,17 @@ namespace cfdl {
 constexpr int kTile = 256;        // cells / faces / halos per CTA
 constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
 constexpr int kNPart = 16;        // partial slots per tile
-constexpr int kVec = 4;           // cells per thread in the solver kernels (tile = kTile*kVec cells)
+constexpr int kVec = 4;           // default cells per thread in the solver kernels
 constexpr int kMixedMaxOuter = 60;   // FP64 refinement cycles of the mixed pressure solve
+// loop-pass counters: [0,4) loops of the solve_uvwp graph, [4,8) the same
+// loops inside the run graph, [8] the run graph's outer loop
+constexpr int kLoopSlots = 9;
 
 // Loop over the cells of a wide solver tile: thread t handles cells
-// first+t, first+t+kTile, ... (coalesced, kVec of them).
+// first+t, first+t+kTile, ... (coalesced); the tile's pad field holds how many
+// cells each thread takes (the tile shape the autotuner chooses).
 #define FOR_CELLS(t) \
-    for (int j_ = 0, i = (t).first + (int)threadIdx.x; j_ < cfdl::kVec; j_++, i += cfdl::kTile) if (i < (t).last)
+    for (int j_ = 0, i = (t).first + (int)threadIdx.x; j_ < (t).pad; j_++, i += cfdl::kTile) if (i < (t).last)
 
 // face geometry planes, precomputed once per mesh (cfdl_case.cpp)
 enum FaceGeo {
@@ -71,6 +75,9 @@ struct SolveScalars {
     float rz32, tol32, alpha32, beta32, rnorm32;
     int active32, iters32;
     double mass_imbalance;
+    // outer-iteration runs (cfdl_run.cu): per-case targets and progress
+    int run_left, outer_done, ncoef, halted, time_due, converged;
+    double conv_tol, mip_abs, mass_ratio;
 };
 
 struct CaseDev {
@@ -106,9 +113,13 @@ struct CaseDev {
     int *counters;                        // [16] last-tile counters, zero between launches
     // parameters
     double dt, alpha_u, alpha_p, rtol_u, rtol_p, tight_rtol;
+    double rdt, ralpha_u;                 // 1/dt (0 when steady), 1/alpha_u
     int nit, solve_mode, tight_maxit, precision, precond;
+    int steady;                           // dt = INFINITY: the transient terms vanish
 };
 
+// A tile of a work list: case c, entities [first, last); pad = entities per
+// thread (1 for the kTile-entity lists, the solver tile shape for cellsv).
 struct Tile { int c, first, last, pad; };
 
 // One work list per entity type, with each case's tile range for reductions.
@@ -129,6 +140,8 @@ struct HostCase {
     CaseDev dev{};                   // host mirror of the device struct
     AmgHierarchy *amg = nullptr;     // host hierarchy, built on first AMG use
     std::vector<void *> amg_allocs;  // device allocations of the hierarchy
+    int id = 0;                      // stable case id within its context
+    size_t bytes = 0;                // device bytes held (mesh, fields, solver, hierarchy)
 };
 
 }  // namespace cfdl
@@ -138,10 +151,12 @@ struct cfdl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::vector<cfdl::HostCase *> cases;
+    int next_id = 0;                     // id given to the next added case
     cfdl::CaseDev *d_cases = nullptr;
     int d_cases_cap = 0;
     cfdl::WorkList cells, faces, halos;
-    cfdl::WorkList cellsv;               // wide tiles (kTile*kVec cells) for the solver kernels
+    cfdl::WorkList cellsv;               // wide tiles (kTile*vec cells) for the solver kernels
+    int vec = cfdl::kVec;                // cells per thread in those tiles (autotuned)
     int last_iters_m = 0, last_iters_p = 0;   // previous inner iteration counts (poll scheduling)
     double *d_partials = nullptr;        // [max tiles][kNPart]
     int partials_cap = 0;                // tiles
@@ -154,7 +169,7 @@ struct cfdl_ctx {
     void *prof = nullptr;                // event profiler state (cfdl_prof.cpp)
     // AMG work lists: amg_cells[l] = level-l cells of cases with nlev >= l,
     // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
-    std::vector<cfdl::WorkList> amg_cells, amg_smooth;
+    std::vector<cfdl::WorkList> amg_cells, amg_smooth, amg_slots;   // amg_slots[l]: W_l*n_l ELL slots
     int amg_lmax = -1;
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;
@@ -162,7 +177,13 @@ struct cfdl_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     int graph_form = -1;
     int64_t graph_static_kernels = 0, graph_body_kernels[4] = {0, 0, 0, 0}, graph_launches = 0;
-    unsigned long long *d_loop_passes = nullptr;   // passes of each loop kind
+    unsigned long long *d_loop_passes = nullptr;   // passes of each loop kind, [kLoopSlots]
+    // runs of many outer iterations as one graph launch (cfdl_run.cu)
+    cudaGraph_t run_graph = nullptr;
+    cudaGraphExec_t run_exec = nullptr;
+    int run_form = -1;
+    int64_t run_static_kernels = 0, run_body_kernels[5] = {0, 0, 0, 0, 0};
+    int *d_run_ctl = nullptr, *h_run_ctl = nullptr;   // [0] outer passes left, [1] cases still running
 };
 
 namespace cfdl {
@@ -228,4 +249,13 @@ int build_graph(cfdl_ctx *ctx);
 void destroy_graph(cfdl_ctx *ctx);
 int solve_uvwp_graph(cfdl_ctx *ctx);
 int64_t graph_loop_kernels(cfdl_ctx *ctx);
+int build_run_graph(cfdl_ctx *ctx);
+int run_graph_launch(cfdl_ctx *ctx);
+
+// runs of many outer iterations (cfdl_run.cu)
+void launch_run_begin(cfdl_ctx *ctx);
+void launch_run_end(cfdl_ctx *ctx);
+void launch_run_cond(cfdl_ctx *ctx, cudaGraphConditionalHandle h, int consume, unsigned long long *passes);
+void launch_run_finish(cfdl_ctx *ctx);
+int run_outer(cfdl_ctx *ctx, int max_outer, int *running);
 }  // namespace cfdl

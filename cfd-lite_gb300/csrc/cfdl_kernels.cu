@@ -17,8 +17,8 @@ namespace {
 #define TILE_PROLOGUE(WL)                         \
     const Tile t = tiles[blockIdx.x];             \
     const CaseDev &C = cases[t.c];                \
-    const int i = t.first + (int)threadIdx.x;     \
-    (void)C;
+    if (C.sc->halted) return;                     \
+    const int i = t.first + (int)threadIdx.x;
 
 // ---------------------------------------------------------------------------
 // update_boundaries -> lid / dirichlet0 / symmetry, mod_physics.f90:38-50,
@@ -103,21 +103,31 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
         const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
         const double sg = fc >= 0 ? 1.0 : -1.0;
-        const double fl = -sg * C.mip[f];
-        const double ak = C.fdiff[f] + fmax(fl, 0.0);
+        // inward flux f = -sg*mip and upwind max(f,0): sign and comparison on
+        // the bit pattern, so they cost no FP64 instruction
+        const double fl = flip_sign(C.mip[f], fc >= 0);
+        const double ak = C.fdiff[f] + positive_part(fl);
         sumf += fl;
         a[k] = ak;
         ap += ak;
         ss0 += sg * C.fS[f]; ss1 += sg * C.fS[nf + f]; ss2 += sg * C.fS[2 * nf + f];
         dd0 += sg * C.fD[f]; dd1 += sg * C.fD[nf + f]; dd2 += sg * C.fD[2 * nf + f];
     }
+    double asum = ap;                       // sum of the anb of this row so far
     const double vol = C.vol[i];
-    const double ap0 = C.rho[i] * vol / C.dt;
-    ap = ap + ap0;
     const double ue = C.u[i], ve = C.v[i], we = C.w[i];
-    double bu = ap0 * C.u0[i] + sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
-    double bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
-    double bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+    double bu, bv, bw;
+    if (C.steady) {                         // ap0 = rho*vol/dt = 0
+        bu = sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
+        bv = sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
+        bw = sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+    } else {
+        const double ap0 = C.rho[i] * vol * C.rdt;
+        ap = ap + ap0;
+        bu = ap0 * C.u0[i] + sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
+        bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
+        bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+    }
     // boundary conditions in BC-loop order (ascending halo index)
     for (int q = 1; q < nb_cnt; q++) {
         int s = bslot[q], j = q - 1;
@@ -139,25 +149,21 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
             bw = bw + dbc * r2 - dbc * we;
         }
         ap = ap + dbc;
+        asum = asum + dbc;
         a[k] = a[k] + dbc;
     }
     if (C.alpha_u != 1.0) {
-        const double apr = ap / C.alpha_u, f1 = (1.0 - C.alpha_u) * apr;
+        const double apr = ap * C.ralpha_u, f1 = (1.0 - C.alpha_u) * apr;
         bu = bu + f1 * ue; bv = bv + f1 * ve; bw = bw + f1 * we;
         ap = apr;
     }
     C.ap[i] = ap;
     C.bu[i] = bu; C.bv[i] = bv; C.bw[i] = bw;
     C.d[i] = vol / ap;
-    double dcs = ap;
 #pragma unroll
-    for (int k = 0; k < kMaxW; k++) {
-        if (k < W) {
-            dcs = dcs - a[k];
-            C.anb[k * ne + i] = a[k];
-        }
-    }
-    C.dc[i] = vol / dcs;
+    for (int k = 0; k < kMaxW; k++)
+        if (k < W) C.anb[k * ne + i] = a[k];
+    C.dc[i] = vol / (ap - asum);            // SIMPLEC: vol / (ap - sum anb)
 }
 
 // ---------------------------------------------------------------------------
@@ -216,10 +222,12 @@ __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ 
         const double gy = omw * C.gp[3 * o + 1] + wt * C.gp[3 * n + 1];
         const double gz = omw * C.gp[3 * o + 2] + wt * C.gp[3 * n + 2];
         const double dip = omw * C.d[o] + wt * C.d[n];
-        const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
         const double rdip = rhoip * dip;
-        mip = mip - rdip * g[FG_ADN * nf + i] * ((C.p[n] - C.p[o]) - (gx * D0 + gy * D1 + gz * D2))
-                  - rhoip / C.dt * dip * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
+        mip = mip - rdip * g[FG_ADN * nf + i] * ((C.p[n] - C.p[o]) - (gx * D0 + gy * D1 + gz * D2));
+        if (!C.steady) {   // the transient term carries 1/dt and vanishes when steady
+            const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
+            mip = mip - rdip * C.rdt * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
+        }
     }
     C.mip[i] = mip;
 }

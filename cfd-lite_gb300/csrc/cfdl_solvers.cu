@@ -33,16 +33,9 @@ __device__ __forceinline__ const double *comp_rhs(const CaseDev &C, int q) { ret
 
 // (A x)_i for the interior operator: ap_i x_i - sum_{interior nb} anb x_nb
 __device__ __forceinline__ double amul_row(const CaseDev &C, const double *x, int i) {
-    const int ne = C.ne;
-    double s = C.ap[i] * x[i];
-#pragma unroll
-    for (int k = 0; k < kMaxW; k++) {
-        if (k >= C.W) break;
-        const int nb = C.hf_nb[k * ne + i];
-        if (nb < 0) break;
-        if (nb < ne) s -= C.anb[k * ne + i] * x[nb];
-    }
-    return s;
+    double y[1];
+    ell_row<1, double>(C.hf_nb, C.anb, C.ap[i], x, 0, C.ne, C.W, i, y);
+    return y[0];
 }
 
 __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->active[0] | S->active[1] | S->active[2]) != 0; }
@@ -51,6 +44,7 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
     const Tile t = tiles[blockIdx.x];                         \
     const CaseDev &C = cases[t.c];                            \
     SolveScalars *S = C.sc;                                   \
+    if (S->halted) return;                                    \
     const int ne = C.ne;                                      \
     (void)ne;
 
@@ -128,13 +122,15 @@ __global__ void __launch_bounds__(kTile) k_mom_v(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[3] = {0, 0, 0};
+    const int act[3] = {S->active[0], S->active[1], S->active[2]};
     FOR_CELLS(t) {
+        double y[3];   // one pass over the row for the three components
+        ell_row<3, double>(C.hf_nb, C.anb, C.ap[i], C.kph, ne, ne, C.W, i, y);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            if (!S->active[q]) continue;
-            const double y = amul_row(C, C.kph + q * ne, i);
-            C.kv[q * ne + i] = y;
-            v[q] += C.krh[q * ne + i] * y;
+            if (!act[q]) continue;
+            C.kv[q * ne + i] = y[q];
+            v[q] += C.krh[q * ne + i] * y[q];
         }
     }
     block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -187,15 +183,17 @@ __global__ void __launch_bounds__(kTile) k_mom_t(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[6] = {0, 0, 0, 0, 0, 0};
+    const int act[3] = {S->active[0] && !S->half[0], S->active[1] && !S->half[1], S->active[2] && !S->half[2]};
     FOR_CELLS(t) {
+        double y[3];
+        ell_row<3, double>(C.hf_nb, C.anb, C.ap[i], C.ksh, ne, ne, C.W, i, y);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            if (!S->active[q] || S->half[q]) continue;
+            if (!act[q]) continue;
             const int j = q * ne + i;
-            const double y = amul_row(C, C.ksh + q * ne, i);
-            C.kt[j] = y;
-            v[q] += y * C.ks[j];
-            v[3 + q] += y * y;
+            C.kt[j] = y[q];
+            v[q] += y[q] * C.ks[j];
+            v[3 + q] += y[q] * y[q];
         }
     }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -472,6 +470,10 @@ int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st) {
     for (int q = 0; q < 3; q++) { st->res_i[q] = S.r0norm[q]; st->res_f[q] = S.rnorm[q]; }
     st->res_i[3] = S.r0norm_p; st->res_f[3] = S.rnorm_p;
     st->mass_imbalance = S.mass_imbalance;
+    st->outer_done = S.outer_done;
+    st->run_left = S.run_left;
+    st->converged = S.converged;
+    st->mass_ratio = S.mass_ratio;
     st->status = 0;
     for (int q = 0; q < 3; q++) if (S.status[q]) st->status = S.status[q];
     if (S.status_p) st->status = S.status_p;

@@ -14,6 +14,7 @@
  */
 #ifndef CFDL_H
 #define CFDL_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -123,6 +124,11 @@ typedef struct cfdl_stats {
     double res_i[4], res_f[4];       /* initial/final residual 2-norms (u,v,w,pc)     */
     double mass_imbalance;           /* ||b||2 of calc_coef_p (net inflow per cell)   */
     int    status;
+    /* progress of cfdl_run (zero until a run target is set) */
+    int    outer_done;               /* outer iterations run since cfdl_case_set_run  */
+    int    run_left;                 /* outer iterations still to run                 */
+    int    converged;                /* 1 once mass_ratio <= the run's tolerance      */
+    double mass_ratio;               /* mass_imbalance / sum_f |mip_f| after the pass */
 } cfdl_stats;
 
 /* Fields in reference layout (host pointers; NULL members are skipped). */
@@ -225,6 +231,43 @@ int cfdl_set_graph_mode(cfdl_ctx *ctx, int on);
  * *nlev coarse levels; n[0..nlev] cells and W[0..nlev] ELL widths per level
  * (level 0 = the mesh); at most maxlev+1 entries are written. */
 int cfdl_amg_info(cfdl_ctx *ctx, int maxlev, int *nlev, int *n, int *W);
+
+/* ---- batches: many independent cases in one context ---------------------
+ * No counterpart in the reference, which holds one case per process.  Every
+ * case of a context is advanced by the same launches (each kernel's work list
+ * holds tiles of all cases; reductions are per case and deterministic), so a
+ * case's results do not depend on the other cases sharing the context.  All
+ * cases share the pressure-solve form (precision, precond); the other
+ * configuration members are per case.  Cases are named by the ids these calls
+ * return (the context's first case has id 0); the context-level entry points
+ * above address the first case for fields and statistics and advance all of
+ * them. */
+int cfdl_batch_create(int ncases, const cfdl_mesh *meshes, const cfdl_config *cfgs, cfdl_ctx **ctx);
+int cfdl_case_add(cfdl_ctx *ctx, const cfdl_mesh *mesh, const cfdl_config *cfg, int *id);
+int cfdl_case_remove(cfdl_ctx *ctx, int id);       /* the last case cannot be removed */
+int cfdl_case_count(const cfdl_ctx *ctx);
+int cfdl_case_ids(const cfdl_ctx *ctx, int *ids);  /* ids[cfdl_case_count()] */
+int cfdl_case_get_array(cfdl_ctx *ctx, int id, const char *name, double *host);
+int cfdl_case_set_array(cfdl_ctx *ctx, int id, const char *name, const double *host);
+int cfdl_case_stats(cfdl_ctx *ctx, int id, cfdl_stats *stats);
+/* cells and device bytes held by one case */
+int cfdl_case_info(const cfdl_ctx *ctx, int id, int *ne, size_t *device_bytes);
+/* upper estimate of the device bytes of a case, before it is created */
+size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W);
+
+/* ---- runs: many outer iterations per launch ------------------------------
+ * The reference's time loop (src/modules/mod_physics.f90:23-36:
+ * update_boundaries, solve_uvwp, update_time every ncoef outer iterations)
+ * with a target per case.  cfdl_case_set_run gives case `id` (-1: every
+ * case) n_outer iterations to run, the update_time cadence ncoef (0: never)
+ * and a tolerance conv_tol on mass_imbalance / sum_f |mip_f| at which the
+ * case stops early (0: none), and resets its progress counters.  cfdl_run
+ * then runs up to max_outer passes; in each pass every case with iterations
+ * left does one outer iteration and the others are left untouched.  With
+ * graphs on (the default) the whole call is one CUDA graph launch.  *running
+ * (optional) receives the number of cases with iterations left. */
+int cfdl_case_set_run(cfdl_ctx *ctx, int id, int n_outer, int ncoef, double conv_tol);
+int cfdl_run(cfdl_ctx *ctx, int max_outer, int *running);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);

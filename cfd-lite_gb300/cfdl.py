@@ -57,6 +57,36 @@ class Stats(C.Structure):
                 "mass_ratio": self.mass_ratio}
 
 
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int), ("tet", C.c_int), ("jitter", C.c_double), ("seed", C.c_uint64),
+                ("re", C.c_double), ("conv_tol", C.c_double), ("max_outer", C.c_int), ("keep_fields", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_double), ("hbm_reserve", C.c_double),
+                ("max_cases", C.c_int), ("chunk", C.c_int), ("prep_threads", C.c_int),
+                ("precision", C.c_int), ("precond", C.c_int), ("tile", C.c_int),
+                ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("ne", C.c_int), ("outer_done", C.c_int),
+                ("converged", C.c_int), ("mass_ratio", C.c_double), ("t_submit", C.c_double),
+                ("t_ready", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("done", C.c_int64), ("queued", C.c_int64), ("launches", C.c_int64),
+                ("resident", C.c_int), ("held_bytes", C.c_double), ("cell_iters", C.c_double),
+                ("busy_s", C.c_double), ("now", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Mesh(C.Structure):
     _fields_ = [("ne", C.c_int), ("nf", C.c_int), ("nbf", C.c_int),
                 ("ef2nb1", C.c_void_p), ("ef2nb2", C.c_void_p), ("ef2nb_idx", C.c_void_p),
@@ -131,6 +161,20 @@ def lib():
     L.cfdl_case_bytes_estimate.restype = C.c_size_t
     L.cfdl_case_set_run.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double]
     L.cfdl_run.argtypes = [vp, C.c_int, ip]
+    L.cfdl_set_tile.argtypes = [vp, C.c_int]
+    L.cfdl_server_config_default.argtypes = [C.POINTER(ServerConfig)]
+    L.cfdl_server_config_default.restype = None
+    L.cfdl_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.cfdl_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_int64)]
+    L.cfdl_server_poll.argtypes = [vp, C.POINTER(Result), C.c_int, ip, C.c_double]
+    L.cfdl_server_fields.argtypes = [vp, C.c_int64, C.c_char_p, vp, C.POINTER(C.c_int64)]
+    L.cfdl_server_drain.argtypes = [vp, C.c_double]
+    L.cfdl_server_query.argtypes = [vp, C.POINTER(ServerInfo)]
+    L.cfdl_server_now.argtypes = [vp]
+    L.cfdl_server_now.restype = C.c_double
+    L.cfdl_server_destroy.argtypes = [vp]
+    L.cfdl_get_tile.argtypes = [vp]
+    L.cfdl_autotune.argtypes = [vp, C.c_int, ip, dp]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]
@@ -304,6 +348,21 @@ class Solver:
         _check(lib().cfdl_run(self._h, int(max_outer), C.byref(running)), "run")
         return running.value
 
+    def set_tile(self, vec):
+        """Cells per thread of the inner-solve kernels (1, 2, 4 or 8)."""
+        _check(lib().cfdl_set_tile(self._h, int(vec)), "set_tile")
+
+    def get_tile(self):
+        return int(lib().cfdl_get_tile(self._h))
+
+    def autotune(self, outer=3):
+        """Times each tile shape on this context's cases (state restored) and
+        keeps the fastest; returns (best, {vec: ms per outer iteration})."""
+        best = C.c_int()
+        ms = (C.c_double * 4)()
+        _check(lib().cfdl_autotune(self._h, int(outer), C.byref(best), ms), "autotune")
+        return best.value, dict(zip((1, 2, 4, 8), list(ms)))
+
     def set_graph_mode(self, on):
         """solve_uvwp as one CUDA graph (True, default) or as individual launches."""
         _check(lib().cfdl_set_graph_mode(self._h, int(bool(on))), "set_graph_mode")
@@ -452,3 +511,64 @@ class Batch(Solver):
 
 def case_bytes_estimate(ne, nf, nbf, W=6):
     return int(lib().cfdl_case_bytes_estimate(int(ne), int(nf), int(nbf), int(W)))
+
+
+def server_config(**kw):
+    c = ServerConfig()
+    lib().cfdl_server_config_default(C.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+class Server:
+    """Continuous-batching cavity solver on one device (see cfdl_server_*)."""
+
+    def __init__(self, config=None, **kw):
+        self.config = config if config is not None else server_config(**kw)
+        self._h = C.c_void_p()
+        _check(lib().cfdl_server_create(C.byref(self.config), C.byref(self._h)), "server_create")
+
+    def submit(self, n, tet=False, jitter=0.0, seed=0, re=100.0, conv_tol=1e-6, max_outer=1000, keep_fields=False):
+        r = Request(int(n), int(bool(tet)), float(jitter), int(seed), float(re), float(conv_tol), int(max_outer),
+                    int(bool(keep_fields)))
+        rid = C.c_int64()
+        _check(lib().cfdl_server_submit(self._h, C.byref(r), C.byref(rid)), "server_submit")
+        return rid.value
+
+    def poll(self, wait_s=0.0, max_results=256):
+        out = (Result * max_results)()
+        n = C.c_int()
+        _check(lib().cfdl_server_poll(self._h, out, max_results, C.byref(n), float(wait_s)), "server_poll")
+        return [out[i] for i in range(n.value)]
+
+    def fields(self, rid, name):
+        n = C.c_int64()
+        _check(lib().cfdl_server_fields(self._h, int(rid), name.encode(), None, C.byref(n)), "server_fields")
+        a = np.zeros(n.value)
+        _check(lib().cfdl_server_fields(self._h, int(rid), name.encode(), _p(a), C.byref(n)), "server_fields")
+        return a
+
+    def drain(self, timeout_s=0.0):
+        _check(lib().cfdl_server_drain(self._h, float(timeout_s)), "server_drain")
+
+    def info(self):
+        i = ServerInfo()
+        _check(lib().cfdl_server_query(self._h, C.byref(i)), "server_query")
+        return i.as_dict()
+
+    def now(self):
+        return lib().cfdl_server_now(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cfdl_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -19,6 +19,7 @@
 #include "cfdl_amg.h"
 #include "cfdl_device.cuh"
 #include <algorithm>
+#include <new>
 
 namespace cfdl {
 namespace {
@@ -389,27 +390,61 @@ template <class T> int dzeros(HostCase *hc, T **d, size_t n) {
     return cuda_status(cudaMemset(*d, 0, std::max<size_t>(1, n) * sizeof(T)));
 }
 
-// Build and upload the hierarchy of one case (mesh-only, once).
-int build_case_amg(HostCase *hc) {
-    if (hc->amg) return CFDL_OK;
-    CaseDev &d = hc->dev;
-    const int ne = hc->ne, W = hc->W, nf = hc->nf;
-    // strength = area/(dr.n) per interior slot, read back from the device planes
-    std::vector<int> nb((size_t)W * ne), fc((size_t)W * ne);
-    std::vector<double> adn(nf);
-    int st;
-    if ((st = cuda_status(cudaMemcpy(nb.data(), d.hf_nb, nb.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
-    if ((st = cuda_status(cudaMemcpy(fc.data(), d.hf_fc, fc.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
-    if ((st = cuda_status(cudaMemcpy(adn.data(), d.fgeo + (size_t)FG_ADN * nf, nf * sizeof(double), cudaMemcpyDeviceToHost)))) return st;
-    std::vector<double> strength((size_t)W * ne, 0.0);
+// strength of each ELL slot = |area/(dr.n)| of its face; -1 marks the slots
+// that are not interior couplings
+void amg_strength(int ne, int W, const int *nb_in, const int *fc, const double *adn, std::vector<int> &nb,
+                  std::vector<double> &strength) {
+    nb.assign(nb_in, nb_in + (size_t)W * ne);
+    strength.assign((size_t)W * ne, 0.0);
     for (size_t s = 0; s < nb.size(); s++) {
         if (nb[s] < 0 || nb[s] >= ne) { nb[s] = -1; continue; }
         int f = fc[s] >= 0 ? fc[s] : ~fc[s];
         strength[s] = std::fabs(adn[f]);
     }
+}
+
+// Build and upload the hierarchy of one case (mesh-only, once).
+int build_case_amg(HostCase *hc) {
+    if (hc->amg) return CFDL_OK;
+    CaseDev &d = hc->dev;
+    const int ne = hc->ne, W = hc->W, nf = hc->nf;
+    // the slot tables and face planes, read back from the device
+    std::vector<int> nb0((size_t)W * ne), fc((size_t)W * ne);
+    std::vector<double> adn(nf);
+    int st;
+    if ((st = cuda_status(cudaMemcpy(nb0.data(), d.hf_nb, nb0.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
+    if ((st = cuda_status(cudaMemcpy(fc.data(), d.hf_fc, fc.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
+    if ((st = cuda_status(cudaMemcpy(adn.data(), d.fgeo + (size_t)FG_ADN * nf, nf * sizeof(double), cudaMemcpyDeviceToHost)))) return st;
+    std::vector<int> nb;
+    std::vector<double> strength;
+    amg_strength(ne, W, nb0.data(), fc.data(), adn.data(), nb, strength);
     AmgHierarchy *H = new AmgHierarchy;
     AmgFineView fv{ne, W, nb.data(), strength.data()};
     if ((st = build_amg_hierarchy(fv, *H))) { delete H; return st; }
+    return upload_case_amg(hc, H);
+}
+
+}  // namespace
+
+int prepare_case_amg(CasePrep *p) {
+    if (!p || p->amg) return p ? CFDL_OK : CFDL_ERR_INVALID;
+    std::vector<int> nb;
+    std::vector<double> strength;
+    amg_strength(p->ne, p->W, p->hf_nb.data(), p->hf_fc.data(), p->fgeo.data() + (size_t)FG_ADN * p->nf, nb, strength);
+    AmgHierarchy *H = new (std::nothrow) AmgHierarchy;
+    if (!H) return CFDL_ERR_OOM;
+    AmgFineView fv{p->ne, p->W, nb.data(), strength.data()};
+    int st = build_amg_hierarchy(fv, *H);
+    if (st) { delete H; return st; }
+    p->amg = H;
+    return CFDL_OK;
+}
+
+// Upload a host-built hierarchy into the case, which takes ownership of it.
+int upload_case_amg(HostCase *hc, AmgHierarchy *H) {
+    CaseDev &d = hc->dev;
+    const int ne = hc->ne;
+    int st;
     hc->amg = H;
     const int nlev = (int)H->levels.size();
     std::vector<AmgLevelDev> devl(nlev);
@@ -444,7 +479,6 @@ int build_case_amg(HostCase *hc) {
     return CFDL_OK;
 }
 
-}  // namespace
 
 int ensure_amg(cfdl_ctx *ctx) {
     bool changed = false;

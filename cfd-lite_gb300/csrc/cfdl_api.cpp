@@ -110,6 +110,16 @@ int finish(cfdl_ctx *ctx, cfdl_stats *st) {
 }  // namespace
 
 namespace cfdl {
+cfdl_ctx *ctx_new() {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return nullptr; }
+    cfdl_ctx *ctx = new (std::nothrow) cfdl_ctx;
+    if (!ctx) return nullptr;
+    cudaGetDevice(&ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return nullptr; }
+    return ctx;
+}
+
 int solve_uvwp_all(cfdl_ctx *ctx) {
     // solve_uvwp, src/equations/mod_uvwp.f90:95-134: as one graph launch unless
     // graphs are off or launches are being profiled one by one

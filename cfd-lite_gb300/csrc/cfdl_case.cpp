@@ -189,9 +189,23 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
 
 }  // namespace
 
-int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostCase **out) {
-    *out = nullptr;
-    if (!m || !cfg) return CFDL_ERR_INVALID;
+CasePrep::~CasePrep() { delete amg; }
+
+void CasePrep::release_tables() {
+    std::vector<int>().swap(ef2nb_idx); std::vector<int>().swap(hf_nb); std::vector<int>().swap(hf_fc);
+    std::vector<int>().swap(f_own); std::vector<int>().swap(f_nb); std::vector<int>().swap(h_own);
+    std::vector<int>().swap(h_face); std::vector<int>().swap(h_kind);
+    std::vector<double>().swap(hf_G); std::vector<double>().swap(fgeo); std::vector<double>().swap(h_vel);
+    std::vector<double>().swap(vol);
+    delete amg;
+    amg = nullptr;
+}
+
+// Host half of create_case: validates the reference-layout arrays and builds
+// every device-layout table.  Touches no device state, so it may run on any
+// host thread (the serving loop prepares meshes ahead of admission).
+int prepare_case(const cfdl_mesh *m, CasePrep *p) {
+    if (!m || !p) return CFDL_ERR_INVALID;
     const int ne = m->ne, nf = m->nf, nbf = m->nbf;
     if (ne <= 0 || nf <= 0 || nbf < 0 || !m->ef2nb1 || !m->ef2nb2 || !m->ef2nb_idx || !m->s2g ||
         (nbf > 0 && !m->bs) || !m->aip || !m->rip || !m->xc || !m->yc || !m->zc || !m->vol)
@@ -200,22 +214,20 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
     const int H = 2 * nf - nbf;
     if (H <= 0 || m->ef2nb_idx[0] != 1 || m->ef2nb_idx[ne] != H + 1) return CFDL_ERR_INVALID;
     const int nc = ne + nbf;
-    HostCase *hc = new (std::nothrow) HostCase;
-    if (!hc) return CFDL_ERR_OOM;
-    int st = CFDL_OK;
     try {
-        hc->ne = ne; hc->nf = nf; hc->nbf = nbf; hc->H = H;
-        hc->ef2nb_idx.assign(m->ef2nb_idx, m->ef2nb_idx + ne + 1);
+        p->ne = ne; p->nf = nf; p->nbf = nbf; p->H = H;
+        p->ef2nb_idx.assign(m->ef2nb_idx, m->ef2nb_idx + ne + 1);
         int W = 0;
         for (int e = 0; e < ne; e++) {
             int cnt = m->ef2nb_idx[e + 1] - m->ef2nb_idx[e];
-            if (cnt <= 0 || cnt > kMaxW) { delete hc; return CFDL_ERR_INVALID; }
+            if (cnt <= 0 || cnt > kMaxW) return CFDL_ERR_INVALID;
             W = std::max(W, cnt);
         }
-        hc->W = W;
+        p->W = W;
         // ---- ELL half-faces + validation of every index ----
-        std::vector<int> hf_nb((size_t)W * ne, -1), hf_fc((size_t)W * ne, 0);
-        std::vector<int> f_own(nf, -1), f_nb(nf, -1);
+        std::vector<int> &hf_nb = p->hf_nb, &hf_fc = p->hf_fc, &f_own = p->f_own, &f_nb = p->f_nb;
+        hf_nb.assign((size_t)W * ne, -1); hf_fc.assign((size_t)W * ne, 0);
+        f_own.assign(nf, -1); f_nb.assign(nf, -1);
         for (int e = 0; e < ne; e++) {
             for (int idx = m->ef2nb_idx[e]; idx < m->ef2nb_idx[e + 1]; idx++) {
                 int k = idx - m->ef2nb_idx[e];
@@ -223,38 +235,40 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
                 get_idx(m->ef2nb1[idx - 1], enb, lfnb);
                 int fg = m->ef2nb2[idx - 1];
                 int fa = fg >= 0 ? fg : -fg;
-                if (enb < 1 || enb > nc || fa < 1 || fa > nf) { delete hc; return CFDL_ERR_INVALID; }
-                if ((lfnb == 0) != (enb > ne)) { delete hc; return CFDL_ERR_INVALID; }
+                if (enb < 1 || enb > nc || fa < 1 || fa > nf) return CFDL_ERR_INVALID;
+                if ((lfnb == 0) != (enb > ne)) return CFDL_ERR_INVALID;
                 hf_nb[(size_t)k * ne + e] = enb - 1;
                 hf_fc[(size_t)k * ne + e] = fg > 0 ? fa - 1 : ~(fa - 1);
                 if (fg > 0) {
-                    if (f_own[fa - 1] != -1) { delete hc; return CFDL_ERR_INVALID; }
+                    if (f_own[fa - 1] != -1) return CFDL_ERR_INVALID;
                     f_own[fa - 1] = e; f_nb[fa - 1] = enb - 1;
                 }
             }
         }
         for (int f = 0; f < nf; f++) {
-            if (f_own[f] < 0) { delete hc; return CFDL_ERR_INVALID; }
+            if (f_own[f] < 0) return CFDL_ERR_INVALID;
             int e, lf;
             get_idx(m->s2g[f], e, lf);           // s2g names the owner side
-            if (e - 1 != f_own[f]) { delete hc; return CFDL_ERR_INVALID; }
+            if (e - 1 != f_own[f]) return CFDL_ERR_INVALID;
         }
         // ---- halos and boundary conditions ----
-        std::vector<int> h_own(std::max(nbf, 1), 0), h_face(std::max(nbf, 1), 0), h_kind(std::max(nbf, 1), 0);
-        std::vector<double> h_vel(3 * (size_t)std::max(nbf, 1), 0.0);
+        std::vector<int> &h_own = p->h_own, &h_face = p->h_face, &h_kind = p->h_kind;
+        std::vector<double> &h_vel = p->h_vel;
+        h_own.assign(std::max(nbf, 1), 0); h_face.assign(std::max(nbf, 1), 0); h_kind.assign(std::max(nbf, 1), 0);
+        h_vel.assign(3 * (size_t)std::max(nbf, 1), 0.0);
         for (int h = 0; h < nbf; h++) {
             int b = m->bs[h] < 0 ? -m->bs[h] : m->bs[h], e, lf;
             get_idx(b, e, lf);
-            if (e < 1 || e > ne || lf < 1 || lf > m->ef2nb_idx[e] - m->ef2nb_idx[e - 1]) { delete hc; return CFDL_ERR_INVALID; }
+            if (e < 1 || e > ne || lf < 1 || lf > m->ef2nb_idx[e] - m->ef2nb_idx[e - 1]) return CFDL_ERR_INVALID;
             int fg = m->ef2nb2[m->ef2nb_idx[e - 1] + lf - 1 - 1];
-            if (fg < 1 || f_nb[fg - 1] != ne + h) { delete hc; return CFDL_ERR_INVALID; }
+            if (fg < 1 || f_nb[fg - 1] != ne + h) return CFDL_ERR_INVALID;
             h_own[h] = e - 1; h_face[h] = fg - 1;
         }
         for (int bc = 0; bc < m->nbc; bc++) {
             int a = m->bc_esec[2 * bc], z = m->bc_esec[2 * bc + 1];
-            if (a < ne + 1 || z > nc || a > z + 1) { delete hc; return CFDL_ERR_INVALID; }
+            if (a < ne + 1 || z > nc || a > z + 1) return CFDL_ERR_INVALID;
             int kind = m->bc_kind[bc];
-            if (kind != CFDL_BC_WALL && kind != CFDL_BC_SYMMETRY) { delete hc; return CFDL_ERR_INVALID; }
+            if (kind != CFDL_BC_WALL && kind != CFDL_BC_SYMMETRY) return CFDL_ERR_INVALID;
             for (int el = a; el <= z; el++) {
                 int h = el - ne - 1;
                 h_kind[h] = kind;
@@ -262,7 +276,8 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
             }
         }
         // ---- face geometry planes ----
-        std::vector<double> fgeo((size_t)FG_N * nf, 0.0);
+        std::vector<double> &fgeo = p->fgeo;
+        fgeo.assign((size_t)FG_N * nf, 0.0);
         auto G = [&](int plane, int f) -> double & { return fgeo[(size_t)plane * nf + f]; };
         for (int f = 0; f < nf; f++) {
             int e = f_own[f], n = f_nb[f];
@@ -296,7 +311,8 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
             }
         }
         // ---- least-squares gradient stencil ----
-        std::vector<double> hf_G(3 * (size_t)W * ne, 0.0);
+        std::vector<double> &hf_G = p->hf_G;
+        hf_G.assign(3 * (size_t)W * ne, 0.0);
         for (int e = 0; e < ne; e++) {
             double A[3][3] = {{0}}, Ai[3][3], wdr[kMaxW][3];
             int cnt = m->ef2nb_idx[e + 1] - m->ef2nb_idx[e];
@@ -318,18 +334,48 @@ int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostC
                 for (int q = 0; q < 3; q++)
                     hf_G[((size_t)q * W + k) * ne + e] = Ai[q][0]*wdr[k][0] + Ai[q][1]*wdr[k][1] + Ai[q][2]*wdr[k][2];
         }
-        // ---- device upload ----
-        st = upload_all(hc, cfg, hf_nb, hf_fc, hf_G, f_own, f_nb, fgeo, h_own, h_face, h_kind, h_vel,
-                        std::vector<double>(m->vol, m->vol + ne));
+        p->vol.assign(m->vol, m->vol + ne);
+    } catch (const std::bad_alloc &) {
+        return CFDL_ERR_OOM;
+    }
+    return CFDL_OK;
+}
+
+// Device half: allocates and uploads the case (and a host-built multigrid
+// hierarchy, whose ownership moves to the case).
+int upload_case(CasePrep &p, const cfdl_config *cfg, HostCase **out) {
+    *out = nullptr;
+    if (!cfg) return CFDL_ERR_INVALID;
+    HostCase *hc = new (std::nothrow) HostCase;
+    if (!hc) return CFDL_ERR_OOM;
+    int st;
+    try {
+        hc->ne = p.ne; hc->nf = p.nf; hc->nbf = p.nbf; hc->H = p.H; hc->W = p.W;
+        hc->ef2nb_idx = p.ef2nb_idx;
+        st = upload_all(hc, cfg, p.hf_nb, p.hf_fc, p.hf_G, p.f_own, p.f_nb, p.fgeo, p.h_own, p.h_face, p.h_kind,
+                        p.h_vel, p.vol);
+        if (!st && p.amg) {
+            st = upload_case_amg(hc, p.amg);   // takes the hierarchy
+            p.amg = nullptr;
+        }
         if (st) { destroy_case(hc); return st; }
         apply_config(hc, cfg);
     } catch (const std::bad_alloc &) {
         destroy_case(hc);
         return CFDL_ERR_OOM;
     }
-    (void)ctx;
     *out = hc;
     return CFDL_OK;
+}
+
+int create_case(cfdl_ctx *ctx, const cfdl_mesh *m, const cfdl_config *cfg, HostCase **out) {
+    *out = nullptr;
+    if (!cfg) return CFDL_ERR_INVALID;
+    CasePrep p;
+    int st = prepare_case(m, &p);
+    if (st) return st;
+    (void)ctx;
+    return upload_case(p, cfg, out);
 }
 
 // Tile work lists over every case of the context.

@@ -192,6 +192,23 @@ int case_alloc(HostCase *hc, void **p, size_t bytes);
 int rebuild_worklists(cfdl_ctx *ctx);
 int upload_case_table(cfdl_ctx *ctx);
 int create_case(cfdl_ctx *ctx, const cfdl_mesh *mesh, const cfdl_config *cfg, HostCase **out);
+// create_case in two halves: host tables (any thread), then device upload
+struct CasePrep {
+    int ne = 0, nf = 0, nbf = 0, W = 0, H = 0;
+    std::vector<int> ef2nb_idx, hf_nb, hf_fc, f_own, f_nb, h_own, h_face, h_kind;
+    std::vector<double> hf_G, fgeo, h_vel, vol;
+    AmgHierarchy *amg = nullptr;     // optional, built on the host by prepare_case_amg
+    CasePrep() = default;
+    CasePrep(const CasePrep &) = delete;
+    CasePrep &operator=(const CasePrep &) = delete;
+    ~CasePrep();
+    void release_tables();           // frees the host tables, keeps the sizes
+};
+int prepare_case(const cfdl_mesh *mesh, CasePrep *p);
+cfdl_ctx *ctx_new();                 // a context with no cases yet (the serving loop's)
+int prepare_case_amg(CasePrep *p);
+int upload_case(CasePrep &p, const cfdl_config *cfg, HostCase **out);
+int upload_case_amg(HostCase *hc, AmgHierarchy *H);
 void destroy_case(HostCase *hc);
 void apply_config(HostCase *hc, const cfdl_config *cfg);
 

@@ -1,0 +1,129 @@
+// cfdl_tune.cpp -- the solver tile shape and its autotuner.
+//
+// The Krylov, multigrid-transfer and reduction kernels of the inner solves
+// run over the "wide" cell work list, whose tiles hold kTile * vec cells (vec
+// cells per thread).  Wide tiles mean fewer partial sums per reduction and
+// more independent loads in flight per thread; narrow tiles mean more CTAs
+// for small cases.  The best vec depends on the mix of case sizes, so the
+// autotuner measures it: for each candidate it times a few outer iterations
+// on the context's own cases, from a snapshot of their state that is put back
+// afterwards, and keeps the fastest.  The tile shape changes the order of the
+// partial sums, so results agree across shapes to rounding, not bit for bit;
+// the shape is a property of the context, and cases compared bit for bit
+// must share it.
+#include "cfdl_internal.h"
+#include <cstring>
+
+using namespace cfdl;
+
+namespace {
+
+constexpr int kTileShapes[] = {1, 2, 4, 8};
+
+struct Snap { double *p; size_t n; };
+
+std::vector<Snap> state_arrays(HostCase *hc) {
+    CaseDev &d = hc->dev;
+    const size_t nc = (size_t)hc->ne + hc->nbf, nf = hc->nf;
+    return {{d.u, nc}, {d.v, nc}, {d.w, nc}, {d.p, nc}, {d.u0, nc}, {d.v0, nc}, {d.w0, nc},
+            {d.gu, 3 * nc}, {d.gv, 3 * nc}, {d.gw, 3 * nc}, {d.gp, 3 * nc}, {d.gpc, 3 * nc},
+            {d.mip, nf}, {d.mip0, nf}};
+}
+
+// Device copy of every case's outer-iteration state and solver scalars.
+struct Snapshot {
+    std::vector<char *> bufs;
+    ~Snapshot() { for (char *b : bufs) cudaFree(b); }
+
+    int take(cfdl_ctx *ctx) {
+        for (HostCase *hc : ctx->cases) {
+            size_t bytes = sizeof(SolveScalars);
+            for (const Snap &s : state_arrays(hc)) bytes += s.n * sizeof(double);
+            char *b = nullptr;
+            int st = cuda_status(cudaMalloc(&b, bytes));
+            if (st) return st;
+            bufs.push_back(b);
+            size_t off = 0;
+            for (const Snap &s : state_arrays(hc)) {
+                if ((st = cuda_status(cudaMemcpyAsync(b + off, s.p, s.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream)))) return st;
+                off += s.n * sizeof(double);
+            }
+            if ((st = cuda_status(cudaMemcpyAsync(b + off, hc->dev.sc, sizeof(SolveScalars), cudaMemcpyDeviceToDevice, ctx->stream)))) return st;
+        }
+        return cuda_status(cudaStreamSynchronize(ctx->stream));
+    }
+
+    int restore(cfdl_ctx *ctx) {
+        for (size_t c = 0; c < ctx->cases.size(); c++) {
+            HostCase *hc = ctx->cases[c];
+            size_t off = 0;
+            int st;
+            for (const Snap &s : state_arrays(hc)) {
+                if ((st = cuda_status(cudaMemcpyAsync(s.p, bufs[c] + off, s.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream)))) return st;
+                off += s.n * sizeof(double);
+            }
+            if ((st = cuda_status(cudaMemcpyAsync(hc->dev.sc, bufs[c] + off, sizeof(SolveScalars), cudaMemcpyDeviceToDevice, ctx->stream)))) return st;
+        }
+        return cuda_status(cudaStreamSynchronize(ctx->stream));
+    }
+};
+
+bool valid_shape(int vec) {
+    for (int v : kTileShapes) if (v == vec) return true;
+    return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfdl_set_tile(cfdl_ctx *ctx, int vec) {
+    if (!ctx || ctx->cases.empty() || !valid_shape(vec)) return CFDL_ERR_INVALID;
+    if (vec == ctx->vec) return CFDL_OK;
+    int st = cuda_status(cudaStreamSynchronize(ctx->stream));
+    if (st) return st;
+    ctx->vec = vec;
+    return rebuild_worklists(ctx);
+}
+
+int cfdl_get_tile(const cfdl_ctx *ctx) { return ctx ? ctx->vec : -1; }
+
+int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms) {
+    if (!ctx || ctx->cases.empty() || outer <= 0) return CFDL_ERR_INVALID;
+    Snapshot snap;
+    int st = snap.take(ctx);
+    if (st) return st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if ((st = cuda_status(cudaEventCreate(&e0)))) return st;
+    if ((st = cuda_status(cudaEventCreate(&e1)))) { cudaEventDestroy(e0); return st; }
+    const int n = (int)(sizeof(kTileShapes) / sizeof(kTileShapes[0]));
+    int pick = ctx->vec;
+    double best_ms = -1.0;
+    for (int k = 0; k < n && !st; k++) {
+        const int v = kTileShapes[k];
+        if ((st = cfdl_set_tile(ctx, v))) break;
+        // warm-up: builds this shape's multigrid lists and graph
+        if ((st = solve_uvwp_all(ctx)) || (st = snap.restore(ctx))) break;
+        cudaEventRecord(e0, ctx->stream);
+        for (int i = 0; i < outer && !st; i++) {
+            launch_bc(ctx);
+            st = solve_uvwp_all(ctx);
+        }
+        if (st) break;
+        cudaEventRecord(e1, ctx->stream);
+        float f = 0.f;
+        if ((st = cuda_status(cudaEventSynchronize(e1)))) break;
+        if ((st = cuda_status(cudaEventElapsedTime(&f, e0, e1)))) break;
+        if (ms) ms[k] = f / outer;
+        if (best_ms < 0.0 || f < best_ms) { best_ms = f; pick = v; }
+        st = snap.restore(ctx);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    if ((st = cfdl_set_tile(ctx, pick))) return st;
+    if (best) *best = pick;
+    return snap.restore(ctx);
+}
+
+}  // extern "C"

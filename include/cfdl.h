@@ -269,6 +269,81 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W);
 int cfdl_case_set_run(cfdl_ctx *ctx, int id, int n_outer, int ncoef, double conv_tol);
 int cfdl_run(cfdl_ctx *ctx, int max_outer, int *running);
 
+/* ---- solver tile shape and its autotuner ---------------------------------
+ * No counterpart in the reference.  The inner-solve kernels give each CTA
+ * 256 * vec cells (vec = 1, 2, 4 or 8; default 4).  cfdl_autotune times
+ * `outer` outer iterations of the context's own cases with each vec, from a
+ * snapshot of their state that it restores afterwards, keeps the fastest and
+ * returns it in *best; ms[4] (optional) receives the time per outer
+ * iteration of each candidate.  The shape changes the order of the partial
+ * sums, so results agree across shapes to rounding, not bit for bit. */
+int cfdl_set_tile(cfdl_ctx *ctx, int vec);
+int cfdl_get_tile(const cfdl_ctx *ctx);
+int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms);
+
+/* ---- serving loop ---------------------------------------------------------
+ * No counterpart in the reference.  Solves lid-driven-cavity requests with
+ * continuous batching on one device: host threads prepare each request's mesh
+ * (zone, set-up, device tables, multigrid hierarchy) while the device runs;
+ * one device thread admits prepared requests in arrival order while a slot is
+ * free and their device bytes fit both hbm_budget and the memory the device
+ * reports free (less hbm_reserve), runs every resident case `chunk` outer
+ * iterations per graph launch (steady SIMPLE, alpha_u/alpha_p, rho = 1,
+ * u_lid = 1, mu = 1/re), and retires a case when its mass ratio reaches
+ * conv_tol or it has run max_outer iterations.  State stays on the device
+ * between outer iterations.  A request's result does not depend on the
+ * requests that shared its launches (same tile shape assumed). */
+typedef struct cfdl_request {
+    int      n;             /* mesh edge: n^3 hexes, or 6 n^3 tets             */
+    int      tet;           /* 1: every hex split into 6 tets                  */
+    double   jitter;        /* interior-node jitter, fraction of the spacing   */
+    uint64_t seed;          /* jitter seed                                     */
+    double   re;            /* Reynolds number                                 */
+    double   conv_tol;      /* stop at mass_imbalance / sum|mip| <= conv_tol   */
+    int      max_outer;     /* outer-iteration cap                             */
+    int      keep_fields;   /* 1: keep u, v, w, p for cfdl_server_fields       */
+} cfdl_request;
+
+typedef struct cfdl_server_config {
+    int    device;
+    double hbm_budget;      /* device bytes the resident cases may hold        */
+    double hbm_reserve;     /* device bytes always left free                   */
+    int    max_cases;       /* resident-case slots                             */
+    int    chunk;           /* outer iterations per launch between admissions  */
+    int    prep_threads;    /* host threads preparing meshes                   */
+    int    precision, precond;   /* pressure-solve form (cfdl_config)          */
+    int    tile;            /* solver tile shape (0: the default)              */
+    double alpha_u, alpha_p;
+} cfdl_server_config;
+
+typedef struct cfdl_result {
+    int64_t id;
+    int     status, ne, outer_done, converged;
+    double  mass_ratio;
+    double  t_submit, t_ready, t_admit, t_done;   /* seconds on the server clock */
+} cfdl_result;
+
+typedef struct cfdl_server_info {
+    int64_t submitted, done, queued, launches;
+    int     resident;
+    double  held_bytes, cell_iters, busy_s, now;
+} cfdl_server_info;
+
+typedef struct cfdl_server cfdl_server;
+void   cfdl_server_config_default(cfdl_server_config *cfg);
+int    cfdl_server_create(const cfdl_server_config *cfg, cfdl_server **srv);
+int    cfdl_server_submit(cfdl_server *srv, const cfdl_request *req, int64_t *id);  /* thread-safe */
+/* up to max finished results not yet returned; waits up to wait_s for one */
+int    cfdl_server_poll(cfdl_server *srv, cfdl_result *out, int max, int *n, double wait_s);
+/* u, v, w or p [ne+nbf] of a finished request with keep_fields; *len = size */
+int    cfdl_server_fields(cfdl_server *srv, int64_t id, const char *name, double *host, int64_t *len);
+/* wait until every submitted request is finished (timeout_s <= 0: no limit) */
+int    cfdl_server_drain(cfdl_server *srv, double timeout_s);
+int    cfdl_server_query(cfdl_server *srv, cfdl_server_info *info);
+double cfdl_server_now(cfdl_server *srv);
+/* stops at once: unfinished requests are dropped */
+int    cfdl_server_destroy(cfdl_server *srv);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);
 /* Human-readable text for a status code. */

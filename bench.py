@@ -52,6 +52,16 @@ def parse():
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served"],
+                    help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
+    ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
+    ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
+    ap.add_argument("--forms", default="0,1", help="batched/served: precisions to run (0 FP64, 1 mixed)")
+    ap.add_argument("--rates", default="5,200", help="served: request rates (req/s)")
+    ap.add_argument("--requests", type=int, default=16, help="served: requests per rate")
+    ap.add_argument("--max-outer", type=int, default=1000, help="served: outer-iteration cap per request")
+    ap.add_argument("--conv-tol", type=float, default=1e-6, help="served: mass-imbalance tolerance")
+    ap.add_argument("--n-range", default="", help="batched/served: override the mesh-edge range lo,hi")
     return ap.parse_args()
 
 
@@ -376,13 +386,186 @@ def run_reference(a, dist):
     return out
 
 
+# ------------------------------------------------------------ batched cases
+def run_batched(a, dist):
+    """Uneven cases in one context, every outer iteration of every case in
+    one graph launch (cfdl_run), one JSON line per pressure-solve form."""
+    import numpy as np
+    import cfdl
+    import workloads
+
+    cfdl.select_device(dist.local)
+    kw = {}
+    if a.n_range:
+        lo, hi = (int(x) for x in a.n_range.split(","))
+        kw = dict(n_lo=lo, n_hi=hi)
+    cases = workloads.batched_cases(seed=a.seed, count=a.cases, **kw)
+    t0 = time.perf_counter()
+    setups = workloads.build_setups(cases)
+    t_setup = time.perf_counter() - t0
+    total_cells = sum(s.ne for s in setups)
+    forms = [int(x) for x in a.forms.split(",")]
+    fields = {}
+    lines = []
+    for prec in forms:
+        cfgs = [cfdl.steady(mu=1.0 / c["re"], precision=prec) for c in cases]
+        t0 = time.perf_counter()
+        b = cfdl.Batch(setups, cfgs)
+        t_create = time.perf_counter() - t0
+        best, tune_ms = b.autotune(outer=2)
+        # warm-up passes (graph build, multigrid set-up), then the timed run
+        b.set_run(a.warmup)
+        b.run(a.warmup)
+        b.set_run(a.outer)
+        clocks = Clocks(dist.local)
+        dist.barrier()
+        clocks.start()
+        l0 = b.launch_count()
+        b.timer_begin()
+        t0 = time.perf_counter()
+        left = b.run(a.outer)
+        ms = b.timer_end()
+        wall = time.perf_counter() - t0
+        launches = b.launch_count() - l0
+        clk = clocks.stop()
+        ms = dist.max(max(ms, 0.0))
+        ids = b.ids()
+        stats = [b.case_stats(c) for c in ids]
+        assert left == 0 and all(st.outer_done == a.outer for st in stats)
+        value = dist.sum(total_cells * a.outer) / (ms / 1e3)
+        fields[prec] = [{f: b.case_get(c, f) for f in ("u", "v", "w", "p")} for c in ids]
+        # end to end: host fields in, the run, host fields out
+        nb_in = sum((4 * (s.ne + s.nbf) + s.nf) * 8 for s in setups)
+        nb_out = sum(4 * (s.ne + s.nbf) * 8 for s in setups)
+        host = [{f: fields[prec][k][f].copy() for f in ("u", "v", "w", "p")} for k in range(len(ids))]
+        mips = [b.case_get(c, "mip") for c in ids]
+        b.set_run(a.outer)
+        t0 = time.perf_counter()
+        for k, c in enumerate(ids):
+            for f in ("u", "v", "w", "p"):
+                b.case_set(c, f, host[k][f])
+            b.case_set(c, "mip", mips[k])
+        b.run(a.outer)
+        for k, c in enumerate(ids):
+            for f in ("u", "v", "w", "p"):
+                host[k][f] = b.case_get(c, f)
+        e2e_s = dist.max(time.perf_counter() - t0)
+        b.close()
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.outer,
+            "warmup": a.warmup, "ms_per_step": ms / a.outer, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == 0 else "f64+f32 (mixed pressure solve)",
+            "data": "synthetic (seeded cavity meshes)",
+            "config": {"workload": "batched: %d lid-driven cavity cases in one run, N~U{%d..%d} (seed %d), half "
+                                   "tet-split, Re log-U[10,1000], %d SIMPLE iterations each" %
+                                   (len(cases), min(c["n"] for c in cases), max(c["n"] for c in cases), a.seed,
+                                    a.outer),
+                       "cases": len(cases), "cells": total_cells, "tile": best,
+                       "autotune_ms_per_outer": {str(k): round(v, 3) for k, v in tune_ms.items()},
+                       "l2": "working set > L2 (no flush needed)", "parallelism": "single"},
+            "gpu_launches": launches,
+            "wall_s": wall, "host_setup_s": t_setup, "batch_create_s": t_create,
+            "e2e": {"value": dist.sum(total_cells * a.outer) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nb_in,
+                    "d2h_bytes_per_step": nb_out, "step": "one run of %d outer iterations" % a.outer,
+                    "api": "cfdl_case_set_array + cfdl_run + cfdl_case_get_array"},
+        }
+        if clk:
+            out["clocks"] = clk
+        lines.append(out)
+    if 0 in fields and 1 in fields:
+        worst = {}
+        for f in ("u", "v", "w", "p"):
+            worst[f] = max(float(np.linalg.norm(m[f] - d[f]) / max(np.linalg.norm(d[f]), 1e-300))
+                           for m, d in zip(fields[1], fields[0]))
+        for out in lines:
+            out["mixed_vs_fp64_rel_l2_max_over_cases"] = worst
+    return lines
+
+
+# ------------------------------------------------------------ served stream
+def run_served(a, dist):
+    """A Poisson stream of cavity requests through the serving loop; one JSON
+    line per (form, rate) with p50/p99 latency and throughput."""
+    import threading
+    import numpy as np
+    import cfdl
+    import workloads
+
+    cfdl.select_device(dist.local)
+    kw = {}
+    if a.n_range:
+        lo, hi = (int(x) for x in a.n_range.split(","))
+        kw = dict(n_lo=lo, n_hi=hi)
+    lines = []
+    for prec in [int(x) for x in a.forms.split(",")]:
+        for rate in [float(x) for x in a.rates.split(",")]:
+            reqs = workloads.served_requests(seed=a.seed, count=a.requests, rate=rate, **kw)
+            srv = cfdl.Server(precision=prec, hbm_budget=150e9)
+            t_start = srv.now()
+
+            def feeder():
+                for r in reqs:
+                    delay = t_start + r["t"] - srv.now()
+                    if delay > 0:
+                        time.sleep(delay)
+                    srv.submit(n=r["n"], tet=r["tet"], jitter=0.0, seed=a.seed, re=r["re"],
+                               conv_tol=a.conv_tol, max_outer=a.max_outer)
+
+            clocks = Clocks(dist.local)
+            clocks.start()
+            th = threading.Thread(target=feeder)
+            th.start()
+            th.join()
+            srv.drain()
+            clk = clocks.stop()
+            res = srv.poll(max_results=4 * len(reqs))
+            info = srv.info()
+            srv.close()
+            lat = np.array([r.t_done - r.t_submit for r in res])
+            dev = np.array([r.t_done - r.t_admit for r in res])
+            span = max(r.t_done for r in res) - min(r.t_submit for r in res)
+            out = {
+                "metric": "served cavity requests: p50/p99 latency (s)", "value": float(np.percentile(lat, 99)),
+                "unit": "s (p99 latency)", "higher_is_better": False, "n_gpus": dist.world,
+                "dtype": "f64" if prec == 0 else "f64+f32 (mixed pressure solve)",
+                "data": "synthetic (seeded Poisson request stream)",
+                "config": {"workload": "served: Poisson stream at %.0f req/s, %d requests, N~U{%d..%d}, hex or "
+                                       "tet-split, Re log-U[10,1000], stop at mass ratio %.0e or %d iterations; "
+                                       "admitted by free HBM against a 150 GB budget" %
+                                       (rate, len(reqs), min(r["n"] for r in reqs), max(r["n"] for r in reqs),
+                                        a.conv_tol, a.max_outer),
+                           "rate_req_s": rate, "requests": len(reqs)},
+                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "device_p50_s": float(np.percentile(dev, 50)), "device_p99_s": float(np.percentile(dev, 99)),
+                "throughput_req_s": len(res) / span, "cell_iters_per_s": info["cell_iters"] / span,
+                "converged": int(sum(r.converged for r in res)), "failed": int(sum(r.status != 0 for r in res)),
+                "outer_iterations": {"min": int(min(r.outer_done for r in res)),
+                                     "median": float(np.median([r.outer_done for r in res])),
+                                     "max": int(max(r.outer_done for r in res))},
+                "launches": info["launches"], "makespan_s": span,
+            }
+            if clk:
+                out["clocks"] = clk
+            lines.append(out)
+    return lines
+
+
 def main():
     a = parse()
     dist = Dist()
     try:
-        out = run_reference(a, dist) if a.impl == "reference" else run_ours(a, dist)
+        if a.impl == "reference":
+            out = run_reference(a, dist)
+        elif a.workload == "batched":
+            out = run_batched(a, dist)
+        elif a.workload == "served":
+            out = run_served(a, dist)
+        else:
+            out = run_ours(a, dist)
         if out is not None and dist.rank == 0:
-            print(json.dumps(out))
+            for line in (out if isinstance(out, list) else [out]):
+                print(json.dumps(line))
+                sys.stdout.flush()
     finally:
         dist.close()
 

@@ -8,6 +8,9 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
+#include <atomic>
+#include <algorithm>
 
 using namespace cfdl;
 
@@ -385,9 +388,26 @@ int cfdl_batch_create(int ncases, const cfdl_mesh *meshes, const cfdl_config *cf
     cfdl_ctx *ctx = nullptr;
     int st = cfdl_ctx_create(&meshes[0], &cfgs[0], &ctx);
     if (st) return st;
-    for (int c = 1; c < ncases; c++) {
+    // host tables (and multigrid hierarchies) of the other cases on host threads
+    std::vector<CasePrep> preps(ncases > 1 ? ncases - 1 : 0);
+    std::vector<int> pst(preps.size(), CFDL_OK);
+    {
+        std::atomic<int> next{0};
+        const int nthr = (int)std::min<size_t>(preps.size(), std::max(1u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthr; t++)
+            pool.emplace_back([&] {
+                for (int k; (k = next++) < (int)preps.size();) {
+                    pst[k] = prepare_case(&meshes[k + 1], &preps[k]);
+                    if (!pst[k] && cfgs[k + 1].precond == 1) pst[k] = prepare_case_amg(&preps[k]);
+                }
+            });
+        for (auto &t : pool) t.join();
+    }
+    for (size_t k = 0; k < preps.size(); k++) {
         HostCase *hc = nullptr;
-        if ((st = create_case(ctx, &meshes[c], &cfgs[c], &hc))) { cfdl_ctx_destroy(ctx); return st; }
+        if ((st = pst[k]) || (st = upload_case(preps[k], &cfgs[k + 1], &hc))) { cfdl_ctx_destroy(ctx); return st; }
+        preps[k].release_tables();
         hc->id = ctx->next_id++;
         ctx->cases.push_back(hc);
     }

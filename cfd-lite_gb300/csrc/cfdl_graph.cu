@@ -33,11 +33,12 @@ namespace {
 enum { LOOP_MOM = 0, LOOP_P = 1, LOOP_INNER = 2, LOOP_OUTER = 3 };
 
 // Loop condition = any case still active for this loop kind; counts the pass.
+// One warp: lane l reads cases l, l+32, ... and the warp votes.
 __global__ void k_setcond(const CaseDev *__restrict__ cases, int ncases, cudaGraphConditionalHandle h, int kind,
                           unsigned long long *loop_passes) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     int any = 0;
-    for (int c = 0; c < ncases; c++) {
+    for (int c = (int)threadIdx.x; c < ncases; c += 32) {
         const SolveScalars *S = cases[c].sc;
         int a;
         if (kind == LOOP_MOM) a = S->active[0] | S->active[1] | S->active[2];
@@ -45,8 +46,11 @@ __global__ void k_setcond(const CaseDev *__restrict__ cases, int ncases, cudaGra
         else a = S->active_p;
         any |= (a != 0);
     }
-    cudaGraphSetConditional(h, any ? 1u : 0u);
-    loop_passes[kind] += 1;
+    any = __any_sync(0xffffffffu, any);
+    if (threadIdx.x == 0) {
+        cudaGraphSetConditional(h, any ? 1u : 0u);
+        loop_passes[kind] += 1;
+    }
 }
 
 __global__ void k_setone(cudaGraphConditionalHandle h) {

@@ -85,22 +85,30 @@ __global__ void __launch_bounds__(kTile) k_run_time_faces(const CaseDev *__restr
 
 // Run-loop condition: a case has iterations left and the launch's pass
 // budget (ctl[0]) is not spent.  consume = 1 at the end of a pass.
+// (one warp; lane l counts cases l, l+32, ...)
+__device__ __forceinline__ int count_running(const CaseDev *__restrict__ cases, int ncases) {
+    int running = 0;
+    for (int c = (int)threadIdx.x; c < ncases; c += 32) running += cases[c].sc->run_left > 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) running += __shfl_xor_sync(0xffffffffu, running, o);
+    return running;
+}
+
 __global__ void k_run_cond(const CaseDev *__restrict__ cases, int ncases, cudaGraphConditionalHandle h, int consume,
                            int *ctl, unsigned long long *passes) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int running = count_running(cases, ncases);
+    if (threadIdx.x != 0) return;
     if (consume) { ctl[0] -= 1; if (passes) *passes += 1; }
-    int running = 0;
-    for (int c = 0; c < ncases; c++) running += cases[c].sc->run_left > 0;
     ctl[1] = running;
     cudaGraphSetConditional(h, (running > 0 && ctl[0] > 0) ? 1u : 0u);
 }
 
 // eager form of the condition: the same count, no graph handle
 __global__ void k_run_count(const CaseDev *__restrict__ cases, int ncases, int *ctl) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int running = 0;
-    for (int c = 0; c < ncases; c++) running += cases[c].sc->run_left > 0;
-    ctl[1] = running;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int running = count_running(cases, ncases);
+    if (threadIdx.x == 0) ctl[1] = running;
 }
 
 __global__ void k_run_finish(const CaseDev *__restrict__ cases, int ncases) {

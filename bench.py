@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served", "pressure"],
                     help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
     ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
@@ -482,6 +482,84 @@ def run_batched(a, dist):
     return lines
 
 
+# ------------------------------------------------------- pressure solve
+def run_pressure(a, dist):
+    """Seconds for one pressure-correction solve to a 1e-8 relative residual,
+    FP64 AMG-PCG against the mixed form (FP32 AMG-PCG inside FP64 iterative
+    refinement), on the same assembled system; then the per-field error of
+    the mixed form against FP64 after the same outer iterations."""
+    import numpy as np
+    import cfdl
+
+    cfdl.select_device(dist.local)
+    n = a.n if a.n != 128 else 256
+    mu = 0.0025
+    t0 = time.perf_counter()
+    zone = cfdl.Zone(n, a.tet, 0.1 if a.jitter == 0.2 else a.jitter, seed=a.seed)
+    setup = cfdl.Setup(zone)
+    t_setup = time.perf_counter() - t0
+    base = dict(mu=mu, solve_mode=1, tight_rtol=1e-8, precond=1)
+    g = cfdl.Solver(setup, cfdl.steady(precision=0, **base))
+    g.step(a.warmup, ncoef=0)                      # a developed flow state
+    names = ("u", "v", "w", "p", "u0", "v0", "w0", "gu", "gv", "gw", "gp", "gpc", "mip", "mip0")
+    state = {f: g.get(f) for f in names}
+
+    def assemble():
+        for f, v in state.items():
+            g.set(f, v)
+        g.update_boundaries()
+        g.calc_coef_uvw()
+        g.solve_momentum()
+        g.calc_grad("uvw")
+        g.calc_mip(True)
+        g.calc_coef_p()
+
+    out_forms = {}
+    for prec in (0, 1):
+        g.set_config(cfdl.steady(precision=prec, **base))
+        assemble()
+        g.solve_pc()                               # warm: hierarchy, graph-free path
+        times, st = [], None
+        for _ in range(max(3, min(a.steps, 10))):
+            assemble()
+            g.timer_begin()
+            st = g.solve_pc()
+            times.append(g.timer_end())
+        out_forms[prec] = {"ms": statistics.median(times), "iters": st.it_p, "res_rel": st.res_f[3] / st.res_i[3],
+                           "phic": g.get("phic")}
+    ref = out_forms[0]["phic"]
+    err_pc = float(np.linalg.norm(out_forms[1]["phic"] - ref) / np.linalg.norm(ref))
+    # fields after the same outer iterations with each form, from the same state
+    fields = {}
+    for prec in (0, 1):
+        g.set_config(cfdl.steady(precision=prec, **base))
+        for f, v in state.items():
+            g.set(f, v)
+        g.step(a.outer if a.outer != 300 else 5, ncoef=0)
+        fields[prec] = {f: g.get(f) for f in ("u", "v", "w", "p")}
+    field_err = {f: float(np.linalg.norm(fields[1][f] - fields[0][f]) / np.linalg.norm(fields[0][f]))
+                 for f in ("u", "v", "w", "p")}
+    ne = setup.ne
+    g.close()
+    out = {
+        "metric": "pressure-correction solve time to 1e-8 relative residual", "value": out_forms[1]["ms"] / 1e3,
+        "unit": "s", "higher_is_better": False, "n_gpus": dist.world, "dtype": "f64+f32 (mixed pressure solve)",
+        "data": "synthetic (seeded jittered unit-cube hex mesh)",
+        "config": {"workload": "pressure solve: cavity %d^3 hex (%d cells), jitter %.2f, Re=400 (mu=0.0025), "
+                               "system of outer iteration %d" % (n, ne, 0.1 if a.jitter == 0.2 else a.jitter,
+                                                                 a.warmup + 1),
+                   "cells": ne, "host_setup_s": t_setup},
+        "fp64": {"s": out_forms[0]["ms"] / 1e3, "pcg_iterations": out_forms[0]["iters"],
+                 "final_rel_residual": out_forms[0]["res_rel"]},
+        "mixed": {"s": out_forms[1]["ms"] / 1e3, "inner_iterations": out_forms[1]["iters"],
+                  "final_rel_residual_fp64": out_forms[1]["res_rel"],
+                  "phic_rel_l2_vs_fp64": err_pc},
+        "speedup_mixed_vs_fp64": out_forms[0]["ms"] / out_forms[1]["ms"],
+        "fields_rel_l2_mixed_vs_fp64_after_%d_outer" % (a.outer if a.outer != 300 else 5): field_err,
+    }
+    return out
+
+
 # ------------------------------------------------------------ served stream
 def run_served(a, dist):
     """A Poisson stream of cavity requests through the serving loop; one JSON
@@ -560,6 +638,8 @@ def main():
             out = run_batched(a, dist)
         elif a.workload == "served":
             out = run_served(a, dist)
+        elif a.workload == "pressure":
+            out = run_pressure(a, dist)
         else:
             out = run_ours(a, dist)
         if out is not None and dist.rank == 0:

@@ -6,11 +6,14 @@
  * against.  Only the test suite, the smoke check and the CPU-baseline leg of
  * the benchmark may load it; the product library never links or calls it.
  *
- * Parity pinning: the reference ships no tests, golden vectors or sample mesh
- * and cannot be compiled in this environment (no Fortran compiler, no
- * libcgns).  The restatement is pinned by hand-derivable invariants and by the
- * hash fixtures under tests/golden/, which were produced by this oracle and
- * cross-checked against the independent C++ mesh builder of the product.
+ * Parity unpinned: the reference ships no tests, golden vectors or sample
+ * mesh and cannot be compiled in this environment (no Fortran compiler, no
+ * libcgns), so no output of the reference itself checks this restatement.
+ * It is held instead by hand-derivable invariants (exact gradients of linear
+ * fields, symmetric zero-row-sum pressure matrices, closed-form face
+ * numbering, mass conservation) and by the hash fixtures under tests/golden/,
+ * which this oracle produced and the product's independent C++ mesh builder
+ * reproduces bit for bit.
  *
  * Conventions follow the reference: all indices are 1-based, packed
  * half-face indices use index_t(e,lf)=e<<5|lf (src/modules/mod_util.f90:1428),

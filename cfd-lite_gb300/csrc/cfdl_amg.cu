@@ -25,7 +25,9 @@ namespace cfdl {
 namespace {
 
 constexpr double kOmega = 0.8;     // damped Jacobi weight
-constexpr double kOverCorrect = 2.0;   // scaling of the prolongated coarse correction
+constexpr double kOverCorrect = 3.0;   // scaling of the prolongated coarse correction
+constexpr int kG = 8;                  // lanes per row on the small coarse levels
+constexpr int kGroupedRows = 65536;    // levels below this many rows (per case) run grouped
 enum { CNT_A0 = 9, CNT_A1, CNT_A2, CNT_A3, CNT_A4, CNT_A5 };
 
 template <class T> struct LP {
@@ -58,38 +60,12 @@ __device__ __forceinline__ bool pactive(const CaseDev &C) { return C.sc->active_
 __device__ __forceinline__ bool mactive(const CaseDev &C) { return C.sc->active32 != 0; }
 
 // ------------------------------------------------------------ Galerkin
-// off-diagonal coefficient of one coarse ELL slot s = k*n + I: the sum of the
-// fine coefficients between the two aggregates, in a fixed order
-__global__ void __launch_bounds__(kTile) k_amg_gal_off(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
-    const Tile t = tiles[blockIdx.x];
-    const CaseDev &C = cases[t.c];
-    const int s = t.first + (int)threadIdx.x;
-    if (s >= t.last || C.sc->halted) return;
-    const AmgLevelDev &L = C.lev[l - 1];
-    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
-    double v = 0.0;
-    for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
-    L.a[s] = v;
-    if (C.precision == 1) L.a32[s] = (float)v;
-}
-
-// diagonal of coarse cell I: member diagonals minus the couplings inside I
-__global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
-    const Tile t = tiles[blockIdx.x];
-    const CaseDev &C = cases[t.c];
-    const int I = t.first + (int)threadIdx.x;
-    if (I >= t.last || C.sc->halted) return;
-    const AmgLevelDev &L = C.lev[l - 1];
-    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
-    const double *df = l == 1 ? C.ap : C.lev[l - 2].dg;
-    const bool mixed = C.precision == 1;
-    double dsum = 0.0;
-    for (int m = L.mem_ptr[I]; m < L.mem_ptr[I + 1]; m++) dsum += df[L.mem[m]];
-    for (int q = L.d_ptr[I]; q < L.d_ptr[I + 1]; q++) dsum -= af[L.d_src[q]];
-    L.dg[I] = dsum;
-    L.rd[I] = 1.0 / dsum;
-    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(1.0 / dsum); }
-}
+// Coarse row I of A_c = P^T A P for unsmoothed aggregation (k_amg_galg below):
+// each off-diagonal slot is the sum of the fine couplings between aggregate I
+// and its neighbour, in a fixed order.  The pressure-correction matrix has
+// zero row sums (calc_coef_p: ap = sum of anb), and so has A_c, whose
+// diagonal is therefore the sum of its row's off-diagonal couplings -- no
+// pass over the aggregate's members or its internal couplings.
 
 // level-0 diagonal inverse and the FP32 copies the mixed form needs
 __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
@@ -197,7 +173,8 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
     P.t[i] = P.r[i] - amul<T>(P, P.z, i);
 }
 
-// r_{l+1}[I] = sum of the residual t_l over the members of aggregate I
+// r_{l1}[I] = sum of the residual t over the members of aggregate I (one
+// thread per coarse row: the large levels, where rows outnumber lanes)
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
     const Tile tl = tiles[blockIdx.x];
@@ -213,7 +190,31 @@ __global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict_
     rc[I] = s;
 }
 
-// coarsest: z_L = Minv r_L (one CTA per case)
+// Galerkin row I, one thread per row (large levels)
+__global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    const Tile t = tiles[blockIdx.x];
+    const CaseDev &C = cases[t.c];
+    const int I = t.first + (int)threadIdx.x;
+    if (I >= t.last || C.sc->halted) return;
+    const AmgLevelDev &L = C.lev[l - 1];
+    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    const bool mixed = C.precision == 1;
+    const int n = L.n;
+    double dsum = 0.0;
+    for (int k = 0; k < L.W; k++) {
+        const int s = k * n + I;
+        double v = 0.0;
+        for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
+        L.a[s] = v;
+        if (mixed) L.a32[s] = (float)v;
+        dsum += v;
+    }
+    L.dg[I] = dsum;
+    L.rd[I] = 1.0 / dsum;
+    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(1.0 / dsum); }
+}
+
+// coarsest: z_L = Minv r_L (one CTA per case, 4 lanes per row)
 template <class T>
 __global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ cases, int ncases) {
     const int c = blockIdx.x;
@@ -222,15 +223,40 @@ __global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ ca
     if (C.precond != 1 || (sizeof(T) == 8 ? !pactive(C) : !mactive(C))) return;
     const LP<T> P = level<T>(C, C.nlev);
     const T *Mi = sizeof(T) == 8 ? (const T *)C.cinv : (const T *)C.cinv32;
-    const int n = P.n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int n = P.n, q = (int)threadIdx.x & 3;
+    for (int i0 = (int)threadIdx.x >> 2; i0 < ((n + 63) & ~63); i0 += 64) {
         T s = 0;
-        for (int j = 0; j < n; j++) s += Mi[i * n + j] * P.r[j];
-        P.z[i] = s;
+        if (i0 < n)
+            for (int j = q; j < n; j += 4) s += Mi[i0 * n + j] * P.r[j];
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (i0 < n && q == 0) P.z[i0] = s;
     }
 }
 
-// t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly)
+// t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly),
+// on the mesh level: the W neighbour indices, then their aggregates, then the
+// values are loaded as three independent batches (no per-slot load chain)
+template <int W, class T>
+__device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__ agg, const T *__restrict__ zc, T sc,
+                                         int i, T xi) {
+    int j[W], ag[W];
+    bool ok[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        j[k] = P.nb[k * P.n + i];
+        ok[k] = (unsigned)j[k] < (unsigned)P.n;
+        if (!ok[k]) j[k] = i;
+    }
+#pragma unroll
+    for (int k = 0; k < W; k++) ag[k] = agg[j[k]];
+    T s = P.dg[i] * xi;
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        if (ok[k]) s -= P.a[k * P.n + i] * (P.z[j[k]] + sc * zc[ag[k]]);
+    return s;
+}
+
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
@@ -243,12 +269,131 @@ __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__
     const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
     const T sc = (T)kOverCorrect;
     const T xi = P.z[i] + sc * zc[L.agg[i]];
-    T s = P.dg[i] * xi;
-    for (int k = 0; k < P.W; k++) {
-        const int j = P.nb[k * P.n + i];
-        if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
+    T s;
+    if (P.W == 6) s = prolong_row<6, T>(P, L.agg, zc, sc, i, xi);
+    else if (P.W == 4) s = prolong_row<4, T>(P, L.agg, zc, sc, i, xi);
+    else {
+        s = P.dg[i] * xi;
+        for (int k = 0; k < P.W; k++) {
+            const int j = P.nb[k * P.n + i];
+            if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
+        }
     }
     P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - s);
+}
+
+// ------------------------------------------------- coarse levels, grouped
+// Coarse rows are wide (up to ~30 couplings) and a thread that walked one
+// alone would issue its index -> value -> vector loads one slot after the
+// other: a chain of dependent loads that left the small levels latency-bound.
+// On levels >= 1 each row is handled by kG lanes that split its slots (and
+// the Galerkin and restriction gather lists) and combine their partial sums
+// with shuffles, in a fixed order.  Tiles hold kTile / kG rows.
+#define GROUP_HEAD                                                   \
+    const Tile tl = tiles[blockIdx.x];                               \
+    const CaseDev &C = cases[tl.c];                                  \
+    const int g = (int)threadIdx.x & (kG - 1);                       \
+    const int i = tl.first + (int)threadIdx.x / kG;                  \
+    const bool ok = i < tl.last;
+
+template <class T> __device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+    for (int o = kG / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// sum_k a_ik x_j over the row's couplings inside the level, split over the group
+template <class T> __device__ __forceinline__ T group_offdiag(const LP<T> &P, const T *x, int i, bool ok, int g) {
+    T s = 0;
+    if (ok)
+        for (int k = g; k < P.W; k += kG) {
+            const int j = P.nb[k * P.n + i];
+            if ((unsigned)j < (unsigned)P.n) s += P.a[k * P.n + i] * x[j];
+        }
+    return group_sum(s);
+}
+
+// z = t + w D^-1 (r - A t)
+template <class T>
+__global__ void __launch_bounds__(kTile) k_vg_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    GROUP_HEAD
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const LP<T> P = level<T>(C, l);
+    const T off = group_offdiag<T>(P, P.t, i, ok, g);
+    if (ok && g == 0) P.z[i] = P.t[i] + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * P.t[i] - off));
+}
+
+// t = r - A z
+template <class T>
+__global__ void __launch_bounds__(kTile) k_vg_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    GROUP_HEAD
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const LP<T> P = level<T>(C, l);
+    const T off = group_offdiag<T>(P, P.z, i, ok, g);
+    if (ok && g == 0) P.t[i] = P.r[i] - (P.dg[i] * P.z[i] - off);
+}
+
+// r_{l1}[I] = sum of the residual t_{l1-1} over the members of aggregate I
+template <class T>
+__global__ void __launch_bounds__(kTile) k_vg_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
+    GROUP_HEAD
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const AmgLevelDev &L = C.lev[l1 - 1];
+    const LP<T> F = level<T>(C, l1 - 1);
+    T s = 0;
+    if (ok)
+        for (int m = L.mem_ptr[i] + g; m < L.mem_ptr[i + 1]; m += kG) s += F.t[L.mem[m]];
+    s = group_sum(s);
+    T *rc = sizeof(T) == 8 ? (T *)L.r : (T *)L.r32;
+    if (ok && g == 0) rc[i] = s;
+}
+
+// t = x + w D^-1 (r - A x) with x = z + s P z_{l+1}
+template <class T>
+__global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    GROUP_HEAD
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const LP<T> P = level<T>(C, l);
+    const AmgLevelDev &L = C.lev[l];
+    const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
+    const T sc = (T)kOverCorrect;
+    T off = 0;
+    if (ok)
+        for (int k = g; k < P.W; k += kG) {
+            const int j = P.nb[k * P.n + i];
+            if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
+        }
+    off = group_sum(off);
+    if (ok && g == 0) {
+        const T xi = P.z[i] + sc * zc[L.agg[i]];
+        P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * xi - off));
+    }
+}
+
+// Galerkin row I of level l: each lane sums the gather lists of its slots
+__global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    GROUP_HEAD
+    if (C.sc->halted) return;
+    const AmgLevelDev &L = C.lev[l - 1];
+    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    const bool mixed = C.precision == 1;
+    const int n = L.n;
+    double dsum = 0.0;
+    if (ok)
+        for (int k = g; k < L.W; k += kG) {
+            const int sl = k * n + i;
+            double v = 0.0;
+            for (int q = L.g_ptr[sl]; q < L.g_ptr[sl + 1]; q++) v += af[L.g_src[q]];
+            L.a[sl] = v;
+            if (mixed) L.a32[sl] = (float)v;
+            dsum += v;
+        }
+    dsum = group_sum(dsum);
+    if (ok && g == 0) {
+        L.dg[i] = dsum;
+        L.rd[i] = 1.0 / dsum;
+        if (mixed) { L.dg32[i] = (float)dsum; L.rd32[i] = (float)(1.0 / dsum); }
+    }
 }
 
 // ------------------------------------------------------------ CG (FP64)
@@ -458,8 +603,6 @@ int upload_case_amg(HostCase *hc, AmgHierarchy *H) {
         if ((st = dupload(hc, (int **)&D.mem, L.mem))) return st;
         if ((st = dupload(hc, (int **)&D.g_ptr, L.g_ptr))) return st;
         if ((st = dupload(hc, (int **)&D.g_src, L.g_src))) return st;
-        if ((st = dupload(hc, (int **)&D.d_ptr, L.d_ptr))) return st;
-        if ((st = dupload(hc, (int **)&D.d_src, L.d_src))) return st;
         if ((st = dzeros(hc, &D.a, (size_t)L.W * L.n))) return st;
         if ((st = dzeros(hc, &D.a32, (size_t)L.W * L.n))) return st;
         double **v64[] = {&D.dg, &D.rd, &D.r, &D.z, &D.t};
@@ -494,23 +637,30 @@ int ensure_amg(cfdl_ctx *ctx) {
     for (HostCase *hc : ctx->cases) lmax = std::max(lmax, hc->dev.nlev);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
-    for (auto &wl : ctx->amg_slots) free_worklist(wl);
+    for (auto &wl : ctx->amg_gcells) free_worklist(wl);
+    for (auto &wl : ctx->amg_gsmooth) free_worklist(wl);
     ctx->amg_cells.assign(lmax + 1, WorkList());
     ctx->amg_smooth.assign(lmax + 1, WorkList());
-    ctx->amg_slots.assign(lmax + 1, WorkList());
+    ctx->amg_gcells.assign(lmax + 1, WorkList());
+    ctx->amg_gsmooth.assign(lmax + 1, WorkList());
+    ctx->amg_grouped.assign(lmax + 1, 0);
     for (int l = 0; l <= lmax; l++) {
-        std::vector<int> cells, smooth, slots;
+        std::vector<int> cells, smooth;
         for (HostCase *hc : ctx->cases) {
             int n = l == 0 ? hc->ne : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].n : 0);
-            int W = l == 0 ? hc->W : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].W : 0);
             cells.push_back(l <= hc->dev.nlev ? n : 0);
             smooth.push_back(l < hc->dev.nlev ? n : 0);
-            slots.push_back(l <= hc->dev.nlev ? n * W : 0);
         }
         int st;
         if ((st = build_worklist(ctx, ctx->amg_cells[l], cells))) return st;
         if ((st = build_worklist(ctx, ctx->amg_smooth[l], smooth))) return st;
-        if ((st = build_worklist(ctx, ctx->amg_slots[l], slots))) return st;
+        // a level runs grouped when every case's level is small
+        const int nmax = *std::max_element(cells.begin(), cells.end());
+        if (l > 0 && nmax < kGroupedRows) {
+            ctx->amg_grouped[l] = 1;
+            if ((st = build_worklist(ctx, ctx->amg_gcells[l], cells, kTile / kG))) return st;
+            if ((st = build_worklist(ctx, ctx->amg_gsmooth[l], smooth, kTile / kG))) return st;
+        }
     }
     ctx->amg_lmax = lmax;
     return upload_case_table(ctx);
@@ -540,25 +690,39 @@ int ensure_amg(cfdl_ctx *ctx) {
 static void amg_setup_operators(cfdl_ctx *ctx) {
     ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
     for (int l = 1; l <= ctx->amg_lmax; l++) {
-        ALAUNCH("k_amg_gal_off", k_amg_gal_off, ctx->amg_slots[l], l);
-        ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+        if (ctx->amg_grouped[l]) ALAUNCH("k_amg_gal", k_amg_galg, ctx->amg_gcells[l], l);
+        else ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
     }
     CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, 256);
 }
 
 // One V-cycle z_0 = M^-1 r_0 on every active case.
 template <class T> static void vcycle(cfdl_ctx *ctx) {
+    // Levels with many rows run one thread per row; small levels run kG lanes
+    // per row (amg_grouped), which shortens each thread's chain of loads.
     const int L = ctx->amg_lmax;
     for (int l = 0; l < L; l++) {
+        const bool gl = ctx->amg_grouped[l], g1 = ctx->amg_grouped[l + 1];
         ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
-        ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
-        ALAUNCH(l ? "k_v_resid_c" : "k_v_resid_f", k_v_resid<T>, ctx->amg_smooth[l], l);
-        ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_cells[l + 1], l + 1);
+        if (gl) {
+            ALAUNCH("k_v_jac_c", k_vg_jac<T>, ctx->amg_gsmooth[l], l);
+            ALAUNCH("k_v_resid_c", k_vg_resid<T>, ctx->amg_gsmooth[l], l);
+        } else {
+            ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+            ALAUNCH(l ? "k_v_resid_c" : "k_v_resid_f", k_v_resid<T>, ctx->amg_smooth[l], l);
+        }
+        if (g1) ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict<T>, ctx->amg_gcells[l + 1], l + 1);
+        else ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_cells[l + 1], l + 1);
     }
     CLAUNCH("k_v_coarse", k_v_coarse<T>, 256);
     for (int l = L - 1; l >= 0; l--) {
-        ALAUNCH(l ? "k_v_prolong_c" : "k_v_prolong_f", k_v_prolong<T>, ctx->amg_smooth[l], l);
-        ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+        if (ctx->amg_grouped[l]) {
+            ALAUNCH("k_v_prolong_c", k_vg_prolong<T>, ctx->amg_gsmooth[l], l);
+            ALAUNCH("k_v_jac_c", k_vg_jac<T>, ctx->amg_gsmooth[l], l);
+        } else {
+            ALAUNCH(l ? "k_v_prolong_c" : "k_v_prolong_f", k_v_prolong<T>, ctx->amg_smooth[l], l);
+            ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+        }
     }
 }
 
@@ -657,8 +821,11 @@ __global__ void __launch_bounds__(kTile) k_mx_start(const CaseDev *__restrict__ 
         sum_partials<1, float>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0) {
             const float rn = sqrtf(s[0]);
-            // inner tolerance: the reference's drop for mode 0, 1e-4 per refinement when tight
-            const float eps = C.solve_mode == 0 ? (float)C.rtol_p : 1e-4f;
+            // inner tolerance: the reference's drop in mode 0; when tight, half the
+            // drop still needed to reach the FP64 target, but no finer than FP32
+            // iterates track the true residual (1e-5) and no coarser than 0.5
+            const float need = rn > 0.f ? (float)(S->tol_p / (double)rn) : 1.f;
+            const float eps = C.solve_mode == 0 ? (float)C.rtol_p : fminf(0.5f, fmaxf(1e-5f, 0.5f * need));
             S->rnorm32 = rn;
             S->tol32 = eps * rn;
             S->rz32 = 0.f;

@@ -23,7 +23,6 @@ struct AmgHostLevel {
     std::vector<int> mem_ptr, mem;     // members of each coarse cell
     std::vector<int> nb;               // [W][n] coarse neighbours, -1 padded
     std::vector<int> g_ptr, g_src;     // fine slots summed into coarse slot s = k*n + c
-    std::vector<int> d_ptr, d_src;     // fine slots internal to coarse cell c
 };
 
 struct AmgHierarchy {
@@ -35,7 +34,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H);
 // One coarse level, device side (all pointers device).
 struct AmgLevelDev {
     int n, W, n_fine, W_fine;
-    const int *nb, *agg, *mem_ptr, *mem, *g_ptr, *g_src, *d_ptr, *d_src;
+    const int *nb, *agg, *mem_ptr, *mem, *g_ptr, *g_src;
     double *a, *dg, *rd, *r, *z, *t;          // FP64 operator and V-cycle vectors
     float *a32, *dg32, *rd32, *r32, *z32, *t32; // FP32 copies (mixed-precision form)
 };

@@ -102,8 +102,6 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
         std::vector<std::vector<int>> cnb(nc);
         std::vector<std::vector<std::vector<int>>> src(nc);
         std::vector<std::vector<double>> cw(nc);
-        L.d_ptr.assign(nc + 1, 0);
-        std::vector<std::vector<int>> dsrc(nc);
         for (int c = 0; c < nc; c++) {
             for (int m = L.mem_ptr[c]; m < L.mem_ptr[c + 1]; m++) {
                 int i = L.mem[m];
@@ -112,7 +110,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
                     if (j < 0) continue;
                     int slot = k * g.n + i;
                     int cj = agg[j];
-                    if (cj == c) { dsrc[c].push_back(slot); continue; }
+                    if (cj == c) continue;           // internal coupling: not a coarse slot
                     size_t q = 0;
                     while (q < cnb[c].size() && cnb[c][q] != cj) q++;
                     if (q == cnb[c].size()) { cnb[c].push_back(cj); src[c].emplace_back(); cw[c].push_back(0.0); }
@@ -140,9 +138,6 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
                     size_t s = (size_t)k * nc + c;
                     std::copy(src[c][k].begin(), src[c][k].end(), L.g_src.begin() + L.g_ptr[s]);
                 }
-        for (int c = 0; c < nc; c++) L.d_ptr[c + 1] = L.d_ptr[c] + (int)dsrc[c].size();
-        L.d_src.assign(L.d_ptr.back(), 0);
-        for (int c = 0; c < nc; c++) std::copy(dsrc[c].begin(), dsrc[c].end(), L.d_src.begin() + L.d_ptr[c]);
         // next graph
         Graph ng;
         ng.n = nc; ng.W = Wc;

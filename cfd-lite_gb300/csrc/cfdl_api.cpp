@@ -233,7 +233,8 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     free_worklist(ctx->cellsv);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
-    for (auto &wl : ctx->amg_slots) free_worklist(wl);
+    for (auto &wl : ctx->amg_gcells) free_worklist(wl);
+    for (auto &wl : ctx->amg_gsmooth) free_worklist(wl);
     cudaFree(ctx->d_cases);
     cudaFree(ctx->d_partials);
     cudaFree(ctx->d_flags);

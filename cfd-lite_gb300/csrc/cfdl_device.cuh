@@ -114,12 +114,27 @@ __device__ __forceinline__ void ell_row(const int *__restrict__ nb, const T *__r
     if (W == 4) { ell_row_w<4, NC, T>(nb, a, diag, x, stride, n, i, y); return; }
 #pragma unroll
     for (int q = 0; q < NC; q++) y[q] = diag * x[q * stride + i];
-    for (int k = 0; k < W; k++) {
-        const int jj = nb[k * n + i];
-        if ((unsigned)jj >= (unsigned)n) continue;
-        const T ak = a[k * n + i];
+    // wide rows (coarse levels): four slots per step, their index, coefficient
+    // and vector loads issued together instead of one dependent chain per slot
+    for (int k0 = 0; k0 < W; k0 += 4) {
+        int jj[4];
+        T ak[4];
 #pragma unroll
-        for (int q = 0; q < NC; q++) y[q] -= ak * x[q * stride + jj];
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < W ? nb[(k0 + u) * n + i] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ok = (unsigned)jj[u] < (unsigned)n;
+            ak[u] = ok ? a[(k0 + u) * n + i] : (T)0;
+            if (!ok) jj[u] = i;
+        }
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
+            T xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) xv[u] = x[q * stride + jj[u]];
+#pragma unroll
+            for (int u = 0; u < 4; u++) y[q] -= ak[u] * xv[u];
+        }
     }
 }
 

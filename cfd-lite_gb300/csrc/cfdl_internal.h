@@ -169,7 +169,9 @@ struct cfdl_ctx {
     void *prof = nullptr;                // event profiler state (cfdl_prof.cpp)
     // AMG work lists: amg_cells[l] = level-l cells of cases with nlev >= l,
     // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
-    std::vector<cfdl::WorkList> amg_cells, amg_smooth, amg_slots;   // amg_slots[l]: W_l*n_l ELL slots
+    std::vector<cfdl::WorkList> amg_cells, amg_smooth;      // per level, kTile rows per tile
+    std::vector<cfdl::WorkList> amg_gcells, amg_gsmooth;    // per small coarse level, kTile/8 rows per tile
+    std::vector<int> amg_grouped;                           // level runs 8 lanes per row
     int amg_lmax = -1;
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;

@@ -102,7 +102,6 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         if (nb < 0) continue;
         if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
         const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
-        const double sg = fc >= 0 ? 1.0 : -1.0;
         // inward flux f = -sg*mip and upwind max(f,0): sign and comparison on
         // the bit pattern, so they cost no FP64 instruction
         const double fl = flip_sign(C.mip[f], fc >= 0);
@@ -110,8 +109,10 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         sumf += fl;
         a[k] = ak;
         ap += ak;
-        ss0 += sg * C.fS[f]; ss1 += sg * C.fS[nf + f]; ss2 += sg * C.fS[2 * nf + f];
-        dd0 += sg * C.fD[f]; dd1 += sg * C.fD[nf + f]; dd2 += sg * C.fD[2 * nf + f];
+        // sg * x as a sign-bit flip: no FP64 multiply
+        const bool ng = fc < 0;
+        ss0 += flip_sign(C.fS[f], ng); ss1 += flip_sign(C.fS[nf + f], ng); ss2 += flip_sign(C.fS[2 * nf + f], ng);
+        dd0 += flip_sign(C.fD[f], ng); dd1 += flip_sign(C.fD[nf + f], ng); dd2 += flip_sign(C.fD[2 * nf + f], ng);
     }
     double asum = ap;                       // sum of the anb of this row so far
     const double vol = C.vol[i];
@@ -261,8 +262,7 @@ __global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict
         if (nb >= ne) bslot[nb_cnt++] = k;
         else if (nb >= 0) {
             const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
-            const double sg = fc >= 0 ? 1.0 : -1.0;
-            sumf += -sg * C.mip[f];
+            sumf += flip_sign(C.mip[f], fc >= 0);   // -sg * mip
             a = C.fdiff[f];
             ap += a;
         }

@@ -50,7 +50,7 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
 
 // ------------------------------ momentum ----------------------------------
 // init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0
-__global__ void __launch_bounds__(kTile) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(kTile, 4) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cas
 }
 
 // v = A ph; alpha = rho / (rh, v)
-__global__ void __launch_bounds__(kTile) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(kTile, 4) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
 }
 
 // t = A sh; omega = (t,s)/(t,t)
-__global__ void __launch_bounds__(kTile) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(kTile, 4) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kTile) k_mom_t(const CaseDev *__restrict__ cas
 }
 
 // x += alpha ph + omega sh; r = s - omega t; rho' = (rh, r); beta
-__global__ void __launch_bounds__(kTile) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+__global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     if (!any_active(S)) return;

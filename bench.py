@@ -208,6 +208,9 @@ def run_ours(a, dist):
 
     for _ in range(a.warmup):
         step()
+    tile, tile_ms = g.autotune(outer=2)     # solver tile shape by measurement (state restored)
+    for _ in range(2):
+        step()
     clocks = Clocks(dist.local)
     dist.barrier()
     g.timer_begin()
@@ -308,7 +311,9 @@ def run_ours(a, dist):
         "config": {"workload": "lid-driven cavity %d^3 %s, jitter %.2f, Re=100 (rho=1, mu=0.01), SIMPLE "
                                "alpha_u=0.7 alpha_p=0.3, FP64" % (a.n, "tet-split" if a.tet else "hex", a.jitter),
                    "cells": ne, "faces": nf, "inner_solve": "10x residual drop / nit=100" if a.mode == 0 else "tight 1e-13",
-                   "pressure_precond": ["jacobi", "amg"][a.precond], "parallelism": "replicas" if dist.world > 1 else "single",
+                   "pressure_precond": ["jacobi", "amg"][a.precond], "tile": tile,
+                   "autotune_ms_per_outer": {str(k): round(v, 3) for k, v in tile_ms.items()},
+                   "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)"},
         "gpu_launches": launches // max(1, 1),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"],

@@ -49,36 +49,54 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
     (void)ne;
 
 // ------------------------------ momentum ----------------------------------
-// init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0
-__global__ void __launch_bounds__(kTile, 4) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+// init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0.
+// The row's slot indices and coefficients are loaded once for the three
+// components; sums run in slot order.
+template <int W>
+__device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, double (&v)[6]) {
+    int nb[W];
+    double a[W];
+    bool in[W], bd[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const int j = C.hf_nb[k * ne + i];
+        in[k] = j >= 0 && j < ne;
+        bd[k] = j >= ne;
+        nb[k] = j >= 0 ? j : i;
+        a[k] = j >= 0 ? C.anb[k * ne + i] : 0.0;
+    }
+    const double api = C.ap[i];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const double *__restrict__ phi = comp_field(C, q);
+        double pv[W];
+#pragma unroll
+        for (int k = 0; k < W; k++) pv[k] = phi[nb[k]];
+        double bb = comp_rhs(C, q)[i];
+        double s = api * phi[i];
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            if (bd[k]) bb += a[k] * pv[k];
+            else if (in[k]) s -= a[k] * pv[k];
+        }
+        const double r = bb - s;
+        C.kb[q * ne + i] = bb;
+        C.kr[q * ne + i] = r;
+        C.krh[q * ne + i] = r;
+        C.kp[q * ne + i] = 0.0;
+        C.kv[q * ne + i] = 0.0;
+        v[q] += bb * bb;
+        v[3 + q] += r * r;
+    }
+}
+
+__global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
-    FOR_CELLS(t) {
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-            const double *phi = comp_field(C, q);
-            double bb = comp_rhs(C, q)[i];
-            double s = C.ap[i] * phi[i];
-#pragma unroll
-            for (int k = 0; k < kMaxW; k++) {
-                if (k >= C.W) break;
-                const int nb = C.hf_nb[k * ne + i];
-                if (nb < 0) break;
-                const double a = C.anb[k * ne + i];
-                if (nb >= ne) bb += a * phi[nb];
-                else s -= a * phi[nb];
-            }
-            const double r = bb - s;
-            C.kb[q * ne + i] = bb;
-            C.kr[q * ne + i] = r;
-            C.krh[q * ne + i] = r;
-            C.kp[q * ne + i] = 0.0;
-            C.kv[q * ne + i] = 0.0;
-            v[q] += bb * bb;
-            v[3 + q] += r * r;
-        }
-    }
+    if (C.W == 6) { FOR_CELLS(t) mom_init_row<6>(C, i, ne, v); }
+    else if (C.W == 4) { FOR_CELLS(t) mom_init_row<4>(C, i, ne, v); }
+    else { FOR_CELLS(t) mom_init_row<kMaxW>(C, i, ne, v); }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M1], cnt[t.c])) {
         __shared__ double s[6];
@@ -103,15 +121,21 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_init(const CaseDev *__restrict
 __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
     if (!any_active(S)) return;
+    // the iteration's scalars, read once
+    const int act[3] = {S->active[0], S->active[1], S->active[2]};
+    const bool first[3] = {S->iters[0] == 0, S->iters[1] == 0, S->iters[2] == 0};
+    const double be[3] = {S->beta[0], S->beta[1], S->beta[2]}, om[3] = {S->omega[0], S->omega[1], S->omega[2]};
+    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ ap = C.ap;
+    double *__restrict__ kp = C.kp, *__restrict__ kph = C.kph;
     FOR_CELLS(t) {
-        const double rap = 1.0 / C.ap[i];
+        const double rap = 1.0 / ap[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            if (!S->active[q]) continue;
+            if (!act[q]) continue;
             const int j = q * ne + i;
-            const double pn = S->iters[q] == 0 ? C.kr[j] : C.kr[j] + S->beta[q] * (C.kp[j] - S->omega[q] * C.kv[j]);
-            C.kp[j] = pn;
-            C.kph[j] = pn * rap;
+            const double pn = first[q] ? kr[j] : kr[j] + be[q] * (kp[j] - om[q] * kv[j]);
+            kp[j] = pn;
+            kph[j] = pn * rap;
         }
     }
 }
@@ -153,15 +177,19 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
     TILE_HEAD
     if (!any_active(S)) return;
     double v[3] = {0, 0, 0};
+    const int act[3] = {S->active[0], S->active[1], S->active[2]};
+    const double al[3] = {S->alpha[0], S->alpha[1], S->alpha[2]};
+    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ ap = C.ap;
+    double *__restrict__ ks = C.ks, *__restrict__ ksh = C.ksh;
     FOR_CELLS(t) {
-        const double rap = 1.0 / C.ap[i];
+        const double rap = 1.0 / ap[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            if (!S->active[q]) continue;
+            if (!act[q]) continue;
             const int j = q * ne + i;
-            const double sv = C.kr[j] - S->alpha[q] * C.kv[j];
-            C.ks[j] = sv;
-            C.ksh[j] = sv * rap;
+            const double sv = kr[j] - al[q] * kv[j];
+            ks[j] = sv;
+            ksh[j] = sv * rap;
             v[q] += sv * sv;
         }
     }
@@ -214,18 +242,22 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
     TILE_HEAD
     if (!any_active(S)) return;
     double v[6] = {0, 0, 0, 0, 0, 0};
+    const int act[3] = {S->active[0], S->active[1], S->active[2]};
+    const double al[3] = {S->alpha[0], S->alpha[1], S->alpha[2]}, om[3] = {S->omega[0], S->omega[1], S->omega[2]};
+    const double *__restrict__ kph = C.kph, *__restrict__ ksh = C.ksh, *__restrict__ ks = C.ks, *__restrict__ kt = C.kt,
+                 *__restrict__ krh = C.krh;
+    double *__restrict__ kr = C.kr;
     FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            if (!S->active[q]) continue;
+            if (!act[q]) continue;
             const int j = q * ne + i;
-            double *x = comp_field(C, q);
-            const double om = S->omega[q];
-            x[i] = x[i] + S->alpha[q] * C.kph[j] + om * C.ksh[j];
-            const double r = om == 0.0 ? C.ks[j] : C.ks[j] - om * C.kt[j];
-            C.kr[j] = r;
+            double *__restrict__ x = comp_field(C, q);
+            x[i] = x[i] + al[q] * kph[j] + om[q] * ksh[j];
+            const double r = om[q] == 0.0 ? ks[j] : ks[j] - om[q] * kt[j];
+            kr[j] = r;
             v[q] += r * r;
-            v[3 + q] += C.krh[j] * r;
+            v[3 + q] += krh[j] * r;
         }
     }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);

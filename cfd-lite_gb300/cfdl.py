@@ -134,6 +134,7 @@ def lib():
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
     L.cfdl_step.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_solve_uvwp_host.argtypes = [vp, C.POINTER(Fields), C.POINTER(Stats)]
+    L.cfdl_step_host.argtypes = [vp, C.POINTER(Fields), C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_calc_grad.argtypes = [vp, C.c_int]
     L.cfdl_calc_mip.argtypes = [vp, C.c_int]
     L.cfdl_get_array.argtypes = [vp, C.c_char_p, vp]

@@ -131,6 +131,7 @@ int solve_uvwp_all(cfdl_ctx *ctx) {
     int st = solve_momentum(ctx);
     if (st) return st;
     launch_grad(ctx, 4);
+    if (ctx->ev_mom) cudaEventRecord(ctx->ev_mom, ctx->stream);
     launch_calc_mip(ctx, 1);
     launch_coef_p(ctx);
     st = solve_pressure(ctx);
@@ -244,6 +245,9 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     destroy_graph(ctx);
     cudaFree(ctx->d_loop_passes);
     cudaFree(ctx->d_run_ctl);
+    if (ctx->ev_mom) cudaEventDestroy(ctx->ev_mom);
+    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->h_run_ctl) cudaFreeHost(ctx->h_run_ctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -283,14 +287,64 @@ int cfdl_step(cfdl_ctx *ctx, int n_outer, int ncoef, cfdl_stats *stats) {
     return finish(ctx, stats);
 }
 
+static int ensure_copy_stream(cfdl_ctx *ctx) {
+    if (ctx->copy_stream) return CFDL_OK;
+    int st;
+    if ((st = cuda_status(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking)))) return st;
+    if ((st = cuda_status(cudaEventCreateWithFlags(&ctx->ev_mom, cudaEventDisableTiming)))) return st;
+    if ((st = cuda_status(cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming)))) return st;
+    destroy_graph(ctx);   // rebuilt with a record of ev_mom after the momentum half
+    return CFDL_OK;
+}
+
+// Downloads f after the last solve_uvwp queued on ctx->stream.  u, v, w and
+// their gradients are final once the momentum solve and calc_grad(u,v,w) are
+// done (update_uvwp corrects p, gp and mip only) and the old-time fields do
+// not change, so they go back on the copy stream while the pressure
+// correction runs; p, gp, gpc and mip follow on the main stream.
+static int download_overlapped(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f) {
+    cfdl_fields early = {}, late = {};
+    early.u = f->u; early.v = f->v; early.w = f->w; early.gu = f->gu; early.gv = f->gv; early.gw = f->gw;
+    early.u0 = f->u0; early.v0 = f->v0; early.w0 = f->w0; early.mip0 = f->mip0;
+    late.p = f->p; late.gp = f->gp; late.gpc = f->gpc; late.mip = f->mip;
+    int st;
+    cudaStream_t main_stream = ctx->stream;
+    if ((st = cuda_status(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_mom, 0)))) return st;
+    ctx->stream = ctx->copy_stream;
+    st = transfer_fields(ctx, hc, &early, true);
+    ctx->stream = main_stream;
+    if (st) return st;
+    if ((st = cuda_status(cudaEventRecord(ctx->ev_copy, ctx->copy_stream)))) return st;
+    if ((st = transfer_fields(ctx, hc, &late, true))) return st;
+    if ((st = cuda_status(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0)))) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
 int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *stats) {
     int st = check_ctx(ctx);
     if (st) return st;
+    if (!f) return CFDL_ERR_INVALID;
     HostCase *hc = ctx->cases[0];
+    if ((st = ensure_copy_stream(ctx))) return st;
     if ((st = transfer_fields(ctx, hc, f, false))) return st;
     if ((st = solve_uvwp_all(ctx))) return st;
-    if ((st = transfer_fields(ctx, hc, f, true))) return st;
-    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    if ((st = download_overlapped(ctx, hc, f))) return st;
+    return finish(ctx, stats);
+}
+
+int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (!f || n_outer < 1) return CFDL_ERR_INVALID;
+    HostCase *hc = ctx->cases[0];
+    if ((st = ensure_copy_stream(ctx))) return st;
+    if ((st = transfer_fields(ctx, hc, f, false))) return st;
+    for (int k = 1; k <= n_outer; k++) {
+        launch_bc(ctx);
+        if ((st = solve_uvwp_all(ctx))) return st;
+        if (ncoef > 0 && k % ncoef == 0) launch_update_time(ctx);
+    }
+    if ((st = download_overlapped(ctx, hc, f))) return st;
     return finish(ctx, stats);
 }
 

@@ -166,7 +166,7 @@ static int ensure_graph_state(cfdl_ctx *ctx) {
 // loop's body.
 template <class Pre, class Post>
 static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre, Post post, int64_t *static_k,
-                       int64_t *body) {
+                       int64_t *body, bool mark) {
     cfdl_ctx *ctx = b.ctx;
     const cfdl_config &cfg = ctx->cases[0]->cfg;
     int st;
@@ -188,8 +188,17 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
     });
     if (st) return st;
     // gradients, Rhie-Chow fluxes, pressure assembly, pressure-solve start
+    if ((st = b.segment(G, prev, [&] { launch_grad(ctx, 4); }, &k))) return st;
+    *static_k += k;
+    if (ctx->ev_mom && mark) {
+        // u, v, w and their gradients are final here (cfdl_solve_uvwp_host
+        // starts their download on this record)
+        cudaGraphNode_t n;
+        cudaError_t e = cudaGraphAddEventRecordNode(&n, G, prev, 1, ctx->ev_mom);
+        if (e != cudaSuccess) return cuda_status(e);
+        *prev = n;
+    }
     if ((st = b.segment(G, prev, [&] {
-             launch_grad(ctx, 4);
              launch_calc_mip(ctx, 1);
              launch_coef_p(ctx);
              if (cfg.precision == 1) mx_init(ctx);
@@ -248,7 +257,7 @@ int build_graph(cfdl_ctx *ctx) {
     ctx->capturing = true;
     cudaGraphNode_t prev = nullptr;
     int64_t stat = 0, body[4] = {0, 0, 0, 0};
-    st = append_uvwp(b, G, &prev, [] {}, [] {}, &stat, body);
+    st = append_uvwp(b, G, &prev, [] {}, [] {}, &stat, body, true);
     ctx->capturing = false;
     if (st) { cudaGraphDestroy(G); return st; }
     cudaGraphExec_t exec = nullptr;
@@ -285,7 +294,8 @@ int build_run_graph(cfdl_ctx *ctx) {
         int64_t inner_static = 0;
         int s2 = append_uvwp(
             b, outer, &op, [&] { launch_run_begin(ctx); launch_bc(ctx); },
-            [&] { launch_run_end(ctx); launch_run_cond(ctx, hr, 1, ctx->d_loop_passes + 8); }, &inner_static, body);
+            [&] { launch_run_end(ctx); launch_run_cond(ctx, hr, 1, ctx->d_loop_passes + 8); }, &inner_static, body,
+            false);
         body[4] = inner_static;
         return s2;
     });

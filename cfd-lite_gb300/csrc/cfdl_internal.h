@@ -150,6 +150,11 @@ struct HostCase {
 struct cfdl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // host drop-in (cfdl_solve_uvwp_host): a copy stream that downloads the
+    // momentum results while the pressure half of the iteration runs
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_mom = nullptr;        // recorded after the momentum solve and calc_grad(u,v,w)
+    cudaEvent_t ev_copy = nullptr;
     std::vector<cfdl::HostCase *> cases;
     int next_id = 0;                     // id given to the next added case
     cfdl::CaseDev *d_cases = nullptr;

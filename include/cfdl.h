@@ -158,8 +158,13 @@ int cfdl_update_time(cfdl_ctx *ctx);                     /* mod_physics.f90:101-
 int cfdl_step(cfdl_ctx *ctx, int n_outer, int ncoef, cfdl_stats *st);
 
 /* Drop-in for the Fortran solve_uvwp with host arrays: uploads the fields
- * solve_uvwp reads, runs it, downloads what it writes. */
+ * solve_uvwp reads, runs it, downloads what it writes (NULL members are
+ * skipped both ways).  u, v, w and their gradients are downloaded while the
+ * pressure correction still runs. */
 int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *st);
+/* cfdl_step with host arrays: upload, n_outer passes of update_boundaries +
+ * solve_uvwp (+ update_time every ncoef), download as above. */
+int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_stats *st);
 
 /* ---- individual routines, for per-routine replacement and parity ---- */
 int cfdl_calc_coef_uvw(cfdl_ctx *ctx);                   /* mod_uvwp.f90:161-286   */

@@ -244,3 +244,26 @@ def test_host_dropin_matches_resident(need_gpu):
         assert cfdl.lib().cfdl_solve_uvwp_host(g2._h, C.byref(fl), C.byref(st)) == 0
     for f in ("u", "v", "w", "p", "mip"):
         assert np.array_equal(g1.get(f), host[f]), f
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_step_host_matches_resident(need_gpu, graph):
+    """cfdl_step_host (upload, BC + solve_uvwp, overlapped download) equals
+    the resident path, with only the steady state's arrays handed over."""
+    import ctypes as C
+    z = cfdl.Zone(7, True, 0.1, seed=4)
+    s = cfdl.Setup(z)
+    g1 = cfdl.Solver(s, cfdl.steady())
+    g2 = cfdl.Solver(s, cfdl.steady())
+    g1.set_graph_mode(graph)
+    g2.set_graph_mode(graph)
+    nc, nf = s.ne + s.nbf, s.nf
+    host = {f: np.zeros(nc) for f in ("u", "v", "w", "p")}
+    host.update({f: np.zeros(3 * nc) for f in ("gu", "gv", "gw", "gp", "gpc")})
+    host["mip"] = g2.get("mip")
+    fl = cfdl.Fields(**{k: v.ctypes.data_as(C.c_void_p) for k, v in host.items()})
+    for _ in range(4):
+        g1.step(1, ncoef=0)
+        assert cfdl.lib().cfdl_step_host(g2._h, C.byref(fl), 1, 0, None) == 0
+    for f in ("u", "v", "w", "p", "mip", "gu", "gp", "gpc"):
+        assert np.array_equal(g1.get(f), host[f]), f

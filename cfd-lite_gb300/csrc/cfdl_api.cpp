@@ -52,6 +52,7 @@ int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool
     Named nm = lookup(hc, name);
     if (!nm.ptr) return CFDL_ERR_NAME;
     if (!host) return CFDL_ERR_INVALID;
+    if (!to_host && (nm.ptr == hc->dev.rho || nm.ptr == hc->dev.mu)) hc->props_dirty = true;
     cudaError_t e;
     if (!nm.ell) {
         e = cudaMemcpyAsync(to_host ? (void *)host : (void *)nm.ptr, to_host ? (const void *)nm.ptr : (const void *)host,
@@ -202,6 +203,7 @@ int cfdl_set_config(cfdl_ctx *ctx, const cfdl_config *cfg) {
     if ((st = validate_config(cfg))) return st;
     for (HostCase *hc : ctx->cases) {
         if (hc->cfg.rho != cfg->rho || hc->cfg.mu != cfg->mu) {
+            hc->props_dirty = true;
             std::vector<double> rho(hc->ne, cfg->rho), mu(hc->ne, cfg->mu);
             if ((st = cuda_status(cudaMemcpy(hc->dev.rho, rho.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
             if ((st = cuda_status(cudaMemcpy(hc->dev.mu, mu.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
@@ -548,6 +550,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 3 * b * 4 + 3 * b * 8 + c * 8;          // halo tables, volume
     bytes += 8 * nc * 8 + 15 * nc * 8 + 2 * f * 8;   // cell fields, gradients, mip/mip0
     bytes += 9 * c * 8 + w * c * 8 + 7 * f * 8;      // coefficients, face intermediates
+    bytes += 10 * f * 8;                              // property planes
     bytes += 27 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
     bytes += 160 * c;                                 // multigrid hierarchy (bound)
     return bytes;

@@ -315,6 +315,7 @@ int build_run_graph(cfdl_ctx *ctx) {
 
 int run_graph_launch(cfdl_ctx *ctx) {
     int st;
+    ensure_face_props(ctx);
     if (!ctx->run_exec || ctx->run_form != graph_form(ctx))
         if ((st = build_run_graph(ctx))) return st;
     ctx->launches += ctx->run_static_kernels;
@@ -326,6 +327,7 @@ int run_graph_launch(cfdl_ctx *ctx) {
 // kernel sequence changes).  Returns a status; falls back to nothing.
 int solve_uvwp_graph(cfdl_ctx *ctx) {
     int st;
+    ensure_face_props(ctx);
     if (!ctx->graph_exec || ctx->graph_form != graph_form(ctx))
         if ((st = build_graph(ctx))) return st;
     ctx->launches += ctx->graph_static_kernels;

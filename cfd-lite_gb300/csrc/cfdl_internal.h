@@ -56,6 +56,18 @@ enum FaceGeo {
     FG_N
 };
 
+// property planes fprop[PR_*][nf]: the mesh planes scaled by the interpolated
+// density and viscosity, recomputed only when rho or mu change
+enum FaceProp {
+    PR_FDIFF = 0,               // mu_ip * area/ds (boundary faces: mu_own * area/ds)
+    PR_MAX, PR_MAY, PR_MAZ,     // mu_ip * area * dr/ds
+    PR_MEX, PR_MEY, PR_MEZ,     // mu_ip * area * (dr_p/ds_p - dr/ds)
+    PR_RHO,                     // rho_ip
+    PR_RHOADN,                  // rho_ip * area/(dr.n)
+    PR_RHOMADN,                 // (rho_own + rho_nb)/2 * area/(dr.n)  (update_uvwp's face density)
+    PR_N
+};
+
 struct AmgLevelDev;
 struct AmgHierarchy;
 
@@ -98,6 +110,7 @@ struct CaseDev {
     double *ap, *anb, *b, *phic;          // phys_t scratch: ap[ne], anb ELL [W][ne], b[ne], phic[ne+nbf]
     // face intermediates of the assemblies
     double *fdiff, *fS, *fD;              // [nf], [3][nf], [3][nf]
+    double *fprop;                        // [PR_N][nf] property planes
     // Krylov work vectors, [3][ne] each (pressure uses plane 0)
     double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt, *kb;
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each
@@ -141,6 +154,7 @@ struct HostCase {
     AmgHierarchy *amg = nullptr;     // host hierarchy, built on first AMG use
     std::vector<void *> amg_allocs;  // device allocations of the hierarchy
     int id = 0;                      // stable case id within its context
+    bool props_dirty = true;         // fprop must be recomputed (rho or mu changed)
     size_t bytes = 0;                // device bytes held (mesh, fields, solver, hierarchy)
 };
 
@@ -221,6 +235,7 @@ void apply_config(HostCase *hc, const cfdl_config *cfg);
 
 // kernel launchers (cfdl_kernels.cu): asynchronous on ctx->stream, all cases
 void launch_bc(cfdl_ctx *ctx);
+void ensure_face_props(cfdl_ctx *ctx);   // recompute the property planes of cases whose rho/mu changed
 void launch_coef_uvw(cfdl_ctx *ctx);
 void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused
 void launch_calc_mip(cfdl_ctx *ctx, int rhie_chow);

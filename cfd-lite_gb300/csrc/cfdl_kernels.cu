@@ -61,16 +61,11 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restri
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
-    const double *g = C.fgeo;
-    if (n >= C.ne) {
-        C.fdiff[i] = C.mu[o] * g[FG_ADS * nf + i];
-        return;
-    }
+    if (n >= C.ne) return;                  // boundary faces: only their (precomputed) diffusion
+    const double *g = C.fgeo, *pr = C.fprop;
     const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
-    const double muip = omw * C.mu[o] + wt * C.mu[n];
-    C.fdiff[i] = muip * g[FG_ADS * nf + i];
-    const double A0 = g[FG_ADRX * nf + i], A1 = g[FG_ADRY * nf + i], A2 = g[FG_ADRZ * nf + i];
-    const double E0 = g[FG_EX * nf + i], E1 = g[FG_EY * nf + i], E2 = g[FG_EZ * nf + i];
+    const double A0 = pr[PR_MAX * nf + i], A1 = pr[PR_MAY * nf + i], A2 = pr[PR_MAZ * nf + i];
+    const double E0 = pr[PR_MEX * nf + i], E1 = pr[PR_MEY * nf + i], E2 = pr[PR_MEZ * nf + i];
     double gi[3][3];   // gi[q][m]: component m of grad(u_q) at the face
     const double *gq[3] = {C.gu, C.gv, C.gw};
 #pragma unroll
@@ -79,11 +74,38 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restri
         for (int m = 0; m < 3; m++) gi[q][m] = omw * gq[q][3 * o + m] + wt * gq[q][3 * n + m];
 #pragma unroll
     for (int m = 0; m < 3; m++) {
-        // sumss(m): gip = (du/dx_m, dv/dx_m, dw/dx_m) . dr
-        C.fS[m * nf + i] = muip * (gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2);
-        // sumdefc(q=m): grad(u_m) . (dr_p/ds_p - dr/ds)
-        C.fD[m * nf + i] = muip * (gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2);
+        // sumss(m): mu_ip (du/dx_m, dv/dx_m, dw/dx_m) . dr (mu_ip folded into the plane)
+        C.fS[m * nf + i] = gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2;
+        // sumdefc(q=m): mu_ip grad(u_m) . (dr_p/ds_p - dr/ds)
+        C.fD[m * nf + i] = gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2;
     }
+}
+
+// Property planes of every face (recomputed when rho or mu change): the mesh
+// planes scaled by the interpolated viscosity and density.
+__global__ void __launch_bounds__(kTile) k_face_props(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    const double *g = C.fgeo;
+    double *pr = C.fprop;
+    if (n >= C.ne) {
+        pr[PR_FDIFF * nf + i] = C.mu[o] * g[FG_ADS * nf + i];
+        for (int k = PR_MAX; k < PR_N; k++) pr[k * nf + i] = 0.0;
+        return;
+    }
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
+    const double muip = omw * C.mu[o] + wt * C.mu[n];
+    const double rhoip = C.rho[o] * omw + C.rho[n] * wt;
+    const double adn = g[FG_ADN * nf + i];
+    pr[PR_FDIFF * nf + i] = muip * g[FG_ADS * nf + i];
+    for (int m = 0; m < 3; m++) {
+        pr[(PR_MAX + m) * nf + i] = muip * g[(FG_ADRX + m) * nf + i];
+        pr[(PR_MEX + m) * nf + i] = muip * g[(FG_EX + m) * nf + i];
+    }
+    pr[PR_RHO * nf + i] = rhoip;
+    pr[PR_RHOADN * nf + i] = rhoip * adn;
+    pr[PR_RHOMADN * nf + i] = (C.rho[o] + C.rho[n]) / 2.0 * adn;
 }
 
 // calc_coef_uvw, cell part (mod_uvwp.f90:174-284) + implicit relaxation.
@@ -105,7 +127,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         // inward flux f = -sg*mip and upwind max(f,0): sign and comparison on
         // the bit pattern, so they cost no FP64 instruction
         const double fl = flip_sign(C.mip[f], fc >= 0);
-        const double ak = C.fdiff[f] + positive_part(fl);
+        const double ak = C.fprop[PR_FDIFF * nf + f] + positive_part(fl);
         sumf += fl;
         a[k] = ak;
         ap += ak;
@@ -139,7 +161,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         const int k = bslot[q], h = C.hf_nb[k * ne + i], f = face_of(C.hf_fc[k * ne + i]);
         const int kind = C.h_kind[h - ne];
         if (kind == 0) continue;
-        const double dbc = C.fdiff[f];
+        const double dbc = C.fprop[PR_FDIFF * nf + f];
         if (kind == CFDL_BC_WALL) {
             const double area = C.fgeo[FG_AREA * nf + f];
             const double n0 = C.fgeo[FG_AX * nf + f] / area, n1 = C.fgeo[FG_AY * nf + f] / area, n2 = C.fgeo[FG_AZ * nf + f] / area;
@@ -215,7 +237,7 @@ __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ 
     const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
     const double A0 = g[FG_AX * nf + i], A1 = g[FG_AY * nf + i], A2 = g[FG_AZ * nf + i];
     const double vx = omw * C.u[o] + wt * C.u[n], vy = omw * C.v[o] + wt * C.v[n], vz = omw * C.w[o] + wt * C.w[n];
-    const double rhoip = C.rho[o] * omw + C.rho[n] * wt;
+    const double rhoip = C.fprop[PR_RHO * nf + i];
     double mip = (vx * A0 + vy * A1 + vz * A2) * rhoip;
     if (rc) {
         const double D0 = g[FG_DRX * nf + i], D1 = g[FG_DRY * nf + i], D2 = g[FG_DRZ * nf + i];
@@ -223,11 +245,10 @@ __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ 
         const double gy = omw * C.gp[3 * o + 1] + wt * C.gp[3 * n + 1];
         const double gz = omw * C.gp[3 * o + 2] + wt * C.gp[3 * n + 2];
         const double dip = omw * C.d[o] + wt * C.d[n];
-        const double rdip = rhoip * dip;
-        mip = mip - rdip * g[FG_ADN * nf + i] * ((C.p[n] - C.p[o]) - (gx * D0 + gy * D1 + gz * D2));
+        mip = mip - dip * C.fprop[PR_RHOADN * nf + i] * ((C.p[n] - C.p[o]) - (gx * D0 + gy * D1 + gz * D2));
         if (!C.steady) {   // the transient term carries 1/dt and vanishes when steady
             const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
-            mip = mip - rdip * C.rdt * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
+            mip = mip - rhoip * dip * C.rdt * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
         }
     }
     C.mip[i] = mip;
@@ -244,8 +265,7 @@ __global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
     if (n >= C.ne) { C.fdiff[i] = 0.0; return; }
     const double wt = C.fgeo[FG_WT * nf + i], omw = 1.0 - wt;
-    const double rhoip = omw * C.rho[o] + wt * C.rho[n];
-    C.fdiff[i] = (omw * C.dc[o] + wt * C.dc[n]) * rhoip * C.fgeo[FG_ADN * nf + i];
+    C.fdiff[i] = (omw * C.dc[o] + wt * C.dc[n]) * C.fprop[PR_RHOADN * nf + i];
 }
 
 __global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
@@ -330,8 +350,7 @@ __global__ void __launch_bounds__(kTile) k_update_faces(const CaseDev *__restric
     if (n >= C.ne) return;
     const double wt = C.fgeo[FG_WT * nf + i], omw = 1.0 - wt;
     const double dip = omw * C.dc[o] + wt * C.dc[n];
-    const double rhoip = (C.rho[o] + C.rho[n]) / 2.0;
-    C.mip[i] = C.mip[i] - rhoip * C.fgeo[FG_ADN * nf + i] * dip * (C.phic[n] - C.phic[o]);
+    C.mip[i] = C.mip[i] - C.fprop[PR_RHOMADN * nf + i] * dip * (C.phic[n] - C.phic[o]);
 }
 
 // update_time, mod_physics.f90:101-112
@@ -351,7 +370,15 @@ __global__ void __launch_bounds__(kTile) k_copy_mip0(const CaseDev *__restrict__
 }  // namespace
 
 void launch_bc(cfdl_ctx *ctx) { CFDL_LAUNCH("k_bc", k_bc, halos); }
+void ensure_face_props(cfdl_ctx *ctx) {
+    bool dirty = false;
+    for (HostCase *hc : ctx->cases) dirty |= hc->props_dirty;
+    if (!dirty || ctx->capturing) return;
+    CFDL_LAUNCH("k_face_props", k_face_props, faces);
+    for (HostCase *hc : ctx->cases) hc->props_dirty = false;
+}
 void launch_coef_uvw(cfdl_ctx *ctx) {
+    ensure_face_props(ctx);
     CFDL_LAUNCH("k_coef_uvw_face", k_coef_uvw_face, faces);
     CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell, cells);
 }
@@ -359,8 +386,12 @@ void launch_grad(cfdl_ctx *ctx, int field) {
     if (field == 4) CFDL_LAUNCH("k_grad3", k_grad<3>, cells, 0);
     else CFDL_LAUNCH("k_grad1", k_grad<1>, cells, field);
 }
-void launch_calc_mip(cfdl_ctx *ctx, int rc) { CFDL_LAUNCH("k_calc_mip", k_calc_mip, faces, rc); }
+void launch_calc_mip(cfdl_ctx *ctx, int rc) {
+    ensure_face_props(ctx);
+    CFDL_LAUNCH("k_calc_mip", k_calc_mip, faces, rc);
+}
 void launch_coef_p(cfdl_ctx *ctx) {
+    ensure_face_props(ctx);
     CFDL_LAUNCH("k_coef_p_face", k_coef_p_face, faces);
     CFDL_LAUNCH("k_coef_p_cell", k_coef_p_cell, cells);
 }
@@ -375,6 +406,7 @@ void launch_adjust_pc(cfdl_ctx *ctx) {
     CFDL_LAUNCH("k_adjust_pc", k_adjust_pc, cells);
 }
 void launch_update_uvwp(cfdl_ctx *ctx) {
+    ensure_face_props(ctx);
     CFDL_LAUNCH("k_update_cells", k_update_cells, cells);
     CFDL_LAUNCH("k_update_faces", k_update_faces, faces);
 }

@@ -309,6 +309,7 @@ def run_ours(a, dist):
                                "alpha_u=0.7 alpha_p=0.3, FP64" % (a.n, "tet-split" if a.tet else "hex", a.jitter),
                    "cells": ne, "faces": nf, "inner_solve": "10x residual drop / nit=100" if a.mode == 0 else "tight 1e-13",
                    "pressure_precond": ["jacobi", "amg"][a.precond], "tile": tile,
+                   "coarse_group": g.get_coarse_group(),
                    "autotune_ms_per_outer": {str(k): round(v, 3) for k, v in tile_ms.items()},
                    "parallelism": "replicas" if dist.world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)"},

@@ -176,6 +176,8 @@ def lib():
     L.cfdl_server_destroy.argtypes = [vp]
     L.cfdl_get_tile.argtypes = [vp]
     L.cfdl_autotune.argtypes = [vp, C.c_int, ip, dp]
+    L.cfdl_set_coarse_group.argtypes = [vp, C.c_int]
+    L.cfdl_get_coarse_group.argtypes = [vp]
     L.cfdl_launch_count.argtypes = [vp]
     L.cfdl_launch_count.restype = C.c_int64
     L.cfdl_status_string.argtypes = [C.c_int]
@@ -355,6 +357,13 @@ class Solver:
 
     def get_tile(self):
         return int(lib().cfdl_get_tile(self._h))
+
+    def set_coarse_group(self, lanes):
+        """Lanes per row on the large coarse multigrid levels (1, 2 or 4)."""
+        _check(lib().cfdl_set_coarse_group(self._h, int(lanes)), "set_coarse_group")
+
+    def get_coarse_group(self):
+        return int(lib().cfdl_get_coarse_group(self._h))
 
     def autotune(self, outer=3):
         """Times each tile shape on this context's cases (state restored) and

@@ -286,55 +286,55 @@ __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__
 // Coarse rows are wide (up to ~30 couplings) and a thread that walked one
 // alone would issue its index -> value -> vector loads one slot after the
 // other: a chain of dependent loads that left the small levels latency-bound.
-// On levels >= 1 each row is handled by kG lanes that split its slots (and
+// On small levels each row is handled by G lanes that split its slots (and
 // the Galerkin and restriction gather lists) and combine their partial sums
-// with shuffles, in a fixed order.  Tiles hold kTile / kG rows.
+// with shuffles, in a fixed order.  Tiles hold kTile / G rows.
 #define GROUP_HEAD                                                   \
     const Tile tl = tiles[blockIdx.x];                               \
     const CaseDev &C = cases[tl.c];                                  \
-    const int g = (int)threadIdx.x & (kG - 1);                       \
-    const int i = tl.first + (int)threadIdx.x / kG;                  \
+    const int g = (int)threadIdx.x & (G - 1);                        \
+    const int i = tl.first + (int)threadIdx.x / G;                   \
     const bool ok = i < tl.last;
 
-template <class T> __device__ __forceinline__ T group_sum(T v) {
+template <int G, class T> __device__ __forceinline__ T group_sum(T v) {
 #pragma unroll
-    for (int o = kG / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
 // sum_k a_ik x_j over the row's couplings inside the level, split over the group
-template <class T> __device__ __forceinline__ T group_offdiag(const LP<T> &P, const T *x, int i, bool ok, int g) {
+template <int G, class T> __device__ __forceinline__ T group_offdiag(const LP<T> &P, const T *x, int i, bool ok, int g) {
     T s = 0;
     if (ok)
-        for (int k = g; k < P.W; k += kG) {
+        for (int k = g; k < P.W; k += G) {
             const int j = P.nb[k * P.n + i];
             if ((unsigned)j < (unsigned)P.n) s += P.a[k * P.n + i] * x[j];
         }
-    return group_sum(s);
+    return group_sum<G>(s);
 }
 
 // z = t + w D^-1 (r - A t)
-template <class T>
+template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
-    const T off = group_offdiag<T>(P, P.t, i, ok, g);
+    const T off = group_offdiag<G, T>(P, P.t, i, ok, g);
     if (ok && g == 0) P.z[i] = P.t[i] + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * P.t[i] - off));
 }
 
 // t = r - A z
-template <class T>
+template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
-    const T off = group_offdiag<T>(P, P.z, i, ok, g);
+    const T off = group_offdiag<G, T>(P, P.z, i, ok, g);
     if (ok && g == 0) P.t[i] = P.r[i] - (P.dg[i] * P.z[i] - off);
 }
 
 // r_{l1}[I] = sum of the residual t_{l1-1} over the members of aggregate I
-template <class T>
+template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -342,14 +342,14 @@ __global__ void __launch_bounds__(kTile) k_vg_restrict(const CaseDev *__restrict
     const LP<T> F = level<T>(C, l1 - 1);
     T s = 0;
     if (ok)
-        for (int m = L.mem_ptr[i] + g; m < L.mem_ptr[i + 1]; m += kG) s += F.t[L.mem[m]];
-    s = group_sum(s);
+        for (int m = L.mem_ptr[i] + g; m < L.mem_ptr[i + 1]; m += G) s += F.t[L.mem[m]];
+    s = group_sum<G>(s);
     T *rc = sizeof(T) == 8 ? (T *)L.r : (T *)L.r32;
     if (ok && g == 0) rc[i] = s;
 }
 
 // t = x + w D^-1 (r - A x) with x = z + s P z_{l+1}
-template <class T>
+template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -359,11 +359,11 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
     const T sc = (T)kOverCorrect;
     T off = 0;
     if (ok)
-        for (int k = g; k < P.W; k += kG) {
+        for (int k = g; k < P.W; k += G) {
             const int j = P.nb[k * P.n + i];
             if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
         }
-    off = group_sum(off);
+    off = group_sum<G>(off);
     if (ok && g == 0) {
         const T xi = P.z[i] + sc * zc[L.agg[i]];
         P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * xi - off));
@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
 }
 
 // Galerkin row I of level l: each lane sums the gather lists of its slots
+template <int G>
 __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     GROUP_HEAD
     if (C.sc->halted) return;
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
     const int n = L.n;
     double dsum = 0.0;
     if (ok)
-        for (int k = g; k < L.W; k += kG) {
+        for (int k = g; k < L.W; k += G) {
             const int sl = k * n + i;
             double v = 0.0;
             for (int q = L.g_ptr[sl]; q < L.g_ptr[sl + 1]; q++) v += af[L.g_src[q]];
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
             if (mixed) L.a32[sl] = (float)v;
             dsum += v;
         }
-    dsum = group_sum(dsum);
+    dsum = group_sum<G>(dsum);
     if (ok && g == 0) {
         L.dg[i] = dsum;
         L.rd[i] = 1.0 / dsum;
@@ -654,12 +655,14 @@ int ensure_amg(cfdl_ctx *ctx) {
         int st;
         if ((st = build_worklist(ctx, ctx->amg_cells[l], cells))) return st;
         if ((st = build_worklist(ctx, ctx->amg_smooth[l], smooth))) return st;
-        // a level runs grouped when every case's level is small
+        // lanes per row: 8 when every case's level is small, else the tuned
+        // cgroup (1 = one thread per row); the mesh level is always 1
         const int nmax = *std::max_element(cells.begin(), cells.end());
-        if (l > 0 && nmax < kGroupedRows) {
-            ctx->amg_grouped[l] = 1;
-            if ((st = build_worklist(ctx, ctx->amg_gcells[l], cells, kTile / kG))) return st;
-            if ((st = build_worklist(ctx, ctx->amg_gsmooth[l], smooth, kTile / kG))) return st;
+        const int G = l == 0 ? 1 : nmax < kGroupedRows ? kG : ctx->cgroup;
+        ctx->amg_grouped[l] = G;
+        if (G > 1) {
+            if ((st = build_worklist(ctx, ctx->amg_gcells[l], cells, kTile / G))) return st;
+            if ((st = build_worklist(ctx, ctx->amg_gsmooth[l], smooth, kTile / G))) return st;
         }
     }
     ctx->amg_lmax = lmax;
@@ -690,35 +693,51 @@ int ensure_amg(cfdl_ctx *ctx) {
 static void amg_setup_operators(cfdl_ctx *ctx) {
     ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
     for (int l = 1; l <= ctx->amg_lmax; l++) {
-        if (ctx->amg_grouped[l]) ALAUNCH("k_amg_gal", k_amg_galg, ctx->amg_gcells[l], l);
-        else ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+        switch (ctx->amg_grouped[l]) {
+        case 8: ALAUNCH("k_amg_gal", k_amg_galg<8>, ctx->amg_gcells[l], l); break;
+        case 4: ALAUNCH("k_amg_gal", k_amg_galg<4>, ctx->amg_gcells[l], l); break;
+        case 2: ALAUNCH("k_amg_gal", k_amg_galg<2>, ctx->amg_gcells[l], l); break;
+        default: ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
+        }
     }
     CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, 256);
 }
 
 // One V-cycle z_0 = M^-1 r_0 on every active case.
+// The kernels of one coarse-level step at a group size (1: one thread per row)
+#define GROUPED(NAME, K, WLG, WL1, ...)                                          \
+    switch (G) {                                                                \
+    case 8: { auto kf_ = K<T, 8>; ALAUNCH(NAME, kf_, WLG, ##__VA_ARGS__); } break; \
+    case 4: { auto kf_ = K<T, 4>; ALAUNCH(NAME, kf_, WLG, ##__VA_ARGS__); } break; \
+    case 2: { auto kf_ = K<T, 2>; ALAUNCH(NAME, kf_, WLG, ##__VA_ARGS__); } break; \
+    default: break;                                                             \
+    }
+
 template <class T> static void vcycle(cfdl_ctx *ctx) {
-    // Levels with many rows run one thread per row; small levels run kG lanes
-    // per row (amg_grouped), which shortens each thread's chain of loads.
+    // Large levels run one thread per row (G = 1) or a few lanes per row
+    // (the autotuned cgroup); small levels run 8 lanes per row, which
+    // shortens each thread's chain of loads (amg_grouped[l] = G).
     const int L = ctx->amg_lmax;
     for (int l = 0; l < L; l++) {
-        const bool gl = ctx->amg_grouped[l], g1 = ctx->amg_grouped[l + 1];
         ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
-        if (gl) {
-            ALAUNCH("k_v_jac_c", k_vg_jac<T>, ctx->amg_gsmooth[l], l);
-            ALAUNCH("k_v_resid_c", k_vg_resid<T>, ctx->amg_gsmooth[l], l);
+        int G = ctx->amg_grouped[l];
+        if (G > 1) {
+            GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
+            GROUPED("k_v_resid_c", k_vg_resid, ctx->amg_gsmooth[l], 0, l)
         } else {
             ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
             ALAUNCH(l ? "k_v_resid_c" : "k_v_resid_f", k_v_resid<T>, ctx->amg_smooth[l], l);
         }
-        if (g1) ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict<T>, ctx->amg_gcells[l + 1], l + 1);
+        G = ctx->amg_grouped[l + 1];
+        if (G > 1) { GROUPED(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict, ctx->amg_gcells[l + 1], 0, l + 1) }
         else ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_cells[l + 1], l + 1);
     }
     CLAUNCH("k_v_coarse", k_v_coarse<T>, 256);
     for (int l = L - 1; l >= 0; l--) {
-        if (ctx->amg_grouped[l]) {
-            ALAUNCH("k_v_prolong_c", k_vg_prolong<T>, ctx->amg_gsmooth[l], l);
-            ALAUNCH("k_v_jac_c", k_vg_jac<T>, ctx->amg_gsmooth[l], l);
+        const int G = ctx->amg_grouped[l];
+        if (G > 1) {
+            GROUPED("k_v_prolong_c", k_vg_prolong, ctx->amg_gsmooth[l], 0, l)
+            GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
         } else {
             ALAUNCH(l ? "k_v_prolong_c" : "k_v_prolong_f", k_v_prolong<T>, ctx->amg_smooth[l], l);
             ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);

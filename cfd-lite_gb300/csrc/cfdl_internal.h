@@ -190,7 +190,8 @@ struct cfdl_ctx {
     // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
     std::vector<cfdl::WorkList> amg_cells, amg_smooth;      // per level, kTile rows per tile
     std::vector<cfdl::WorkList> amg_gcells, amg_gsmooth;    // per small coarse level, kTile/8 rows per tile
-    std::vector<int> amg_grouped;                           // level runs 8 lanes per row
+    std::vector<int> amg_grouped;                           // lanes per row of each level (1: one thread per row)
+    int cgroup = 1;                                          // lanes per row on the large coarse levels (autotuned)
     int amg_lmax = -1;
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;

@@ -88,6 +88,37 @@ int cfdl_set_tile(cfdl_ctx *ctx, int vec) {
 
 int cfdl_get_tile(const cfdl_ctx *ctx) { return ctx ? ctx->vec : -1; }
 
+int cfdl_set_coarse_group(cfdl_ctx *ctx, int lanes) {
+    if (!ctx || ctx->cases.empty() || !(lanes == 1 || lanes == 2 || lanes == 4)) return CFDL_ERR_INVALID;
+    if (lanes == ctx->cgroup) return CFDL_OK;
+    int st = cuda_status(cudaStreamSynchronize(ctx->stream));
+    if (st) return st;
+    ctx->cgroup = lanes;
+    ctx->amg_lmax = -1;      // multigrid work lists are rebuilt on the next solve
+    destroy_graph(ctx);
+    return CFDL_OK;
+}
+
+int cfdl_get_coarse_group(const cfdl_ctx *ctx) { return ctx ? ctx->cgroup : -1; }
+
+// Times `outer` outer iterations from the snapshot; returns ms per iteration.
+static int time_outer(cfdl_ctx *ctx, Snapshot &snap, int outer, cudaEvent_t e0, cudaEvent_t e1, double *ms) {
+    int st;
+    // warm-up: builds this shape's multigrid lists and graph
+    if ((st = solve_uvwp_all(ctx)) || (st = snap.restore(ctx))) return st;
+    cudaEventRecord(e0, ctx->stream);
+    for (int i = 0; i < outer; i++) {
+        launch_bc(ctx);
+        if ((st = solve_uvwp_all(ctx))) return st;
+    }
+    cudaEventRecord(e1, ctx->stream);
+    float f = 0.f;
+    if ((st = cuda_status(cudaEventSynchronize(e1)))) return st;
+    if ((st = cuda_status(cudaEventElapsedTime(&f, e0, e1)))) return st;
+    *ms = f / outer;
+    return snap.restore(ctx);
+}
+
 int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms) {
     if (!ctx || ctx->cases.empty() || outer <= 0) return CFDL_ERR_INVALID;
     Snapshot snap;
@@ -96,32 +127,31 @@ int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if ((st = cuda_status(cudaEventCreate(&e0)))) return st;
     if ((st = cuda_status(cudaEventCreate(&e1)))) { cudaEventDestroy(e0); return st; }
+    // the solver tile shape first, then the lanes per row of the large coarse
+    // multigrid levels at that shape
     const int n = (int)(sizeof(kTileShapes) / sizeof(kTileShapes[0]));
     int pick = ctx->vec;
     double best_ms = -1.0;
     for (int k = 0; k < n && !st; k++) {
         const int v = kTileShapes[k];
-        if ((st = cfdl_set_tile(ctx, v))) break;
-        // warm-up: builds this shape's multigrid lists and graph
-        if ((st = solve_uvwp_all(ctx)) || (st = snap.restore(ctx))) break;
-        cudaEventRecord(e0, ctx->stream);
-        for (int i = 0; i < outer && !st; i++) {
-            launch_bc(ctx);
-            st = solve_uvwp_all(ctx);
-        }
-        if (st) break;
-        cudaEventRecord(e1, ctx->stream);
-        float f = 0.f;
-        if ((st = cuda_status(cudaEventSynchronize(e1)))) break;
-        if ((st = cuda_status(cudaEventElapsedTime(&f, e0, e1)))) break;
-        if (ms) ms[k] = f / outer;
-        if (best_ms < 0.0 || f < best_ms) { best_ms = f; pick = v; }
-        st = snap.restore(ctx);
+        double t = 0.0;
+        if ((st = cfdl_set_tile(ctx, v)) || (st = time_outer(ctx, snap, outer, e0, e1, &t))) break;
+        if (ms) ms[k] = t;
+        if (best_ms < 0.0 || t < best_ms) { best_ms = t; pick = v; }
+    }
+    if (!st) st = cfdl_set_tile(ctx, pick);
+    int gpick = ctx->cgroup;
+    const int groups[] = {1, 2, 4};
+    double gbest = -1.0;
+    for (int k = 0; k < 3 && !st; k++) {
+        double t = 0.0;
+        if ((st = cfdl_set_coarse_group(ctx, groups[k])) || (st = time_outer(ctx, snap, outer, e0, e1, &t))) break;
+        if (gbest < 0.0 || t < gbest) { gbest = t; gpick = groups[k]; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st) return st;
-    if ((st = cfdl_set_tile(ctx, pick))) return st;
+    if ((st = cfdl_set_coarse_group(ctx, gpick))) return st;
     if (best) *best = pick;
     return snap.restore(ctx);
 }

@@ -284,6 +284,10 @@ int cfdl_run(cfdl_ctx *ctx, int max_outer, int *running);
  * sums, so results agree across shapes to rounding, not bit for bit. */
 int cfdl_set_tile(cfdl_ctx *ctx, int vec);
 int cfdl_get_tile(const cfdl_ctx *ctx);
+/* Lanes per row (1, 2 or 4; default 1) on the large coarse multigrid levels
+ * (small levels always use 8).  cfdl_autotune also picks this, after vec. */
+int cfdl_set_coarse_group(cfdl_ctx *ctx, int lanes);
+int cfdl_get_coarse_group(const cfdl_ctx *ctx);
 int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms);
 
 /* ---- serving loop ---------------------------------------------------------

@@ -42,6 +42,7 @@ def test_autotune_restores_state_and_picks_a_shape(need_gpu):
     before = {(c, f): b.case_get(c, f) for c in range(3) for f in ("u", "v", "w", "p", "mip")}
     best, ms = b.autotune(outer=2)
     assert best in (1, 2, 4, 8) and b.get_tile() == best
+    assert b.get_coarse_group() in (1, 2, 4)
     assert all(v > 0 for v in ms.values())
     for (c, f), v in before.items():
         assert np.array_equal(b.case_get(c, f), v), (c, f)
@@ -56,3 +57,21 @@ def test_invalid_tile_rejected(need_gpu):
     with pytest.raises(cfdl.CfdlError):
         g.set_tile(3)
     g.close()
+
+
+def test_coarse_group_shapes_agree(need_gpu):
+    """Large coarse levels (>= 65536 rows) run 1, 2 or 4 lanes per row; all
+    three give the same tight-mode fields to rounding."""
+    z = cfdl.Zone(84, False, 0.1, seed=3)
+    s = cfdl.Setup(z)
+    out = {}
+    for lanes in (1, 2, 4):
+        g = cfdl.Solver(s, cfdl.steady(solve_mode=1, tight_rtol=1e-12))
+        g.set_coarse_group(lanes)
+        assert g.get_coarse_group() == lanes
+        g.step(3, ncoef=0)
+        out[lanes] = {f: g.get(f) for f in ("u", "v", "w", "p")}
+        g.close()
+    for lanes in (2, 4):
+        for f in ("u", "v", "w", "p"):
+            assert rel_l2(out[lanes][f], out[1][f]) < 1e-9, (lanes, f)

@@ -17,15 +17,15 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
     table = {
         # update_boundaries: halo tables + halo u,v,w,p writes, owner p, mip
         "k_bc": nbf * (4 + 4 + 4 + 24 + 32 + 8 + 8),
-        # momentum face terms: own/nb, 8 geometry planes, 7 outputs; mu + 9 gradient comps per cell
-        "k_coef_uvw_face": nfi * (8 + 64 + 56) + nbf * (8 + 8 + 8) + ne * (8 + 72),
-        # momentum cell gather: ELL nb/fc, 8 face doubles, 13 cell doubles in, 6 out, anb ELL out
-        "k_coef_uvw_cell": 2 * ell_i + nf * 64 + ne * (104 + 48) + ell_d + nbf * (24 + 4 + 32),
+        # momentum face terms: own/nb, weight + 6 property planes, 3 outputs; 9 gradient comps per cell
+        "k_coef_uvw_face": nfi * (8 + 56 + 24) + ne * 72,
+        # momentum cell gather: ELL nb/fc, 5 face doubles, 13 cell doubles in, 6 out, anb ELL out
+        "k_coef_uvw_cell": 2 * ell_i + nf * 40 + ne * (104 + 48) + ell_d + nbf * (24 + 4 + 32),
         "k_grad3": ell_i + 3 * ell_d + 24 * (ne + nbf) + 72 * ne,
         "k_grad1": ell_i + 3 * ell_d + 8 * (ne + nbf) + 24 * ne,
         # Rhie-Chow: own/nb, 8 geometry planes, mip0 in, mip out; 12 cell doubles
-        "k_calc_mip": nfi * (8 + 64 + 16) + ne * 96,
-        "k_coef_p_face": nfi * (8 + 16 + 8) + nbf * 8 + ne * 16,
+        "k_calc_mip": nfi * (8 + 72 + 16) + ne * 80,
+        "k_coef_p_face": nfi * (8 + 16 + 8) + nbf * 8 + ne * 8,
         "k_coef_p_cell": 2 * ell_i + nf * 16 + ell_d + ne * 16,
         "k_adjust_pc": ell_i + ne * 16 + nbf * 8,
         "k_update_cells": ne * (8 + 8 + 8 + 24 + 24 + 24),

@@ -173,7 +173,6 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
     if ((st = zeros(hc, &d.anb, (size_t)W * ne))) return st;
     if ((st = zeros(hc, &d.fdiff, (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fS, 3 * (size_t)nf))) return st;
-    if ((st = zeros(hc, &d.fD, 3 * (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fprop, (size_t)PR_N * nf))) return st;
     double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt, &d.kb};
     for (double **pp : kv) if ((st = zeros(hc, pp, 3 * (size_t)ne))) return st;

@@ -109,7 +109,7 @@ struct CaseDev {
     double *bu, *bv, *bw, *d, *dc, *rho, *mu;
     double *ap, *anb, *b, *phic;          // phys_t scratch: ap[ne], anb ELL [W][ne], b[ne], phic[ne+nbf]
     // face intermediates of the assemblies
-    double *fdiff, *fS, *fD;              // [nf], [3][nf], [3][nf]
+    double *fdiff, *fS;                   // [nf] pressure face coefficient, [3][nf] explicit momentum face terms
     double *fprop;                        // [PR_N][nf] property planes
     // Krylov work vectors, [3][ne] each (pressure uses plane 0)
     double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt, *kb;

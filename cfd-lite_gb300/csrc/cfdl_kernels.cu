@@ -72,13 +72,14 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restri
     for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int m = 0; m < 3; m++) gi[q][m] = omw * gq[q][3 * o + m] + wt * gq[q][3 * n + m];
+    // the two explicit face terms of component m, which the cell sums add to
+    // the same right-hand side, stored as one value:
+    //   sumss(m):   mu_ip (du/dx_m, dv/dx_m, dw/dx_m) . dr
+    //   sumdefc(m): mu_ip grad(u_m) . (dr_p/ds_p - dr/ds)
+    // (mu_ip is folded into the property planes)
 #pragma unroll
-    for (int m = 0; m < 3; m++) {
-        // sumss(m): mu_ip (du/dx_m, dv/dx_m, dw/dx_m) . dr (mu_ip folded into the plane)
-        C.fS[m * nf + i] = gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2;
-        // sumdefc(q=m): mu_ip grad(u_m) . (dr_p/ds_p - dr/ds)
-        C.fD[m * nf + i] = gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2;
-    }
+    for (int m = 0; m < 3; m++)
+        C.fS[m * nf + i] = (gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2) + (gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2);
 }
 
 // Property planes of every face (recomputed when rho or mu change): the mesh
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, nf = C.nf, W = C.W;
-    double ap = 0.0, sumf = 0.0, ss0 = 0.0, ss1 = 0.0, ss2 = 0.0, dd0 = 0.0, dd1 = 0.0, dd2 = 0.0;
+    double ap = 0.0, sumf = 0.0, ss0 = 0.0, ss1 = 0.0, ss2 = 0.0;
     double a[kMaxW];
     int bslot[kMaxW], nb_cnt = 0;
 #pragma unroll
@@ -134,22 +135,21 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         // sg * x as a sign-bit flip: no FP64 multiply
         const bool ng = fc < 0;
         ss0 += flip_sign(C.fS[f], ng); ss1 += flip_sign(C.fS[nf + f], ng); ss2 += flip_sign(C.fS[2 * nf + f], ng);
-        dd0 += flip_sign(C.fD[f], ng); dd1 += flip_sign(C.fD[nf + f], ng); dd2 += flip_sign(C.fD[2 * nf + f], ng);
     }
     double asum = ap;                       // sum of the anb of this row so far
     const double vol = C.vol[i];
     const double ue = C.u[i], ve = C.v[i], we = C.w[i];
     double bu, bv, bw;
     if (C.steady) {                         // ap0 = rho*vol/dt = 0
-        bu = sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
-        bv = sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
-        bw = sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+        bu = sumf * ue - vol * C.gp[3 * i] + ss0;
+        bv = sumf * ve - vol * C.gp[3 * i + 1] + ss1;
+        bw = sumf * we - vol * C.gp[3 * i + 2] + ss2;
     } else {
         const double ap0 = C.rho[i] * vol * C.rdt;
         ap = ap + ap0;
-        bu = ap0 * C.u0[i] + sumf * ue - vol * C.gp[3 * i] + ss0 + dd0;
-        bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1 + dd1;
-        bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2 + dd2;
+        bu = ap0 * C.u0[i] + sumf * ue - vol * C.gp[3 * i] + ss0;
+        bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1;
+        bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2;
     }
     // boundary conditions in BC-loop order (ascending halo index)
     for (int q = 1; q < nb_cnt; q++) {

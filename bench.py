@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--n", "--edge", dest="n", type=int, default=128, help="mesh edge: n^3 hex cells")
     ap.add_argument("--jitter", type=float, default=0.2)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tet", action="store_true")

@@ -160,3 +160,31 @@ def test_form_mismatch_rejected(need_gpu):
     with pytest.raises(cfdl.CfdlError):
         b.remove(0)          # the last case stays
     b.close()
+
+
+def test_nonfinite_case_stops_alone(need_gpu):
+    """A case whose state turns non-finite stops with CFDL_ERR_NONFINITE;
+    the other cases of the batch run on, unaffected (failure injected on the
+    host: a NaN written into one cell's velocity)."""
+    setups = [case_setup(*s[:4]) for s in SPECS[:2]]
+    b = cfdl.Batch(setups, [cavity_cfg(s[4]) for s in SPECS[:2]])
+    u = b.case_get(1, "u")
+    u[3] = float("nan")
+    b.case_set(1, "u", u)
+    b.set_run(6)
+    assert b.run(6) == 0
+    bad, good = b.case_stats(1), b.case_stats(0)
+    assert bad.status == cfdl.CFDL_ERR_NONFINITE and bad.run_left == 0 and bad.outer_done == 1
+    assert good.status == 0 and good.outer_done == 6
+    ref = alone(SPECS[0], 6)
+    for f in FIELDS:
+        assert np.array_equal(b.case_get(0, f), ref[f]), f
+    b.close()
+    g = cfdl.Solver(case_setup(*SPECS[1][:4]), cavity_cfg(SPECS[1][4]))
+    v = g.get("v")
+    v[0] = float("inf")
+    g.set("v", v)
+    with pytest.raises(cfdl.CfdlError) as ei:
+        g.solve_uvwp()
+    assert ei.value.status == cfdl.CFDL_ERR_NONFINITE
+    g.close()

@@ -50,6 +50,7 @@ struct Resident {
     std::unique_ptr<Request> req;
     HostCase *hc = nullptr;
     int outer_seen = 0;
+    size_t reserved = 0;     // bytes held against the budget: max(estimate, allocated)
 };
 
 struct Finished {
@@ -226,7 +227,7 @@ void device_loop(cfdl_server *S) {
                 }
                 if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) status = CFDL_ERR_CUDA;
             }
-            const size_t bytes = R.hc->bytes;
+            const size_t bytes = R.reserved;
             destroy_case(R.hc);
             ctx->cases.erase(ctx->cases.begin() + c);
             finish_request(S, *R.req, status, &sc[c], nullptr, std::move(f));
@@ -287,13 +288,17 @@ void device_loop(cfdl_server *S) {
             ctx->cases.push_back(hc);
             q->t_admit = S->now();
             q->prep.release_tables();   // host tables no longer needed
+            // the budget holds the larger of the estimate and what was
+            // allocated, so later allocations of the case stay covered
+            const size_t reserved = std::max(q->est, hc->bytes);
             {
                 std::lock_guard<std::mutex> lk(S->mu);
-                S->held_bytes += hc->bytes;
+                S->held_bytes += reserved;
             }
             Resident R;
             R.req = std::move(q);
             R.hc = hc;
+            R.reserved = reserved;
             res.push_back(std::move(R));
             changed = true;
         }

@@ -116,7 +116,7 @@ struct CaseDev {
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each
     float *fr, *fz, *fp, *fq, *fx, *fdiag, *fanb;   // fanb ELL [W][ne]
     float *ft, *frap;
-    // pressure preconditioner: 1/ap of the pressure operator, AMG levels, coarsest inverse
+    // 1/ap of the operator being solved (momentum, then pressure), AMG levels, coarsest inverse
     double *rap;
     int nlev, ncoarse;                    // coarse levels; cells of the coarsest level
     const AmgLevelDev *lev;               // [nlev] device array

@@ -66,6 +66,7 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
         a[k] = j >= 0 ? C.anb[k * ne + i] : 0.0;
     }
     const double api = C.ap[i];
+    C.rap[i] = 1.0 / api;                   // the Jacobi scaling of the whole solve, divided once
 #pragma unroll
     for (int q = 0; q < 3; q++) {
         const double *__restrict__ phi = comp_field(C, q);
@@ -125,10 +126,10 @@ __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cas
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
     const bool first[3] = {S->iters[0] == 0, S->iters[1] == 0, S->iters[2] == 0};
     const double be[3] = {S->beta[0], S->beta[1], S->beta[2]}, om[3] = {S->omega[0], S->omega[1], S->omega[2]};
-    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ ap = C.ap;
+    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ rapv = C.rap;
     double *__restrict__ kp = C.kp, *__restrict__ kph = C.kph;
     FOR_CELLS(t) {
-        const double rap = 1.0 / ap[i];
+        const double rap = rapv[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
@@ -179,10 +180,10 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
     double v[3] = {0, 0, 0};
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
     const double al[3] = {S->alpha[0], S->alpha[1], S->alpha[2]};
-    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ ap = C.ap;
+    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ rapv = C.rap;
     double *__restrict__ ks = C.ks, *__restrict__ ksh = C.ksh;
     FOR_CELLS(t) {
-        const double rap = 1.0 / ap[i];
+        const double rap = rapv[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;

@@ -34,7 +34,8 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
         "k_update_time_halo": nbf * 48,
         "k_copy_mip0": nf * 16,
         # momentum BiCGStab, m active components
-        "k_mom_init": ne * 8 + ell_d + ell_i + m * ne * (8 + 8 + 40) + m * nbf * 8,
+        # ap, rap out; per component: b, phi in, r and rh out
+        "k_mom_init": ne * 16 + ell_d + ell_i + m * ne * (8 + 8 + 16) + m * nbf * 8,
         "k_mom_p": ne * 8 + m * ne * (24 + 16),
         "k_mom_v": ne * 8 + ell_d + ell_i + m * ne * (8 + 8 + 8),
         "k_mom_s": ne * 8 + m * ne * (16 + 16),
@@ -54,10 +55,10 @@ def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
     """One V-cycle kernel at one level of n cells and ELL width W."""
     ell_i = 4 * W * n
     return {
-        "jac0": 3 * s * n,
-        "jac": 5 * s * n + W * s * n + ell_i,
-        "resid": 4 * s * n + W * s * n + ell_i,
-        "prolong": (5 * s + 4) * n + W * s * n + ell_i + n_next * s,
+        "jac0": 3 * s * n,                                  # r, w/D in; t out
+        "jac": 4 * s * n + W * s * n + ell_i,               # t, r, w/D in; z out; ELL values and indices
+        "resid": 4 * s * n + W * s * n + ell_i,             # z, r, D in; t out
+        "prolong": (4 * s + 4) * n + W * s * n + ell_i + n_next * s,   # z, r, w/D, agg in; t out; coarse z
         "restrict": n_prev * (s + 4) + n * (4 + s),     # into this level from the finer one
     }[kind]
 

@@ -33,7 +33,7 @@ enum { CNT_A0 = 9, CNT_A1, CNT_A2, CNT_A3, CNT_A4, CNT_A5 };
 template <class T> struct LP {
     int n, W;
     const int *nb;
-    const T *a, *dg, *rd;
+    const T *a, *dg, *rd;   // rd = omega / diagonal (the damped Jacobi scaling)
     T *r, *z, *t;
 };
 
@@ -56,6 +56,50 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
     return y[0];
 }
 
+// sum_j a_ij x_j over the row's couplings inside the level (the ELL values
+// are the off-diagonal magnitudes: A = D - offdiag)
+template <int W, class T> __device__ __forceinline__ T offsum_w(const LP<T> &P, const T *x, int i) {
+    int j[W];
+    T c[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const int jj = P.nb[k * P.n + i];
+        const bool ok = (unsigned)jj < (unsigned)P.n;
+        j[k] = ok ? jj : i;
+        c[k] = ok ? P.a[k * P.n + i] : (T)0;
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) s += c[k] * x[j[k]];
+    return s;
+}
+template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
+    if (P.W == 6) return offsum_w<6, T>(P, x, i);
+    if (P.W == 4) return offsum_w<4, T>(P, x, i);
+    // wide coarse rows: four slots per step, loads issued together
+    T s = 0;
+    for (int k0 = 0; k0 < P.W; k0 += 4) {
+        int jj[4];
+        T c[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < P.W ? P.nb[(k0 + u) * P.n + i] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ok = (unsigned)jj[u] < (unsigned)P.n;
+            c[u] = ok ? P.a[(k0 + u) * P.n + i] : (T)0;
+            xv[u] = x[ok ? jj[u] : i];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) s += c[u] * xv[u];
+    }
+    return s;
+}
+
+// damped Jacobi sweep from x: x + w D^-1 (r - A x) = (1 - w) x + (w/D)(r + offsum)
+template <class T> __device__ __forceinline__ T jacobi_step(T x, T r, T wrd, T off) {
+    return (T)(1.0 - kOmega) * x + wrd * (r + off);
+}
+
 __device__ __forceinline__ bool pactive(const CaseDev &C) { return C.sc->active_p != 0; }
 __device__ __forceinline__ bool mactive(const CaseDev &C) { return C.sc->active32 != 0; }
 
@@ -74,10 +118,10 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     const int i = t.first + (int)threadIdx.x;
     if (i >= t.last || C.sc->halted) return;
     const double ap = C.ap[i];
-    C.rap[i] = 1.0 / ap;
+    C.rap[i] = kOmega / ap;
     if (C.precision == 1) {
         C.fdiag[i] = (float)ap;
-        C.frap[i] = (float)(1.0 / ap);
+        C.frap[i] = (float)(kOmega / ap);
         for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = (float)C.anb[k * C.ne + i];
     }
 }
@@ -146,7 +190,7 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.t[i] = (T)kOmega * P.rd[i] * P.r[i];
+    P.t[i] = P.rd[i] * P.r[i];
 }
 
 // z = t + w D^-1 (r - A t)
@@ -158,7 +202,7 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.z[i] = P.t[i] + (T)kOmega * P.rd[i] * (P.r[i] - amul<T>(P, P.t, i));
+    P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
 }
 
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
@@ -210,8 +254,8 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
         dsum += v;
     }
     L.dg[I] = dsum;
-    L.rd[I] = 1.0 / dsum;
-    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(1.0 / dsum); }
+    L.rd[I] = kOmega / dsum;
+    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(kOmega / dsum); }
 }
 
 // coarsest: z_L = Minv r_L (one CTA per case, 4 lanes per row)
@@ -239,7 +283,7 @@ __global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ ca
 // values are loaded as three independent batches (no per-slot load chain)
 template <int W, class T>
 __device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__ agg, const T *__restrict__ zc, T sc,
-                                         int i, T xi) {
+                                         int i) {
     int j[W], ag[W];
     bool ok[W];
 #pragma unroll
@@ -250,10 +294,10 @@ __device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__
     }
 #pragma unroll
     for (int k = 0; k < W; k++) ag[k] = agg[j[k]];
-    T s = P.dg[i] * xi;
+    T s = 0;
 #pragma unroll
     for (int k = 0; k < W; k++)
-        if (ok[k]) s -= P.a[k * P.n + i] * (P.z[j[k]] + sc * zc[ag[k]]);
+        if (ok[k]) s += P.a[k * P.n + i] * (P.z[j[k]] + sc * zc[ag[k]]);
     return s;
 }
 
@@ -269,17 +313,17 @@ __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__
     const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
     const T sc = (T)kOverCorrect;
     const T xi = P.z[i] + sc * zc[L.agg[i]];
-    T s;
-    if (P.W == 6) s = prolong_row<6, T>(P, L.agg, zc, sc, i, xi);
-    else if (P.W == 4) s = prolong_row<4, T>(P, L.agg, zc, sc, i, xi);
+    T off;
+    if (P.W == 6) off = prolong_row<6, T>(P, L.agg, zc, sc, i);
+    else if (P.W == 4) off = prolong_row<4, T>(P, L.agg, zc, sc, i);
     else {
-        s = P.dg[i] * xi;
+        off = 0;
         for (int k = 0; k < P.W; k++) {
             const int j = P.nb[k * P.n + i];
-            if (j >= 0 && j < P.n) s -= P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
+            if (j >= 0 && j < P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
         }
     }
-    P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - s);
+    P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
 }
 
 // ------------------------------------------------- coarse levels, grouped
@@ -320,7 +364,7 @@ __global__ void __launch_bounds__(kTile) k_vg_jac(const CaseDev *__restrict__ ca
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
     const T off = group_offdiag<G, T>(P, P.t, i, ok, g);
-    if (ok && g == 0) P.z[i] = P.t[i] + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * P.t[i] - off));
+    if (ok && g == 0) P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], off);
 }
 
 // t = r - A z
@@ -366,7 +410,7 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
     off = group_sum<G>(off);
     if (ok && g == 0) {
         const T xi = P.z[i] + sc * zc[L.agg[i]];
-        P.t[i] = xi + (T)kOmega * P.rd[i] * (P.r[i] - (P.dg[i] * xi - off));
+        P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
     }
 }
 
@@ -392,8 +436,8 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
     dsum = group_sum<G>(dsum);
     if (ok && g == 0) {
         L.dg[i] = dsum;
-        L.rd[i] = 1.0 / dsum;
-        if (mixed) { L.dg32[i] = (float)dsum; L.rd32[i] = (float)(1.0 / dsum); }
+        L.rd[i] = kOmega / dsum;
+        if (mixed) { L.dg32[i] = (float)dsum; L.rd32[i] = (float)(kOmega / dsum); }
     }
 }
 

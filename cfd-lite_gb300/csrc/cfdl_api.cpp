@@ -551,7 +551,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 8 * nc * 8 + 15 * nc * 8 + 2 * f * 8;   // cell fields, gradients, mip/mip0
     bytes += 9 * c * 8 + w * c * 8 + 4 * f * 8;      // coefficients, face intermediates
     bytes += 10 * f * 8;                              // property planes
-    bytes += 27 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
+    bytes += 24 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
     bytes += 160 * c;                                 // multigrid hierarchy (bound)
     return bytes;
 }

@@ -174,7 +174,7 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
     if ((st = zeros(hc, &d.fdiff, (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fS, 3 * (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fprop, (size_t)PR_N * nf))) return st;
-    double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt, &d.kb};
+    double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt};
     for (double **pp : kv) if ((st = zeros(hc, pp, 3 * (size_t)ne))) return st;
     float **fv[] = {&d.fr, &d.fz, &d.fp, &d.fq, &d.fx, &d.fdiag, &d.ft, &d.frap};
     for (float **pp : fv) if ((st = zeros(hc, pp, (size_t)ne))) return st;

@@ -112,7 +112,7 @@ struct CaseDev {
     double *fdiff, *fS;                   // [nf] pressure face coefficient, [3][nf] explicit momentum face terms
     double *fprop;                        // [PR_N][nf] property planes
     // Krylov work vectors, [3][ne] each (pressure uses plane 0)
-    double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt, *kb;
+    double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt;
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each
     float *fr, *fz, *fp, *fq, *fx, *fdiag, *fanb;   // fanb ELL [W][ne]
     float *ft, *frap;

@@ -49,7 +49,7 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
     (void)ne;
 
 // ------------------------------ momentum ----------------------------------
-// init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r, p = v = 0.
+// init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r.
 // The row's slot indices and coefficients are loaded once for the three
 // components; sums run in slot order.
 template <int W>
@@ -81,11 +81,9 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
             else if (in[k]) s -= a[k] * pv[k];
         }
         const double r = bb - s;
-        C.kb[q * ne + i] = bb;
+        // p and v need no clearing: the first iteration sets p = r (k_mom_p)
         C.kr[q * ne + i] = r;
         C.krh[q * ne + i] = r;
-        C.kp[q * ne + i] = 0.0;
-        C.kv[q * ne + i] = 0.0;
         v[q] += bb * bb;
         v[3 + q] += r * r;
     }

@@ -604,6 +604,7 @@ def run_served(a, dist):
             srv.close()
             lat = np.array([r.t_done - r.t_submit for r in res])
             dev = np.array([r.t_done - r.t_admit for r in res])
+            prep = np.array([r.t_ready - r.t_submit for r in res])
             span = max(r.t_done for r in res) - min(r.t_submit for r in res)
             out = {
                 "metric": "served cavity requests: p50/p99 latency (s)", "value": float(np.percentile(lat, 99)),
@@ -618,6 +619,7 @@ def run_served(a, dist):
                            "rate_req_s": rate, "requests": len(reqs)},
                 "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                 "device_p50_s": float(np.percentile(dev, 50)), "device_p99_s": float(np.percentile(dev, 99)),
+                "host_prep_p50_s": float(np.percentile(prep, 50)), "host_prep_p99_s": float(np.percentile(prep, 99)),
                 "throughput_req_s": len(res) / span, "cell_iters_per_s": info["cell_iters"] / span,
                 "converged": int(sum(r.converged for r in res)), "failed": int(sum(r.status != 0 for r in res)),
                 "outer_iterations": {"min": int(min(r.outer_done for r in res)),

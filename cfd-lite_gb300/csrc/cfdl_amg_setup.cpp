@@ -14,6 +14,7 @@
 // A_c = P^T A P (P piecewise constant) from gather lists prepared here, so the
 // coarse coefficients are sums in a fixed order (deterministic).
 #include "cfdl_amg.h"
+#include "cfdl_par.h"
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -102,7 +103,8 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
         std::vector<std::vector<int>> cnb(nc);
         std::vector<std::vector<std::vector<int>>> src(nc);
         std::vector<std::vector<double>> cw(nc);
-        for (int c = 0; c < nc; c++) {
+        parallel_for(nc, [&](long cb, long ce) {
+        for (int c = (int)cb; c < (int)ce; c++) {
             for (int m = L.mem_ptr[c]; m < L.mem_ptr[c + 1]; m++) {
                 int i = L.mem[m];
                 for (int k = 0; k < g.W; k++) {
@@ -119,6 +121,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
                 }
             }
         }
+        }, 2048);
         int Wc = 1;
         for (int c = 0; c < nc; c++) Wc = std::max<int>(Wc, (int)cnb[c].size());
         L.W = Wc;

@@ -14,6 +14,7 @@
 // (mod_solver.f90:8-38) including its trace fallback.
 #include "cfdl_internal.h"
 #include "cfdl_amg.h"
+#include "cfdl_par.h"
 #include <algorithm>
 #include <cmath>
 #include <cfloat>
@@ -279,7 +280,8 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
         std::vector<double> &fgeo = p->fgeo;
         fgeo.assign((size_t)FG_N * nf, 0.0);
         auto G = [&](int plane, int f) -> double & { return fgeo[(size_t)plane * nf + f]; };
-        for (int f = 0; f < nf; f++) {
+        parallel_for(nf, [&](long fb, long fe) {
+        for (int f = (int)fb; f < (int)fe; f++) {
             int e = f_own[f], n = f_nb[f];
             const double *a = &m->aip[3 * (size_t)f], *ri = &m->rip[3 * (size_t)f];
             double rp[3] = {m->xc[e], m->yc[e], m->zc[e]}, rn[3] = {m->xc[n], m->yc[n], m->zc[n]};
@@ -310,10 +312,12 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
                 }
             }
         }
+        });
         // ---- least-squares gradient stencil ----
         std::vector<double> &hf_G = p->hf_G;
         hf_G.assign(3 * (size_t)W * ne, 0.0);
-        for (int e = 0; e < ne; e++) {
+        parallel_for(ne, [&](long cb, long ce) {
+        for (int e = (int)cb; e < (int)ce; e++) {
             double A[3][3] = {{0}}, Ai[3][3], wdr[kMaxW][3];
             int cnt = m->ef2nb_idx[e + 1] - m->ef2nb_idx[e];
             for (int k = 0; k < cnt; k++) {
@@ -334,6 +338,7 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
                 for (int q = 0; q < 3; q++)
                     hf_G[((size_t)q * W + k) * ne + e] = Ai[q][0]*wdr[k][0] + Ai[q][1]*wdr[k][1] + Ai[q][2]*wdr[k][2];
         }
+        });
         p->vol.assign(m->vol, m->vol + ne);
     } catch (const std::bad_alloc &) {
         return CFDL_ERR_OOM;

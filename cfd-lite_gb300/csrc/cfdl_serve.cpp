@@ -19,6 +19,7 @@
 // case and every reduction sums a case's own partials in a fixed order, so a
 // request's result does not depend on which requests shared its launches.
 #include "cfdl_internal.h"
+#include "cfdl_par.h"
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -131,6 +132,9 @@ int prepare(const cfdl_server_config &s, Request &q) {
 }
 
 void prep_loop(cfdl_server *S) {
+    // the preparation threads share the host cores for their parallel loops
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    host_threads() = std::max(1, hw / S->cfg.prep_threads);
     for (;;) {
         std::unique_ptr<Request> q;
         {

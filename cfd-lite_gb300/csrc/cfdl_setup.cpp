@@ -15,7 +15,9 @@
 // by operation (compiled without FP contraction), so the doubles are the
 // reference's bit for bit.
 #include "cfdl.h"
+#include "cfdl_par.h"
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -111,23 +113,31 @@ int build(cfdl_setup &S) {
     }
     const int H = S.ef2nb_idx[ng] - 1;
     if (H != 2 * S.nf - S.nbf) return CFDL_ERR_MESH;
-    std::vector<FaceKey> keys;
-    keys.reserve((size_t)H + S.nbf);
-    for (int e = 1; e <= S.nelem; e++) {
-        int t = S.etype[sec_of(e)];
-        for (int f = 1; f <= kElementNFace[t]; f++) {
-            int lst[4], nl;
-            if (!face_vxlist(&S.e2vx[(size_t)(e - 1) * m], t, f, lst, nl)) return CFDL_ERR_MESH;
-            FaceKey k;
-            k.v[0] = 0;
-            for (int q = 0; q < nl; q++) k.v[4 - nl + q] = lst[q];
-            std::sort(k.v + 4 - nl, k.v + 4);
-            k.minv = k.v[4 - nl];
-            k.e = e; k.f = f;
-            keys.push_back(k);
+    // one key per element face: volume element e's faces at its CSR slots,
+    // each 2D element's single face after them (disjoint writes, any order)
+    std::vector<FaceKey> keys((size_t)H + (S.nelem - ng));
+    std::atomic<int> bad{0};
+    cfdl::parallel_for(S.nelem, [&](long b, long e_end) {
+        for (long e0 = b; e0 < e_end; e0++) {
+            const int e = (int)e0 + 1;
+            const int t = S.etype[sec_of(e)];
+            const size_t base = e <= ng ? (size_t)S.ef2nb_idx[e - 1] - 1 : (size_t)H + (e - ng - 1);
+            if (e > ng && kElementNFace[t] != 1) { bad = 1; return; }
+            for (int f = 1; f <= kElementNFace[t]; f++) {
+                int lst[4], nl;
+                if (!face_vxlist(&S.e2vx[(size_t)(e - 1) * m], t, f, lst, nl)) { bad = 1; return; }
+                FaceKey k;
+                k.v[0] = 0;
+                for (int q = 0; q < nl; q++) k.v[4 - nl + q] = lst[q];
+                std::sort(k.v + 4 - nl, k.v + 4);
+                k.minv = k.v[4 - nl];
+                k.e = e; k.f = f;
+                keys[base + f - 1] = k;
+            }
         }
-    }
-    std::sort(keys.begin(), keys.end());
+    });
+    if (bad) return CFDL_ERR_MESH;
+    cfdl::parallel_sort(keys, [](const FaceKey &a, const FaceKey &b) { return a < b; });
     struct Pair { int minv, e1, f1, e2, f2; };
     std::vector<Pair> pairs;
     pairs.reserve(S.nf);
@@ -141,13 +151,14 @@ int build(cfdl_setup &S) {
         i = j;
     }
     if ((int)pairs.size() != S.nf) return CFDL_ERR_MESH;
-    std::sort(pairs.begin(), pairs.end(), [](const Pair &p, const Pair &q) {
+    cfdl::parallel_sort(pairs, [](const Pair &p, const Pair &q) {
         if (p.minv != q.minv) return p.minv < q.minv;
         if (p.e1 != q.e1) return p.e1 < q.e1;
         return p.f1 < q.f1;
     });
     S.ef2nb1.assign(H, 0); S.ef2nb2.assign(H, 0); S.s2g.assign(S.nf, 0); S.bs.assign(S.nbf, 0);
-    for (int fg = 1; fg <= S.nf; fg++) {
+    cfdl::parallel_for(S.nf, [&](long b, long e_end) {
+    for (int fg = (int)b + 1; fg <= (int)e_end; fg++) {
         const Pair &p = pairs[fg - 1];
         int idx1 = S.ef2nb_idx[p.e1 - 1] + p.f1 - 1;
         if (p.e2 > ng) {
@@ -164,6 +175,7 @@ int build(cfdl_setup &S) {
             S.s2g[fg - 1] = index_t(p.e1, p.f1);
         }
     }
+    });
     // edge boundary faces (mod_mg_lvl_uns.f90:421-433)
     for (int e1 = ng + 1; e1 <= S.nelem; e1++) {
         int &b1 = S.bs[e1 - ng - 1];
@@ -212,7 +224,8 @@ int build(cfdl_setup &S) {
     }
     // calc_aip_xyzip_uns (calc_aip_xyzip.f90:7-74)
     S.aip.assign(3 * (size_t)S.nf, 0.0); S.rip.assign(3 * (size_t)S.nf, 0.0);
-    for (int fg = 1; fg <= S.nf; fg++) {
+    cfdl::parallel_for(S.nf, [&](long b, long e_end) {
+    for (int fg = (int)b + 1; fg <= (int)e_end; fg++) {
         int e, fl; get_idx(S.s2g[fg - 1], e, fl);
         int t = S.etype[sec_of(e)], lst[4], nl;
         face_vxlist(&S.e2vx[(size_t)(e - 1) * m], t, fl, lst, nl);
@@ -235,9 +248,12 @@ int build(cfdl_setup &S) {
         double dd = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
         for (int q = 0; q < 3; q++) ri[q] = (sumc[q][0] * a[0] + sumc[q][1] * a[1] + sumc[q][2] * a[2]) / dd;
     }
+    });
     // calc_vol_cv_centers_uns (calc_vol_cv_centers.f90:4-61)
     S.xc.assign(S.nelem, 0.0); S.yc.assign(S.nelem, 0.0); S.zc.assign(S.nelem, 0.0); S.vol.assign(ng, 0.0);
-    for (int e = 1; e <= ng; e++) {
+    std::atomic<int> flat{0};
+    cfdl::parallel_for(ng, [&](long b, long e_end) {
+    for (int e = (int)b + 1; e <= (int)e_end; e++) {
         int t = S.etype[sec_of(e)], nv = kElementNVx[t];
         double gc[3] = {0, 0, 0}, rc[3] = {0, 0, 0}, sum_vol = 0;
         for (int q = 1; q <= nv; q++) {
@@ -259,9 +275,10 @@ int build(cfdl_setup &S) {
         for (int q = 0; q < 3; q++) rc[q] = rc[q] / sum_vol;
         S.xc[e - 1] = rc[0]; S.yc[e - 1] = rc[1]; S.zc[e - 1] = rc[2];
         S.vol[e - 1] = sum_vol;
-        if (!(sum_vol > 1e-20)) return CFDL_ERR_MESH;  // the reference only warns here
+        if (!(sum_vol > 1e-20)) flat = 1;  // the reference only warns here
     }
-    return CFDL_OK;
+    });
+    return flat ? CFDL_ERR_MESH : CFDL_OK;
 }
 
 }  // namespace

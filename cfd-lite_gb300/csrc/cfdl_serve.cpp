@@ -132,9 +132,7 @@ int prepare(const cfdl_server_config &s, Request &q) {
 }
 
 void prep_loop(cfdl_server *S) {
-    // the preparation threads share the host cores for their parallel loops
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    host_threads() = std::max(1, hw / S->cfg.prep_threads);
     for (;;) {
         std::unique_ptr<Request> q;
         {
@@ -144,6 +142,9 @@ void prep_loop(cfdl_server *S) {
             q = std::move(S->pending.front());
             S->pending.pop_front();
             S->preparing++;
+            // the requests being prepared share the host cores for their
+            // parallel loops: a lone request gets them all
+            host_threads() = std::max(1, hw / S->preparing);
         }
         q->status = prepare(S->cfg, *q);
         std::lock_guard<std::mutex> lk(S->mu);

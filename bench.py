@@ -32,6 +32,8 @@ PKG = os.path.join(ROOT, "cfd-lite_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "SIMPLE cell-iters/s"
+DTYPES = {0: "f64", 1: "f64+f32 (mixed pressure solve)",
+          2: "f64+f32 (mixed pressure solve, FP32 momentum corrections)"}
 UNIT = "cell-iters/s"
 
 
@@ -46,7 +48,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tet", action="store_true")
     ap.add_argument("--mode", type=int, default=0, help="0: reference stopping rule, 1: tight")
-    ap.add_argument("--precision", type=int, default=0, help="0: FP64, 1: mixed pressure solve")
+    ap.add_argument("--precision", type=int, default=0, help="0: FP64, 1: mixed pressure solve, "
+                    "2: also FP32 momentum corrections")
     ap.add_argument("--precond", type=int, default=1, help="pressure preconditioner: 0 Jacobi, 1 AMG")
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of the graph")
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
@@ -56,7 +59,8 @@ def parse():
                     help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
     ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
-    ap.add_argument("--forms", default="0,1", help="batched/served: precisions to run (0 FP64, 1 mixed)")
+    ap.add_argument("--forms", default="0,1,2", help="batched/served: precisions to run (0 FP64, 1 mixed pressure, "
+                    "2 mixed pressure + FP32 momentum corrections)")
     ap.add_argument("--rates", default="5,200", help="served: request rates (req/s)")
     ap.add_argument("--requests", type=int, default=16, help="served: requests per rate")
     ap.add_argument("--max-outer", type=int, default=1000, help="served: outer-iteration cap per request")
@@ -247,7 +251,7 @@ def run_ours(a, dist):
         ns, ws = (C.c_int * 16)(), (C.c_int * 16)()
         cfdl._check(cfdl.lib().cfdl_amg_info(g._h, 15, C.byref(nl), ns, ws), "amg_info")
         levels = [(ns[l], ws[l]) for l in range(nl.value + 1)]
-        val = 4 if (a.precision == 1 and (dominant.startswith("k_v_") or dominant.startswith("k_mx_"))) else 8
+        val = 4 if (a.precision >= 1 and (dominant.startswith("k_v_") or dominant.startswith("k_mx_"))) else 8
         nbytes = amg_kernel_bytes(dominant, levels, val)
     achieved = nbytes / avg_s / 1e9 if nbytes else None
     traffic = ncu_traffic(dominant, a.n)
@@ -303,7 +307,7 @@ def run_ours(a, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if a.precision == 0 else "f64+f32 (mixed pressure solve)",
+        "dtype": DTYPES[a.precision],
         "data": "synthetic (seeded jittered unit-cube hex mesh; the reference's sample mesh is unavailable)",
         "config": {"workload": "lid-driven cavity %d^3 %s, jitter %.2f, Re=100 (rho=1, mu=0.01), SIMPLE "
                                "alpha_u=0.7 alpha_p=0.3, FP64" % (a.n, "tet-split" if a.tet else "hex", a.jitter),
@@ -457,7 +461,7 @@ def run_batched(a, dist):
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.outer,
             "warmup": a.warmup, "ms_per_step": ms / a.outer, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == 0 else "f64+f32 (mixed pressure solve)",
+            "vs_baseline": None, "dtype": DTYPES[prec],
             "data": "synthetic (seeded cavity meshes)",
             "config": {"workload": "batched: %d lid-driven cavity cases in one run, N~U{%d..%d} (seed %d), half "
                                    "tet-split, Re log-U[10,1000], %d SIMPLE iterations each" %
@@ -475,13 +479,15 @@ def run_batched(a, dist):
         if clk:
             out["clocks"] = clk
         lines.append(out)
-    if 0 in fields and 1 in fields:
-        worst = {}
-        for f in ("u", "v", "w", "p"):
-            worst[f] = max(float(np.linalg.norm(m[f] - d[f]) / max(np.linalg.norm(d[f]), 1e-300))
-                           for m, d in zip(fields[1], fields[0]))
-        for out in lines:
-            out["mixed_vs_fp64_rel_l2_max_over_cases"] = worst
+    if 0 in fields:
+        for out, prec in zip(lines, forms):
+            if prec == 0:
+                continue
+            worst = {}
+            for f in ("u", "v", "w", "p"):
+                worst[f] = max(float(np.linalg.norm(m[f] - d[f]) / max(np.linalg.norm(d[f]), 1e-300))
+                               for m, d in zip(fields[prec], fields[0]))
+            out["vs_fp64_rel_l2_max_over_cases_after_run"] = worst
     return lines
 
 
@@ -609,7 +615,7 @@ def run_served(a, dist):
             out = {
                 "metric": "served cavity requests: p50/p99 latency (s)", "value": float(np.percentile(lat, 99)),
                 "unit": "s (p99 latency)", "higher_is_better": False, "n_gpus": dist.world,
-                "dtype": "f64" if prec == 0 else "f64+f32 (mixed pressure solve)",
+                "dtype": DTYPES[prec],
                 "data": "synthetic (seeded Poisson request stream)",
                 "config": {"workload": "served: Poisson stream at %.0f req/s, %d requests, N~U{%d..%d}, hex or "
                                        "tet-split, Re log-U[10,1000], stop at mass ratio %.0e or %d iterations; "

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     if (i >= t.last || C.sc->halted) return;
     const double ap = C.ap[i];
     C.rap[i] = kOmega / ap;
-    if (C.precision == 1) {
+    if (C.precision >= 1) {
         C.fdiag[i] = (float)ap;
         C.frap[i] = (float)(kOmega / ap);
         for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = (float)C.anb[k * C.ne + i];
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restric
     }
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         C.cinv[e] = M[e];
-        if (C.precision == 1) C.cinv32[e] = (float)M[e];
+        if (C.precision >= 1) C.cinv32[e] = (float)M[e];
     }
 }
 
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
     if (I >= t.last || C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
     const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
-    const bool mixed = C.precision == 1;
+    const bool mixed = C.precision >= 1;
     const int n = L.n;
     double dsum = 0.0;
     for (int k = 0; k < L.W; k++) {
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
     if (C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
     const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
-    const bool mixed = C.precision == 1;
+    const bool mixed = C.precision >= 1;
     const int n = L.n;
     double dsum = 0.0;
     if (ok)

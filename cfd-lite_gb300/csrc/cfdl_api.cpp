@@ -22,7 +22,8 @@ int validate_config(const cfdl_config *c) {
     if (!c) return CFDL_ERR_INVALID;
     if (!(c->rho > 0) || !(c->mu >= 0) || !(c->dt > 0) || !(c->alpha_u > 0 && c->alpha_u <= 1) ||
         !(c->alpha_p > 0 && c->alpha_p <= 1) || c->nit < 0 || c->tight_maxit < 0 ||
-        (c->solve_mode != 0 && c->solve_mode != 1) || (c->precision != 0 && c->precision != 1) ||
+        (c->solve_mode != 0 && c->solve_mode != 1) || c->precision < 0 || c->precision > 2 ||
+        (c->precision == 2 && c->solve_mode != 0) ||
         !(c->rtol_u > 0) || !(c->rtol_p > 0) || !(c->tight_rtol > 0) || (c->precond != 0 && c->precond != 1))
         return CFDL_ERR_INVALID;
     return CFDL_OK;

@@ -19,6 +19,7 @@ namespace cfdl {
 
 void mom_init(cfdl_ctx *ctx);
 void mom_iter(cfdl_ctx *ctx);
+void mom_finish(cfdl_ctx *ctx);
 void pcj_init(cfdl_ctx *ctx);
 void pcj_iter(cfdl_ctx *ctx);
 void apc_init(cfdl_ctx *ctx);
@@ -188,7 +189,7 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
     });
     if (st) return st;
     // gradients, Rhie-Chow fluxes, pressure assembly, pressure-solve start
-    if ((st = b.segment(G, prev, [&] { launch_grad(ctx, 4); }, &k))) return st;
+    if ((st = b.segment(G, prev, [&] { mom_finish(ctx); launch_grad(ctx, 4); }, &k))) return st;
     *static_k += k;
     if (ctx->ev_mom && mark) {
         // u, v, w and their gradients are final here (cfdl_solve_uvwp_host
@@ -201,7 +202,7 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
     if ((st = b.segment(G, prev, [&] {
              launch_calc_mip(ctx, 1);
              launch_coef_p(ctx);
-             if (cfg.precision == 1) mx_init(ctx);
+             if (cfg.precision >= 1) mx_init(ctx);
              else if (cfg.precond == 1) apc_init(ctx);
              else pcj_init(ctx);
              b.setone(hp);

@@ -53,7 +53,7 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
 // The row's slot indices and coefficients are loaded once for the three
 // components; sums run in slot order.
 template <int W>
-__device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, double (&v)[6]) {
+__device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, double (&v)[6], bool m32) {
     int nb[W];
     double a[W];
     bool in[W], bd[W];
@@ -67,6 +67,12 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
     }
     const double api = C.ap[i];
     C.rap[i] = 1.0 / api;                   // the Jacobi scaling of the whole solve, divided once
+    if (m32) {                              // the operator in FP32 for the correction solve
+        C.fdiag[i] = (float)api;
+        C.frap[i] = (float)(1.0 / api);
+#pragma unroll
+        for (int k = 0; k < W; k++) C.fanb[k * ne + i] = (float)a[k];
+    }
 #pragma unroll
     for (int q = 0; q < 3; q++) {
         const double *__restrict__ phi = comp_field(C, q);
@@ -82,8 +88,16 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
         }
         const double r = bb - s;
         // p and v need no clearing: the first iteration sets p = r (k_mom_p)
-        C.kr[q * ne + i] = r;
-        C.krh[q * ne + i] = r;
+        if (m32) {
+            // FP32 correction solve A d = r from d = 0 (first halves of kr, krh; d after kt's)
+            const float rf = (float)r;
+            ((float *)C.kr)[q * ne + i] = rf;
+            ((float *)C.krh)[q * ne + i] = rf;
+            ((float *)C.kt)[3 * (size_t)ne + q * ne + i] = 0.f;
+        } else {
+            C.kr[q * ne + i] = r;
+            C.krh[q * ne + i] = r;
+        }
         v[q] += bb * bb;
         v[3 + q] += r * r;
     }
@@ -93,9 +107,10 @@ __global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
-    if (C.W == 6) { FOR_CELLS(t) mom_init_row<6>(C, i, ne, v); }
-    else if (C.W == 4) { FOR_CELLS(t) mom_init_row<4>(C, i, ne, v); }
-    else { FOR_CELLS(t) mom_init_row<kMaxW>(C, i, ne, v); }
+    const bool m32 = C.precision == 2;
+    if (C.W == 6) { FOR_CELLS(t) mom_init_row<6>(C, i, ne, v, m32); }
+    else if (C.W == 4) { FOR_CELLS(t) mom_init_row<4>(C, i, ne, v, m32); }
+    else { FOR_CELLS(t) mom_init_row<kMaxW>(C, i, ne, v, m32); }
     block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M1], cnt[t.c])) {
         __shared__ double s[6];
@@ -116,158 +131,184 @@ __global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict
     }
 }
 
+// The BiCGStab vectors and operator of a case's momentum solve, [3][ne] per
+// vector.  FP64: the solve updates u, v, w in place.  FP32 (precision 2): the
+// solve finds the correction d of A d = r (r the FP64 residual of k_mom_init)
+// in single precision, in the first halves of the FP64 vectors' storage, and
+// k_mom_apply adds it to u, v, w in FP64.
+template <class T> struct MomVec {
+    T *r, *rh, *p, *ph, *v, *s, *sh, *t;
+    T *x[3];
+    const T *a, *ap, *rap;
+};
+template <class T> __device__ __forceinline__ MomVec<T> mom_vec(const CaseDev &C);
+template <> __device__ __forceinline__ MomVec<double> mom_vec<double>(const CaseDev &C) {
+    return {C.kr, C.krh, C.kp, C.kph, C.kv, C.ks, C.ksh, C.kt, {C.u, C.v, C.w}, C.anb, C.ap, C.rap};
+}
+template <> __device__ __forceinline__ MomVec<float> mom_vec<float>(const CaseDev &C) {
+    const int ne = C.ne;
+    float *xf = (float *)C.kt + 3 * (size_t)ne;   // second half of kt's storage
+    return {(float *)C.kr, (float *)C.krh, (float *)C.kp, (float *)C.kph, (float *)C.kv, (float *)C.ks,
+            (float *)C.ksh, (float *)C.kt, {xf, xf + ne, xf + 2 * (size_t)ne}, C.fanb, C.fdiag, C.frap};
+}
+
 // p = r + beta (p - omega v); ph = p / ap
+template <class T>
 __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
     if (!any_active(S)) return;
+    const MomVec<T> M = mom_vec<T>(C);
     // the iteration's scalars, read once
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
     const bool first[3] = {S->iters[0] == 0, S->iters[1] == 0, S->iters[2] == 0};
-    const double be[3] = {S->beta[0], S->beta[1], S->beta[2]}, om[3] = {S->omega[0], S->omega[1], S->omega[2]};
-    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ rapv = C.rap;
-    double *__restrict__ kp = C.kp, *__restrict__ kph = C.kph;
+    const T be[3] = {(T)S->beta[0], (T)S->beta[1], (T)S->beta[2]}, om[3] = {(T)S->omega[0], (T)S->omega[1], (T)S->omega[2]};
     FOR_CELLS(t) {
-        const double rap = rapv[i];
+        const T rap = M.rap[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
-            const double pn = first[q] ? kr[j] : kr[j] + be[q] * (kp[j] - om[q] * kv[j]);
-            kp[j] = pn;
-            kph[j] = pn * rap;
+            const T pn = first[q] ? M.r[j] : M.r[j] + be[q] * (M.p[j] - om[q] * M.v[j]);
+            M.p[j] = pn;
+            M.ph[j] = pn * rap;
         }
     }
 }
 
 // v = A ph; alpha = rho / (rh, v)
+template <class T>
 __global__ void __launch_bounds__(kTile, 4) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
-                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
-    double v[3] = {0, 0, 0};
+    const MomVec<T> M = mom_vec<T>(C);
+    T v[3] = {0, 0, 0};
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
     FOR_CELLS(t) {
-        double y[3];   // one pass over the row for the three components
-        ell_row<3, double>(C.hf_nb, C.anb, C.ap[i], C.kph, ne, ne, C.W, i, y);
+        T y[3];   // one pass over the row for the three components
+        ell_row<3, T>(C.hf_nb, M.a, M.ap[i], M.ph, ne, ne, C.W, i, y);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
-            C.kv[q * ne + i] = y[q];
-            v[q] += C.krh[q * ne + i] * y[q];
+            M.v[q * ne + i] = y[q];
+            v[q] += M.rh[q * ne + i] * y[q];
         }
     }
-    block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<3, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M2], cnt[t.c])) {
-        __shared__ double s[3];
-        sum_partials<3>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[3];
+        sum_partials<3, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
             for (int q = 0; q < 3; q++) {
                 if (!S->active[q]) continue;
-                const double a = S->rho[q] / s[q];
-                if (s[q] == 0.0 || !isfinite(a)) { S->active[q] = 0; S->status[q] = isfinite(a) || s[q] == 0.0 ? S->status[q] : CFDL_ERR_NONFINITE; continue; }
+                const double sq = (double)s[q];
+                const double a = S->rho[q] / sq;
+                if (sq == 0.0 || !isfinite(a)) { S->active[q] = 0; S->status[q] = isfinite(a) || sq == 0.0 ? S->status[q] : CFDL_ERR_NONFINITE; continue; }
                 S->alpha[q] = a;
             }
     }
 }
 
 // s = r - alpha v; sh = s / ap; early exit when ||s|| <= tol
+template <class T>
 __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
-                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
-    double v[3] = {0, 0, 0};
+    const MomVec<T> M = mom_vec<T>(C);
+    T v[3] = {0, 0, 0};
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    const double al[3] = {S->alpha[0], S->alpha[1], S->alpha[2]};
-    const double *__restrict__ kr = C.kr, *__restrict__ kv = C.kv, *__restrict__ rapv = C.rap;
-    double *__restrict__ ks = C.ks, *__restrict__ ksh = C.ksh;
+    const T al[3] = {(T)S->alpha[0], (T)S->alpha[1], (T)S->alpha[2]};
     FOR_CELLS(t) {
-        const double rap = rapv[i];
+        const T rap = M.rap[i];
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
-            const double sv = kr[j] - al[q] * kv[j];
-            ks[j] = sv;
-            ksh[j] = sv * rap;
+            const T sv = M.r[j] - al[q] * M.v[j];
+            M.s[j] = sv;
+            M.sh[j] = sv * rap;
             v[q] += sv * sv;
         }
     }
-    block_reduce<3>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<3, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M3], cnt[t.c])) {
-        __shared__ double s[3];
-        sum_partials<3>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[3];
+        sum_partials<3, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
             for (int q = 0; q < 3; q++) {
                 if (!S->active[q]) continue;
-                S->half[q] = sqrt(s[q]) <= S->tol[q];
+                S->half[q] = sqrt((double)s[q]) <= S->tol[q];
             }
     }
 }
 
 // t = A sh; omega = (t,s)/(t,t)
+template <class T>
 __global__ void __launch_bounds__(kTile, 4) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
-                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
-    double v[6] = {0, 0, 0, 0, 0, 0};
+    const MomVec<T> M = mom_vec<T>(C);
+    T v[6] = {0, 0, 0, 0, 0, 0};
     const int act[3] = {S->active[0] && !S->half[0], S->active[1] && !S->half[1], S->active[2] && !S->half[2]};
     FOR_CELLS(t) {
-        double y[3];
-        ell_row<3, double>(C.hf_nb, C.anb, C.ap[i], C.ksh, ne, ne, C.W, i, y);
+        T y[3];
+        ell_row<3, T>(C.hf_nb, M.a, M.ap[i], M.sh, ne, ne, C.W, i, y);
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
-            C.kt[j] = y[q];
-            v[q] += y[q] * C.ks[j];
+            M.t[j] = y[q];
+            v[q] += y[q] * M.s[j];
             v[3 + q] += y[q] * y[q];
         }
     }
-    block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<6, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M4], cnt[t.c])) {
-        __shared__ double s[6];
-        sum_partials<6>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[6];
+        sum_partials<6, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
             for (int q = 0; q < 3; q++) {
                 if (!S->active[q]) continue;
-                S->omega[q] = S->half[q] ? 0.0 : (s[3 + q] > 0.0 ? s[q] / s[3 + q] : 0.0);
+                const double ts = (double)s[q], tt = (double)s[3 + q];
+                S->omega[q] = S->half[q] ? 0.0 : (tt > 0.0 ? ts / tt : 0.0);
             }
     }
 }
 
 // x += alpha ph + omega sh; r = s - omega t; rho' = (rh, r); beta
+template <class T>
 __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
-                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
     if (!any_active(S)) return;
-    double v[6] = {0, 0, 0, 0, 0, 0};
+    const MomVec<T> M = mom_vec<T>(C);
+    T v[6] = {0, 0, 0, 0, 0, 0};
     const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    const double al[3] = {S->alpha[0], S->alpha[1], S->alpha[2]}, om[3] = {S->omega[0], S->omega[1], S->omega[2]};
-    const double *__restrict__ kph = C.kph, *__restrict__ ksh = C.ksh, *__restrict__ ks = C.ks, *__restrict__ kt = C.kt,
-                 *__restrict__ krh = C.krh;
-    double *__restrict__ kr = C.kr;
+    const T al[3] = {(T)S->alpha[0], (T)S->alpha[1], (T)S->alpha[2]}, om[3] = {(T)S->omega[0], (T)S->omega[1], (T)S->omega[2]};
     FOR_CELLS(t) {
 #pragma unroll
         for (int q = 0; q < 3; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
-            double *__restrict__ x = comp_field(C, q);
-            x[i] = x[i] + al[q] * kph[j] + om[q] * ksh[j];
-            const double r = om[q] == 0.0 ? ks[j] : ks[j] - om[q] * kt[j];
-            kr[j] = r;
+            T *__restrict__ x = M.x[q];
+            x[i] = x[i] + al[q] * M.ph[j] + om[q] * M.sh[j];
+            const T r = om[q] == (T)0 ? M.s[j] : M.s[j] - om[q] * M.t[j];
+            M.r[j] = r;
             v[q] += r * r;
-            v[3 + q] += krh[j] * r;
+            v[3 + q] += M.rh[j] * r;
         }
     }
-    block_reduce<6>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<6, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M5], cnt[t.c])) {
-        __shared__ double s[6];
-        sum_partials<6>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[6];
+        sum_partials<6, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0) {
             const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
             for (int q = 0; q < 3; q++) {
                 if (!S->active[q]) continue;
-                const double rn = sqrt(s[q]), rho_new = s[3 + q];
+                const double rn = sqrt((double)s[q]), rho_new = (double)s[3 + q];
                 S->rnorm[q] = rn;
                 S->iters[q] += 1;
                 const double om = S->omega[q];
@@ -280,6 +321,17 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
                 S->active[q] = act;
             }
         }
+    }
+}
+
+// precision 2: u, v, w += the FP32 correction of the momentum solve
+__global__ void __launch_bounds__(kTile) k_mom_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_HEAD
+    const MomVec<float> M = mom_vec<float>(C);
+    double *xs[3] = {C.u, C.v, C.w};
+    FOR_CELLS(t) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) xs[q][i] = xs[q][i] + (double)M.x[q][i];
     }
 }
 
@@ -437,12 +489,27 @@ static int max_cap(cfdl_ctx *ctx) {
 
 void mom_init(cfdl_ctx *ctx) { CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED); }
 
+#define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
+
 void mom_iter(cfdl_ctx *ctx) {
-    CFDL_LAUNCH("k_mom_p", k_mom_p, cellsv);
-    CFDL_LAUNCH("k_mom_v", k_mom_v, cellsv, RED);
-    CFDL_LAUNCH("k_mom_s", k_mom_s, cellsv, RED);
-    CFDL_LAUNCH("k_mom_t", k_mom_t, cellsv, RED);
-    CFDL_LAUNCH("k_mom_x", k_mom_x, cellsv, RED);
+    if (ctx->cases[0]->cfg.precision == 2) {
+        CFDL_LAUNCH("k_mom_p", k_mom_p<float>, cellsv);
+        CFDL_LAUNCH("k_mom_v", k_mom_v<float>, cellsv, RED32);
+        CFDL_LAUNCH("k_mom_s", k_mom_s<float>, cellsv, RED32);
+        CFDL_LAUNCH("k_mom_t", k_mom_t<float>, cellsv, RED32);
+        CFDL_LAUNCH("k_mom_x", k_mom_x<float>, cellsv, RED32);
+        return;
+    }
+    CFDL_LAUNCH("k_mom_p", k_mom_p<double>, cellsv);
+    CFDL_LAUNCH("k_mom_v", k_mom_v<double>, cellsv, RED);
+    CFDL_LAUNCH("k_mom_s", k_mom_s<double>, cellsv, RED);
+    CFDL_LAUNCH("k_mom_t", k_mom_t<double>, cellsv, RED);
+    CFDL_LAUNCH("k_mom_x", k_mom_x<double>, cellsv, RED);
+}
+
+// the end of the momentum solve: precision 2 applies its FP32 correction
+void mom_finish(cfdl_ctx *ctx) {
+    if (ctx->cases[0]->cfg.precision == 2) CFDL_LAUNCH("k_mom_apply", k_mom_apply, cellsv);
 }
 
 void pcj_init(cfdl_ctx *ctx) {
@@ -469,6 +536,7 @@ int solve_momentum(cfdl_ctx *ctx) {
         if (a == 0) break;
     }
     ctx->last_iters_m = maxit;
+    mom_finish(ctx);
     return cuda_status(cudaGetLastError());
 }
 
@@ -476,7 +544,7 @@ void launch_pc_mean(cfdl_ctx *ctx) { CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv,
 
 int solve_pressure(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    if (ctx->cases[0]->cfg.precision == 1) return solve_pressure_mixed(ctx);
+    if (ctx->cases[0]->cfg.precision >= 1) return solve_pressure_mixed(ctx);
     if (ctx->cases[0]->cfg.precond == 1) return solve_pressure_amg(ctx);
     pcj_init(ctx);
     const int cap = max_cap(ctx);

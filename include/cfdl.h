@@ -115,7 +115,10 @@ typedef struct cfdl_config {
     double tight_rtol;     /* mode 1 tolerance                                           */
     int    tight_maxit;    /* mode 1 iteration cap                                       */
     int    precision;      /* 0: FP64 throughout; 1: mixed pressure solve (FP32 SpMV,
-                              preconditioner and inner CG, FP64 residual/refinement)    */
+                              preconditioner and inner CG, FP64 residual/refinement);
+                              2: as 1, and each momentum solve finds its correction
+                              to the FP64 residual with FP32 BiCGStab (solve_mode 0
+                              only: the reference's 10x drop, no refinement needed)   */
     int    precond;        /* pressure preconditioner: 0 Jacobi, 1 aggregation AMG      */
 } cfdl_config;
 

@@ -48,7 +48,7 @@ def alone(spec, n_outer, precision=0, ncoef=0, graph=True):
     return out
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_batch_equals_alone_bitwise(need_gpu, precision):
     setups = [case_setup(*s[:4]) for s in SPECS]
     cfgs = [cavity_cfg(s[4], precision) for s in SPECS]
@@ -160,6 +160,8 @@ def test_form_mismatch_rejected(need_gpu):
     with pytest.raises(cfdl.CfdlError):
         b.remove(0)          # the last case stays
     b.close()
+    with pytest.raises(cfdl.CfdlError):   # FP32 momentum corrections need the 10x-drop stopping rule
+        cfdl.Solver(s, cavity_cfg(100.0, 2, solve_mode=1))
 
 
 def test_nonfinite_case_stops_alone(need_gpu):

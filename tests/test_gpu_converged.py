@@ -34,7 +34,7 @@ def test_converged_fields_match_oracle(need_gpu, n, tet, re):
     o.run(outer, ncoef=0)
     ref = {f: o.get(f)[: s.ne] for f in ("u", "v", "w", "p")}
     o.close()
-    for precision in (0, 1):
+    for precision in (0, 1, 2):
         g = cfdl.Solver(s, cfdl.steady(mu=1.0 / re, precision=precision))
         g.set_run(outer)
         assert g.run(outer) == 0

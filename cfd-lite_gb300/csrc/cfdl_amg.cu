@@ -18,6 +18,7 @@
 // at every pressure solve from the current coefficients (A_c = P^T A P).
 #include "cfdl_amg.h"
 #include "cfdl_device.cuh"
+#include "cfdl_par.h"
 #include <algorithm>
 #include <new>
 
@@ -586,11 +587,13 @@ void amg_strength(int ne, int W, const int *nb_in, const int *fc, const double *
                   std::vector<double> &strength) {
     nb.assign(nb_in, nb_in + (size_t)W * ne);
     strength.assign((size_t)W * ne, 0.0);
-    for (size_t s = 0; s < nb.size(); s++) {
-        if (nb[s] < 0 || nb[s] >= ne) { nb[s] = -1; continue; }
-        int f = fc[s] >= 0 ? fc[s] : ~fc[s];
-        strength[s] = std::fabs(adn[f]);
-    }
+    parallel_for((long)nb.size(), [&](long b, long e) {
+        for (long s = b; s < e; s++) {
+            if (nb[s] < 0 || nb[s] >= ne) { nb[s] = -1; continue; }
+            const int f = fc[s] >= 0 ? fc[s] : ~fc[s];
+            strength[s] = std::fabs(adn[f]);
+        }
+    });
 }
 
 // Build and upload the hierarchy of one case (mesh-only, once).

@@ -78,11 +78,12 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
     g.n = fine.n; g.W = fine.W;
     g.nb.assign((size_t)g.W * g.n, -1);
     g.w.assign((size_t)g.W * g.n, 0.0);
-    for (int k = 0; k < g.W; k++)
-        for (int i = 0; i < g.n; i++) {
-            int j = fine.nb[(size_t)k * g.n + i];
-            if (j >= 0 && j < g.n) { g.nb[(size_t)k * g.n + i] = j; g.w[(size_t)k * g.n + i] = fine.strength[(size_t)k * g.n + i]; }
+    parallel_for((long)g.W * g.n, [&](long b, long e) {
+        for (long s = b; s < e; s++) {
+            const int j = fine.nb[s];
+            if (j >= 0 && j < g.n) { g.nb[s] = j; g.w[s] = fine.strength[s]; }
         }
+    });
     while (g.n > kAmgCoarsest && (int)H.levels.size() < kAmgMaxLevels) {
         std::vector<int> agg;
         int nc = aggregate(g, agg);
@@ -99,56 +100,93 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
             std::vector<int> fill(L.mem_ptr.begin(), L.mem_ptr.end() - 1);
             for (int i = 0; i < g.n; i++) L.mem[fill[agg[i]]++] = i;
         }
-        // coarse neighbours in first-met order, and the fine slots feeding each
-        std::vector<std::vector<int>> cnb(nc);
-        std::vector<std::vector<std::vector<int>>> src(nc);
-        std::vector<std::vector<double>> cw(nc);
+        // Coarse neighbours of each aggregate in first-met order (members in
+        // increasing order, slots in increasing k), and the fine slots feeding
+        // each coarse slot, built in two parallel passes over flat arrays:
+        // pass 1 finds each aggregate's neighbours, slot counts and strength
+        // sums (in a region sized by its members' slots), pass 2 files the
+        // slots once the coarse slot offsets are known.
+        std::vector<long> cap(nc + 1, 0);
+        for (int c = 0; c < nc; c++) cap[c + 1] = cap[c] + (long)(L.mem_ptr[c + 1] - L.mem_ptr[c]) * g.W;
+        std::vector<int> nbr(cap[nc]), cntq(cap[nc]), ncnb(nc);
+        std::vector<double> wq(cap[nc]);
         parallel_for(nc, [&](long cb, long ce) {
-        for (int c = (int)cb; c < (int)ce; c++) {
-            for (int m = L.mem_ptr[c]; m < L.mem_ptr[c + 1]; m++) {
-                int i = L.mem[m];
-                for (int k = 0; k < g.W; k++) {
-                    int j = g.nb[(size_t)k * g.n + i];
-                    if (j < 0) continue;
-                    int slot = k * g.n + i;
-                    int cj = agg[j];
-                    if (cj == c) continue;           // internal coupling: not a coarse slot
-                    size_t q = 0;
-                    while (q < cnb[c].size() && cnb[c][q] != cj) q++;
-                    if (q == cnb[c].size()) { cnb[c].push_back(cj); src[c].emplace_back(); cw[c].push_back(0.0); }
-                    src[c][q].push_back(slot);
-                    cw[c][q] += g.w[(size_t)slot];
+            for (int c = (int)cb; c < (int)ce; c++) {
+                int *nb_c = &nbr[cap[c]], *cn_c = &cntq[cap[c]];
+                double *w_c = &wq[cap[c]];
+                int nq = 0;
+                for (int m = L.mem_ptr[c]; m < L.mem_ptr[c + 1]; m++) {
+                    const int i = L.mem[m];
+                    for (int k = 0; k < g.W; k++) {
+                        const int j = g.nb[(size_t)k * g.n + i];
+                        if (j < 0) continue;
+                        const int cj = agg[j];
+                        if (cj == c) continue;           // internal coupling: not a coarse slot
+                        int q = 0;
+                        while (q < nq && nb_c[q] != cj) q++;
+                        if (q == nq) { nb_c[q] = cj; cn_c[q] = 0; w_c[q] = 0.0; nq++; }
+                        cn_c[q]++;
+                        w_c[q] += g.w[(size_t)k * g.n + i];
+                    }
                 }
+                ncnb[c] = nq;
             }
-        }
         }, 2048);
         int Wc = 1;
-        for (int c = 0; c < nc; c++) Wc = std::max<int>(Wc, (int)cnb[c].size());
+        for (int c = 0; c < nc; c++) Wc = std::max(Wc, ncnb[c]);
         L.W = Wc;
         L.nb.assign((size_t)Wc * nc, -1);
         L.g_ptr.assign((size_t)Wc * nc + 1, 0);
-        for (int k = 0; k < Wc; k++)
-            for (int c = 0; c < nc; c++) {
-                size_t s = (size_t)k * nc + c;
-                int cnt = k < (int)cnb[c].size() ? (int)src[c][k].size() : 0;
-                L.g_ptr[s + 1] = L.g_ptr[s] + cnt;
-                if (k < (int)cnb[c].size()) L.nb[s] = cnb[c][k];
-            }
-        L.g_src.assign(L.g_ptr.back(), 0);
-        for (int k = 0; k < Wc; k++)
-            for (int c = 0; c < nc; c++)
-                if (k < (int)cnb[c].size()) {
-                    size_t s = (size_t)k * nc + c;
-                    std::copy(src[c][k].begin(), src[c][k].end(), L.g_src.begin() + L.g_ptr[s]);
+        // slot-major offsets: each slot plane k scanned on its own, then the
+        // planes' totals carried over in order
+        std::vector<long> plane_total(Wc + 1, 0);
+        parallel_for(Wc, [&](long kb, long ke) {
+            for (int k = (int)kb; k < (int)ke; k++) {
+                long run = 0;
+                for (int c = 0; c < nc; c++) {
+                    const size_t sl = (size_t)k * nc + c;
+                    const bool has = k < ncnb[c];
+                    run += has ? cntq[cap[c] + k] : 0;
+                    L.g_ptr[sl + 1] = (int)run;
+                    if (has) L.nb[sl] = nbr[cap[c] + k];
                 }
+                plane_total[k + 1] = run;
+            }
+        }, 1);
+        for (int k = 0; k < Wc; k++) plane_total[k + 1] += plane_total[k];
+        parallel_for(Wc, [&](long kb, long ke) {
+            for (int k = (int)kb; k < (int)ke; k++)
+                for (int c = 0; c < nc; c++) L.g_ptr[(size_t)k * nc + c + 1] += (int)plane_total[k];
+        }, 1);
+        L.g_src.assign(L.g_ptr.back(), 0);
+        parallel_for(nc, [&](long cb, long ce) {
+            std::vector<int> fill;
+            for (int c = (int)cb; c < (int)ce; c++) {
+                const int *nb_c = &nbr[cap[c]], nq = ncnb[c];
+                fill.assign(nq, 0);
+                for (int m = L.mem_ptr[c]; m < L.mem_ptr[c + 1]; m++) {
+                    const int i = L.mem[m];
+                    for (int k = 0; k < g.W; k++) {
+                        const int j = g.nb[(size_t)k * g.n + i];
+                        if (j < 0) continue;
+                        const int cj = agg[j];
+                        if (cj == c) continue;
+                        int q = 0;
+                        while (nb_c[q] != cj) q++;
+                        L.g_src[L.g_ptr[(size_t)q * nc + c] + fill[q]++] = k * g.n + i;
+                    }
+                }
+            }
+        }, 2048);
         // next graph
         Graph ng;
         ng.n = nc; ng.W = Wc;
         ng.nb = L.nb;
         ng.w.assign((size_t)Wc * nc, 0.0);
-        for (int k = 0; k < Wc; k++)
-            for (int c = 0; c < nc; c++)
-                if (k < (int)cnb[c].size()) ng.w[(size_t)k * nc + c] = cw[c][k];
+        parallel_for(nc, [&](long cb, long ce) {
+            for (int c = (int)cb; c < (int)ce; c++)
+                for (int k = 0; k < ncnb[c]; k++) ng.w[(size_t)k * nc + c] = wq[cap[c] + k];
+        });
         H.levels.push_back(std::move(L));
         g = std::move(ng);
     }

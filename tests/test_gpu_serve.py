@@ -73,7 +73,8 @@ def test_admission_respects_the_budget(need_gpu):
     res = {r.id: r for r in srv.poll(max_results=8)}
     assert res[a].status == 0 and res[b].status == 0
     assert res[a].outer_done == 20 and res[b].outer_done == 20
-    assert res[b].t_admit >= res[a].t_done
+    # one resident at a time, whichever was prepared first
+    assert res[b].t_admit >= res[a].t_done or res[a].t_admit >= res[b].t_done
     srv.close()
 
 

@@ -468,14 +468,14 @@ class Batch(Solver):
 
     def __init__(self, setups, configs, u_lids=None):
         setups = list(setups)
-        configs = list(configs)
-        if not setups or len(setups) != len(configs):
+        cfg_list = list(configs)
+        if not setups or len(setups) != len(cfg_list):
             raise ValueError("one config per setup")
         u_lids = list(u_lids) if u_lids is not None else [1.0] * len(setups)
         self.setup = setups[0]
-        self.config = configs[0]
+        self.config = cfg_list[0]
         meshes = (Mesh * len(setups))(*[s.mesh(u) for s, u in zip(setups, u_lids)])
-        cfgs = (Config * len(configs))(*configs)
+        cfgs = (Config * len(cfg_list))(*cfg_list)
         self._h = C.c_void_p()
         _check(lib().cfdl_batch_create(len(setups), C.cast(meshes, C.c_void_p), C.cast(cfgs, C.c_void_p),
                                        C.byref(self._h)), "batch_create")

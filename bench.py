@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served", "pressure"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served", "pressure", "setup"],
                     help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
     ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
@@ -569,6 +569,41 @@ def run_pressure(a, dist):
     return out
 
 
+# ------------------------------------------------------------ mesh set-up
+def run_setup(a, dist):
+    """Mesh set-up (face matching, numbering, geometry) of the largest served
+    mesh, on the host builder and on the GPU; the arrays are compared."""
+    import numpy as np
+    import cfdl
+
+    cfdl.select_device(dist.local)
+    n = a.n if a.n != 128 else 96
+    tet = True if not a.tet else a.tet
+    zone = cfdl.Zone(n, tet, 0.1, seed=a.seed)
+    cfdl.Setup(cfdl.Zone(4, tet), device=True)          # warm: CUDA context and module load
+    times = {}
+    setups = {}
+    for dev in (False, True):
+        best = None
+        for _ in range(3):
+            t0 = time.perf_counter()
+            s = cfdl.Setup(zone, device=dev)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        times[dev] = best
+        setups[dev] = s
+    same = all(np.array_equal(setups[False].get_int(k), setups[True].get_int(k))
+               for k in ("ef2nb1", "ef2nb2", "s2g", "bs", "red")) and \
+        all(np.array_equal(setups[False].get_dbl(k), setups[True].get_dbl(k)) for k in ("aip", "rip", "xc", "vol"))
+    return {"metric": "mesh set-up time", "value": times[True], "unit": "s", "higher_is_better": False,
+            "n_gpus": dist.world, "dtype": "f64", "data": "synthetic (seeded jittered unit-cube mesh)",
+            "config": {"workload": "mesh set-up of a %d^3 %s cavity (%d cells, %d faces)" %
+                                   (n, "tet-split" if tet else "hex", setups[True].ne, setups[True].nf),
+                       "host_threads": os.cpu_count()},
+            "host_s": times[False], "device_s": times[True], "speedup": times[False] / times[True],
+            "bit_identical": bool(same)}
+
+
 # ------------------------------------------------------------ served stream
 def run_served(a, dist):
     """A Poisson stream of cavity requests through the serving loop; one JSON
@@ -651,6 +686,8 @@ def main():
             out = run_served(a, dist)
         elif a.workload == "pressure":
             out = run_pressure(a, dist)
+        elif a.workload == "setup":
+            out = run_setup(a, dist)
         else:
             out = run_ours(a, dist)
         if out is not None and dist.rank == 0:

@@ -21,7 +21,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 SOURCES = ["cfdl_zone.cpp", "cfdl_setup.cpp", "cfdl_case.cpp", "cfdl_api.cpp",
-           "cfdl_prof.cpp", "cfdl_tune.cpp", "cfdl_serve.cpp", "cfdl_amg_setup.cpp", "cfdl_kernels.cu", "cfdl_amg.cu", "cfdl_solvers.cu", "cfdl_graph.cu", "cfdl_run.cu", "cfdl_noalloc.cu"]
+           "cfdl_prof.cpp", "cfdl_tune.cpp", "cfdl_serve.cpp", "cfdl_amg_setup.cpp", "cfdl_kernels.cu", "cfdl_amg.cu", "cfdl_solvers.cu", "cfdl_graph.cu", "cfdl_run.cu", "cfdl_noalloc.cu", "cfdl_gsetup.cu"]
+# the device mesh set-up reproduces the host builder's doubles: no FMA contraction
+EXTRA = {"cfdl_gsetup.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -33,7 +35,7 @@ def _nvcc():
 
 def _compile(src, verbose):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [_nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + ARCH + COMMON
+    cmd = [_nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + ARCH + COMMON + EXTRA.get(src, [])
     if src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"] if verbose else []
     r = subprocess.run(cmd, capture_output=True, text=True)

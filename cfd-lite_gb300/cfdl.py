@@ -118,6 +118,7 @@ def lib():
     L.cfdl_box_zone_sizes.argtypes = [C.c_int, C.c_int, ip, ip, ip, ip]
     L.cfdl_box_zone_fill.argtypes = [C.c_int, C.c_int, C.c_double, C.c_uint64, vp, vp, vp, vp, vp, vp, C.c_char_p]
     L.cfdl_setup_create.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_char_p, vp, vp, C.c_int, vp, C.POINTER(vp)]
+    L.cfdl_setup_create_device.argtypes = L.cfdl_setup_create.argtypes
     L.cfdl_setup_sizes.argtypes = [vp, vp]
     L.cfdl_setup_mesh.argtypes = [vp, C.c_double, C.POINTER(Mesh)]
     L.cfdl_setup_get_int.argtypes = [vp, C.c_char_p, vp]
@@ -223,11 +224,14 @@ class Zone:
 class Setup:
     """Connectivity and geometry of a zone, in the reference's arrays."""
 
-    def __init__(self, zone):
+    def __init__(self, zone, device=False):
+        """device=True matches faces and computes the geometry on the GPU
+        (cfdl_setup_create_device); the arrays are the same bit for bit."""
         L = lib()
         self._h = C.c_void_p()
-        _check(L.cfdl_setup_create(zone.nvx, _p(zone.x), _p(zone.y), _p(zone.z), zone.nsec, zone.names,
-                                   _p(zone.etype), _p(zone.esec), zone.ne2vxmax, _p(zone.e2vx), C.byref(self._h)),
+        fn = L.cfdl_setup_create_device if device else L.cfdl_setup_create
+        _check(fn(zone.nvx, _p(zone.x), _p(zone.y), _p(zone.z), zone.nsec, zone.names,
+                  _p(zone.etype), _p(zone.esec), zone.ne2vxmax, _p(zone.e2vx), C.byref(self._h)),
                "mesh set-up")
         sz = np.zeros(5, np.int32)
         L.cfdl_setup_sizes(self._h, _p(sz))

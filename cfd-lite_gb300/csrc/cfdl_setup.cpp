@@ -14,7 +14,7 @@
 // calc_vol_cv_centers_uns (src/setup/calc_vol_cv_centers.f90:4-61) operation
 // by operation (compiled without FP contraction), so the doubles are the
 // reference's bit for bit.
-#include "cfdl.h"
+#include "cfdl_setup_int.h"
 #include "cfdl_par.h"
 #include <algorithm>
 #include <atomic>
@@ -25,33 +25,8 @@
 #include <string>
 #include <vector>
 
+namespace cfdl_setup_detail {
 namespace {
-
-// element tables, src/modules/mod_util.f90:54-169
-const int kFacesTetra4[4][4] = {{1, 3, 2, 0}, {1, 2, 4, 0}, {2, 3, 4, 0}, {3, 1, 4, 0}};
-const int kFacesPyra5[5][4] = {{1, 4, 3, 2}, {1, 2, 5, 0}, {2, 3, 5, 0}, {3, 4, 5, 0}, {4, 1, 5, 0}};
-const int kNFacesPyra5[5] = {4, 3, 3, 3, 3};
-const int kFacesPenta6[5][4] = {{1, 2, 5, 4}, {2, 3, 6, 5}, {3, 1, 4, 6}, {1, 3, 2, 0}, {4, 5, 6, 0}};
-const int kNFacesPenta6[5] = {4, 4, 4, 3, 3};
-const int kFacesHexa8[6][4] = {{1, 4, 3, 2}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {1, 5, 8, 4}, {5, 6, 7, 8}};
-const int kElementNFace[21] = {0, 6, 0, 0, 0, 1, 1, 1, 1, 1, 4, 4, 5, 5, 5, 5, 5, 6, 6, 6, 0};
-const int kElementNVx[21] = {0, 8, 1, 2, 3, 3, 6, 4, 8, 9, 4, 10, 5, 14, 6, 15, 18, 8, 20, 27, 0};
-
-inline int index_t(int g, int s) { return (int)(((unsigned)g << 5) | (unsigned)s); }
-inline void get_idx(int idx, int &g, int &s) { s = (int)((unsigned)idx & 31u); g = (int)((unsigned)idx >> 5); }
-
-// face_vxlist, src/modules/mod_util.f90:1361-1423
-bool face_vxlist(const int *vx, int t, int f, int *lst, int &nl) {
-    switch (t) {
-    case CFDL_TETRA_4: nl = 3; for (int l = 0; l < 3; l++) lst[l] = vx[kFacesTetra4[f - 1][l] - 1]; return true;
-    case 12: nl = kNFacesPyra5[f - 1]; for (int l = 0; l < nl; l++) lst[l] = vx[kFacesPyra5[f - 1][l] - 1]; return true;
-    case 14: nl = kNFacesPenta6[f - 1]; for (int l = 0; l < nl; l++) lst[l] = vx[kFacesPenta6[f - 1][l] - 1]; return true;
-    case CFDL_HEXA_8: nl = 4; for (int l = 0; l < 4; l++) lst[l] = vx[kFacesHexa8[f - 1][l] - 1]; return true;
-    case CFDL_TRI_3: nl = 3; for (int l = 0; l < 3; l++) lst[l] = vx[l]; return true;
-    case CFDL_QUAD_4: nl = 4; for (int l = 0; l < 4; l++) lst[l] = vx[l]; return true;
-    default: return false;
-    }
-}
 
 struct FaceKey {
     int v[4];     // sorted vertex ids, 0-padded at the front for triangles
@@ -66,22 +41,14 @@ struct FaceKey {
 
 }  // namespace
 
-struct cfdl_setup {
-    int nvx = 0, nelem = 0, ne = 0, nf = 0, nbf = 0, nsec = 0, m = 0, nred = 0, nintf = 0;
-    std::vector<double> x, y, z;
-    std::vector<int> e2vx, esec, etype, sec2intf, intf2sec;
-    std::vector<std::string> names;          // file order, as mg%sectionName
-    std::vector<int> ef2nb1, ef2nb2, ef2nb_idx, s2g, bs, red;
-    std::vector<double> aip, rip, xc, yc, zc, vol;
-    // boundary-condition binding produced by cfdl_setup_mesh
-    mutable std::vector<int> bc_esec, bc_kind;
-    mutable std::vector<double> bc_vel;
-};
+int sec_of(const cfdl_setup &S, int e) {
+    for (int s = 0; s < S.nsec; s++) if (e <= S.esec[2 * s + 1]) return s;
+    return S.nsec - 1;
+}
 
-namespace {
-
-int build(cfdl_setup &S) {
-    const int ng = S.ne, m = S.m;
+// Section order and the half-face CSR.
+int order_sections(cfdl_setup &S) {
+    const int ng = S.ne;
     // order section ranges (add_meshds, mod_mg_lvl_uns.f90:154-168)
     {
         std::vector<int> es = S.esec, et = S.etype;
@@ -102,17 +69,22 @@ int build(cfdl_setup &S) {
             if (S.etype[s] < 10) { S.intf2sec.push_back(s + 1); S.sec2intf[s] = (int)S.intf2sec.size(); }
         S.nintf = (int)S.intf2sec.size();
     }
-    auto sec_of = [&](int e) { for (int s = 0; s < S.nsec; s++) if (e <= S.esec[2 * s + 1]) return s; return S.nsec - 1; };
     // CSR (gs2nb_idx) and element faces
     S.ef2nb_idx.assign(ng + 1, 0);
     S.ef2nb_idx[0] = 1;
     for (int e = 1; e <= ng; e++) {
-        int t = S.etype[sec_of(e)];
+        int t = S.etype[sec_of(S, e)];
         if (t < 10 || t > 20) return CFDL_ERR_MESH;  // volume elements must come first
-        S.ef2nb_idx[e] = S.ef2nb_idx[e - 1] + kElementNFace[t];
+        S.ef2nb_idx[e] = S.ef2nb_idx[e - 1] + element_nface(t);
     }
     const int H = S.ef2nb_idx[ng] - 1;
     if (H != 2 * S.nf - S.nbf) return CFDL_ERR_MESH;
+    return CFDL_OK;
+}
+
+// Face matching and numbering: ef2nb1, ef2nb2, s2g, bs.
+int match_faces_host(cfdl_setup &S) {
+    const int ng = S.ne, m = S.m, H = S.ef2nb_idx[ng] - 1;
     // one key per element face: volume element e's faces at its CSR slots,
     // each 2D element's single face after them (disjoint writes, any order)
     std::vector<FaceKey> keys((size_t)H + (S.nelem - ng));
@@ -120,10 +92,10 @@ int build(cfdl_setup &S) {
     cfdl::parallel_for(S.nelem, [&](long b, long e_end) {
         for (long e0 = b; e0 < e_end; e0++) {
             const int e = (int)e0 + 1;
-            const int t = S.etype[sec_of(e)];
+            const int t = S.etype[sec_of(S, e)];
             const size_t base = e <= ng ? (size_t)S.ef2nb_idx[e - 1] - 1 : (size_t)H + (e - ng - 1);
-            if (e > ng && kElementNFace[t] != 1) { bad = 1; return; }
-            for (int f = 1; f <= kElementNFace[t]; f++) {
+            if (e > ng && element_nface(t) != 1) { bad = 1; return; }
+            for (int f = 1; f <= element_nface(t); f++) {
                 int lst[4], nl;
                 if (!face_vxlist(&S.e2vx[(size_t)(e - 1) * m], t, f, lst, nl)) { bad = 1; return; }
                 FaceKey k;
@@ -176,6 +148,13 @@ int build(cfdl_setup &S) {
         }
     }
     });
+    return CFDL_OK;
+}
+
+// Edge boundary marking and the red/black order (sequential in the reference
+// and here: both depend on visiting order).
+int finish_topology(cfdl_setup &S) {
+    const int ng = S.ne;
     // edge boundary faces (mod_mg_lvl_uns.f90:421-433)
     for (int e1 = ng + 1; e1 <= S.nelem; e1++) {
         int &b1 = S.bs[e1 - ng - 1];
@@ -222,12 +201,18 @@ int build(cfdl_setup &S) {
         }
         S.nred = nred;
     }
+    return CFDL_OK;
+}
+
+// Face areas and centroids, cell volumes and centres.
+int geometry_host(cfdl_setup &S) {
+    const int ng = S.ne, m = S.m;
     // calc_aip_xyzip_uns (calc_aip_xyzip.f90:7-74)
     S.aip.assign(3 * (size_t)S.nf, 0.0); S.rip.assign(3 * (size_t)S.nf, 0.0);
     cfdl::parallel_for(S.nf, [&](long b, long e_end) {
     for (int fg = (int)b + 1; fg <= (int)e_end; fg++) {
         int e, fl; get_idx(S.s2g[fg - 1], e, fl);
-        int t = S.etype[sec_of(e)], lst[4], nl;
+        int t = S.etype[sec_of(S, e)], lst[4], nl;
         face_vxlist(&S.e2vx[(size_t)(e - 1) * m], t, fl, lst, nl);
         double r[4][3], dr1[3], dr2[3], av[3], sub[3], sumc[3][3];
         double *a = &S.aip[3 * (size_t)(fg - 1)], *ri = &S.rip[3 * (size_t)(fg - 1)];
@@ -254,7 +239,7 @@ int build(cfdl_setup &S) {
     std::atomic<int> flat{0};
     cfdl::parallel_for(ng, [&](long b, long e_end) {
     for (int e = (int)b + 1; e <= (int)e_end; e++) {
-        int t = S.etype[sec_of(e)], nv = kElementNVx[t];
+        int t = S.etype[sec_of(S, e)], nv = element_nvx(t);
         double gc[3] = {0, 0, 0}, rc[3] = {0, 0, 0}, sum_vol = 0;
         for (int q = 1; q <= nv; q++) {
             int v = S.e2vx[(size_t)(e - 1) * m + q - 1];
@@ -281,41 +266,65 @@ int build(cfdl_setup &S) {
     return flat ? CFDL_ERR_MESH : CFDL_OK;
 }
 
-}  // namespace
+// Argument checks and the copies of the zone arrays.
+int init_setup(cfdl_setup &S, int nvx, const double *x, const double *y, const double *z, int nsec,
+               const char *names, const int *etype, const int *esec, int ne2vxmax, const int *e2vx) {
+    S.nvx = nvx; S.nsec = nsec; S.m = ne2vxmax;
+    int cvs1 = 0, cvs2 = 0, cvs3 = 0;  // cell_input.f90:55-72
+    for (int s = 0; s < nsec; s++) {
+        int t = etype[s], cnt = esec[2 * s + 1] - esec[2 * s] + 1;
+        if (t < 0 || t > 20 || cnt <= 0) return CFDL_ERR_INVALID;
+        if (t >= 10 && t <= 20) { cvs1 += cnt; cvs2 += element_nface(t) * cnt; } else cvs3 += cnt;
+        S.names.emplace_back(std::string(names + 33 * s, strnlen(names + 33 * s, 32)));
+    }
+    S.ne = cvs1; S.nbf = cvs3; S.nf = (cvs2 + cvs3) / 2; S.nelem = cvs1 + cvs3;
+    if ((long long)S.nelem >= (1LL << 26)) return CFDL_ERR_INVALID;
+    S.x.assign(x, x + nvx); S.y.assign(y, y + nvx); S.z.assign(z, z + nvx);
+    S.e2vx.assign(e2vx, e2vx + (size_t)ne2vxmax * S.nelem);
+    for (size_t q = 0; q < S.e2vx.size(); q++)
+        if (S.e2vx[q] < 0 || S.e2vx[q] > nvx) return CFDL_ERR_INVALID;
+    S.esec.assign(esec, esec + 2 * nsec);
+    S.etype.assign(etype, etype + nsec);
+    return CFDL_OK;
+}
 
-extern "C" int cfdl_setup_create(int nvx, const double *x, const double *y, const double *z,
-                                 int nsec, const char *names, const int *etype, const int *esec,
-                                 int ne2vxmax, const int *e2vx, cfdl_setup **out) {
+}  // namespace cfdl_setup_detail
+
+using namespace cfdl_setup_detail;
+
+static int create_setup(int nvx, const double *x, const double *y, const double *z, int nsec, const char *names,
+                        const int *etype, const int *esec, int ne2vxmax, const int *e2vx, cfdl_setup **out,
+                        bool device) {
     if (!out || nvx <= 0 || nsec <= 0 || ne2vxmax <= 0 || !x || !y || !z || !names || !etype || !esec || !e2vx)
         return CFDL_ERR_INVALID;
     *out = nullptr;
     cfdl_setup *S = new (std::nothrow) cfdl_setup;
     if (!S) return CFDL_ERR_OOM;
+    int st;
     try {
-        S->nvx = nvx; S->nsec = nsec; S->m = ne2vxmax;
-        int cvs1 = 0, cvs2 = 0, cvs3 = 0;  // cell_input.f90:55-72
-        for (int s = 0; s < nsec; s++) {
-            int t = etype[s], cnt = esec[2 * s + 1] - esec[2 * s] + 1;
-            if (t < 0 || t > 20 || cnt <= 0) { delete S; return CFDL_ERR_INVALID; }
-            if (t >= 10 && t <= 20) { cvs1 += cnt; cvs2 += kElementNFace[t] * cnt; } else cvs3 += cnt;
-            S->names.emplace_back(std::string(names + 33 * s, strnlen(names + 33 * s, 32)));
-        }
-        S->ne = cvs1; S->nbf = cvs3; S->nf = (cvs2 + cvs3) / 2; S->nelem = cvs1 + cvs3;
-        if ((long long)S->nelem >= (1LL << 26)) { delete S; return CFDL_ERR_INVALID; }
-        S->x.assign(x, x + nvx); S->y.assign(y, y + nvx); S->z.assign(z, z + nvx);
-        S->e2vx.assign(e2vx, e2vx + (size_t)ne2vxmax * S->nelem);
-        for (size_t q = 0; q < S->e2vx.size(); q++)
-            if (S->e2vx[q] < 0 || S->e2vx[q] > nvx) { delete S; return CFDL_ERR_INVALID; }
-        S->esec.assign(esec, esec + 2 * nsec);
-        S->etype.assign(etype, etype + nsec);
-        int st = build(*S);
-        if (st) { delete S; return st; }
+        st = init_setup(*S, nvx, x, y, z, nsec, names, etype, esec, ne2vxmax, e2vx);
+        if (!st) st = order_sections(*S);
+        if (!st) st = device ? match_faces_device(*S) : match_faces_host(*S);
+        if (!st) st = finish_topology(*S);
+        if (!st) st = device ? geometry_device(*S) : geometry_host(*S);
     } catch (const std::bad_alloc &) {
-        delete S;
-        return CFDL_ERR_OOM;
+        st = CFDL_ERR_OOM;
     }
+    if (st) { delete S; return st; }
     *out = S;
     return CFDL_OK;
+}
+
+extern "C" int cfdl_setup_create(int nvx, const double *x, const double *y, const double *z,
+                                 int nsec, const char *names, const int *etype, const int *esec,
+                                 int ne2vxmax, const int *e2vx, cfdl_setup **out) {
+    return create_setup(nvx, x, y, z, nsec, names, etype, esec, ne2vxmax, e2vx, out, false);
+}
+
+extern "C" int cfdl_setup_create_device(int nvx, const double *x, const double *y, const double *z,
+                                        int nsec, const char *names, const int *etype, const int *esec,
+                                        int ne2vxmax, const int *e2vx, cfdl_setup **out) {
+    return create_setup(nvx, x, y, z, nsec, names, etype, esec, ne2vxmax, e2vx, out, true);
 }
 
 extern "C" int cfdl_setup_sizes(const cfdl_setup *s, int *sz) {

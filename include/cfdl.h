@@ -85,6 +85,14 @@ typedef struct cfdl_mesh {
 int cfdl_setup_create(int nvx, const double *x, const double *y, const double *z,
                       int nsec, const char *names, const int *etype, const int *esec,
                       int ne2vxmax, const int *e2vx, cfdl_setup **out);
+/* The same set-up with the face matching, face numbering and geometry on
+ * the current CUDA device (bucketed by smallest vertex instead of a global
+ * sort); the arrays equal cfdl_setup_create's bit for bit.  The reference's
+ * counterpart is the same cell_input path (next item of the hot-path scope:
+ * the connectivity builder for large meshes). */
+int cfdl_setup_create_device(int nvx, const double *x, const double *y, const double *z,
+                             int nsec, const char *names, const int *etype, const int *esec,
+                             int ne2vxmax, const int *e2vx, cfdl_setup **out);
 /* sizes[0..4] = ne, nf, nbf, nsec, nred */
 int cfdl_setup_sizes(const cfdl_setup *s, int *sizes);
 /* Fill a cfdl_mesh whose pointers stay valid until cfdl_setup_destroy.

@@ -69,7 +69,7 @@ class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget", C.c_double), ("hbm_reserve", C.c_double),
                 ("max_cases", C.c_int), ("chunk", C.c_int), ("prep_threads", C.c_int),
                 ("precision", C.c_int), ("precond", C.c_int), ("tile", C.c_int),
-                ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
+                ("alpha_u", C.c_double), ("alpha_p", C.c_double), ("device_setup", C.c_int)]
 
 
 class Result(C.Structure):

@@ -115,8 +115,9 @@ int prepare(const cfdl_server_config &s, Request &q) {
                                      esec.data(), names.data())))
             return st;
         cfdl_setup *su = nullptr;
-        if ((st = cfdl_setup_create(nvx, x.data(), y.data(), z.data(), nsec, names.data(), etype.data(), esec.data(), m,
-                                    e2vx.data(), &su)))
+        auto create = s.device_setup ? cfdl_setup_create_device : cfdl_setup_create;
+        if ((st = create(nvx, x.data(), y.data(), z.data(), nsec, names.data(), etype.data(), esec.data(), m,
+                         e2vx.data(), &su)))
             return st;
         cfdl_mesh mesh;
         st = cfdl_setup_mesh(su, 1.0, &mesh);
@@ -133,6 +134,7 @@ int prepare(const cfdl_server_config &s, Request &q) {
 
 void prep_loop(cfdl_server *S) {
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (S->cfg.device_setup) cudaSetDevice(S->cfg.device);   // the set-up kernels' device
     for (;;) {
         std::unique_ptr<Request> q;
         {
@@ -343,6 +345,7 @@ void cfdl_server_config_default(cfdl_server_config *c) {
     c->tile = 0;
     c->alpha_u = 0.7;
     c->alpha_p = 0.3;
+    c->device_setup = 1;
 }
 
 int cfdl_server_create(const cfdl_server_config *cfg, cfdl_server **out) {

@@ -334,6 +334,7 @@ typedef struct cfdl_server_config {
     int    precision, precond;   /* pressure-solve form (cfdl_config)          */
     int    tile;            /* solver tile shape (0: the default)              */
     double alpha_u, alpha_p;
+    int    device_setup;    /* 1: mesh set-up on the GPU (cfdl_setup_create_device) */
 } cfdl_server_config;
 
 typedef struct cfdl_result {

@@ -167,6 +167,7 @@ def lib():
     L.cfdl_case_set_run.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double]
     L.cfdl_run.argtypes = [vp, C.c_int, ip]
     L.cfdl_set_tile.argtypes = [vp, C.c_int]
+    L.cfdl_write_vtu.argtypes = [vp, C.c_int, vp, C.c_char_p]
     L.cfdl_server_config_default.argtypes = [C.POINTER(ServerConfig)]
     L.cfdl_server_config_default.restype = None
     L.cfdl_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
@@ -346,6 +347,11 @@ class Solver:
 
     def update_uvwp(self):
         _check(lib().cfdl_update_uvwp(self._h), "update_uvwp")
+
+    def write_vtu(self, path, setup=None, cid=0):
+        """The case's fields in the reference's VTU layout (write_vtubin)."""
+        setup = setup if setup is not None else self.setup
+        _check(lib().cfdl_write_vtu(self._h, int(cid), setup._h, str(path).encode()), "write_vtu")
 
     def set_run(self, n_outer, ncoef=0, conv_tol=0.0, cid=-1):
         """Give case cid (-1: every case) n_outer outer iterations to run, an

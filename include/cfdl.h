@@ -365,6 +365,14 @@ double cfdl_server_now(cfdl_server *srv);
 /* stops at once: unfinished requests are dropped */
 int    cfdl_server_destroy(cfdl_server *srv);
 
+/* ---- output --------------------------------------------------------------
+ * write_vtubin (src/modules/mod_vtu_output.f90:6-328) for the uvwp equation:
+ * the case's u, v, w, p, gpc and net cell mass flux ("mip") read from the
+ * device, with the mesh of `setup`, in the reference's VTU byte layout (XML
+ * header, raw appended data with UInt64 counts).  path is the file to write
+ * (the reference's VTK/output-<iout>/uvwp.vtu; the caller makes the folder). */
+int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *setup, const char *path);
+
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);
 /* Human-readable text for a status code. */

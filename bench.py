@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "batched", "served", "pressure", "setup"],
+    ap.add_argument("--workload", default="cavity",
+                    choices=["cavity", "batched", "served", "pressure", "setup", "energy"],
                     help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
     ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
@@ -569,6 +570,137 @@ def run_pressure(a, dist):
     return out
 
 
+# ------------------------------------------------------------ energy equation
+def run_energy(a, dist):
+    """The energy equation (src/equations/mod_energy.f90) on the cavity
+    workload: one step = one solve_energy (calc_grad of t and phi,
+    calc_coef_energy, the phi solve to the reference's 10x residual drop,
+    calc_temperature) after an outer pass of solve_uvwp, so every solve sees a
+    new flow field; value = cells x energy solves / s over the solve_energy
+    calls alone.  Also: the outer pass with and without the energy solve, the
+    dominant energy kernel against the HBM roofline, and the CPU oracle's
+    solve_energy (the reference's Gauss-Seidel) on a bounded sample."""
+    import cfdl
+    from bytes_model import kernel_bytes
+
+    cfdl.select_device(dist.local)
+    zone = cfdl.Zone(a.n, a.tet, a.jitter, seed=a.seed)
+    setup = cfdl.Setup(zone)
+    cfg = cfdl.steady(solve_mode=a.mode, precision=a.precision, precond=a.precond)
+    W = 4 if a.tet else 6
+    ne, nf, nbf = setup.ne, setup.nf, setup.nbf
+    g = cfdl.Solver(setup, cfg)
+    g.energy_init()
+    for _ in range(a.warmup):                  # developed flow and temperature
+        g.step(1, ncoef=0)
+    clocks = Clocks(dist.local)
+    e_ms, o_ms, iters = [], [], []
+    l0, launches_e = g.launch_count(), 0
+    dist.barrier()
+    clocks.start()
+    for _ in range(a.steps):
+        g.update_boundaries()
+        g.timer_begin()
+        g.solve_uvwp(stats=False)
+        o_ms.append(g.timer_end())
+        l1 = g.launch_count()
+        g.timer_begin()
+        st = g.solve_energy()
+        e_ms.append(g.timer_end())
+        launches_e += g.launch_count() - l1
+        iters.append(st.it_e)
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(sum(e_ms))
+    value = dist.sum(ne * a.steps) / (ms / 1e3)
+    # per-kernel shares of the energy solve and the dominant kernel's launches
+    g.profile_start(None)
+    for _ in range(3):
+        g.step(1, ncoef=0)
+    prof = {k: v for k, v in g.profile_stop().items() if k.startswith("k_en_") or k == "k_grad2"}
+    dominant = max(prof.items(), key=lambda kv: kv[1][1])[0]
+    g.profile_start(dominant)
+    for _ in range(a.steps):
+        g.update_boundaries(); g.solve_uvwp(stats=False); g.solve_energy()
+    dp = g.profile_stop()[dominant]
+    avg_s = dp[1] / dp[0] / 1e3
+    peaks, peak_kind = measured_peaks()
+    nbytes = kernel_bytes(dominant, ne, nf, nbf, W)
+    achieved = nbytes / avg_s / 1e9
+    total = sum(v[1] for v in prof.values())
+    shares = {k: round(t / total, 4) for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    # the outer pass without the energy equation, same mesh and state
+    g2 = cfdl.Solver(setup, cfg)
+    for _ in range(a.warmup):
+        g2.step(1, ncoef=0)
+    g2.timer_begin()
+    for _ in range(a.steps):
+        g2.update_boundaries(); g2.solve_uvwp(stats=False)
+    ms_plain = g2.timer_end()
+    g2.close()
+    t_range = g.get("t")[:ne]
+    g.close()
+    cpu = None
+    if not a.no_cpu and dist.rank == 0 and dist.world == 1:
+        cpu = cpu_energy_baseline(a)
+    ms_outer = statistics.median(o_ms)
+    out = {
+        "metric": "energy solve cell-updates/s", "value": value, "unit": "cells x solves/s",
+        "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered unit-cube hex mesh)",
+        "config": {"workload": "energy equation on the lid-driven cavity %d^3 %s, jitter %.2f, Re=100, hot lid "
+                               "373 / walls 273, cp=1000, tc=5; solve_energy after each outer pass"
+                               % (a.n, "tet-split" if a.tet else "hex", a.jitter),
+                   "cells": ne, "inner_solve": "10x residual drop / nit=100" if a.mode == 0 else "tight 1e-13",
+                   "l2": "working set > L2 (no flush needed)"},
+        "gpu_launches": launches_e,
+        "energy_iterations_median": statistics.median(iters),
+        "outer_pass_ms": {"solve_uvwp": ms_outer, "solve_energy": statistics.median(e_ms),
+                          "solve_uvwp_without_energy_setup": ms_plain / a.steps},
+        "temperature_range": [float(t_range.min()), float(t_range.max())],
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": ncu_traffic(dominant, a.n),
+                     "algorithmic_bytes": nbytes, "avg_launch_us": avg_s * 1e6, "launches": dp[0],
+                     "peak_source": peak_kind},
+        "kernel_shares": shares,
+    }
+    if clk:
+        out["clocks"] = clk
+    if cpu:
+        out["cpu_baseline"] = cpu
+    return out
+
+
+def cpu_energy_baseline(a, budget_s=15.0):
+    """The reference's solve_energy (CPU oracle, Gauss-Seidel to a 10x drop),
+    single thread, on a 32^3 sample of the same cavity after a few outer
+    passes; cells x solves / s."""
+    import cfdl
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    n = min(a.n, 32)
+    zone = cfdl.Zone(n, a.tet, a.jitter, seed=a.seed)
+    setup = cfdl.Setup(zone)
+    o = oracle_lib.Oracle(zone, n_subdomains=4, setup=setup)
+    o.physics_init(oracle_lib.steady(mode=0))
+    o.energy_init()
+    o.run(3, 0)
+    k, dt = 0, 0.0
+    while dt < budget_s and k < 200:
+        o.update_boundaries()
+        o.solve_uvwp()
+        t0 = time.perf_counter()
+        o.solve_energy()
+        dt += time.perf_counter() - t0
+        k += 1
+    ne = o.ne
+    o.close()
+    return {"value": ne * k / dt, "unit": "cells x solves/s", "cores": 1, "kind": "port",
+            "sample": "%d solve_energy calls on a %d^3 mesh (%d cells) after 3 outer passes, %.1f s of solves"
+                      % (k, n, ne, dt)}
+
+
 # ------------------------------------------------------------ mesh set-up
 def run_setup(a, dist):
     """Mesh set-up (face matching, numbering, geometry) of the largest served
@@ -686,6 +818,8 @@ def main():
             out = run_served(a, dist)
         elif a.workload == "pressure":
             out = run_pressure(a, dist)
+        elif a.workload == "energy":
+            out = run_energy(a, dist)
         elif a.workload == "setup":
             out = run_setup(a, dist)
         else:

@@ -47,6 +47,24 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
         "k_pc_q": ne * (8 + 8 + 8) + ell_d + ell_i,
         "k_pc_x": ne * (16 + 8 + 16 + 8 + 8 + 8),
         "k_pc_p": ne * 24,
+        # energy equation: halo BC (kind, owner, wall t, owner cp in; t, phi out)
+        "k_en_bc": nbf * (4 + 4 + 8 + 8 + 16),
+        "k_en_time": ne * 16,
+        "k_en_time_halo": nbf * 16,
+        "k_grad2": ell_i + 3 * ell_d + 16 * (ne + nbf) + 48 * ne,
+        # face terms: own/nb, weight, area/(dr.n), area vector, 2 outputs; boundary: own/nb, area/ds, 1 output;
+        # cell tc, cp and the two gradients
+        "k_en_face": nfi * (8 + 8 + 8 + 24 + 16) + nbf * (8 + 8 + 8) + ne * (16 + 48),
+        # cell gather: ELL nb/fc, mip + 2 face planes; phi, phi0, rho, vol in, ap, b out; anb ELL out; halo kinds
+        "k_en_cell": 2 * ell_i + nf * 24 + ne * (32 + 16) + ell_d + nbf * 4,
+        # solver init: ap, rap, b, phi, r, rh, anb ELL + halo phi
+        "k_en_init": ne * 48 + ell_d + ell_i + nbf * 8,
+        "k_en_p": ne * 8 + ne * (24 + 16),
+        "k_en_v": ne * 8 + ell_d + ell_i + ne * (8 + 8 + 8),
+        "k_en_s": ne * 8 + ne * (16 + 16),
+        "k_en_t": ne * 8 + ell_d + ell_i + ne * (8 + 8 + 8),
+        "k_en_x": ne * (16 + 8 + 8 + 8 + 8 + 8 + 8),
+        "k_en_temp": ne * 24,
     }
     return table.get(name)
 

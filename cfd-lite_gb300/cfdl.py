@@ -51,13 +51,13 @@ class Stats(C.Structure):
                 ("res_i", C.c_double * 4), ("res_f", C.c_double * 4),
                 ("mass_imbalance", C.c_double), ("status", C.c_int),
                 ("outer_done", C.c_int), ("run_left", C.c_int), ("converged", C.c_int),
-                ("mass_ratio", C.c_double)]
+                ("mass_ratio", C.c_double), ("it_e", C.c_int), ("res_e", C.c_double * 2)]
 
     def as_dict(self):
         return {"it": [self.it_u, self.it_v, self.it_w, self.it_p], "res_i": list(self.res_i),
                 "res_f": list(self.res_f), "mass_imbalance": self.mass_imbalance, "status": self.status,
                 "outer_done": self.outer_done, "run_left": self.run_left, "converged": self.converged,
-                "mass_ratio": self.mass_ratio}
+                "mass_ratio": self.mass_ratio, "it_e": self.it_e, "res_e": list(self.res_e)}
 
 
 class Request(C.Structure):
@@ -95,7 +95,8 @@ class Mesh(C.Structure):
                 ("ef2nb1", C.c_void_p), ("ef2nb2", C.c_void_p), ("ef2nb_idx", C.c_void_p),
                 ("s2g", C.c_void_p), ("bs", C.c_void_p), ("aip", C.c_void_p), ("rip", C.c_void_p),
                 ("xc", C.c_void_p), ("yc", C.c_void_p), ("zc", C.c_void_p), ("vol", C.c_void_p),
-                ("nbc", C.c_int), ("bc_esec", C.c_void_p), ("bc_kind", C.c_void_p), ("bc_vel", C.c_void_p)]
+                ("nbc", C.c_int), ("bc_esec", C.c_void_p), ("bc_kind", C.c_void_p), ("bc_vel", C.c_void_p),
+                ("bc_temp", C.c_void_p)]
 
 
 class Fields(C.Structure):
@@ -134,8 +135,10 @@ def lib():
     for n in ("cfdl_update_boundaries", "cfdl_update_time", "cfdl_calc_coef_uvw", "cfdl_calc_coef_p",
               "cfdl_adjust_pc", "cfdl_update_uvwp"):
         getattr(L, n).argtypes = [vp]
-    for n in ("cfdl_solve_uvwp", "cfdl_solve_momentum", "cfdl_solve_pc"):
+    for n in ("cfdl_solve_uvwp", "cfdl_solve_momentum", "cfdl_solve_pc", "cfdl_solve_energy"):
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
+    L.cfdl_energy_init.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.cfdl_calc_coef_energy.argtypes = [vp]
     L.cfdl_step.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_solve_uvwp_host.argtypes = [vp, C.POINTER(Fields), C.POINTER(Stats)]
     L.cfdl_step_host.argtypes = [vp, C.POINTER(Fields), C.c_int, C.c_int, C.POINTER(Stats)]
@@ -168,6 +171,7 @@ def lib():
     L.cfdl_run.argtypes = [vp, C.c_int, ip]
     L.cfdl_set_tile.argtypes = [vp, C.c_int]
     L.cfdl_write_vtu.argtypes = [vp, C.c_int, vp, C.c_char_p]
+    L.cfdl_write_vtu_energy.argtypes = [vp, C.c_int, vp, C.c_char_p]
     L.cfdl_server_config_default.argtypes = [C.POINTER(ServerConfig)]
     L.cfdl_server_config_default.restype = None
     L.cfdl_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
@@ -328,11 +332,25 @@ class Solver:
         return st
 
     def calc_grad(self, field):
-        idx = {"u": 0, "v": 1, "w": 2, "phic": 3, "pc": 3, "uvw": 4}[field]
+        idx = {"u": 0, "v": 1, "w": 2, "phic": 3, "pc": 3, "uvw": 4, "energy": 5}[field]
         _check(lib().cfdl_calc_grad(self._h, idx), "calc_grad")
 
     def calc_mip(self, rhie_chow=True):
         _check(lib().cfdl_calc_mip(self._h, int(bool(rhie_chow))), "calc_mip")
+
+    # -- energy equation (src/equations/mod_energy.f90) --------------------------
+    def energy_init(self, cp=1000.0, tc=5.0, t_init=273.0):
+        """construct_energy for every case; from then on update_boundaries,
+        update_time, step and run include the energy equation."""
+        _check(lib().cfdl_energy_init(self._h, float(cp), float(tc), float(t_init)), "energy_init")
+
+    def solve_energy(self):
+        st = Stats()
+        _check(lib().cfdl_solve_energy(self._h, C.byref(st)), "solve_energy")
+        return st
+
+    def calc_coef_energy(self):
+        _check(lib().cfdl_calc_coef_energy(self._h), "calc_coef_energy")
 
     def calc_coef_p(self):
         _check(lib().cfdl_calc_coef_p(self._h), "calc_coef_p")
@@ -352,6 +370,11 @@ class Solver:
         """The case's fields in the reference's VTU layout (write_vtubin)."""
         setup = setup if setup is not None else self.setup
         _check(lib().cfdl_write_vtu(self._h, int(cid), setup._h, str(path).encode()), "write_vtu")
+
+    def write_vtu_energy(self, path, setup=None, cid=0):
+        """The energy equation's fields in the reference's VTU layout."""
+        setup = setup if setup is not None else self.setup
+        _check(lib().cfdl_write_vtu_energy(self._h, int(cid), setup._h, str(path).encode()), "write_vtu_energy")
 
     def set_run(self, n_outer, ncoef=0, conv_tol=0.0, cid=-1):
         """Give case cid (-1: every case) n_outer outer iterations to run, an
@@ -397,9 +420,9 @@ class Solver:
     # -- arrays ------------------------------------------------------------
     def _len(self, name):
         nc = self.ne + self.nbf
-        if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic"):
+        if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic", "t", "e", "e0"):
             return nc
-        if name in ("gu", "gv", "gw", "gp", "gpc"):
+        if name in ("gu", "gv", "gw", "gp", "gpc", "gt", "ge"):
             return 3 * nc
         if name in ("mip", "mip0"):
             return self.nf
@@ -459,9 +482,9 @@ class Solver:
 
 def _array_len(name, ne, nf, nbf, H):
     nc = ne + nbf
-    if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic"):
+    if name in ("u", "v", "w", "p", "u0", "v0", "w0", "phic", "t", "e", "e0"):
         return nc
-    if name in ("gu", "gv", "gw", "gp", "gpc"):
+    if name in ("gu", "gv", "gw", "gp", "gpc", "gt", "ge"):
         return 3 * nc
     if name in ("mip", "mip0"):
         return nf

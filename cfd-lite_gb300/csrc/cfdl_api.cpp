@@ -43,6 +43,9 @@ Named lookup(HostCase *hc, const char *name) {
         {"mip", d.mip, nf}, {"mip0", d.mip0, nf},
         {"ap", d.ap, ne}, {"b", d.b, ne}, {"bu", d.bu, ne}, {"bv", d.bv, ne}, {"bw", d.bw, ne},
         {"d", d.d, ne}, {"dc", d.dc, ne}, {"rho", d.rho, ne}, {"mu", d.mu, ne},
+        // energy equation (null until cfdl_energy_init)
+        {"t", d.et, nc}, {"e", d.ee, nc}, {"e0", d.ee0, nc}, {"gt", d.egt, 3 * nc}, {"ge", d.ege, 3 * nc},
+        {"cp", d.ecp, ne}, {"tc", d.etc, ne},
     };
     for (const E &e : tab) if (s == e.nm) return {e.p, e.n, false};
     if (s == "anb") return {d.anb, (size_t)hc->H, true};
@@ -285,6 +288,7 @@ int cfdl_step(cfdl_ctx *ctx, int n_outer, int ncoef, cfdl_stats *stats) {
     for (int k = 1; k <= n_outer; k++) {
         launch_bc(ctx);
         if ((st = solve_uvwp_all(ctx))) return st;
+        if ((st = solve_energy_all(ctx))) return st;    // main.f90:58, when set up
         if (ncoef > 0 && k % ncoef == 0) launch_update_time(ctx);
     }
     return finish(ctx, stats);
@@ -345,6 +349,7 @@ int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_s
     for (int k = 1; k <= n_outer; k++) {
         launch_bc(ctx);
         if ((st = solve_uvwp_all(ctx))) return st;
+        if ((st = solve_energy_all(ctx))) return st;    // main.f90:58, when set up
         if (ncoef > 0 && k % ncoef == 0) launch_update_time(ctx);
     }
     if ((st = download_overlapped(ctx, hc, f))) return st;
@@ -368,7 +373,7 @@ int cfdl_solve_momentum(cfdl_ctx *ctx, cfdl_stats *stats) {
 int cfdl_calc_grad(cfdl_ctx *ctx, int field) {
     int st = check_ctx(ctx);
     if (st) return st;
-    if (field < 0 || field > 4) return CFDL_ERR_INVALID;
+    if (field < 0 || field > 5 || (field == 5 && !energy_on(ctx))) return CFDL_ERR_INVALID;
     launch_grad(ctx, field);
     return cuda_status(cudaStreamSynchronize(ctx->stream));
 }
@@ -405,6 +410,37 @@ int cfdl_update_uvwp(cfdl_ctx *ctx) {
     int st = check_ctx(ctx);
     if (st) return st;
     launch_update_uvwp(ctx);
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_energy_init(cfdl_ctx *ctx, double cp, double tc, double t_init) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (!(cp > 0) || !(tc >= 0) || !std::isfinite(cp) || !std::isfinite(tc) || !std::isfinite(t_init))
+        return CFDL_ERR_INVALID;
+    for (HostCase *hc : ctx->cases)
+        if (hc->h_temp.empty()) return CFDL_ERR_INVALID;   // the mesh carried no energy BCs
+    for (HostCase *hc : ctx->cases)
+        if ((st = energy_init_case(ctx, hc, cp, tc, t_init))) return st;
+    destroy_graph(ctx);   // the run graph is captured without the energy launches
+    if ((st = upload_case_table(ctx))) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_solve_energy(cfdl_ctx *ctx, cfdl_stats *stats) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (!energy_on(ctx)) return CFDL_ERR_INVALID;
+    if ((st = solve_energy_all(ctx))) return st;
+    if ((st = finish(ctx, stats))) return st;
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int cfdl_calc_coef_energy(cfdl_ctx *ctx) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if (!energy_on(ctx)) return CFDL_ERR_INVALID;
+    launch_coef_energy(ctx);
     return cuda_status(cudaStreamSynchronize(ctx->stream));
 }
 

@@ -197,7 +197,7 @@ void CasePrep::release_tables() {
     std::vector<int>().swap(f_own); std::vector<int>().swap(f_nb); std::vector<int>().swap(h_own);
     std::vector<int>().swap(h_face); std::vector<int>().swap(h_kind);
     std::vector<double>().swap(hf_G); std::vector<double>().swap(fgeo); std::vector<double>().swap(h_vel);
-    std::vector<double>().swap(vol);
+    std::vector<double>().swap(vol); std::vector<double>().swap(h_temp);
     delete amg;
     amg = nullptr;
 }
@@ -275,6 +275,13 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
                 h_kind[h] = kind;
                 for (int q = 0; q < 3; q++) h_vel[3 * (size_t)h + q] = m->bc_vel[3 * bc + q];
             }
+        }
+        // energy wall temperatures, when the mesh carries them
+        p->h_temp.clear();
+        if (m->bc_temp) {
+            p->h_temp.assign(std::max(nbf, 1), 0.0);
+            for (int bc = 0; bc < m->nbc; bc++)
+                for (int el = m->bc_esec[2 * bc]; el <= m->bc_esec[2 * bc + 1]; el++) p->h_temp[el - ne - 1] = m->bc_temp[bc];
         }
         // ---- face geometry planes ----
         std::vector<double> &fgeo = p->fgeo;
@@ -357,6 +364,7 @@ int upload_case(CasePrep &p, const cfdl_config *cfg, HostCase **out) {
     try {
         hc->ne = p.ne; hc->nf = p.nf; hc->nbf = p.nbf; hc->H = p.H; hc->W = p.W;
         hc->ef2nb_idx = p.ef2nb_idx;
+        hc->h_temp = p.h_temp;
         st = upload_all(hc, cfg, p.hf_nb, p.hf_fc, p.hf_G, p.f_own, p.f_nb, p.fgeo, p.h_own, p.h_face, p.h_kind,
                         p.h_vel, p.vol);
         if (!st && p.amg) {

@@ -1,0 +1,229 @@
+// cfdl_energy.cu -- the energy equation of the reference
+// (src/equations/mod_energy.f90) on the device, FP64.
+//
+// The equation is for phi = cp*t: upwind advection by the face mass fluxes of
+// solve_uvwp, diffusion tc/cp with a deferred correction carrying the
+// difference between grad t and grad(phi)/cp, the transient rho*vol/dt, and
+// Dirichlet walls.  As in the momentum assembly, the per-face quantities that
+// the reference computes from both sides of a face are computed once per face
+// (k_en_face) and gathered by the cells in the reference's half-face order
+// (k_en_cell); the boundary terms follow in the BC loop's order (ascending
+// halo index).  The assembly leaves ap, anb, b in the case's shared scratch,
+// as the reference's phys%ap/anb/b, and uses the momentum face-term planes
+// fS as its face scratch.  The phi solve reuses the momentum BiCGStab kernels
+// on one right-hand side (cfdl_solvers.cu).
+//
+// Every kernel returns at once for a case without the energy equation (its
+// energy arrays are null) and for a case whose run has halted, so a batch may
+// mix cases with and without it.
+#include "cfdl_device.cuh"
+#include <algorithm>
+
+namespace cfdl {
+namespace {
+
+#define EN_PROLOGUE                               \
+    const Tile t = tiles[blockIdx.x];             \
+    const CaseDev &C = cases[t.c];                \
+    if (!C.ee || C.sc->halted) return;            \
+    const int i = t.first + (int)threadIdx.x;
+
+// lid / dirichlet0 of the energy equation (mod_energy.f90:173-212): the halo
+// takes the wall temperature and phi = cp(owner)*t.  One thread per halo.
+__global__ void __launch_bounds__(kTile) k_en_bc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    EN_PROLOGUE
+    if (i >= t.last || C.h_kind[i] == 0) return;
+    const int h = C.ne + i;
+    const double tw = C.eh_t[i];
+    C.et[h] = tw;
+    C.ee[h] = C.ecp[C.h_own[i]] * tw;
+}
+
+// update_time's phi0 = phi (mod_physics.f90:111) over cells (halo = 0) or
+// halos (halo = 1); run_due: only the cases whose run cadence is due.
+__global__ void __launch_bounds__(kTile) k_en_time(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                   int halo, int run_due) {
+    EN_PROLOGUE
+    if (run_due && !C.sc->time_due) return;
+    if (i >= t.last) return;
+    const int j = halo ? C.ne + i : i;
+    C.ee0[j] = C.ee[j];
+}
+
+// calc_coef_energy, face part (mod_energy.f90:96-140): per interior face, from
+// the owner's side, the diffusion coefficient tc_ip/cp_ip * area/(dr.n)
+// (the same from both sides) and the deferred term
+// tc_ip * area * (grad t_ip . n - grad phi_ip . n / cp_ip) (the neighbour sees
+// the opposite normal and the complementary weight, so it takes the negative);
+// boundary faces: the Dirichlet coefficient tc*area/ds/cp of the BC loop
+// (mod_energy.f90:146-168).  Planes: fS[0] coefficient, fS[1] deferred term.
+__global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    EN_PROLOGUE
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    const double *g = C.fgeo;
+    double *fd = C.fS, *fx = C.fS + nf;
+    if (n >= C.ne) {
+        fd[i] = C.etc[o] * g[FG_ADS * nf + i] / C.ecp[o];
+        return;
+    }
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
+    const double tci = omw * C.etc[o] + wt * C.etc[n];
+    const double cpi = omw * C.ecp[o] + wt * C.ecp[n];
+    fd[i] = tci / cpi * g[FG_ADN * nf + i];
+    const double A[3] = {g[FG_AX * nf + i], g[FG_AY * nf + i], g[FG_AZ * nf + i]};
+    double gtn = 0.0, ghn = 0.0;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+        gtn += (omw * C.egt[3 * o + m] + wt * C.egt[3 * n + m]) * A[m];
+        ghn += (omw * C.ege[3 * o + m] + wt * C.ege[3 * n + m]) * A[m];
+    }
+    fx[i] = tci * (gtn - ghn / cpi);
+}
+
+// calc_coef_energy, cell part (mod_energy.f90:92-143, then the BC loop
+// :146-168): anb = d + max(f,0) with f = -sg*mip the inward flux,
+// ap = sum anb + rho*vol/dt + the wall coefficients,
+// b = ap0*phi0 + sumf*phi + sumdefc.
+__global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    EN_PROLOGUE
+    if (i >= t.last) return;
+    const int ne = C.ne, nf = C.nf, W = C.W;
+    const double *fd = C.fS, *fx = C.fS + nf;
+    double ap = 0.0, sumf = 0.0, sumdefc = 0.0;
+    double a[kMaxW];
+    int bslot[kMaxW], nb_cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        a[k] = 0.0;
+        if (k >= W) continue;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb < 0) continue;
+        if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
+        const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
+        const double fl = flip_sign(C.mip[f], fc >= 0);   // -sg * mip
+        const double ak = fd[f] + positive_part(fl);
+        sumf += fl;
+        a[k] = ak;
+        ap += ak;
+        sumdefc += flip_sign(fx[f], fc < 0);              // sg * deferred term
+    }
+    const double phi = C.ee[i];
+    double b;
+    if (C.steady) {                                       // ap0 = rho*vol/dt = 0
+        b = sumf * phi + sumdefc;
+    } else {
+        const double ap0 = C.rho[i] * C.vol[i] * C.rdt;
+        ap = ap + ap0;
+        b = ap0 * C.ee0[i] + sumf * phi + sumdefc;
+    }
+    // walls in BC-loop order (ascending halo index); every bound BC is 'dirichlet'
+    for (int q = 1; q < nb_cnt; q++) {
+        int s = bslot[q], j = q - 1;
+        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
+        bslot[j + 1] = s;
+    }
+    for (int q = 0; q < nb_cnt; q++) {
+        const int k = bslot[q], h = C.hf_nb[k * ne + i];
+        if (C.h_kind[h - ne] == 0) continue;
+        const double d = fd[face_of(C.hf_fc[k * ne + i])];
+        ap = ap + d;
+        a[k] = a[k] + d;
+    }
+    C.ap[i] = ap;
+    C.b[i] = b;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++)
+        if (k < W) C.anb[k * ne + i] = a[k];
+}
+
+// calc_temperature, mod_properties.f90:214-221: t = phi/cp on the cells
+__global__ void __launch_bounds__(kTile) k_en_temp(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    EN_PROLOGUE
+    if (i < t.last) C.et[i] = C.ee[i] / C.ecp[i];
+}
+
+// t = t_init, phi = cp*t, phi0 = phi over cells and halos (construct_energy,
+// mod_energy.f90:33-37); the halos take the cp of their owner
+__global__ void k_en_fill(double *t, double *e, double *e0, const double *cp, const int *h_own, int ne, int nbf,
+                          double t_init) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ne + nbf) return;
+    const double c = cp[j < ne ? j : h_own[j - ne]];
+    t[j] = t_init;
+    e[j] = t_init * c;
+    e0[j] = e[j];
+}
+
+__global__ void k_fill(double *x, size_t n, double v) {
+    const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j < n) x[j] = v;
+}
+
+}  // namespace
+
+bool energy_on(const cfdl_ctx *ctx) {
+    for (const HostCase *hc : ctx->cases)
+        if (hc->dev.ee) return true;
+    return false;
+}
+
+void launch_energy_bc(cfdl_ctx *ctx) {
+    if (energy_on(ctx)) CFDL_LAUNCH("k_en_bc", k_en_bc, halos);
+}
+
+void launch_energy_time(cfdl_ctx *ctx, bool run_due) {
+    if (!energy_on(ctx)) return;
+    CFDL_LAUNCH("k_en_time", k_en_time, cells, 0, run_due ? 1 : 0);
+    CFDL_LAUNCH("k_en_time_halo", k_en_time, halos, 1, run_due ? 1 : 0);
+}
+
+void launch_coef_energy(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_en_face", k_en_face, faces);
+    CFDL_LAUNCH("k_en_cell", k_en_cell, cells);
+}
+
+// solve_energy, mod_energy.f90:59-80
+int solve_energy_all(cfdl_ctx *ctx) {
+    if (!energy_on(ctx)) return CFDL_OK;
+    launch_grad(ctx, 5);                  // calc_grad(t -> gt), calc_grad(phi -> grad), one pass
+    launch_coef_energy(ctx);
+    int st = solve_energy_phi(ctx);
+    if (st) return st;
+    CFDL_LAUNCH("k_en_temp", k_en_temp, cells);
+    return cuda_status(cudaGetLastError());
+}
+
+// construct_energy for one case: allocates the energy arrays on first use and
+// sets the initial state; the case table is uploaded by the caller.
+int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t_init) {
+    if (hc->h_temp.empty() || (int)hc->h_temp.size() < hc->nbf) return CFDL_ERR_INVALID;
+    CaseDev &d = hc->dev;
+    const size_t ne = hc->ne, nc = ne + hc->nbf;
+    int st;
+    if (!d.ee) {
+        void *p;
+        struct A { double **dst; size_t n; } list[] = {
+            {&d.et, nc}, {&d.ee, nc}, {&d.ee0, nc}, {&d.egt, 3 * nc}, {&d.ege, 3 * nc}, {&d.ecp, ne}, {&d.etc, ne}};
+        for (const A &a : list) {
+            if ((st = case_alloc(hc, &p, a.n * sizeof(double)))) return st;
+            *a.dst = (double *)p;
+        }
+        if ((st = case_alloc(hc, &p, std::max<size_t>(hc->nbf, 1) * sizeof(double)))) return st;
+        d.eh_t = (const double *)p;
+        if ((st = cuda_status(cudaMemcpyAsync(p, hc->h_temp.data(), hc->nbf * sizeof(double), cudaMemcpyHostToDevice,
+                                              ctx->stream))))
+            return st;
+    }
+    const int tb = 256;
+    k_fill<<<(unsigned)((ne + tb - 1) / tb), tb, 0, ctx->stream>>>(d.ecp, ne, cp);
+    k_fill<<<(unsigned)((ne + tb - 1) / tb), tb, 0, ctx->stream>>>(d.etc, ne, tc);
+    k_en_fill<<<(unsigned)((nc + tb - 1) / tb), tb, 0, ctx->stream>>>(d.et, d.ee, d.ee0, d.ecp, d.h_own, (int)ne,
+                                                                       hc->nbf, t_init);
+    ctx->launches += 3;
+    if ((st = cuda_status(cudaMemsetAsync(d.egt, 0, 3 * nc * sizeof(double), ctx->stream)))) return st;
+    if ((st = cuda_status(cudaMemsetAsync(d.ege, 0, 3 * nc * sizeof(double), ctx->stream)))) return st;
+    return cuda_status(cudaGetLastError());
+}
+
+}  // namespace cfdl

@@ -71,13 +71,18 @@ enum FaceProp {
 struct AmgLevelDev;
 struct AmgHierarchy;
 
-// Per-case solver state on the device.
-struct SolveScalars {
-    // momentum BiCGStab, one lane per component u, v, w
+// BiCGStab scalars, one lane per right-hand side
+struct KLanes {
     double rho[3], alpha[3], omega[3], beta[3];
     int half[3];
     double rnorm[3], r0norm[3], bnorm[3], tol[3];
     int active[3], iters[3], status[3];
+};
+
+// Per-case solver state on the device.  The base lanes are the momentum
+// solve's (u, v, w); en lane 0 is the energy solve's.
+struct SolveScalars : KLanes {
+    KLanes en;
     // pressure CG
     double rz, rnorm_p, r0norm_p, tol_p, alpha_p, beta_p, mean_b, pref;
     int active_p, iters_p, status_p;
@@ -124,6 +129,11 @@ struct CaseDev {
     float *cinv32;
     SolveScalars *sc;
     int *counters;                        // [16] last-tile counters, zero between launches
+    // energy equation (null until cfdl_energy_init): t, phi = cp*t, phi0
+    // [ne+nbf]; their gradients [3(ne+nbf)]; cp, tc [ne]; wall temperature
+    // of each halo [nbf]
+    double *et, *ee, *ee0, *egt, *ege, *ecp, *etc;
+    const double *eh_t;
     // parameters
     double dt, alpha_u, alpha_p, rtol_u, rtol_p, tight_rtol;
     double rdt, ralpha_u;                 // 1/dt (0 when steady), 1/alpha_u
@@ -156,6 +166,7 @@ struct HostCase {
     int id = 0;                      // stable case id within its context
     bool props_dirty = true;         // fprop must be recomputed (rho or mu changed)
     size_t bytes = 0;                // device bytes held (mesh, fields, solver, hierarchy)
+    std::vector<double> h_temp;      // [nbf] energy wall temperature of each halo (empty: none)
 };
 
 }  // namespace cfdl
@@ -176,7 +187,7 @@ struct cfdl_ctx {
     cfdl::WorkList cells, faces, halos;
     cfdl::WorkList cellsv;               // wide tiles (kTile*vec cells) for the solver kernels
     int vec = cfdl::kVec;                // cells per thread in those tiles (autotuned)
-    int last_iters_m = 0, last_iters_p = 0;   // previous inner iteration counts (poll scheduling)
+    int last_iters_m = 0, last_iters_p = 0, last_iters_e = 0;   // previous inner iteration counts (poll scheduling)
     double *d_partials = nullptr;        // [max tiles][kNPart]
     int partials_cap = 0;                // tiles
     int64_t launches = 0;
@@ -219,6 +230,7 @@ struct CasePrep {
     int ne = 0, nf = 0, nbf = 0, W = 0, H = 0;
     std::vector<int> ef2nb_idx, hf_nb, hf_fc, f_own, f_nb, h_own, h_face, h_kind;
     std::vector<double> hf_G, fgeo, h_vel, vol;
+    std::vector<double> h_temp;      // energy wall temperatures (empty when the mesh has none)
     AmgHierarchy *amg = nullptr;     // optional, built on the host by prepare_case_amg
     CasePrep() = default;
     CasePrep(const CasePrep &) = delete;
@@ -238,13 +250,23 @@ void apply_config(HostCase *hc, const cfdl_config *cfg);
 void launch_bc(cfdl_ctx *ctx);
 void ensure_face_props(cfdl_ctx *ctx);   // recompute the property planes of cases whose rho/mu changed
 void launch_coef_uvw(cfdl_ctx *ctx);
-void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused
+void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused, 5 = energy t, phi
 void launch_calc_mip(cfdl_ctx *ctx, int rhie_chow);
 void launch_coef_p(cfdl_ctx *ctx);
 void launch_adjust_pc(cfdl_ctx *ctx);
 void launch_update_uvwp(cfdl_ctx *ctx);
 void launch_update_time(cfdl_ctx *ctx);
 void launch_set_mip0(cfdl_ctx *ctx);
+
+// energy equation (cfdl_energy.cu)
+bool energy_on(const cfdl_ctx *ctx);          // some case of the context has it
+void launch_energy_bc(cfdl_ctx *ctx);
+void launch_energy_time(cfdl_ctx *ctx, bool run_due);   // run_due: only cases whose run cadence is due
+void launch_coef_energy(cfdl_ctx *ctx);
+int solve_energy_all(cfdl_ctx *ctx);
+int solve_energy_phi(cfdl_ctx *ctx);          // the phi solve alone (cfdl_solvers.cu)
+void energy_iter(cfdl_ctx *ctx);
+int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t_init);
 
 // event profiler (cfdl_prof.cpp)
 bool prof_wants(cfdl_ctx *ctx, const char *name);

@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
 
 // ---------------------------------------------------------------------------
 // calc_grad, mod_solver.f90:40-81, as the stencil sum grad = sum_k G_k dphi_k.
-// NF fields at once (u,v,w share the stencil loads).
+// NF fields at once (u,v,w or the energy equation's t and phi share the
+// stencil loads).
 // ---------------------------------------------------------------------------
 template <int NF>
 __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int field) {
@@ -201,7 +202,10 @@ __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ case
     const double *phi[NF];
     double *grad[NF];
     if (NF == 3) { phi[0] = C.u; phi[1 % NF] = C.v; phi[2 % NF] = C.w; grad[0] = C.gu; grad[1 % NF] = C.gv; grad[2 % NF] = C.gw; }
-    else {
+    else if (NF == 2) {
+        if (!C.ee) return;                  // no energy equation in this case
+        phi[0] = C.et; phi[1 % NF] = C.ee; grad[0] = C.egt; grad[1 % NF] = C.ege;
+    } else {
         phi[0] = field == 0 ? C.u : field == 1 ? C.v : field == 2 ? C.w : C.phic;
         grad[0] = field == 0 ? C.gu : field == 1 ? C.gv : field == 2 ? C.gw : C.gpc;
     }
@@ -369,7 +373,10 @@ __global__ void __launch_bounds__(kTile) k_copy_mip0(const CaseDev *__restrict__
 
 }  // namespace
 
-void launch_bc(cfdl_ctx *ctx) { CFDL_LAUNCH("k_bc", k_bc, halos); }
+void launch_bc(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_bc", k_bc, halos);
+    launch_energy_bc(ctx);                  // mod_physics.f90:47
+}
 void ensure_face_props(cfdl_ctx *ctx) {
     bool dirty = false;
     for (HostCase *hc : ctx->cases) dirty |= hc->props_dirty;
@@ -384,6 +391,7 @@ void launch_coef_uvw(cfdl_ctx *ctx) {
 }
 void launch_grad(cfdl_ctx *ctx, int field) {
     if (field == 4) CFDL_LAUNCH("k_grad3", k_grad<3>, cells, 0);
+    else if (field == 5) CFDL_LAUNCH("k_grad2", k_grad<2>, cells, 0);
     else CFDL_LAUNCH("k_grad1", k_grad<1>, cells, field);
 }
 void launch_calc_mip(cfdl_ctx *ctx, int rc) {
@@ -414,6 +422,7 @@ void launch_update_time(cfdl_ctx *ctx) {
     CFDL_LAUNCH("k_update_time", k_update_time, cells);
     CFDL_LAUNCH("k_update_time_halo", k_update_time_halo, halos);
     CFDL_LAUNCH("k_copy_mip0", k_copy_mip0, faces);
+    launch_energy_time(ctx, false);         // mod_physics.f90:111
 }
 void launch_set_mip0(cfdl_ctx *ctx) { CFDL_LAUNCH("k_copy_mip0", k_copy_mip0, faces); }
 

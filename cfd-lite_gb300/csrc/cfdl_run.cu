@@ -130,6 +130,7 @@ void launch_run_end(cfdl_ctx *ctx) {
     CFDL_LAUNCH("k_run_time_cells", k_run_time_cells, cells);
     CFDL_LAUNCH("k_run_time_halos", k_run_time_halos, halos);
     CFDL_LAUNCH("k_run_time_faces", k_run_time_faces, faces);
+    launch_energy_time(ctx, true);
 }
 
 void launch_run_cond(cfdl_ctx *ctx, cudaGraphConditionalHandle h, int consume, unsigned long long *passes) {
@@ -161,7 +162,8 @@ int run_outer(cfdl_ctx *ctx, int max_outer, int *running) {
                                           ctx->stream))))
         return st;
     const int n = (int)ctx->cases.size();
-    if (ctx->use_graph && !prof_active(ctx)) {
+    // the energy equation runs in the eager form (its solve has no graph loop)
+    if (ctx->use_graph && !prof_active(ctx) && !energy_on(ctx)) {
         if ((st = run_graph_launch(ctx))) return st;
     } else {
         for (int k = 0; k < max_outer; k++) {
@@ -175,6 +177,7 @@ int run_outer(cfdl_ctx *ctx, int max_outer, int *running) {
             launch_run_begin(ctx);
             launch_bc(ctx);
             if ((st = solve_uvwp_all(ctx))) return st;
+            if ((st = solve_energy_all(ctx))) return st;
             launch_run_end(ctx);
         }
         k_run_count<<<1, 32, 0, ctx->stream>>>(ctx->d_cases, n, ctx->d_run_ctl);

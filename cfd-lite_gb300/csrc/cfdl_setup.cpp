@@ -342,6 +342,7 @@ extern "C" int cfdl_setup_mesh(const cfdl_setup *s, double u_lid, cfdl_mesh *mes
     s->bc_esec.assign(2 * (size_t)s->nintf, 0);
     s->bc_kind.assign(s->nintf, 0);
     s->bc_vel.assign(3 * (size_t)s->nintf, 0.0);
+    s->bc_temp.assign(s->nintf, 0.0);
     for (int b = 0; b < 6; b++) {
         for (int i = 0; i < s->nintf; i++) {
             int sec = s->intf2sec[i];
@@ -355,6 +356,8 @@ extern "C" int cfdl_setup_mesh(const cfdl_setup *s, double u_lid, cfdl_mesh *mes
                 s->bc_vel[3 * i] = b == 0 ? u_lid : 0.0;
                 s->bc_vel[3 * i + 1] = 0.0;
                 s->bc_vel[3 * i + 2] = 0.0;
+                // construct_energy's binding (mod_energy.f90:40-45): lid 373, dirichlet0 273
+                s->bc_temp[i] = b == 0 ? 373.0 : 273.0;
             }
         }
     }
@@ -365,6 +368,7 @@ extern "C" int cfdl_setup_mesh(const cfdl_setup *s, double u_lid, cfdl_mesh *mes
     mesh->xc = s->xc.data(); mesh->yc = s->yc.data(); mesh->zc = s->zc.data(); mesh->vol = s->vol.data();
     mesh->nbc = s->nintf; mesh->bc_esec = s->bc_esec.data(); mesh->bc_kind = s->bc_kind.data();
     mesh->bc_vel = s->bc_vel.data();
+    mesh->bc_temp = s->bc_temp.data();
     return CFDL_OK;
 }
 

@@ -67,7 +67,7 @@ struct cfdl_setup {
     std::vector<double> aip, rip, xc, yc, zc, vol;
     // boundary-condition binding produced by cfdl_setup_mesh
     mutable std::vector<int> bc_esec, bc_kind;
-    mutable std::vector<double> bc_vel;
+    mutable std::vector<double> bc_vel, bc_temp;
 };
 
 namespace cfdl_setup_detail {

@@ -131,41 +131,59 @@ __global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict
     }
 }
 
-// The BiCGStab vectors and operator of a case's momentum solve, [3][ne] per
-// vector.  FP64: the solve updates u, v, w in place.  FP32 (precision 2): the
-// solve finds the correction d of A d = r (r the FP64 residual of k_mom_init)
-// in single precision, in the first halves of the FP64 vectors' storage, and
-// k_mom_apply adds it to u, v, w in FP64.
+// The BiCGStab vectors and operator of a case's solve, [NC][ne] per vector.
+// NC = 3, the momentum solve: FP64 updates u, v, w in place; FP32
+// (precision 2) finds the correction d of A d = r (r the FP64 residual of
+// k_mom_init) in single precision, in the first halves of the FP64 vectors'
+// storage, and k_mom_apply adds it to u, v, w in FP64.  NC = 1, the energy
+// solve (cfdl_energy.cu): FP64, phi = C.ee in place, plane 0 of the vectors.
 template <class T> struct MomVec {
     T *r, *rh, *p, *ph, *v, *s, *sh, *t;
     T *x[3];
     const T *a, *ap, *rap;
 };
-template <class T> __device__ __forceinline__ MomVec<T> mom_vec(const CaseDev &C);
-template <> __device__ __forceinline__ MomVec<double> mom_vec<double>(const CaseDev &C) {
+template <class T, int NC> __device__ __forceinline__ MomVec<T> mom_vec(const CaseDev &C);
+template <> __device__ __forceinline__ MomVec<double> mom_vec<double, 3>(const CaseDev &C) {
     return {C.kr, C.krh, C.kp, C.kph, C.kv, C.ks, C.ksh, C.kt, {C.u, C.v, C.w}, C.anb, C.ap, C.rap};
 }
-template <> __device__ __forceinline__ MomVec<float> mom_vec<float>(const CaseDev &C) {
+template <> __device__ __forceinline__ MomVec<float> mom_vec<float, 3>(const CaseDev &C) {
     const int ne = C.ne;
     float *xf = (float *)C.kt + 3 * (size_t)ne;   // second half of kt's storage
     return {(float *)C.kr, (float *)C.krh, (float *)C.kp, (float *)C.kph, (float *)C.kv, (float *)C.ks,
             (float *)C.ksh, (float *)C.kt, {xf, xf + ne, xf + 2 * (size_t)ne}, C.fanb, C.fdiag, C.frap};
 }
+template <> __device__ __forceinline__ MomVec<double> mom_vec<double, 1>(const CaseDev &C) {
+    return {C.kr, C.krh, C.kp, C.kph, C.kv, C.ks, C.ksh, C.kt, {C.ee, nullptr, nullptr}, C.anb, C.ap, C.rap};
+}
+
+// the lanes of the solve: momentum u, v, w or the energy lane
+template <int NC> __device__ __forceinline__ KLanes *lanes(SolveScalars *S) { return NC == 3 ? (KLanes *)S : &S->en; }
+template <int NC> __device__ __forceinline__ bool lanes_active(const KLanes *L) {
+    int a = 0;
+#pragma unroll
+    for (int q = 0; q < NC; q++) a |= L->active[q];
+    return a != 0;
+}
 
 // p = r + beta (p - omega v); ph = p / ap
-template <class T>
+template <class T, int NC>
 __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
-    if (!any_active(S)) return;
-    const MomVec<T> M = mom_vec<T>(C);
+    const KLanes *L = lanes<NC>(S);
+    if (!lanes_active<NC>(L)) return;
+    const MomVec<T> M = mom_vec<T, NC>(C);
     // the iteration's scalars, read once
-    const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    const bool first[3] = {S->iters[0] == 0, S->iters[1] == 0, S->iters[2] == 0};
-    const T be[3] = {(T)S->beta[0], (T)S->beta[1], (T)S->beta[2]}, om[3] = {(T)S->omega[0], (T)S->omega[1], (T)S->omega[2]};
+    int act[NC];
+    bool first[NC];
+    T be[NC], om[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        act[q] = L->active[q]; first[q] = L->iters[q] == 0; be[q] = (T)L->beta[q]; om[q] = (T)L->omega[q];
+    }
     FOR_CELLS(t) {
         const T rap = M.rap[i];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < NC; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
             const T pn = first[q] ? M.r[j] : M.r[j] + be[q] * (M.p[j] - om[q] * M.v[j]);
@@ -176,53 +194,58 @@ __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cas
 }
 
 // v = A ph; alpha = rho / (rh, v)
-template <class T>
+template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
-    if (!any_active(S)) return;
-    const MomVec<T> M = mom_vec<T>(C);
-    T v[3] = {0, 0, 0};
-    const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    FOR_CELLS(t) {
-        T y[3];   // one pass over the row for the three components
-        ell_row<3, T>(C.hf_nb, M.a, M.ap[i], M.ph, ne, ne, C.W, i, y);
+    KLanes *L = lanes<NC>(S);
+    if (!lanes_active<NC>(L)) return;
+    const MomVec<T> M = mom_vec<T, NC>(C);
+    T v[NC];
+    int act[NC];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+    for (int q = 0; q < NC; q++) { v[q] = 0; act[q] = L->active[q]; }
+    FOR_CELLS(t) {
+        T y[NC];   // one pass over the row for the components
+        ell_row<NC, T>(C.hf_nb, M.a, M.ap[i], M.ph, ne, ne, C.W, i, y);
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
             if (!act[q]) continue;
             M.v[q * ne + i] = y[q];
             v[q] += M.rh[q * ne + i] * y[q];
         }
     }
-    block_reduce<3, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<NC, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M2], cnt[t.c])) {
-        __shared__ T s[3];
-        sum_partials<3, T>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[NC];
+        sum_partials<NC, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
-            for (int q = 0; q < 3; q++) {
-                if (!S->active[q]) continue;
+            for (int q = 0; q < NC; q++) {
+                if (!L->active[q]) continue;
                 const double sq = (double)s[q];
-                const double a = S->rho[q] / sq;
-                if (sq == 0.0 || !isfinite(a)) { S->active[q] = 0; S->status[q] = isfinite(a) || sq == 0.0 ? S->status[q] : CFDL_ERR_NONFINITE; continue; }
-                S->alpha[q] = a;
+                const double a = L->rho[q] / sq;
+                if (sq == 0.0 || !isfinite(a)) { L->active[q] = 0; L->status[q] = isfinite(a) || sq == 0.0 ? L->status[q] : CFDL_ERR_NONFINITE; continue; }
+                L->alpha[q] = a;
             }
     }
 }
 
 // s = r - alpha v; sh = s / ap; early exit when ||s|| <= tol
-template <class T>
+template <class T, int NC>
 __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
-    if (!any_active(S)) return;
-    const MomVec<T> M = mom_vec<T>(C);
-    T v[3] = {0, 0, 0};
-    const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    const T al[3] = {(T)S->alpha[0], (T)S->alpha[1], (T)S->alpha[2]};
+    KLanes *L = lanes<NC>(S);
+    if (!lanes_active<NC>(L)) return;
+    const MomVec<T> M = mom_vec<T, NC>(C);
+    T v[NC], al[NC];
+    int act[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) { v[q] = 0; act[q] = L->active[q]; al[q] = (T)L->alpha[q]; }
     FOR_CELLS(t) {
         const T rap = M.rap[i];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < NC; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
             const T sv = M.r[j] - al[q] * M.v[j];
@@ -231,65 +254,72 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
             v[q] += sv * sv;
         }
     }
-    block_reduce<3, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<NC, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M3], cnt[t.c])) {
-        __shared__ T s[3];
-        sum_partials<3, T>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[NC];
+        sum_partials<NC, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
-            for (int q = 0; q < 3; q++) {
-                if (!S->active[q]) continue;
-                S->half[q] = sqrt((double)s[q]) <= S->tol[q];
+            for (int q = 0; q < NC; q++) {
+                if (!L->active[q]) continue;
+                L->half[q] = sqrt((double)s[q]) <= L->tol[q];
             }
     }
 }
 
 // t = A sh; omega = (t,s)/(t,t)
-template <class T>
+template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
-    if (!any_active(S)) return;
-    const MomVec<T> M = mom_vec<T>(C);
-    T v[6] = {0, 0, 0, 0, 0, 0};
-    const int act[3] = {S->active[0] && !S->half[0], S->active[1] && !S->half[1], S->active[2] && !S->half[2]};
-    FOR_CELLS(t) {
-        T y[3];
-        ell_row<3, T>(C.hf_nb, M.a, M.ap[i], M.sh, ne, ne, C.W, i, y);
+    KLanes *L = lanes<NC>(S);
+    if (!lanes_active<NC>(L)) return;
+    const MomVec<T> M = mom_vec<T, NC>(C);
+    T v[2 * NC];
+    int act[NC];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+    for (int q = 0; q < NC; q++) { v[q] = v[NC + q] = 0; act[q] = L->active[q] && !L->half[q]; }
+    FOR_CELLS(t) {
+        T y[NC];
+        ell_row<NC, T>(C.hf_nb, M.a, M.ap[i], M.sh, ne, ne, C.W, i, y);
+#pragma unroll
+        for (int q = 0; q < NC; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
             M.t[j] = y[q];
             v[q] += y[q] * M.s[j];
-            v[3 + q] += y[q] * y[q];
+            v[NC + q] += y[q] * y[q];
         }
     }
-    block_reduce<6, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<2 * NC, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M4], cnt[t.c])) {
-        __shared__ T s[6];
-        sum_partials<6, T>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[2 * NC];
+        sum_partials<2 * NC, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0)
-            for (int q = 0; q < 3; q++) {
-                if (!S->active[q]) continue;
-                const double ts = (double)s[q], tt = (double)s[3 + q];
-                S->omega[q] = S->half[q] ? 0.0 : (tt > 0.0 ? ts / tt : 0.0);
+            for (int q = 0; q < NC; q++) {
+                if (!L->active[q]) continue;
+                const double ts = (double)s[q], tt = (double)s[NC + q];
+                L->omega[q] = L->half[q] ? 0.0 : (tt > 0.0 ? ts / tt : 0.0);
             }
     }
 }
 
 // x += alpha ph + omega sh; r = s - omega t; rho' = (rh, r); beta
-template <class T>
+template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
     TILE_HEAD
-    if (!any_active(S)) return;
-    const MomVec<T> M = mom_vec<T>(C);
-    T v[6] = {0, 0, 0, 0, 0, 0};
-    const int act[3] = {S->active[0], S->active[1], S->active[2]};
-    const T al[3] = {(T)S->alpha[0], (T)S->alpha[1], (T)S->alpha[2]}, om[3] = {(T)S->omega[0], (T)S->omega[1], (T)S->omega[2]};
+    KLanes *L = lanes<NC>(S);
+    if (!lanes_active<NC>(L)) return;
+    const MomVec<T> M = mom_vec<T, NC>(C);
+    T v[2 * NC], al[NC], om[NC];
+    int act[NC];
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        v[q] = v[NC + q] = 0; act[q] = L->active[q]; al[q] = (T)L->alpha[q]; om[q] = (T)L->omega[q];
+    }
     FOR_CELLS(t) {
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < NC; q++) {
             if (!act[q]) continue;
             const int j = q * ne + i;
             T *__restrict__ x = M.x[q];
@@ -297,29 +327,83 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
             const T r = om[q] == (T)0 ? M.s[j] : M.s[j] - om[q] * M.t[j];
             M.r[j] = r;
             v[q] += r * r;
-            v[3 + q] += M.rh[j] * r;
+            v[NC + q] += M.rh[j] * r;
         }
     }
-    block_reduce<6, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    block_reduce<2 * NC, T>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M5], cnt[t.c])) {
-        __shared__ T s[6];
-        sum_partials<6, T>(partials, cfirst[t.c], cnt[t.c], s);
+        __shared__ T s[2 * NC];
+        sum_partials<2 * NC, T>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0) {
             const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
-            for (int q = 0; q < 3; q++) {
-                if (!S->active[q]) continue;
-                const double rn = sqrt((double)s[q]), rho_new = (double)s[3 + q];
-                S->rnorm[q] = rn;
-                S->iters[q] += 1;
-                const double om = S->omega[q];
-                S->beta[q] = (om != 0.0 && S->rho[q] != 0.0) ? (rho_new / S->rho[q]) * (S->alpha[q] / om) : 0.0;
-                S->rho[q] = rho_new;
-                int act = rn > S->tol[q];
-                if (!isfinite(rn)) { act = 0; S->status[q] = CFDL_ERR_NONFINITE; }
+            for (int q = 0; q < NC; q++) {
+                if (!L->active[q]) continue;
+                const double rn = sqrt((double)s[q]), rho_new = (double)s[NC + q];
+                L->rnorm[q] = rn;
+                L->iters[q] += 1;
+                const double om = L->omega[q];
+                L->beta[q] = (om != 0.0 && L->rho[q] != 0.0) ? (rho_new / L->rho[q]) * (L->alpha[q] / om) : 0.0;
+                L->rho[q] = rho_new;
+                int act = rn > L->tol[q];
+                if (!isfinite(rn)) { act = 0; L->status[q] = CFDL_ERR_NONFINITE; }
                 else if (act && (om == 0.0 || rho_new == 0.0)) act = 0;           // breakdown: stop here
-                else if (act && S->iters[q] >= cap) { act = 0; if (C.solve_mode == 1) S->status[q] = CFDL_ERR_ITER_CAP; }
-                S->active[q] = act;
+                else if (act && L->iters[q] >= cap) { act = 0; if (C.solve_mode == 1) L->status[q] = CFDL_ERR_ITER_CAP; }
+                L->active[q] = act;
             }
+        }
+    }
+}
+
+// ------------------------------- energy -----------------------------------
+// init of the phi solve of solve_energy (mod_energy.f90:75): b' = b +
+// sum_bdry anb*phi_halo, r = b' - A phi, rh = r; cases without the energy
+// equation contribute nothing and stay inactive.
+template <int W>
+__device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, double (&v)[2]) {
+    const double api = C.ap[i];
+    C.rap[i] = 1.0 / api;
+    const double *__restrict__ phi = C.ee;
+    double bb = C.b[i], s = api * phi[i];
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const int j = C.hf_nb[k * ne + i];
+        if (j < 0) continue;
+        const double a = C.anb[k * ne + i];
+        if (j >= ne) bb += a * phi[j];
+        else s -= a * phi[j];
+    }
+    const double r = bb - s;
+    C.kr[i] = r;
+    C.krh[i] = r;
+    v[0] += bb * bb;
+    v[1] += r * r;
+}
+
+__global__ void __launch_bounds__(kTile, 3) k_en_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
+                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    TILE_HEAD
+    double v[2] = {0, 0};
+    if (C.ee) {
+        if (C.W == 6) { FOR_CELLS(t) en_init_row<6>(C, i, ne, v); }
+        else if (C.W == 4) { FOR_CELLS(t) en_init_row<4>(C, i, ne, v); }
+        else { FOR_CELLS(t) en_init_row<kMaxW>(C, i, ne, v); }
+    }
+    block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
+    if (last_tile_of_case(&C.counters[CNT_M1], cnt[t.c])) {
+        __shared__ double s[2];
+        sum_partials<2>(partials, cfirst[t.c], cnt[t.c], s);
+        if (threadIdx.x == 0) {
+            KLanes *L = &S->en;
+            const int cap = C.solve_mode == 0 ? C.nit : C.tight_maxit;
+            L->bnorm[0] = sqrt(s[0]);
+            L->r0norm[0] = L->rnorm[0] = sqrt(s[1]);
+            L->rho[0] = s[1];
+            L->alpha[0] = 1.0; L->omega[0] = 1.0; L->beta[0] = 0.0; L->half[0] = 0;
+            L->iters[0] = 0; L->status[0] = 0;
+            L->tol[0] = C.solve_mode == 0 ? C.rtol_u * L->r0norm[0] : C.tight_rtol * L->bnorm[0];
+            L->active[0] = C.ee != nullptr && L->r0norm[0] > L->tol[0] && cap > 0;
+            if (!isfinite(L->r0norm[0]) || !isfinite(L->bnorm[0])) { L->active[0] = 0; L->status[0] = CFDL_ERR_NONFINITE; }
+            L->active[1] = L->active[2] = 0;
         }
     }
 }
@@ -327,7 +411,7 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
 // precision 2: u, v, w += the FP32 correction of the momentum solve
 __global__ void __launch_bounds__(kTile) k_mom_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_HEAD
-    const MomVec<float> M = mom_vec<float>(C);
+    const MomVec<float> M = mom_vec<float, 3>(C);
     double *xs[3] = {C.u, C.v, C.w};
     FOR_CELLS(t) {
 #pragma unroll
@@ -439,7 +523,8 @@ __global__ void __launch_bounds__(kTile) k_pc_p(const CaseDev *__restrict__ case
 }
 
 // Per-case activity flag and iteration count for the host poll.
-// kind 0 momentum, 1 pressure CG, 2 mixed inner CG, 3 mixed outer refinement.
+// kind 0 momentum, 1 pressure CG, 2 mixed inner CG, 3 mixed outer refinement,
+// 4 energy.
 __global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags, int kind) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncases) return;
@@ -448,7 +533,8 @@ __global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags
     if (kind == 0) { act = any_active(S); its = max(S->iters[0], max(S->iters[1], S->iters[2])); }
     else if (kind == 1) { act = S->active_p; its = S->iters_p; }
     else if (kind == 2) { act = S->active32; its = S->iters32; }
-    else { act = S->active_p; its = S->outer_p; }
+    else if (kind == 3) { act = S->active_p; its = S->outer_p; }
+    else { act = S->en.active[0]; its = S->en.iters[0]; }
     flags[2 * c] = act != 0;
     flags[2 * c + 1] = its;
 }
@@ -493,18 +579,45 @@ void mom_init(cfdl_ctx *ctx) { CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED
 
 void mom_iter(cfdl_ctx *ctx) {
     if (ctx->cases[0]->cfg.precision == 2) {
-        CFDL_LAUNCH("k_mom_p", k_mom_p<float>, cellsv);
-        CFDL_LAUNCH("k_mom_v", k_mom_v<float>, cellsv, RED32);
-        CFDL_LAUNCH("k_mom_s", k_mom_s<float>, cellsv, RED32);
-        CFDL_LAUNCH("k_mom_t", k_mom_t<float>, cellsv, RED32);
-        CFDL_LAUNCH("k_mom_x", k_mom_x<float>, cellsv, RED32);
+        CFDL_LAUNCH("k_mom_p", (k_mom_p<float, 3>), cellsv);
+        CFDL_LAUNCH("k_mom_v", (k_mom_v<float, 3>), cellsv, RED32);
+        CFDL_LAUNCH("k_mom_s", (k_mom_s<float, 3>), cellsv, RED32);
+        CFDL_LAUNCH("k_mom_t", (k_mom_t<float, 3>), cellsv, RED32);
+        CFDL_LAUNCH("k_mom_x", (k_mom_x<float, 3>), cellsv, RED32);
         return;
     }
-    CFDL_LAUNCH("k_mom_p", k_mom_p<double>, cellsv);
-    CFDL_LAUNCH("k_mom_v", k_mom_v<double>, cellsv, RED);
-    CFDL_LAUNCH("k_mom_s", k_mom_s<double>, cellsv, RED);
-    CFDL_LAUNCH("k_mom_t", k_mom_t<double>, cellsv, RED);
-    CFDL_LAUNCH("k_mom_x", k_mom_x<double>, cellsv, RED);
+    CFDL_LAUNCH("k_mom_p", (k_mom_p<double, 3>), cellsv);
+    CFDL_LAUNCH("k_mom_v", (k_mom_v<double, 3>), cellsv, RED);
+    CFDL_LAUNCH("k_mom_s", (k_mom_s<double, 3>), cellsv, RED);
+    CFDL_LAUNCH("k_mom_t", (k_mom_t<double, 3>), cellsv, RED);
+    CFDL_LAUNCH("k_mom_x", (k_mom_x<double, 3>), cellsv, RED);
+}
+
+// Jacobi-preconditioned BiCGStab on the energy system, with the momentum
+// solve's kernels on one right-hand side and the energy lane
+int solve_energy_phi(cfdl_ctx *ctx) {
+    if (ctx->cells.ntiles == 0) return CFDL_OK;
+    CFDL_LAUNCH("k_en_init", k_en_init, cellsv, RED);
+    const int cap = max_cap(ctx);
+    int it = 0, maxit = 0;
+    while (it < cap) {
+        const int chunk = poll_chunk(it, ctx->last_iters_e);
+        for (int k = 0; k < chunk && it < cap; k++, it++) energy_iter(ctx);
+        int a = poll_kind(ctx, 4, &maxit);
+        if (a < 0) return CFDL_ERR_CUDA;
+        if (a == 0) break;
+    }
+    ctx->last_iters_e = maxit;
+    return cuda_status(cudaGetLastError());
+}
+
+// one BiCGStab iteration of the energy solve (one right-hand side, FP64)
+void energy_iter(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_en_p", (k_mom_p<double, 1>), cellsv);
+    CFDL_LAUNCH("k_en_v", (k_mom_v<double, 1>), cellsv, RED);
+    CFDL_LAUNCH("k_en_s", (k_mom_s<double, 1>), cellsv, RED);
+    CFDL_LAUNCH("k_en_t", (k_mom_t<double, 1>), cellsv, RED);
+    CFDL_LAUNCH("k_en_x", (k_mom_x<double, 1>), cellsv, RED);
 }
 
 // the end of the momentum solve: precision 2 applies its FP32 correction
@@ -573,8 +686,11 @@ int read_stats(cfdl_ctx *ctx, int c, cfdl_stats *st) {
     st->run_left = S.run_left;
     st->converged = S.converged;
     st->mass_ratio = S.mass_ratio;
+    st->it_e = S.en.iters[0];
+    st->res_e[0] = S.en.r0norm[0]; st->res_e[1] = S.en.rnorm[0];
     st->status = 0;
     for (int q = 0; q < 3; q++) if (S.status[q]) st->status = S.status[q];
+    if (S.en.status[0]) st->status = S.en.status[0];
     if (S.status_p) st->status = S.status_p;
     return CFDL_OK;
 }

@@ -1,15 +1,17 @@
 // cfdl_vtu.cpp -- headless VTU output of a case's fields, in the format of
 // the reference's write_vtubin (src/modules/mod_vtu_output.f90:6-328).
 //
-// The fields are read from the device (u, v, w, p, gpc, mip); the file is the
-// reference's byte layout: an XML header naming each DataArray's offset into
-// the appended block, then, after '_', each array as a UInt64 byte count and
-// its raw little-endian values.  Cell data, in order: u, v, w, p (Float64),
-// gpc (3 components), and under the name "mip" the net face mass flux of each
-// cell (sum over its half-faces of mip(fg) times the sign of fg; the reference
-// computes it into eqn%dc, mod_vtu_output.f90:113-123 -- here it goes to the
-// file only and the device coefficients are left alone).  Then the vertices,
-// the volume elements' connectivity (0-based), offsets and VTK cell types.
+// The fields are read from the device; the file is the reference's byte
+// layout: an XML header naming each DataArray's offset into the appended
+// block, then, after '_', each array as a UInt64 byte count and its raw
+// little-endian values.  Cell data of the uvwp equation, in order: u, v, w, p
+// (Float64), gpc (3 components), and under the name "mip" the net face mass
+// flux of each cell (sum over its half-faces of mip(fg) times the sign of fg;
+// the reference computes it into eqn%dc, mod_vtu_output.f90:113-123 -- here
+// it goes to the file only and the device coefficients are left alone).  Cell
+// data of the energy equation (mod_vtu_output.f90:124-132): enthalpy (phi),
+// grad_enthalpy, temperature, grad_temperature.  Then the vertices, the volume
+// elements' connectivity (0-based), offsets and VTK cell types.
 #include "cfdl_internal.h"
 #include "cfdl_setup_int.h"
 #include <cstdio>
@@ -45,29 +47,44 @@ struct Out {
     void u64(unsigned long long v) { raw(&v, 1); }
 };
 
+struct Var { const char *name; int dim; const double *a; };
+
+HostCase *find_case(cfdl_ctx *ctx, int case_id, const cfdl_setup *s) {
+    for (HostCase *hc : ctx->cases)
+        if (hc->id == case_id)
+            return hc->ne == s->ne && hc->nf == s->nf && hc->nbf == s->nbf ? hc : nullptr;
+    return nullptr;
+}
+
+bool sections_writable(const cfdl_setup *s) {
+    for (int q = 0; q < s->nsec; q++)
+        if (s->etype[q] >= 10 && vtk_type(s->etype[q]) < 0) return false;   // the reference stops here
+    return true;
+}
+
+// device arrays -> host vectors, one copy each
+int fetch(cfdl_ctx *ctx, std::vector<std::vector<double> *> dst, std::vector<const double *> src) {
+    for (size_t k = 0; k < dst.size(); k++) {
+        cudaError_t e = cudaMemcpyAsync(dst[k]->data(), src[k], dst[k]->size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    return cuda_status(cudaStreamSynchronize(ctx->stream));
+}
+
+int write_vtubin(const cfdl_setup *s, const Var *vars, int nvar, const char *path);
+
 }  // namespace
 
 extern "C" int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, const char *path) {
     if (!ctx || !s || !path) return CFDL_ERR_INVALID;
-    int c = -1;
-    for (size_t k = 0; k < ctx->cases.size(); k++) if (ctx->cases[k]->id == case_id) c = (int)k;
-    if (c < 0) return CFDL_ERR_INVALID;
-    HostCase *hc = ctx->cases[c];
-    if (hc->ne != s->ne || hc->nf != s->nf || hc->nbf != s->nbf) return CFDL_ERR_INVALID;
+    HostCase *hc = find_case(ctx, case_id, s);
+    if (!hc || !sections_writable(s)) return CFDL_ERR_INVALID;
     const int ne = s->ne, nc = ne + s->nbf;
-    for (int q = 0; q < s->nsec; q++)
-        if (s->etype[q] >= 10 && vtk_type(s->etype[q]) < 0) return CFDL_ERR_INVALID;   // the reference stops here
     // the case's fields, from the device
     std::vector<double> u(nc), v(nc), w(nc), p(nc), gpc(3 * (size_t)nc), mip(s->nf);
     const CaseDev &d = hc->dev;
-    struct Cp { double *h; const double *dv; size_t n; } cps[] = {
-        {u.data(), d.u, (size_t)nc}, {v.data(), d.v, (size_t)nc}, {w.data(), d.w, (size_t)nc}, {p.data(), d.p, (size_t)nc},
-        {gpc.data(), d.gpc, 3 * (size_t)nc}, {mip.data(), d.mip, (size_t)s->nf}};
-    for (const Cp &q : cps) {
-        cudaError_t e = cudaMemcpyAsync(q.h, q.dv, q.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-        if (e != cudaSuccess) return cuda_status(e);
-    }
-    int st = cuda_status(cudaStreamSynchronize(ctx->stream));
+    int st = fetch(ctx, {&u, &v, &w, &p, &gpc, &mip}, {d.u, d.v, d.w, d.p, d.gpc, d.mip});
     if (st) return st;
     // net face mass flux per cell, in half-face order (mod_vtu_output.f90:113-123)
     std::vector<double> net(ne, 0.0);
@@ -78,9 +95,30 @@ extern "C" int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, c
             fg = std::abs(fg);
             net[e] = net[e] + mip[fg - 1] * sg;
         }
-    struct Var { const char *name; int dim; const double *a; } vars[6] = {
+    const Var vars[6] = {
         {"u", 1, u.data()}, {"v", 1, v.data()}, {"w", 1, w.data()}, {"p", 1, p.data()}, {"gpc", 3, gpc.data()},
         {"mip", 1, net.data()}};
+    return write_vtubin(s, vars, 6, path);
+}
+
+extern "C" int cfdl_write_vtu_energy(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, const char *path) {
+    if (!ctx || !s || !path) return CFDL_ERR_INVALID;
+    HostCase *hc = find_case(ctx, case_id, s);
+    if (!hc || !hc->dev.ee || !sections_writable(s)) return CFDL_ERR_INVALID;
+    const size_t nc = (size_t)s->ne + s->nbf;
+    std::vector<double> e(nc), ge(3 * nc), t(nc), gt(3 * nc);
+    const CaseDev &d = hc->dev;
+    int st = fetch(ctx, {&e, &ge, &t, &gt}, {d.ee, d.ege, d.et, d.egt});
+    if (st) return st;
+    const Var vars[4] = {{"enthalpy", 1, e.data()}, {"grad_enthalpy", 3, ge.data()}, {"temperature", 1, t.data()},
+                         {"grad_temperature", 3, gt.data()}};
+    return write_vtubin(s, vars, 4, path);
+}
+
+namespace {
+
+int write_vtubin(const cfdl_setup *s, const Var *vars, int nvar, const char *path) {
+    const int ne = s->ne;
     // volume sections, as the reference walks them
     long long nconn = 0, ncell = 0;
     for (int q = 0; q < s->nsec; q++) {
@@ -99,8 +137,8 @@ extern "C" int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, c
     o.str(" <UnstructuredGrid>" + lf);
     o.str("  <Piece NumberOfPoints=\"" + std::to_string(s->nvx) + "\" NumberOfCells=\"" + std::to_string(ne) + "\">" + lf);
     o.str("   <CellData Scalars=\"scalars\">" + lf);
-    unsigned long long nbytes[6];
-    for (int k = 0; k < 6; k++) {
+    std::vector<unsigned long long> nbytes(nvar);
+    for (int k = 0; k < nvar; k++) {
         o.str("    <DataArray type=\"Float64\" Name=\"" + std::string(vars[k].name) + "\" NumberOfComponents=\"" +
               std::to_string(vars[k].dim) + "\" format=\"appended\" offset=\"" + i12(noffset) + "\" />" + lf);
         nbytes[k] = (unsigned long long)ne * vars[k].dim * 8;
@@ -124,7 +162,7 @@ extern "C" int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, c
     o.str(" </UnstructuredGrid>" + lf);
     o.str(" <AppendedData encoding=\"raw\">" + lf);
     o.str("_");
-    for (int k = 0; k < 6; k++) {
+    for (int k = 0; k < nvar; k++) {
         o.u64(nbytes[k]);
         for (int q = 0; q < s->nsec; q++) {
             if (s->etype[q] < 10) continue;
@@ -162,3 +200,5 @@ extern "C" int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *s, c
     const bool ok = o.ok && fclose(f) == 0;
     return ok ? CFDL_OK : CFDL_ERR_INVALID;
 }
+
+}  // namespace

@@ -80,6 +80,9 @@ typedef struct cfdl_mesh {
     const int *bc_esec;          /* [2nbc] halo element range of each bc      */
     const int *bc_kind;          /* [nbc]  CFDL_BC_*                          */
     const double *bc_vel;        /* [3nbc] wall velocity (lid: (U,0,0))       */
+    const double *bc_temp;       /* [nbc] wall temperature of the energy BCs
+                                    (lid 373, dirichlet0 273; mod_energy.f90:
+                                    173-212); NULL: no energy equation        */
 } cfdl_mesh;
 
 int cfdl_setup_create(int nvx, const double *x, const double *y, const double *z,
@@ -97,7 +100,9 @@ int cfdl_setup_create_device(int nvx, const double *x, const double *y, const do
 int cfdl_setup_sizes(const cfdl_setup *s, int *sizes);
 /* Fill a cfdl_mesh whose pointers stay valid until cfdl_setup_destroy.
  * Boundary conditions are bound by section name as construct_uvwp does:
- * 'top' -> moving wall (u_lid,0,0), every other 2D section -> wall at rest. */
+ * 'top' -> moving wall (u_lid,0,0), every other 2D section -> wall at rest;
+ * the energy BCs as construct_energy binds them: 'top' -> lid (373), every
+ * other section -> dirichlet0 (273). */
 int cfdl_setup_mesh(const cfdl_setup *s, double u_lid, cfdl_mesh *mesh);
 /* Copy out named integer arrays: ef2nb1, ef2nb2, ef2nb_idx, s2g, bs, esec,
  * etype, red (calc_redblack order, src/setup/mod_meshds_uns.f90:134-204). */
@@ -140,6 +145,9 @@ typedef struct cfdl_stats {
     int    run_left;                 /* outer iterations still to run                 */
     int    converged;                /* 1 once mass_ratio <= the run's tolerance      */
     double mass_ratio;               /* mass_imbalance / sum_f |mip_f| after the pass */
+    /* the last energy solve (cfdl_solve_energy) */
+    int    it_e;                     /* inner iterations                              */
+    double res_e[2];                 /* initial and final residual 2-norms            */
 } cfdl_stats;
 
 /* Fields in reference layout (host pointers; NULL members are skipped). */
@@ -180,7 +188,8 @@ int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_s
 /* ---- individual routines, for per-routine replacement and parity ---- */
 int cfdl_calc_coef_uvw(cfdl_ctx *ctx);                   /* mod_uvwp.f90:161-286   */
 int cfdl_solve_momentum(cfdl_ctx *ctx, cfdl_stats *st);  /* mod_uvwp.f90:114-116 (solve_gs x3) */
-/* field: 0 u, 1 v, 2 w, 3 phic; gradient into gu/gv/gw/gpc (mod_solver.f90:40-81) */
+/* field: 0 u, 1 v, 2 w, 3 phic, 5 energy t and phi; gradient into gu/gv/gw/gpc
+ * or gt/ge (mod_solver.f90:40-81) */
 int cfdl_calc_grad(cfdl_ctx *ctx, int field);
 int cfdl_calc_mip(cfdl_ctx *ctx, int rhie_chow);         /* mod_uvwp.f90:438-490   */
 int cfdl_calc_coef_p(cfdl_ctx *ctx);                     /* mod_uvwp.f90:289-368   */
@@ -188,9 +197,31 @@ int cfdl_solve_pc(cfdl_ctx *ctx, cfdl_stats *st);        /* mod_uvwp.f90:126-127
 int cfdl_adjust_pc(cfdl_ctx *ctx);                       /* mod_uvwp.f90:136-158   */
 int cfdl_update_uvwp(cfdl_ctx *ctx);                     /* mod_uvwp.f90:370-436   */
 
+/* ---- energy equation (src/equations/mod_energy.f90) ----
+ * The reference builds it (construct_energy, :14-47) and applies its BCs in
+ * update_boundaries, but its solve is commented out of the time loop
+ * (main.f90:58).  cfdl_energy_init is construct_energy for every case of the
+ * context (cases whose mesh has no bc_temp are refused): properties cp, tc
+ * per cell (reference 1000, 5; mod_properties.f90:88-89), t = t_init
+ * (reference 273), phi = cp*t, phi0 = phi.  From then on
+ * cfdl_update_boundaries also applies the energy BCs (t = wall temperature,
+ * phi = cp(owner)*t on the halos), cfdl_update_time also copies phi0 = phi
+ * (mod_physics.f90:111), and every outer pass of cfdl_step, cfdl_step_host and
+ * cfdl_run solves the energy equation after solve_uvwp, where main.f90:58
+ * has the call.  cfdl_solve_energy is solve_energy (:59-80): calc_grad of t
+ * and phi, calc_coef_energy (:82-169) into ap/anb/b, the phi solve (mode 0:
+ * BiCGStab to the reference's 10x residual drop, mode 1: to tight_rtol), and
+ * calc_temperature t = phi/cp (mod_properties.f90:214-221).  FP64 in every
+ * precision form. */
+int cfdl_energy_init(cfdl_ctx *ctx, double cp, double tc, double t_init);
+int cfdl_solve_energy(cfdl_ctx *ctx, cfdl_stats *st);
+int cfdl_calc_coef_energy(cfdl_ctx *ctx);                /* mod_energy.f90:82-169  */
+
 /* Copy a named device array to/from a host buffer in reference layout.
  * Names: u v w p u0 v0 w0 phic (ne+nbf), gu gv gw gp gpc (3(ne+nbf)),
- * mip mip0 (nf), ap b bu bv bw d dc rho mu (ne), anb (2nf-nbf). */
+ * mip mip0 (nf), ap b bu bv bw d dc rho mu (ne), anb (2nf-nbf); after
+ * cfdl_energy_init also t, e (phi = cp*t), e0 (phi0) (ne+nbf), gt, ge
+ * (3(ne+nbf)), cp, tc (ne). */
 int cfdl_get_array(cfdl_ctx *ctx, const char *name, double *host);
 int cfdl_set_array(cfdl_ctx *ctx, const char *name, const double *host);
 
@@ -372,6 +403,10 @@ int    cfdl_server_destroy(cfdl_server *srv);
  * header, raw appended data with UInt64 counts).  path is the file to write
  * (the reference's VTK/output-<iout>/uvwp.vtu; the caller makes the folder). */
 int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *setup, const char *path);
+/* write_vtubin for the energy equation (mod_vtu_output.f90:124-132): enthalpy
+ * (phi), grad_enthalpy, temperature, grad_temperature; the reference's
+ * VTK/output-<iout>/energy.vtu.  Needs cfdl_energy_init. */
+int cfdl_write_vtu_energy(cfdl_ctx *ctx, int case_id, const cfdl_setup *setup, const char *path);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);

@@ -49,6 +49,8 @@ typedef struct {
 typedef struct {
     int    it_u, it_v, it_w, it_p;          /* inner iterations           */
     double res_i[4], res_f[4], res_max[4];  /* u,v,w,pc residual norms    */
+    int    it_e;                            /* energy solve (or_solve_energy) */
+    double res_e[3];                        /* its initial, final, max residual */
 } or_stats;
 
 /* Build the mesh data structures from a CGNS-shaped zone (what cell_input
@@ -107,6 +109,22 @@ void or_adjust_pc(ocase *c);                                   /* mod_uvwp.f90:1
 void or_update_uvwp(ocase *c);                                 /* mod_uvwp.f90:370  */
 /* one momentum component solve: comp 0,1,2 = u,v,w; mod_solver.f90:255 */
 void or_solve_momentum(ocase *c, int comp, or_stats *st);
+
+/* Energy equation, src/equations/mod_energy.f90 (its solve is commented out
+ * of the reference's time loop, main.f90:58; here it runs after solve_uvwp in
+ * or_run once set up).  or_energy_init = construct_energy (:14-47) with the
+ * properties of init_properties (mod_properties.f90:83-89): cp, tc per cell,
+ * t = t_init (reference 273), phi = cp*t, phi0 = phi; the BCs are bound by
+ * section name like the uvwp ones: 'top' -> lid (t_lid, reference 373), the
+ * other walls -> dirichlet0 (t_wall, reference 273).  After it,
+ * or_update_boundaries applies the energy BCs (:173-212) and or_update_time
+ * copies phi0 = phi (mod_physics.f90:111).  Field names for or_get_dbl /
+ * or_set_dbl: t, e (phi), e0 (phi0) [ne+nbf], gt, ge [3(ne+nbf)], cp, tc [ne].
+ * The assembly leaves ap, anb, b in the shared phys_t scratch, as the
+ * reference does. */
+int  or_energy_init(ocase *c, double cp, double tc, double t_init, double t_lid, double t_wall);
+void or_calc_coef_energy(ocase *c);                  /* mod_energy.f90:82-169 */
+void or_solve_energy(ocase *c, or_stats *st);        /* mod_energy.f90:59-80  */
 
 /* Timing helper for the CPU baseline: monotonic seconds. */
 double or_wtime(void);

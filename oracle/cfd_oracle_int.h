@@ -64,6 +64,12 @@ struct ocase {
     double *bu, *bv, *bw, *d, *dc;           /* [1..ne] */
     double *ap, *b, *anb, *phic;             /* scratch of phys_t */
     obc *bcs;                                /* [1..nintf_c2b] */
+    /* ---- energy equation (mod_energy.f90:5-9), set up by or_energy_init ---- */
+    int energy_on;
+    double *t, *ephi, *ephi0;                /* [1..ne+nbf] temperature, phi = cp*t, phi0 */
+    double *gt, *gephi;                      /* [1..3(ne+nbf)] grad t, grad phi */
+    double *cp, *tc;                         /* [1..ne] properties (mod_properties.f90:83-89) */
+    double *ebc_t;                           /* [1..nintf_c2b] wall temperature of each bound BC */
 };
 
 #define BS(c, e) ((c)->bs_store[(e) - (c)->ne])
@@ -79,6 +85,17 @@ static inline void o_get_idx(int idx, int *g, int *s) {
 static inline int o_sgn(int x) { return x >= 0 ? 1 : -1; }
 
 void *o_alloc(size_t n, size_t sz);
+/* shared with the energy equation (cfd_oracle_energy.c) */
+double o_vec_weight(const double *r0, const double *r1, const double *r2);
+void o_calc_grad(ocase *c, const double *phi, double *grad);
+void o_solve_gs(int is_pc, double *phi, const double *ap, const double *anb, const double *b,
+                const int *ef2nb_idx, const int *ef2nb, int ne, int nit,
+                int *it_out, double *ri, double *rf, double *rmax);
+int o_bicgstab(const ocase *c, const double *ap, const double *anb, const double *b, double *phi,
+               double rtol, int maxit, double *r0n, double *rfn);
+void o_energy_bc(ocase *c);
+void o_energy_time(ocase *c);
+void o_energy_free(ocase *c);
 int o_build_mesh(ocase *c);
 int o_build_partition(ocase *c, int nsubd);
 

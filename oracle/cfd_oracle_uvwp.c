@@ -177,6 +177,7 @@ void or_destroy(ocase *c) {
     free(c->gp); free(c->gpc); free(c->mip); free(c->mip0); free(c->bu); free(c->bv);
     free(c->bw); free(c->d); free(c->dc); free(c->ap); free(c->b); free(c->anb); free(c->phic);
     free(c->bcs);
+    o_energy_free(c);
     free(c);
 }
 
@@ -218,6 +219,8 @@ static double **dbl_field(ocase *c, const char *name, size_t *n) {
     F("bu", bu, c->ne) F("bv", bv, c->ne) F("bw", bw, c->ne) F("d", d, c->ne) F("dc", dc, c->ne)
     F("ap", ap, c->ne) F("b", b, c->ne) F("anb", anb, c->H) F("phic", phic, nc)
     F("rho", rho, c->ne) F("mu", mu, c->ne)
+    F("t", t, nc) F("e", ephi, nc) F("e0", ephi0, nc) F("gt", gt, 3 * nc) F("ge", gephi, 3 * nc)
+    F("cp", cp, c->ne) F("tc", tc, c->ne)
 #undef F
     return NULL;
 }
@@ -297,6 +300,7 @@ static void apply_bc(ocase *c, obc *bc) {
 
 void or_update_boundaries(ocase *c) {
     for (int i = 1; i <= c->nintf_c2b; i++) apply_bc(c, &c->bcs[i]);
+    if (c->energy_on) o_energy_bc(c);        /* mod_physics.f90:47 */
 }
 
 void or_update_time(ocase *c) {
@@ -305,6 +309,7 @@ void or_update_time(ocase *c) {
     memcpy(c->v0 + 1, c->v + 1, nc * sizeof(double));
     memcpy(c->w0 + 1, c->w + 1, nc * sizeof(double));
     memcpy(c->mip0 + 1, c->mip + 1, (size_t)c->nf * sizeof(double));
+    if (c->energy_on) o_energy_time(c);      /* mod_physics.f90:111 */
 }
 
 void or_set_config(ocase *c, const or_config *cfg) {
@@ -994,11 +999,26 @@ void or_solve_uvwp(ocase *c, or_stats *st) {
     (void)nc;
 }
 
-/* main.f90:50-63 */
+/* main.f90:50-63; with the energy equation set up, its solve follows
+ * solve_uvwp where main.f90:58 has it (commented out in the reference). */
 void or_run(ocase *c, int n_outer, int ncoef, or_stats *last) {
     for (int k = 1; k <= n_outer; k++) {
         or_update_boundaries(c);
         or_solve_uvwp(c, last);
+        if (c->energy_on) or_solve_energy(c, last);
         if (ncoef > 0 && k % ncoef == 0) or_update_time(c);
     }
+}
+
+/* the routines the energy equation shares with solve_uvwp */
+double o_vec_weight(const double *r0, const double *r1, const double *r2) { return vec_weight(r0, r1, r2); }
+void o_calc_grad(ocase *c, const double *phi, double *grad) { calc_grad(c, phi, grad); }
+void o_solve_gs(int is_pc, double *phi, const double *ap, const double *anb, const double *b,
+                const int *ef2nb_idx, const int *ef2nb, int ne, int nit,
+                int *it_out, double *ri, double *rf, double *rmax) {
+    solve_gs(is_pc, phi, ap, anb, b, ef2nb_idx, ef2nb, ne, nit, it_out, ri, rf, rmax);
+}
+int o_bicgstab(const ocase *c, const double *ap, const double *anb, const double *b, double *phi,
+               double rtol, int maxit, double *r0n, double *rfn) {
+    return bicgstab(c, ap, anb, b, phi, rtol, maxit, r0n, rfn);
 }

@@ -23,7 +23,8 @@ class OrConfig(C.Structure):
 
 class OrStats(C.Structure):
     _fields_ = [("it_u", C.c_int), ("it_v", C.c_int), ("it_w", C.c_int), ("it_p", C.c_int),
-                ("res_i", C.c_double * 4), ("res_f", C.c_double * 4), ("res_max", C.c_double * 4)]
+                ("res_i", C.c_double * 4), ("res_f", C.c_double * 4), ("res_max", C.c_double * 4),
+                ("it_e", C.c_int), ("res_e", C.c_double * 3)]
 
 
 _lib = None
@@ -71,6 +72,11 @@ def lib():
         L.or_solve_momentum.restype = None
         L.or_subdomain_sizes.argtypes = [vp, C.c_int, vp]
         L.or_subdomain_get.argtypes = [vp, C.c_int, vp, vp]
+        L.or_energy_init.argtypes = [vp] + [C.c_double] * 5
+        L.or_calc_coef_energy.argtypes = [vp]
+        L.or_calc_coef_energy.restype = None
+        L.or_solve_energy.argtypes = [vp, C.POINTER(OrStats)]
+        L.or_solve_energy.restype = None
         L.or_wtime.restype = C.c_double
         _lib = L
     return _lib
@@ -129,9 +135,9 @@ class Oracle:
                  "aip": 3 * self.nf, "rip": 3 * self.nf, "mip": self.nf, "mip0": self.nf, "anb": self.H}
         if name in table:
             return table[name]
-        if name in ("xc", "yc", "zc", "u", "v", "w", "p", "u0", "v0", "w0", "phic"):
+        if name in ("xc", "yc", "zc", "u", "v", "w", "p", "u0", "v0", "w0", "phic", "t", "e", "e0"):
             return nc
-        if name in ("gu", "gv", "gw", "gp", "gpc"):
+        if name in ("gu", "gv", "gw", "gp", "gpc", "gt", "ge"):
             return 3 * nc
         return self.ne
 
@@ -173,6 +179,18 @@ class Oracle:
     def run(self, n_outer, ncoef=3):
         st = OrStats()
         lib().or_run(self._h, int(n_outer), int(ncoef), C.byref(st))
+        return st
+
+    def energy_init(self, cp=1000.0, tc=5.0, t_init=273.0, t_lid=373.0, t_wall=273.0):
+        if lib().or_energy_init(self._h, cp, tc, t_init, t_lid, t_wall) != 0:
+            raise RuntimeError("or_energy_init needs physics_init first")
+
+    def calc_coef_energy(self):
+        lib().or_calc_coef_energy(self._h)
+
+    def solve_energy(self):
+        st = OrStats()
+        lib().or_solve_energy(self._h, C.byref(st))
         return st
 
     def calc_grad(self, phi, grad_in=None):

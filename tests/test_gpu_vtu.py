@@ -18,11 +18,9 @@ def i12(v):
     return "%12d" % v
 
 
-def restated_vtu(s, fields):
-    """Bytes of write_vtubin for the uvwp equation (test restatement)."""
-    ne, nvx = s.ne, fields["nvx"]
-    esec, etype = s.get_int("esec"), s.get_int("etype")
-    vol = [(int(esec[2 * q]), int(esec[2 * q + 1]), int(etype[q])) for q in range(s.nsec) if etype[q] >= 10]
+def uvwp_vars(s, fields):
+    """write_vtubin's variable list for the uvwp equation (mod_vtu_output.f90:101-123)."""
+    ne = s.ne
     idx, ef2 = s.get_int("ef2nb_idx"), s.get_int("ef2nb2")
     mip = fields["mip"]
     net = np.zeros(ne)
@@ -31,8 +29,15 @@ def restated_vtu(s, fields):
             fg = int(ef2[h - 1])
             sg = 1 if fg > 0 else -1
             net[e] = net[e] + mip[abs(fg) - 1] * sg
-    vars_ = [("u", 1, fields["u"]), ("v", 1, fields["v"]), ("w", 1, fields["w"]), ("p", 1, fields["p"]),
-             ("gpc", 3, fields["gpc"]), ("mip", 1, net)]
+    return [("u", 1, fields["u"]), ("v", 1, fields["v"]), ("w", 1, fields["w"]), ("p", 1, fields["p"]),
+            ("gpc", 3, fields["gpc"]), ("mip", 1, net)]
+
+
+def restated_vtu(s, fields, vars_):
+    """Bytes of write_vtubin for the variable list vars_ (test restatement)."""
+    ne, nvx = s.ne, fields["nvx"]
+    esec, etype = s.get_int("esec"), s.get_int("etype")
+    vol = [(int(esec[2 * q]), int(esec[2 * q + 1]), int(etype[q])) for q in range(s.nsec) if etype[q] >= 10]
     lf = "\n"
     out = [b'<?xml version="1.0"?>' + b"\n",
            b'<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" header_type="UInt64">\n',
@@ -94,6 +99,25 @@ def test_vtu_bytes_match_the_reference_layout(need_gpu, tmp_path, n, tet):
     fields = {f: g.get(f) for f in ("u", "v", "w", "p", "gpc", "mip")}
     fields.update(x=z.x, y=z.y, z=z.z, nvx=z.nvx, e2vx=z.e2vx, m=z.ne2vxmax)
     got = path.read_bytes()
-    want = restated_vtu(s, fields)
+    want = restated_vtu(s, fields, uvwp_vars(s, fields))
     assert got == want
+    g.close()
+
+
+def test_vtu_energy_bytes(need_gpu, tmp_path):
+    """write_vtubin for the energy equation (mod_vtu_output.f90:124-132)."""
+    z = cfdl.Zone(4, True, 0.1, seed=5)
+    s = cfdl.Setup(z)
+    g = cfdl.Solver(s, cfdl.default_config())
+    with pytest.raises(cfdl.CfdlError):
+        g.write_vtu_energy(tmp_path / "none.vtu")
+    g.energy_init()
+    g.step(3, ncoef=3)
+    path = tmp_path / "energy.vtu"
+    g.write_vtu_energy(path)
+    f = {k: g.get(k) for k in ("e", "ge", "t", "gt")}
+    vars_ = [("enthalpy", 1, f["e"]), ("grad_enthalpy", 3, f["ge"]), ("temperature", 1, f["t"]),
+             ("grad_temperature", 3, f["gt"])]
+    fields = dict(x=z.x, y=z.y, z=z.z, nvx=z.nvx, e2vx=z.e2vx, m=z.ne2vxmax)
+    assert path.read_bytes() == restated_vtu(s, fields, vars_)
     g.close()

@@ -109,3 +109,73 @@ def test_mass_conservation_improves():
     o.run(40)
     o.update_boundaries(); o.calc_coef_uvw(); o.calc_mip(True); o.calc_coef_p()
     assert np.linalg.norm(o.get("b")) < 0.2 * b0
+
+
+# ---- energy equation (src/equations/mod_energy.f90) ----------------------------
+
+def test_energy_pure_diffusion_matrix():
+    """With no flow and zero gradients, calc_coef_energy is pure diffusion:
+    symmetric interior coefficients tc/cp*area/(dr.n), wall coefficients
+    tc*area/ds/cp on the boundary half-faces, ap = sum of the row's anb
+    (steady: ap0 = 0) and b = 0."""
+    z, o = _fresh(n=4, jit=0.2, cfg=oracle_lib.steady(mode=1))
+    o.energy_init(cp=800.0, tc=4.0)
+    o.update_boundaries()
+    assert np.all(o.get("mip") == 0.0)
+    o.calc_coef_energy()
+    ap, anb, b = o.get("ap"), o.get("anb"), o.get("b")
+    ef1, idx = o.get_int("ef2nb1"), o.get_int("ef2nb_idx")
+    A = {}
+    nwall = 0
+    for e in range(o.ne):
+        row = 0.0
+        for h in range(idx[e] - 1, idx[e + 1] - 1):
+            enb, lf = ef1[h] >> 5, ef1[h] & 31
+            row += anb[h]
+            assert anb[h] > 0.0
+            if lf:
+                A[(e, enb - 1)] = anb[h]
+            else:
+                nwall += 1
+        assert abs(row - ap[e]) <= 1e-14 * ap[e]
+    assert nwall == o.nbf
+    for (i, j), a in A.items():
+        assert abs(a - A[(j, i)]) <= 1e-13 * a
+    assert np.all(b == 0.0)
+    # on the undistorted mesh every coefficient is tc/cp * h (area h^2, distance h; walls h/2)
+    z, o = _fresh(n=4, jit=0.0, cfg=oracle_lib.steady(mode=1))
+    o.energy_init(cp=800.0, tc=4.0)
+    o.update_boundaries()
+    o.calc_coef_energy()
+    anb = o.get("anb")
+    h = 1.0 / 4
+    vals = np.unique(np.round(anb / (4.0 / 800.0 * h), 12))
+    assert set(vals.tolist()) <= {1.0, 2.0}, vals
+
+
+def test_energy_uniform_temperature_is_kept():
+    """Walls and interior at one temperature stay there while the flow
+    develops: the advection is conservative (b carries sumf*phi) and the
+    fluxes are divergence-free to the tight pressure tolerance."""
+    z, o = _fresh(n=5, jit=0.1, cfg=oracle_lib.config(mode=1))
+    o.energy_init(t_init=300.0, t_lid=300.0, t_wall=300.0)
+    for _ in range(6):
+        o.update_boundaries()
+        o.solve_uvwp()
+        st = o.solve_energy()
+    assert np.abs(o.get("t")[:o.ne] - 300.0).max() < 1e-8
+    assert np.abs(o.get("u")).max() > 1e-3
+
+
+def test_energy_ref_and_tight_reach_the_same_steady_state():
+    """Gauss-Seidel (solve_gs 'e') and the tight BiCGStab energy solves reach
+    the same steady temperature; the hot lid warms the cavity."""
+    runs = {}
+    for mode in (0, 1):
+        z, o = _fresh(n=4, cfg=oracle_lib.steady(mode=mode))
+        o.energy_init()
+        o.run(260)
+        runs[mode] = o
+    a, b = runs[0].get("t")[:runs[0].ne], runs[1].get("t")[:runs[1].ne]
+    assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
+    assert b.min() > 273.0 - 1e-6 and b.max() < 373.0 and b.max() > 280.0

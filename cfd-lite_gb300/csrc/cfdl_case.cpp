@@ -300,10 +300,11 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
             G(FG_AREA, f) = area;
             G(FG_DRX, f) = dr[0]; G(FG_DRY, f) = dr[1]; G(FG_DRZ, f) = dr[2];
             G(FG_ADS, f) = area / ds;
+            // boundary faces too: the energy equation's wall coefficient uses it
+            const double dn = dr[0]*nrm[0] + dr[1]*nrm[1] + dr[2]*nrm[2];
+            G(FG_ADN, f) = area / dn;
             if (n < ne) {
                 G(FG_WT, f) = vec_weight(ri, rp, rn);
-                double dn = dr[0]*nrm[0] + dr[1]*nrm[1] + dr[2]*nrm[2];
-                G(FG_ADN, f) = area / dn;
                 double drip[3], t, rpp[3], rnp[3], drp[3];
                 for (int q = 0; q < 3; q++) drip[q] = ri[q] - rp[q];
                 t = drip[0]*nrm[0] + drip[1]*nrm[1] + drip[2]*nrm[2];

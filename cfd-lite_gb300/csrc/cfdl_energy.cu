@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(kTile) k_en_time(const CaseDev *__restrict__ c
 // tc_ip * area * (grad t_ip . n - grad phi_ip . n / cp_ip) (the neighbour sees
 // the opposite normal and the complementary weight, so it takes the negative);
 // boundary faces: the Dirichlet coefficient tc*area/ds/cp of the BC loop
-// (mod_energy.f90:146-168).  Planes: fS[0] coefficient, fS[1] deferred term.
+// (mod_energy.f90:146-168), where ds = dr.n (the momentum walls use |dr|).
+// Planes: fS[0] coefficient, fS[1] deferred term.
 __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     EN_PROLOGUE
     if (i >= t.last) return;
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ c
     const double *g = C.fgeo;
     double *fd = C.fS, *fx = C.fS + nf;
     if (n >= C.ne) {
-        fd[i] = C.etc[o] * g[FG_ADS * nf + i] / C.ecp[o];
+        fd[i] = C.etc[o] * g[FG_ADN * nf + i] / C.ecp[o];
         return;
     }
     const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
@@ -183,14 +184,17 @@ void launch_coef_energy(cfdl_ctx *ctx) {
     CFDL_LAUNCH("k_en_cell", k_en_cell, cells);
 }
 
-// solve_energy, mod_energy.f90:59-80
+void launch_energy_temp(cfdl_ctx *ctx) { CFDL_LAUNCH("k_en_temp", k_en_temp, cells); }
+
+// solve_energy, mod_energy.f90:59-80 (the run graph has the same sequence
+// with the solve as a device-side loop, cfdl_graph.cu)
 int solve_energy_all(cfdl_ctx *ctx) {
     if (!energy_on(ctx)) return CFDL_OK;
     launch_grad(ctx, 5);                  // calc_grad(t -> gt), calc_grad(phi -> grad), one pass
     launch_coef_energy(ctx);
     int st = solve_energy_phi(ctx);
     if (st) return st;
-    CFDL_LAUNCH("k_en_temp", k_en_temp, cells);
+    launch_energy_temp(ctx);
     return cuda_status(cudaGetLastError());
 }
 

@@ -31,7 +31,7 @@ void mx_finish(cfdl_ctx *ctx);
 
 namespace {
 
-enum { LOOP_MOM = 0, LOOP_P = 1, LOOP_INNER = 2, LOOP_OUTER = 3 };
+enum { LOOP_MOM = 0, LOOP_P = 1, LOOP_INNER = 2, LOOP_OUTER = 3, LOOP_EN = 4 };
 
 // Loop condition = any case still active for this loop kind; counts the pass.
 // One warp: lane l reads cases l, l+32, ... and the warp votes.
@@ -44,13 +44,14 @@ __global__ void k_setcond(const CaseDev *__restrict__ cases, int ncases, cudaGra
         int a;
         if (kind == LOOP_MOM) a = S->active[0] | S->active[1] | S->active[2];
         else if (kind == LOOP_INNER) a = S->active32;
+        else if (kind == LOOP_EN) a = S->en.active[0];
         else a = S->active_p;
         any |= (a != 0);
     }
     any = __any_sync(0xffffffffu, any);
     if (threadIdx.x == 0) {
         cudaGraphSetConditional(h, any ? 1u : 0u);
-        loop_passes[kind] += 1;
+        loop_passes[kind == LOOP_EN ? 5 : kind] += 1;   // the run graph's energy slot is base + 5
     }
 }
 
@@ -145,7 +146,7 @@ void destroy_graph(cfdl_ctx *ctx) {
 
 static int graph_form(const cfdl_ctx *ctx) {
     const cfdl_config &c = ctx->cases[0]->cfg;
-    return c.precision * 2 + c.precond;
+    return c.precision * 2 + c.precond + (energy_on(ctx) ? 8 : 0);
 }
 
 static int ensure_graph_state(cfdl_ctx *ctx) {
@@ -271,10 +272,38 @@ int build_graph(cfdl_ctx *ctx) {
     return CFDL_OK;
 }
 
+// solve_energy (mod_energy.f90:59-80) after *prev: gradients and assembly,
+// the BiCGStab loop on the energy lane, calc_temperature, then post().
+template <class Post>
+static int append_energy(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Post post, int64_t *static_k,
+                         int64_t *body) {
+    cfdl_ctx *ctx = b.ctx;
+    int st;
+    int64_t k = 0;
+    cudaGraphConditionalHandle he;
+    if ((st = cuda_status(cudaGraphConditionalHandleCreate(&he, G, 0, 0)))) return st;
+    if ((st = b.segment(G, prev, [&] {
+             launch_grad(ctx, 5);
+             launch_coef_energy(ctx);
+             energy_init_solve(ctx);
+             b.setone(he);
+         }, &k)))
+        return st;
+    *static_k += k;
+    st = b.loop(G, prev, he, [&](cudaGraph_t body_g) {
+        return b.capture_into(body_g, [&] { energy_iter(ctx); b.setcond(he, LOOP_EN); }, body);
+    });
+    if (st) return st;
+    if ((st = b.segment(G, prev, [&] { launch_energy_temp(ctx); post(); }, &k))) return st;
+    *static_k += k;
+    return CFDL_OK;
+}
+
 // The run graph: while (a case has outer iterations left and the launch's
 // budget is not spent) { per-case start; update_boundaries; solve_uvwp;
-// per-case end with the convergence test; gated update_time }.  Cases whose
-// run is over are skipped by every kernel until the host gives them more.
+// solve_energy when set up; per-case end with the convergence test; gated
+// update_time }.  Cases whose run is over are skipped by every kernel until
+// the host gives them more.
 int build_run_graph(cfdl_ctx *ctx) {
     drop_run_graph(ctx);
     int st;
@@ -284,7 +313,7 @@ int build_run_graph(cfdl_ctx *ctx) {
     Builder b{ctx, ctx->d_loop_passes + 4};
     ctx->capturing = true;
     cudaGraphNode_t prev = nullptr;
-    int64_t stat = 0, k = 0, body[5] = {0, 0, 0, 0, 0};
+    int64_t stat = 0, k = 0, body[6] = {0, 0, 0, 0, 0, 0};
     cudaGraphConditionalHandle hr;
     auto fail = [&](int s) { ctx->capturing = false; cudaGraphDestroy(G); return s; };
     if ((st = cuda_status(cudaGraphConditionalHandleCreate(&hr, G, 0, 0)))) return fail(st);
@@ -293,10 +322,13 @@ int build_run_graph(cfdl_ctx *ctx) {
     st = b.loop(G, &prev, hr, [&](cudaGraph_t outer) {
         cudaGraphNode_t op = nullptr;
         int64_t inner_static = 0;
-        int s2 = append_uvwp(
-            b, outer, &op, [&] { launch_run_begin(ctx); launch_bc(ctx); },
-            [&] { launch_run_end(ctx); launch_run_cond(ctx, hr, 1, ctx->d_loop_passes + 8); }, &inner_static, body,
-            false);
+        auto tail = [&] { launch_run_end(ctx); launch_run_cond(ctx, hr, 1, ctx->d_loop_passes + 8); };
+        const bool energy = energy_on(ctx);
+        int s2 = energy ? append_uvwp(b, outer, &op, [&] { launch_run_begin(ctx); launch_bc(ctx); }, [] {},
+                                      &inner_static, body, false)
+                        : append_uvwp(b, outer, &op, [&] { launch_run_begin(ctx); launch_bc(ctx); }, tail,
+                                      &inner_static, body, false);
+        if (!s2 && energy) s2 = append_energy(b, outer, &op, tail, &inner_static, &body[5]);
         body[4] = inner_static;
         return s2;
     });
@@ -310,7 +342,7 @@ int build_run_graph(cfdl_ctx *ctx) {
     ctx->run_exec = exec;
     ctx->run_form = graph_form(ctx);
     ctx->run_static_kernels = stat;
-    for (int i = 0; i < 5; i++) ctx->run_body_kernels[i] = body[i];
+    for (int i = 0; i < 6; i++) ctx->run_body_kernels[i] = body[i];
     return CFDL_OK;
 }
 
@@ -347,6 +379,7 @@ int64_t graph_loop_kernels(cfdl_ctx *ctx) {
     for (int i = 0; i < 4; i++) n += (int64_t)passes[i] * ctx->graph_body_kernels[i];
     for (int i = 0; i < 4; i++) n += (int64_t)passes[4 + i] * ctx->run_body_kernels[i];
     n += (int64_t)passes[8] * ctx->run_body_kernels[4];
+    n += (int64_t)passes[9] * ctx->run_body_kernels[5];
     return n;
 }
 

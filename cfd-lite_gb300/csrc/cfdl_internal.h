@@ -34,8 +34,9 @@ constexpr int kNPart = 16;        // partial slots per tile
 constexpr int kVec = 4;           // default cells per thread in the solver kernels
 constexpr int kMixedMaxOuter = 60;   // FP64 refinement cycles of the mixed pressure solve
 // loop-pass counters: [0,4) loops of the solve_uvwp graph, [4,8) the same
-// loops inside the run graph, [8] the run graph's outer loop
-constexpr int kLoopSlots = 9;
+// loops inside the run graph, [8] the run graph's outer loop, [9] its energy
+// solve loop
+constexpr int kLoopSlots = 10;
 
 // Loop over the cells of a wide solver tile: thread t handles cells
 // first+t, first+t+kTile, ... (coalesced); the tile's pad field holds how many
@@ -48,7 +49,7 @@ enum FaceGeo {
     FG_WT = 0,              // vec_weight(rip, r_own, r_nb)
     FG_AX, FG_AY, FG_AZ,    // aip (area vector, outward from the owner)
     FG_AREA,                // |aip|
-    FG_ADN,                 // area / (dr . n)
+    FG_ADN,                 // area / (dr . n) (boundary faces: dr to the halo centre)
     FG_DRX, FG_DRY, FG_DRZ, // dr = r_nb - r_own
     FG_ADS,                 // area / ds
     FG_ADRX, FG_ADRY, FG_ADRZ,  // area * dr / ds
@@ -215,7 +216,7 @@ struct cfdl_ctx {
     cudaGraph_t run_graph = nullptr;
     cudaGraphExec_t run_exec = nullptr;
     int run_form = -1;
-    int64_t run_static_kernels = 0, run_body_kernels[5] = {0, 0, 0, 0, 0};
+    int64_t run_static_kernels = 0, run_body_kernels[6] = {0, 0, 0, 0, 0, 0};
     int *d_run_ctl = nullptr, *h_run_ctl = nullptr;   // [0] outer passes left, [1] cases still running
 };
 
@@ -265,7 +266,9 @@ void launch_energy_time(cfdl_ctx *ctx, bool run_due);   // run_due: only cases w
 void launch_coef_energy(cfdl_ctx *ctx);
 int solve_energy_all(cfdl_ctx *ctx);
 int solve_energy_phi(cfdl_ctx *ctx);          // the phi solve alone (cfdl_solvers.cu)
+void energy_init_solve(cfdl_ctx *ctx);
 void energy_iter(cfdl_ctx *ctx);
+void launch_energy_temp(cfdl_ctx *ctx);
 int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t_init);
 
 // event profiler (cfdl_prof.cpp)

@@ -29,6 +29,7 @@ __global__ void k_run_begin(const CaseDev *__restrict__ cases, int ncases) {
         S->active[0] = S->active[1] = S->active[2] = 0;
         S->active_p = 0;
         S->active32 = 0;
+        S->en.active[0] = 0;
     }
 }
 
@@ -162,8 +163,7 @@ int run_outer(cfdl_ctx *ctx, int max_outer, int *running) {
                                           ctx->stream))))
         return st;
     const int n = (int)ctx->cases.size();
-    // the energy equation runs in the eager form (its solve has no graph loop)
-    if (ctx->use_graph && !prof_active(ctx) && !energy_on(ctx)) {
+    if (ctx->use_graph && !prof_active(ctx)) {
         if ((st = run_graph_launch(ctx))) return st;
     } else {
         for (int k = 0; k < max_outer; k++) {

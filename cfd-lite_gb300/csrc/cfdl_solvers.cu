@@ -595,9 +595,11 @@ void mom_iter(cfdl_ctx *ctx) {
 
 // Jacobi-preconditioned BiCGStab on the energy system, with the momentum
 // solve's kernels on one right-hand side and the energy lane
+void energy_init_solve(cfdl_ctx *ctx) { CFDL_LAUNCH("k_en_init", k_en_init, cellsv, RED); }
+
 int solve_energy_phi(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
-    CFDL_LAUNCH("k_en_init", k_en_init, cellsv, RED);
+    energy_init_solve(ctx);
     const int cap = max_cap(ctx);
     int it = 0, maxit = 0;
     while (it < cap) {

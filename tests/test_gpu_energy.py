@@ -124,17 +124,43 @@ def test_energy_converged_default_mode(need_gpu):
         g.close()
 
 
-def test_energy_run_equals_step(need_gpu):
+@pytest.mark.parametrize("graph", [True, False])
+def test_energy_run_equals_step(need_gpu, graph):
+    """cfdl_run (one graph launch with the energy solve as a device-side loop,
+    or its eager form) gives the fields of cfdl_step bit for bit."""
     z = cfdl.Zone(6, True, 0.1, seed=3)
     s = cfdl.Setup(z)
     cfg = cfdl.default_config(rho=5.0)
     a, b = cfdl.Solver(s, cfg), cfdl.Solver(s, cfg)
     a.energy_init(); b.energy_init()
+    b.set_graph_mode(graph)
     a.step(9, 3)
     b.set_run(9, 3)
     assert b.run(20) == 0
     for f in ("t", "e", "e0", "u", "p", "mip0"):
         assert np.array_equal(a.get(f), b.get(f)), f
+
+
+def test_energy_batched_run_with_uneven_targets(need_gpu):
+    """Two cases with the energy equation in one run graph, one stopping after
+    4 outer passes, the other after 11: each equals the same case run alone."""
+    zs = [cfdl.Zone(5, False, 0.2, seed=1), cfdl.Zone(4, True, 0.1, seed=2)]
+    ss = [cfdl.Setup(z) for z in zs]
+    cfg = cfdl.steady()
+    bt = cfdl.Batch(ss, [cfg, cfg])
+    bt.energy_init()
+    ids = bt.ids()
+    bt.set_run(4, 0, cid=ids[0])
+    bt.set_run(11, 0, cid=ids[1])
+    assert bt.run(50) == 0
+    for cid, s, n in zip(ids, ss, (4, 11)):
+        g = cfdl.Solver(s, cfg)
+        g.energy_init()
+        g.set_run(n, 0)
+        assert g.run(50) == 0
+        for f in ("t", "e", "u", "p"):
+            assert np.array_equal(bt.case_get(cid, f), g.get(f)), (cid, f)
+        g.close()
 
 
 def test_energy_in_a_mixed_batch(need_gpu):

@@ -593,6 +593,7 @@ def run_energy(a, dist):
     g.energy_init()
     for _ in range(a.warmup):                  # developed flow and temperature
         g.step(1, ncoef=0)
+    tile, _ = g.autotune(outer=2)              # solver and energy tile shapes by measurement (state restored)
     clocks = Clocks(dist.local)
     e_ms, o_ms, iters = [], [], []
     l0, launches_e = g.launch_count(), 0
@@ -629,6 +630,11 @@ def run_energy(a, dist):
     achieved = nbytes / avg_s / 1e9
     total = sum(v[1] for v in prof.values())
     shares = {k: round(t / total, 4) for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    per_launch = {k: {"launches": c, "avg_us": round(t / c * 1e3, 1),
+                      "gbs": round(kernel_bytes(k, ne, nf, nbf, W) / (t / c / 1e3) / 1e9, 1)
+                      if kernel_bytes(k, ne, nf, nbf, W) else None}
+                  for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    energy_tile = g.get_energy_tile()
     # the outer pass without the energy equation, same mesh and state
     g2 = cfdl.Solver(setup, cfg)
     for _ in range(a.warmup):
@@ -653,6 +659,7 @@ def run_energy(a, dist):
                                "373 / walls 273, cp=1000, tc=5; solve_energy after each outer pass"
                                % (a.n, "tet-split" if a.tet else "hex", a.jitter),
                    "cells": ne, "inner_solve": "10x residual drop / nit=100" if a.mode == 0 else "tight 1e-13",
+                   "tile": tile, "energy_tile": energy_tile,
                    "l2": "working set > L2 (no flush needed)"},
         "gpu_launches": launches_e,
         "energy_iterations_median": statistics.median(iters),
@@ -664,6 +671,7 @@ def run_energy(a, dist):
                      "algorithmic_bytes": nbytes, "avg_launch_us": avg_s * 1e6, "launches": dp[0],
                      "peak_source": peak_kind},
         "kernel_shares": shares,
+        "kernels": per_launch,
     }
     if clk:
         out["clocks"] = clk

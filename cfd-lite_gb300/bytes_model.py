@@ -52,11 +52,13 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
         "k_en_time": ne * 16,
         "k_en_time_halo": nbf * 16,
         "k_grad2": ell_i + 3 * ell_d + 16 * (ne + nbf) + 48 * ne,
-        # face terms: own/nb, weight, area/(dr.n), area vector, 2 outputs; boundary: own/nb, area/ds, 1 output;
-        # cell tc, cp and the two gradients
-        "k_en_face": nfi * (8 + 8 + 8 + 24 + 16) + nbf * (8 + 8 + 8) + ne * (16 + 48),
-        # cell gather: ELL nb/fc, mip + 2 face planes; phi, phi0, rho, vol in, ap, b out; anb ELL out; halo kinds
-        "k_en_cell": 2 * ell_i + nf * 24 + ne * (32 + 16) + ell_d + nbf * 4,
+        # property planes (when cp/tc change): own/nb, weight, area/(dr.n), 3 outputs; cell tc, cp
+        "k_en_props": nfi * (8 + 8 + 8 + 24) + nbf * (8 + 8 + 24) + ne * 16,
+        # deferred face term: own/nb, weight, area vector, tc_ip and tc_ip/cp_ip, 1 output; the two gradients
+        "k_en_face": nfi * (8 + 8 + 24 + 16 + 8) + ne * 48,
+        # cell gather: ELL nb/fc, mip + coefficient plane (all faces), deferred term (interior);
+        # phi, phi0, rho, vol in, ap, b out; anb ELL out; halo kinds
+        "k_en_cell": 2 * ell_i + nf * 16 + nfi * 8 + ne * (32 + 16) + ell_d + nbf * 4,
         # solver init: ap, rap, b, phi, r, rh, anb ELL + halo phi
         "k_en_init": ne * 48 + ell_d + ell_i + nbf * 8,
         "k_en_p": ne * 8 + ne * (24 + 16),

@@ -138,6 +138,8 @@ def lib():
     for n in ("cfdl_solve_uvwp", "cfdl_solve_momentum", "cfdl_solve_pc", "cfdl_solve_energy"):
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
     L.cfdl_energy_init.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.cfdl_set_energy_tile.argtypes = [vp, C.c_int]
+    L.cfdl_get_energy_tile.argtypes = [vp]
     L.cfdl_calc_coef_energy.argtypes = [vp]
     L.cfdl_step.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_solve_uvwp_host.argtypes = [vp, C.POINTER(Fields), C.POINTER(Stats)]
@@ -351,6 +353,12 @@ class Solver:
 
     def calc_coef_energy(self):
         _check(lib().cfdl_calc_coef_energy(self._h), "calc_coef_energy")
+
+    def set_energy_tile(self, vec):
+        _check(lib().cfdl_set_energy_tile(self._h, int(vec)), "set_energy_tile")
+
+    def get_energy_tile(self):
+        return lib().cfdl_get_energy_tile(self._h)
 
     def calc_coef_p(self):
         _check(lib().cfdl_calc_coef_p(self._h), "calc_coef_p")

@@ -57,6 +57,7 @@ int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool
     if (!nm.ptr) return CFDL_ERR_NAME;
     if (!host) return CFDL_ERR_INVALID;
     if (!to_host && (nm.ptr == hc->dev.rho || nm.ptr == hc->dev.mu)) hc->props_dirty = true;
+    if (!to_host && nm.ptr && (nm.ptr == hc->dev.ecp || nm.ptr == hc->dev.etc)) hc->eprops_dirty = true;
     cudaError_t e;
     if (!nm.ell) {
         e = cudaMemcpyAsync(to_host ? (void *)host : (void *)nm.ptr, to_host ? (const void *)nm.ptr : (const void *)host,
@@ -238,6 +239,7 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     WorkList *wls[3] = {&ctx->cells, &ctx->faces, &ctx->halos};
     for (WorkList *wl : wls) free_worklist(*wl);
     free_worklist(ctx->cellsv);
+    free_worklist(ctx->cellse);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);

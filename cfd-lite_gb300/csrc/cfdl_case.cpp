@@ -401,6 +401,7 @@ int rebuild_worklists(cfdl_ctx *ctx) {
     if ((st = build_worklist(ctx, ctx->faces, nfc))) return st;
     if ((st = build_worklist(ctx, ctx->halos, nh))) return st;
     if ((st = build_worklist(ctx, ctx->cellsv, nc, kTile * ctx->vec))) return st;
+    if ((st = build_worklist(ctx, ctx->cellse, nc, kTile * ctx->en_vec))) return st;
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);

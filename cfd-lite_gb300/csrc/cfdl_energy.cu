@@ -8,9 +8,11 @@
 // the reference computes from both sides of a face are computed once per face
 // (k_en_face) and gathered by the cells in the reference's half-face order
 // (k_en_cell); the boundary terms follow in the BC loop's order (ascending
-// halo index).  The assembly leaves ap, anb, b in the case's shared scratch,
-// as the reference's phys%ap/anb/b, and uses the momentum face-term planes
-// fS as its face scratch.  The phi solve reuses the momentum BiCGStab kernels
+// halo index).  The cp/tc-only face terms (the diffusion coefficients) are
+// kept in property planes recomputed only when cp or tc change.  The assembly
+// leaves ap, anb, b in the case's shared scratch, as the reference's
+// phys%ap/anb/b, and uses the momentum face-term plane fS[0] as its face
+// scratch.  The phi solve reuses the momentum BiCGStab kernels
 // on one right-hand side (cfdl_solvers.cu).
 //
 // Every kernel returns at once for a case without the energy equation (its
@@ -50,28 +52,46 @@ __global__ void __launch_bounds__(kTile) k_en_time(const CaseDev *__restrict__ c
     C.ee0[j] = C.ee[j];
 }
 
-// calc_coef_energy, face part (mod_energy.f90:96-140): per interior face, from
-// the owner's side, the diffusion coefficient tc_ip/cp_ip * area/(dr.n)
-// (the same from both sides) and the deferred term
-// tc_ip * area * (grad t_ip . n - grad phi_ip . n / cp_ip) (the neighbour sees
-// the opposite normal and the complementary weight, so it takes the negative);
-// boundary faces: the Dirichlet coefficient tc*area/ds/cp of the BC loop
-// (mod_energy.f90:146-168), where ds = dr.n (the momentum walls use |dr|).
-// Planes: fS[0] coefficient, fS[1] deferred term.
-__global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+// Energy property planes of every face (recomputed when cp or tc change):
+// per interior face tc_ip, tc_ip/cp_ip and the diffusion coefficient
+// tc_ip/cp_ip * area/(dr.n) of calc_coef_energy (mod_energy.f90:123-125, the
+// same from both sides); per boundary face the Dirichlet coefficient
+// tc*area/ds/cp of the BC loop (mod_energy.f90:157), where ds = dr.n (the
+// momentum walls use |dr|).  The divisions are done here, once.
+__global__ void __launch_bounds__(kTile) k_en_props(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     EN_PROLOGUE
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
     const double *g = C.fgeo;
-    double *fd = C.fS, *fx = C.fS + nf;
+    double *ep = C.eprop;
     if (n >= C.ne) {
-        fd[i] = C.etc[o] * g[FG_ADN * nf + i] / C.ecp[o];
+        ep[EP_D * nf + i] = C.etc[o] * g[FG_ADN * nf + i] / C.ecp[o];
+        ep[EP_TC * nf + i] = 0.0;
+        ep[EP_TCR * nf + i] = 0.0;
         return;
     }
     const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
     const double tci = omw * C.etc[o] + wt * C.etc[n];
     const double cpi = omw * C.ecp[o] + wt * C.ecp[n];
-    fd[i] = tci / cpi * g[FG_ADN * nf + i];
+    const double r = tci / cpi;
+    ep[EP_D * nf + i] = r * g[FG_ADN * nf + i];
+    ep[EP_TC * nf + i] = tci;
+    ep[EP_TCR * nf + i] = r;
+}
+
+// calc_coef_energy, face part (mod_energy.f90:126-128): per interior face, from
+// the owner's side, the deferred term
+// tc_ip * area * (grad t_ip . n - grad phi_ip . n / cp_ip)
+//   = tc_ip * (grad t_ip . A) - tc_ip/cp_ip * (grad phi_ip . A)
+// (A the area vector; the neighbour sees the opposite normal and the
+// complementary weight, so it takes the negative), into fS[0].
+__global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    EN_PROLOGUE
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= C.ne) return;
+    const double *g = C.fgeo;
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
     const double A[3] = {g[FG_AX * nf + i], g[FG_AY * nf + i], g[FG_AZ * nf + i]};
     double gtn = 0.0, ghn = 0.0;
 #pragma unroll
@@ -79,7 +99,7 @@ __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ c
         gtn += (omw * C.egt[3 * o + m] + wt * C.egt[3 * n + m]) * A[m];
         ghn += (omw * C.ege[3 * o + m] + wt * C.ege[3 * n + m]) * A[m];
     }
-    fx[i] = tci * (gtn - ghn / cpi);
+    C.fS[i] = C.eprop[EP_TC * nf + i] * gtn - C.eprop[EP_TCR * nf + i] * ghn;
 }
 
 // calc_coef_energy, cell part (mod_energy.f90:92-143, then the BC loop
@@ -89,8 +109,8 @@ __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ c
 __global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     EN_PROLOGUE
     if (i >= t.last) return;
-    const int ne = C.ne, nf = C.nf, W = C.W;
-    const double *fd = C.fS, *fx = C.fS + nf;
+    const int ne = C.ne, W = C.W;
+    const double *fd = C.eprop + EP_D * C.nf, *fx = C.fS;
     double ap = 0.0, sumf = 0.0, sumdefc = 0.0;
     double a[kMaxW];
     int bslot[kMaxW], nb_cnt = 0;
@@ -179,7 +199,16 @@ void launch_energy_time(cfdl_ctx *ctx, bool run_due) {
     CFDL_LAUNCH("k_en_time_halo", k_en_time, halos, 1, run_due ? 1 : 0);
 }
 
+void ensure_energy_props(cfdl_ctx *ctx) {
+    bool dirty = false;
+    for (HostCase *hc : ctx->cases) dirty |= hc->dev.ee && hc->eprops_dirty;
+    if (!dirty || ctx->capturing) return;
+    CFDL_LAUNCH("k_en_props", k_en_props, faces);
+    for (HostCase *hc : ctx->cases) hc->eprops_dirty = false;
+}
+
 void launch_coef_energy(cfdl_ctx *ctx) {
+    ensure_energy_props(ctx);
     CFDL_LAUNCH("k_en_face", k_en_face, faces);
     CFDL_LAUNCH("k_en_cell", k_en_cell, cells);
 }
@@ -190,6 +219,7 @@ void launch_energy_temp(cfdl_ctx *ctx) { CFDL_LAUNCH("k_en_temp", k_en_temp, cel
 // with the solve as a device-side loop, cfdl_graph.cu)
 int solve_energy_all(cfdl_ctx *ctx) {
     if (!energy_on(ctx)) return CFDL_OK;
+    if (ctx->use_graph && !prof_active(ctx)) return solve_energy_graph(ctx);
     launch_grad(ctx, 5);                  // calc_grad(t -> gt), calc_grad(phi -> grad), one pass
     launch_coef_energy(ctx);
     int st = solve_energy_phi(ctx);
@@ -208,7 +238,8 @@ int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t
     if (!d.ee) {
         void *p;
         struct A { double **dst; size_t n; } list[] = {
-            {&d.et, nc}, {&d.ee, nc}, {&d.ee0, nc}, {&d.egt, 3 * nc}, {&d.ege, 3 * nc}, {&d.ecp, ne}, {&d.etc, ne}};
+            {&d.et, nc}, {&d.ee, nc}, {&d.ee0, nc}, {&d.egt, 3 * nc}, {&d.ege, 3 * nc}, {&d.ecp, ne}, {&d.etc, ne},
+            {&d.eprop, (size_t)EP_N * hc->nf}};
         for (const A &a : list) {
             if ((st = case_alloc(hc, &p, a.n * sizeof(double)))) return st;
             *a.dst = (double *)p;
@@ -225,6 +256,7 @@ int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t
     k_en_fill<<<(unsigned)((nc + tb - 1) / tb), tb, 0, ctx->stream>>>(d.et, d.ee, d.ee0, d.ecp, d.h_own, (int)ne,
                                                                        hc->nbf, t_init);
     ctx->launches += 3;
+    hc->eprops_dirty = true;
     if ((st = cuda_status(cudaMemsetAsync(d.egt, 0, 3 * nc * sizeof(double), ctx->stream)))) return st;
     if ((st = cuda_status(cudaMemsetAsync(d.ege, 0, 3 * nc * sizeof(double), ctx->stream)))) return st;
     return cuda_status(cudaGetLastError());

@@ -139,9 +139,18 @@ static void drop_run_graph(cfdl_ctx *ctx) {
     ctx->run_form = -1;
 }
 
+static void drop_energy_graph(cfdl_ctx *ctx) {
+    if (ctx->energy_exec) cudaGraphExecDestroy(ctx->energy_exec);
+    if (ctx->energy_graph) cudaGraphDestroy(ctx->energy_graph);
+    ctx->energy_exec = nullptr;
+    ctx->energy_graph = nullptr;
+    ctx->energy_form = -1;
+}
+
 void destroy_graph(cfdl_ctx *ctx) {
     drop_uvwp_graph(ctx);
     drop_run_graph(ctx);
+    drop_energy_graph(ctx);
 }
 
 static int graph_form(const cfdl_ctx *ctx) {
@@ -346,9 +355,45 @@ int build_run_graph(cfdl_ctx *ctx) {
     return CFDL_OK;
 }
 
+// solve_energy alone as one graph: assembly, the BiCGStab loop on the device,
+// calc_temperature (cfdl_solve_energy, cfdl_step)
+static int build_energy_graph(cfdl_ctx *ctx) {
+    drop_energy_graph(ctx);
+    int st;
+    if ((st = ensure_graph_state(ctx))) return st;
+    cudaGraph_t G = nullptr;
+    if ((st = cuda_status(cudaGraphCreate(&G, 0)))) return st;
+    Builder b{ctx, ctx->d_loop_passes + 5};          // its loop counts in slot 10
+    ctx->capturing = true;
+    cudaGraphNode_t prev = nullptr;
+    int64_t stat = 0, body = 0;
+    st = append_energy(b, G, &prev, [] {}, &stat, &body);
+    ctx->capturing = false;
+    if (st) { cudaGraphDestroy(G); return st; }
+    cudaGraphExec_t exec = nullptr;
+    if ((st = cuda_status(cudaGraphInstantiate(&exec, G, 0)))) { cudaGraphDestroy(G); return st; }
+    ctx->energy_graph = G;
+    ctx->energy_exec = exec;
+    ctx->energy_form = graph_form(ctx);
+    ctx->energy_static_kernels = stat;
+    ctx->energy_body_kernels = body;
+    return CFDL_OK;
+}
+
+int solve_energy_graph(cfdl_ctx *ctx) {
+    int st;
+    ensure_energy_props(ctx);
+    if (!ctx->energy_exec || ctx->energy_form != graph_form(ctx))
+        if ((st = build_energy_graph(ctx))) return st;
+    ctx->launches += ctx->energy_static_kernels;
+    ctx->graph_launches++;
+    return cuda_status(cudaGraphLaunch(ctx->energy_exec, ctx->stream));
+}
+
 int run_graph_launch(cfdl_ctx *ctx) {
     int st;
     ensure_face_props(ctx);
+    ensure_energy_props(ctx);
     if (!ctx->run_exec || ctx->run_form != graph_form(ctx))
         if ((st = build_run_graph(ctx))) return st;
     ctx->launches += ctx->run_static_kernels;
@@ -380,6 +425,7 @@ int64_t graph_loop_kernels(cfdl_ctx *ctx) {
     for (int i = 0; i < 4; i++) n += (int64_t)passes[4 + i] * ctx->run_body_kernels[i];
     n += (int64_t)passes[8] * ctx->run_body_kernels[4];
     n += (int64_t)passes[9] * ctx->run_body_kernels[5];
+    n += (int64_t)passes[10] * ctx->energy_body_kernels;
     return n;
 }
 

@@ -35,8 +35,8 @@ constexpr int kVec = 4;           // default cells per thread in the solver kern
 constexpr int kMixedMaxOuter = 60;   // FP64 refinement cycles of the mixed pressure solve
 // loop-pass counters: [0,4) loops of the solve_uvwp graph, [4,8) the same
 // loops inside the run graph, [8] the run graph's outer loop, [9] its energy
-// solve loop
-constexpr int kLoopSlots = 10;
+// solve loop, [10] the loop of the solve_energy graph
+constexpr int kLoopSlots = 11;
 
 // Loop over the cells of a wide solver tile: thread t handles cells
 // first+t, first+t+kTile, ... (coalesced); the tile's pad field holds how many
@@ -55,6 +55,14 @@ enum FaceGeo {
     FG_ADRX, FG_ADRY, FG_ADRZ,  // area * dr / ds
     FG_EX, FG_EY, FG_EZ,        // area * (dr_p/ds_p - dr/ds)
     FG_N
+};
+
+// energy property planes eprop[EP_*][nf], recomputed only when cp or tc change
+enum EnergyProp {
+    EP_D = 0,                   // tc_ip/cp_ip * area/(dr.n) (boundary faces: tc/cp of the owner * area/(dr.n))
+    EP_TC,                      // tc_ip
+    EP_TCR,                     // tc_ip/cp_ip
+    EP_N
 };
 
 // property planes fprop[PR_*][nf]: the mesh planes scaled by the interpolated
@@ -135,6 +143,7 @@ struct CaseDev {
     // of each halo [nbf]
     double *et, *ee, *ee0, *egt, *ege, *ecp, *etc;
     const double *eh_t;
+    double *eprop;                        // [EP_N][nf] energy property planes
     // parameters
     double dt, alpha_u, alpha_p, rtol_u, rtol_p, tight_rtol;
     double rdt, ralpha_u;                 // 1/dt (0 when steady), 1/alpha_u
@@ -168,6 +177,7 @@ struct HostCase {
     bool props_dirty = true;         // fprop must be recomputed (rho or mu changed)
     size_t bytes = 0;                // device bytes held (mesh, fields, solver, hierarchy)
     std::vector<double> h_temp;      // [nbf] energy wall temperature of each halo (empty: none)
+    bool eprops_dirty = true;        // eprop must be recomputed (cp or tc changed)
 };
 
 }  // namespace cfdl
@@ -188,6 +198,8 @@ struct cfdl_ctx {
     cfdl::WorkList cells, faces, halos;
     cfdl::WorkList cellsv;               // wide tiles (kTile*vec cells) for the solver kernels
     int vec = cfdl::kVec;                // cells per thread in those tiles (autotuned)
+    cfdl::WorkList cellse;               // tiles of the energy solve (kTile*en_vec cells)
+    int en_vec = 1;                      // cells per thread in those tiles (autotuned with the energy equation)
     int last_iters_m = 0, last_iters_p = 0, last_iters_e = 0;   // previous inner iteration counts (poll scheduling)
     double *d_partials = nullptr;        // [max tiles][kNPart]
     int partials_cap = 0;                // tiles
@@ -211,6 +223,11 @@ struct cfdl_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     int graph_form = -1;
     int64_t graph_static_kernels = 0, graph_body_kernels[4] = {0, 0, 0, 0}, graph_launches = 0;
+    // solve_energy as one CUDA graph (cfdl_graph.cu)
+    cudaGraph_t energy_graph = nullptr;
+    cudaGraphExec_t energy_exec = nullptr;
+    int energy_form = -1;
+    int64_t energy_static_kernels = 0, energy_body_kernels = 0;
     unsigned long long *d_loop_passes = nullptr;   // passes of each loop kind, [kLoopSlots]
     // runs of many outer iterations as one graph launch (cfdl_run.cu)
     cudaGraph_t run_graph = nullptr;
@@ -264,6 +281,7 @@ bool energy_on(const cfdl_ctx *ctx);          // some case of the context has it
 void launch_energy_bc(cfdl_ctx *ctx);
 void launch_energy_time(cfdl_ctx *ctx, bool run_due);   // run_due: only cases whose run cadence is due
 void launch_coef_energy(cfdl_ctx *ctx);
+void ensure_energy_props(cfdl_ctx *ctx);      // recompute eprop of cases whose cp/tc changed
 int solve_energy_all(cfdl_ctx *ctx);
 int solve_energy_phi(cfdl_ctx *ctx);          // the phi solve alone (cfdl_solvers.cu)
 void energy_init_solve(cfdl_ctx *ctx);
@@ -316,6 +334,7 @@ int solve_uvwp_graph(cfdl_ctx *ctx);
 int64_t graph_loop_kernels(cfdl_ctx *ctx);
 int build_run_graph(cfdl_ctx *ctx);
 int run_graph_launch(cfdl_ctx *ctx);
+int solve_energy_graph(cfdl_ctx *ctx);
 
 // runs of many outer iterations (cfdl_run.cu)
 void launch_run_begin(cfdl_ctx *ctx);

@@ -595,7 +595,9 @@ void mom_iter(cfdl_ctx *ctx) {
 
 // Jacobi-preconditioned BiCGStab on the energy system, with the momentum
 // solve's kernels on one right-hand side and the energy lane
-void energy_init_solve(cfdl_ctx *ctx) { CFDL_LAUNCH("k_en_init", k_en_init, cellsv, RED); }
+#define REDE ctx->cellse.d_case_first, ctx->cellse.d_case_ntiles, ctx->d_partials
+
+void energy_init_solve(cfdl_ctx *ctx) { CFDL_LAUNCH("k_en_init", k_en_init, cellse, REDE); }
 
 int solve_energy_phi(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
@@ -615,11 +617,11 @@ int solve_energy_phi(cfdl_ctx *ctx) {
 
 // one BiCGStab iteration of the energy solve (one right-hand side, FP64)
 void energy_iter(cfdl_ctx *ctx) {
-    CFDL_LAUNCH("k_en_p", (k_mom_p<double, 1>), cellsv);
-    CFDL_LAUNCH("k_en_v", (k_mom_v<double, 1>), cellsv, RED);
-    CFDL_LAUNCH("k_en_s", (k_mom_s<double, 1>), cellsv, RED);
-    CFDL_LAUNCH("k_en_t", (k_mom_t<double, 1>), cellsv, RED);
-    CFDL_LAUNCH("k_en_x", (k_mom_x<double, 1>), cellsv, RED);
+    CFDL_LAUNCH("k_en_p", (k_mom_p<double, 1>), cellse);
+    CFDL_LAUNCH("k_en_v", (k_mom_v<double, 1>), cellse, REDE);
+    CFDL_LAUNCH("k_en_s", (k_mom_s<double, 1>), cellse, REDE);
+    CFDL_LAUNCH("k_en_t", (k_mom_t<double, 1>), cellse, REDE);
+    CFDL_LAUNCH("k_en_x", (k_mom_x<double, 1>), cellse, REDE);
 }
 
 // the end of the momentum solve: precision 2 applies its FP32 correction

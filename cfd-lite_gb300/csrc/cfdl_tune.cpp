@@ -7,7 +7,9 @@
 // for small cases.  The best vec depends on the mix of case sizes, so the
 // autotuner measures it: for each candidate it times a few outer iterations
 // on the context's own cases, from a snapshot of their state that is put back
-// afterwards, and keeps the fastest.  The tile shape changes the order of the
+// afterwards, and keeps the fastest; with the energy equation set up, the
+// tile shape of the energy solve is tuned the same way, on energy solves
+// alone.  The tile shape changes the order of the
 // partial sums, so results agree across shapes to rounding, not bit for bit;
 // the shape is a property of the context, and cases compared bit for bit
 // must share it.
@@ -25,9 +27,14 @@ struct Snap { double *p; size_t n; };
 std::vector<Snap> state_arrays(HostCase *hc) {
     CaseDev &d = hc->dev;
     const size_t nc = (size_t)hc->ne + hc->nbf, nf = hc->nf;
-    return {{d.u, nc}, {d.v, nc}, {d.w, nc}, {d.p, nc}, {d.u0, nc}, {d.v0, nc}, {d.w0, nc},
-            {d.gu, 3 * nc}, {d.gv, 3 * nc}, {d.gw, 3 * nc}, {d.gp, 3 * nc}, {d.gpc, 3 * nc},
-            {d.mip, nf}, {d.mip0, nf}};
+    std::vector<Snap> v = {{d.u, nc}, {d.v, nc}, {d.w, nc}, {d.p, nc}, {d.u0, nc}, {d.v0, nc}, {d.w0, nc},
+                           {d.gu, 3 * nc}, {d.gv, 3 * nc}, {d.gw, 3 * nc}, {d.gp, 3 * nc}, {d.gpc, 3 * nc},
+                           {d.mip, nf}, {d.mip0, nf}};
+    if (d.ee) {   // the energy equation's state
+        const Snap e[] = {{d.et, nc}, {d.ee, nc}, {d.ee0, nc}, {d.egt, 3 * nc}, {d.ege, 3 * nc}};
+        v.insert(v.end(), e, e + 5);
+    }
+    return v;
 }
 
 // Device copy of every case's outer-iteration state and solver scalars.
@@ -88,6 +95,17 @@ int cfdl_set_tile(cfdl_ctx *ctx, int vec) {
 
 int cfdl_get_tile(const cfdl_ctx *ctx) { return ctx ? ctx->vec : -1; }
 
+int cfdl_set_energy_tile(cfdl_ctx *ctx, int vec) {
+    if (!ctx || ctx->cases.empty() || !valid_shape(vec)) return CFDL_ERR_INVALID;
+    if (vec == ctx->en_vec) return CFDL_OK;
+    int st = cuda_status(cudaStreamSynchronize(ctx->stream));
+    if (st) return st;
+    ctx->en_vec = vec;
+    return rebuild_worklists(ctx);
+}
+
+int cfdl_get_energy_tile(const cfdl_ctx *ctx) { return ctx ? ctx->en_vec : -1; }
+
 int cfdl_set_coarse_group(cfdl_ctx *ctx, int lanes) {
     if (!ctx || ctx->cases.empty() || !(lanes == 1 || lanes == 2 || lanes == 4)) return CFDL_ERR_INVALID;
     if (lanes == ctx->cgroup) return CFDL_OK;
@@ -111,6 +129,21 @@ static int time_outer(cfdl_ctx *ctx, Snapshot &snap, int outer, cudaEvent_t e0, 
         launch_bc(ctx);
         if ((st = solve_uvwp_all(ctx))) return st;
     }
+    cudaEventRecord(e1, ctx->stream);
+    float f = 0.f;
+    if ((st = cuda_status(cudaEventSynchronize(e1)))) return st;
+    if ((st = cuda_status(cudaEventElapsedTime(&f, e0, e1)))) return st;
+    *ms = f / outer;
+    return snap.restore(ctx);
+}
+
+// Times `outer` energy solves from the snapshot; ms per solve.
+static int time_energy(cfdl_ctx *ctx, Snapshot &snap, int outer, cudaEvent_t e0, cudaEvent_t e1, double *ms) {
+    int st;
+    if ((st = solve_energy_all(ctx)) || (st = snap.restore(ctx))) return st;
+    cudaEventRecord(e0, ctx->stream);
+    for (int i = 0; i < outer; i++)
+        if ((st = solve_energy_all(ctx))) return st;
     cudaEventRecord(e1, ctx->stream);
     float f = 0.f;
     if ((st = cuda_status(cudaEventSynchronize(e1)))) return st;
@@ -148,10 +181,21 @@ int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms) {
         if ((st = cfdl_set_coarse_group(ctx, groups[k])) || (st = time_outer(ctx, snap, outer, e0, e1, &t))) break;
         if (gbest < 0.0 || t < gbest) { gbest = t; gpick = groups[k]; }
     }
+    if (!st) st = cfdl_set_coarse_group(ctx, gpick);
+    // with the energy equation, the tile shape of its solve
+    if (!st && energy_on(ctx)) {
+        int epick = ctx->en_vec;
+        double ebest = -1.0;
+        for (int k = 0; k < n && !st; k++) {
+            double t = 0.0;
+            if ((st = cfdl_set_energy_tile(ctx, kTileShapes[k])) || (st = time_energy(ctx, snap, outer, e0, e1, &t))) break;
+            if (ebest < 0.0 || t < ebest) { ebest = t; epick = kTileShapes[k]; }
+        }
+        if (!st) st = cfdl_set_energy_tile(ctx, epick);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st) return st;
-    if ((st = cfdl_set_coarse_group(ctx, gpick))) return st;
     if (best) *best = pick;
     return snap.restore(ctx);
 }

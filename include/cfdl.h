@@ -331,6 +331,10 @@ int cfdl_get_tile(const cfdl_ctx *ctx);
 int cfdl_set_coarse_group(cfdl_ctx *ctx, int lanes);
 int cfdl_get_coarse_group(const cfdl_ctx *ctx);
 int cfdl_autotune(cfdl_ctx *ctx, int outer, int *best, double *ms);
+/* Tile shape (cells per thread: 1, 2, 4, 8) of the energy solve's kernels;
+ * cfdl_autotune tunes it too when the energy equation is set up. */
+int cfdl_set_energy_tile(cfdl_ctx *ctx, int vec);
+int cfdl_get_energy_tile(const cfdl_ctx *ctx);
 
 /* ---- serving loop ---------------------------------------------------------
  * No counterpart in the reference.  Solves lid-driven-cavity requests with

@@ -197,3 +197,44 @@ def test_energy_needs_init(need_gpu):
     g.energy_init()
     st = g.solve_energy()
     assert st.status == 0
+
+
+def test_energy_tile_shapes_and_autotune(need_gpu):
+    """The energy solve's tile shape changes only the order of partial sums;
+    the autotuner puts the state back exactly."""
+    s = cfdl.Setup(cfdl.Zone(7, False, 0.2, seed=4))
+    cfg = cfdl.steady()
+    ref = None
+    for vec in (1, 2, 4, 8):
+        g = cfdl.Solver(s, cfg)
+        g.energy_init()
+        g.set_energy_tile(vec)
+        assert g.get_energy_tile() == vec
+        g.step(4, 0)
+        t = g.get("t")
+        if ref is None:
+            ref = t
+        assert rel_l2(t, ref) < 1e-12, vec
+        before = {f: g.get(f) for f in ("t", "e", "u", "p")}
+        g.autotune(outer=1)
+        assert g.get_energy_tile() in (1, 2, 4, 8)
+        for f, v in before.items():
+            assert np.array_equal(g.get(f), v), f
+        g.close()
+
+
+def test_energy_graph_equals_eager(need_gpu):
+    """solve_energy as one graph launch (device-side BiCGStab loop) and as
+    eager launches with host polls give the same fields bit for bit."""
+    s = cfdl.Setup(cfdl.Zone(6, False, 0.2, seed=8))
+    cfg = cfdl.default_config(rho=5.0)
+    a, b = cfdl.Solver(s, cfg), cfdl.Solver(s, cfg)
+    b.set_graph_mode(False)
+    for g in (a, b):
+        g.energy_init()
+        g.step(5, 3)
+    for f in ("t", "e", "e0", "ge", "u", "p"):
+        assert np.array_equal(a.get(f), b.get(f)), f
+    sa, sb = a.solve_energy(), b.solve_energy()
+    assert sa.it_e == sb.it_e and sa.res_e[1] == sb.res_e[1]
+    assert np.array_equal(a.get("t"), b.get("t"))

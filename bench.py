@@ -590,6 +590,7 @@ def run_energy(a, dist):
     W = 4 if a.tet else 6
     ne, nf, nbf = setup.ne, setup.nf, setup.nbf
     g = cfdl.Solver(setup, cfg)
+    g.set_graph_mode(not a.eager)
     g.energy_init()
     for _ in range(a.warmup):                  # developed flow and temperature
         g.step(1, ncoef=0)

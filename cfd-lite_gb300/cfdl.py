@@ -206,14 +206,25 @@ def _check(st, what):
         raise CfdlError(st, what)
 
 
-class Zone:
-    """CGNS-shaped zone of the synthetic cavity (what cell_input reads)."""
+ZONE_KINDS = {"hex": 0, "tet": 1, "prism": 2, "pyramid": 3, "mixed": 4}
 
-    def __init__(self, n, tet=False, jitter=0.0, seed=0):
+
+class Zone:
+    """CGNS-shaped zone of the synthetic cavity (what cell_input reads).
+    tet=True is the six-tet split; kind ("hex", "tet", "prism", "pyramid",
+    "mixed" = hex and pyramid cubes), or a kind name given as tet, overrides
+    it."""
+
+    def __init__(self, n, tet=False, jitter=0.0, seed=0, kind=None):
         L = lib()
+        if isinstance(tet, str):
+            kind = tet
+        k = ZONE_KINDS[kind] if kind is not None else int(bool(tet))
+        tet = k
         nvx, nelem, nsec, m = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         _check(L.cfdl_box_zone_sizes(n, int(tet), C.byref(nvx), C.byref(nelem), C.byref(nsec), C.byref(m)), "zone sizes")
-        self.n, self.tet, self.jitter, self.seed = n, bool(tet), jitter, seed
+        self.n, self.tet, self.jitter, self.seed = n, k == 1, jitter, seed
+        self.kind = k
         self.nvx, self.nelem, self.nsec, self.ne2vxmax = nvx.value, nelem.value, nsec.value, m.value
         self.x = np.zeros(self.nvx); self.y = np.zeros(self.nvx); self.z = np.zeros(self.nvx)
         self.e2vx = np.zeros(self.ne2vxmax * self.nelem, np.int32)

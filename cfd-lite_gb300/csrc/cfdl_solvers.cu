@@ -51,7 +51,8 @@ __device__ __forceinline__ bool any_active(const SolveScalars *S) { return (S->a
 // ------------------------------ momentum ----------------------------------
 // init: b' = b + sum_bdry anb*phi_halo, r = b' - A phi, rh = r.
 // The row's slot indices and coefficients are loaded once for the three
-// components; sums run in slot order.
+// components; sums run in slot order.  W is the compile-time slot bound
+// (6, 4, or kMaxW for other widths, which stops at the case's C.W).
 template <int W>
 __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, double (&v)[6], bool m32) {
     int nb[W];
@@ -59,7 +60,7 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
     bool in[W], bd[W];
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        const int j = C.hf_nb[k * ne + i];
+        const int j = k < C.W ? C.hf_nb[k * ne + i] : -1;
         in[k] = j >= 0 && j < ne;
         bd[k] = j >= ne;
         nb[k] = j >= 0 ? j : i;
@@ -71,7 +72,8 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
         C.fdiag[i] = (float)api;
         C.frap[i] = (float)(1.0 / api);
 #pragma unroll
-        for (int k = 0; k < W; k++) C.fanb[k * ne + i] = (float)a[k];
+        for (int k = 0; k < W; k++)
+            if (k < C.W) C.fanb[k * ne + i] = (float)a[k];
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -366,7 +368,7 @@ __device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, dou
     double bb = C.b[i], s = api * phi[i];
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        const int j = C.hf_nb[k * ne + i];
+        const int j = k < C.W ? C.hf_nb[k * ne + i] : -1;
         if (j < 0) continue;
         const double a = C.anb[k * ne + i];
         if (j >= ne) bb += a * phi[j];

@@ -36,6 +36,8 @@ extern "C" {
 #define CFDL_TRI_3    5
 #define CFDL_QUAD_4   7
 #define CFDL_TETRA_4 10
+#define CFDL_PYRA_5  12
+#define CFDL_PENTA_6 14
 #define CFDL_HEXA_8  17
 
 /* Boundary condition kinds, the procedures the reference binds per section
@@ -45,11 +47,16 @@ extern "C" {
 
 /* ======================================================================
  * 1. Synthetic CGNS-shaped zone (the input the reference reads with
- *    cell_input, src/setup/cell_input.f90:36-99).  Unit cube, n^3 hexes
- *    (HEXA_8) or 6 Kuhn tets per hex (TETRA_4); sections: volume, then
- *    bottom, top, south, north, west, east (QUAD_4 / TRI_3).  Interior
- *    vertices are jittered by U(-jitter,jitter)*h per coordinate, drawn from
- *    SplitMix64(seed) in vertex order.  names: nsec blocks of 33 chars.
+ *    cell_input, src/setup/cell_input.f90:36-99).  Unit cube of n^3 cubes;
+ *    `tet` is the element kind: 0 one HEXA_8 per cube, 1 six Kuhn TETRA_4,
+ *    2 two PENTA_6 (split along the x-y diagonal), 3 six PYRA_5 with the
+ *    apex at the cube centre (an extra vertex per cube), 4 HEXA_8 and
+ *    6-pyramid cubes in a checkerboard (two volume sections).  Sections:
+ *    volume, then bottom, top, south, north, west, east (QUAD_4, or TRI_3
+ *    where the cubes' faces are split).  Interior lattice vertices are
+ *    jittered by U(-jitter,jitter)*h per coordinate, drawn from
+ *    SplitMix64(seed) in vertex order; an apex is the mean of its cube's
+ *    corners.  names: nsec blocks of 33 chars.
  * ====================================================================== */
 int cfdl_box_zone_sizes(int n, int tet, int *nvx, int *nelem, int *nsec, int *ne2vxmax);
 int cfdl_box_zone_fill(int n, int tet, double jitter, uint64_t seed,

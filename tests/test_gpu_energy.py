@@ -63,7 +63,8 @@ def seed_state(o, g, rng):
         g.set(f, v)
 
 
-@pytest.mark.parametrize("n,tet,jit", [(6, False, 0.2), (4, True, 0.0), (3, True, 0.1)])
+@pytest.mark.parametrize("n,tet,jit", [(6, False, 0.2), (4, True, 0.0), (3, True, 0.1), (4, "mixed", 0.2),
+                                       (4, "prism", 0.1)])
 def test_energy_routines_match_oracle(need_gpu, n, tet, jit):
     s, o, g = tight_pair(n, tet, jit, steady=False)
     seed_state(o, g, np.random.default_rng(99))
@@ -94,6 +95,7 @@ def test_energy_routines_match_oracle(need_gpu, n, tet, jit):
     (8, False, 0.2, True, 30),     # jittered hex, steady under-relaxed SIMPLE
     (6, False, 0.0, False, 12),    # reference physics: rho=5, dt=0.01, phi0 updated every 3 passes
     (4, True, 0.0, True, 20),      # tet split
+    (4, "pyramid", 0.1, False, 9),  # six pyramids per cube
 ])
 def test_energy_end_to_end_tight_parity(need_gpu, n, tet, jit, steady, nout):
     s, o, g = tight_pair(n, tet, jit, steady)

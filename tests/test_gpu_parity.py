@@ -67,7 +67,8 @@ def seed_state(o, g, rng):
     return vals
 
 
-@pytest.mark.parametrize("n,tet,jit", [(6, False, 0.2), (4, True, 0.0), (3, True, 0.1)])
+@pytest.mark.parametrize("n,tet,jit", [(6, False, 0.2), (4, True, 0.0), (3, True, 0.1), (4, "prism", 0.2),
+                                       (3, "pyramid", 0.1), (4, "mixed", 0.2)])
 def test_routines_match_oracle(need_gpu, n, tet, jit):
     z, s, o, g = tight_pair(n, tet, jit, steady=False)
     rng = np.random.default_rng(1234)
@@ -126,6 +127,9 @@ def test_momentum_solve_tight(need_gpu):
     (8, False, 0.2, True, 40),     # jittered hex, steady under-relaxed SIMPLE
     (6, False, 0.0, False, 12),    # reference physics: pseudo-transient, rho=5, dt=0.01
     (4, True, 0.0, True, 25),      # tet split
+    (5, "prism", 0.2, True, 20),   # two prisms per cube (W = 5, triangle and quad faces)
+    (3, "pyramid", 0.1, False, 10),  # six pyramids per cube
+    (5, "mixed", 0.2, True, 20),   # hex and pyramid cubes: ELL rows of 6 and 5 slots
 ])
 def test_end_to_end_tight_parity(need_gpu, n, tet, jit, steady, nout):
     z, s, o, g = tight_pair(n, tet, jit, steady=steady)
@@ -138,7 +142,7 @@ def test_end_to_end_tight_parity(need_gpu, n, tet, jit, steady, nout):
 
 
 @pytest.mark.parametrize("precond,precision", [(1, 0), (0, 1), (1, 1)])
-@pytest.mark.parametrize("n,tet,jit", [(8, False, 0.2), (4, True, 0.0), (4, False, 0.0)])
+@pytest.mark.parametrize("n,tet,jit", [(8, False, 0.2), (4, True, 0.0), (4, False, 0.0), (5, "mixed", 0.1)])
 def test_pressure_solver_forms_tight_parity(need_gpu, n, tet, jit, precond, precision):
     """AMG-preconditioned CG and the mixed-precision form (FP32 inner PCG, FP64
     residual and refinement), tight, against the oracle after 20 iterations."""

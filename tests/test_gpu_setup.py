@@ -16,7 +16,8 @@ INTS = ("ef2nb1", "ef2nb2", "ef2nb_idx", "s2g", "bs", "esec", "etype", "red")
 DBLS = ("aip", "rip", "xc", "yc", "zc", "vol")
 
 
-@pytest.mark.parametrize("n,tet,jit", [(5, False, 0.0), (7, True, 0.2), (12, False, 0.2), (9, True, 0.0), (1, True, 0.0)])
+@pytest.mark.parametrize("n,tet,jit", [(5, False, 0.0), (7, True, 0.2), (12, False, 0.2), (9, True, 0.0), (1, True, 0.0),
+                                       (6, "prism", 0.2), (5, "pyramid", 0.1), (7, "mixed", 0.2)])
 def test_device_setup_equals_host(need_gpu, n, tet, jit):
     z = cfdl.Zone(n, tet, jit, seed=n)
     h, d = cfdl.Setup(z), cfdl.Setup(z, device=True)

@@ -88,7 +88,7 @@ def restated_vtu(s, fields, vars_):
     return b"".join(out)
 
 
-@pytest.mark.parametrize("n,tet", [(5, False), (4, True)])
+@pytest.mark.parametrize("n,tet", [(5, False), (4, True), (3, "prism"), (3, "mixed")])
 def test_vtu_bytes_match_the_reference_layout(need_gpu, tmp_path, n, tet):
     z = cfdl.Zone(n, tet, 0.1, seed=3)
     s = cfdl.Setup(z)

@@ -19,7 +19,8 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-@pytest.mark.parametrize("n,tet,jit", [(4, False, 0.0), (5, False, 0.2), (3, True, 0.0)])
+@pytest.mark.parametrize("n,tet,jit", [(4, False, 0.0), (5, False, 0.2), (3, True, 0.0), (3, "prism", 0.2),
+                                       (3, "pyramid", 0.2), (4, "mixed", 0.1)])
 def test_grad_exact_for_linear_fields(n, tet, jit):
     """calc_grad is exact for linear fields, halos included: halo centres sit
     on the boundary face centroids (calc_vol_cv_centers.f90:37-42)."""
@@ -38,8 +39,9 @@ def _fresh(n=5, tet=False, jit=0.2, cfg=None, nsub=4):
     return z, o
 
 
-def test_pressure_matrix_symmetric_rows_sum_to_zero():
-    z, o = _fresh()
+@pytest.mark.parametrize("kind", ["hex", "prism", "pyramid", "mixed"])
+def test_pressure_matrix_symmetric_rows_sum_to_zero(kind):
+    z, o = _fresh(tet=kind)
     o.run(3)
     o.update_boundaries()
     o.calc_coef_uvw()

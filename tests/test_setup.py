@@ -17,7 +17,23 @@ import oracle_lib
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden", "setup_hashes.json")
 
-CASES = [(2, False, 0.0), (4, False, 0.2), (8, False, 0.2), (3, True, 0.0), (6, True, 0.1), (12, False, 0.1)]
+CASES = [(2, False, 0.0), (4, False, 0.2), (8, False, 0.2), (3, True, 0.0), (6, True, 0.1), (12, False, 0.1),
+         (4, "prism", 0.2), (3, "pyramid", 0.1), (5, "mixed", 0.2), (1, "pyramid", 0.0)]
+
+
+def expected_sizes(n, tet):
+    """(cells, boundary faces, half-faces) of the synthetic zone of each kind."""
+    c = n ** 3
+    if tet is True or tet == "tet":
+        return 6 * c, 12 * n * n, 24 * c
+    if tet == "prism":
+        return 2 * c, 8 * n * n, 10 * c
+    if tet == "pyramid":
+        return 6 * c, 6 * n * n, 30 * c
+    if tet == "mixed":
+        p = c // 2
+        return (c - p) + 6 * p, 6 * n * n, 6 * (c - p) + 30 * p
+    return c, 6 * n * n, 6 * c
 
 
 def sha(a):
@@ -37,15 +53,11 @@ def test_setup_matches_oracle_bit_exact(n, tet, jit):
         assert np.array_equal(a, b), name  # bit-exact doubles
 
 
-@pytest.mark.parametrize("n,tet", [(2, False), (5, False), (3, True)])
+@pytest.mark.parametrize("n,tet", [(2, False), (5, False), (3, True), (3, "prism"), (3, "pyramid"), (4, "mixed")])
 def test_sizes_and_invariants(n, tet):
     z = cfdl.Zone(n, tet, 0.15, seed=3)
     s = cfdl.Setup(z)
-    per = 6 if tet else 1
-    assert s.ne == per * n ** 3
-    assert s.nbf == 6 * n * n * (2 if tet else 1)
-    nface = 4 if tet else 6
-    assert s.H == nface * s.ne
+    assert (s.ne, s.nbf, s.H) == expected_sizes(n, tet)
     vol = s.get_dbl("vol")
     assert (vol > 0).all()
     assert abs(vol.sum() - 1.0) < 1e-13                     # unit cube

@@ -305,9 +305,17 @@ def steady(**kw):
 class Solver:
     """One case resident on the GPU, driven like the reference's phys_t."""
 
-    def __init__(self, setup, config=None, u_lid=1.0):
+    def __init__(self, setup, config=None, u_lid=1.0, bc_kinds=None):
+        """bc_kinds (optional): {bc index: BC_WALL or BC_SYMMETRY} overriding the
+        binding of cfdl_setup_mesh (eqn%bcs order)."""
         self.setup = setup
         self.mesh = setup.mesh(u_lid)
+        if bc_kinds:
+            kinds = np.ctypeslib.as_array(C.cast(self.mesh.bc_kind, C.POINTER(C.c_int)), (self.mesh.nbc,)).copy()
+            for i, k in bc_kinds.items():
+                kinds[i] = k
+            self._bc_kinds = kinds
+            self.mesh.bc_kind = kinds.ctypes.data_as(C.c_void_p)
         self.config = config if config is not None else default_config()
         self.ne, self.nf, self.nbf, self.H = setup.ne, setup.nf, setup.nbf, setup.H
         self._h = C.c_void_p()

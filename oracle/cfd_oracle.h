@@ -92,6 +92,10 @@ int or_subdomain_get(const ocase *c, int sd, int *ef2nb_idx, int *ef2nb);
  * src/equations/mod_uvwp.f90:20-84). */
 int  or_physics_init(ocase *c, const or_config *cfg);
 void or_set_config(ocase *c, const or_config *cfg);
+/* Rebind boundary condition i (1-based, eqn%bcs order) to another of the
+ * reference's BC procedures, as an edited construct_uvwp would:
+ * 1 lid, 2 dirichlet0, 3 symmetry (mod_uvwp.f90:493-570). */
+int  or_set_bc_kind(ocase *c, int i, int kind);
 void or_update_boundaries(ocase *c);                 /* mod_physics.f90:38  */
 void or_solve_uvwp(ocase *c, or_stats *st);          /* mod_uvwp.f90:95     */
 void or_update_time(ocase *c);                       /* mod_physics.f90:101 */

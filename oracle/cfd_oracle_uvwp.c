@@ -312,6 +312,15 @@ void or_update_time(ocase *c) {
     if (c->energy_on) o_energy_time(c);      /* mod_physics.f90:111 */
 }
 
+int or_set_bc_kind(ocase *c, int i, int kind) {
+    if (!c->bcs || i < 1 || i > c->nintf_c2b || c->bcs[i].kind == BC_NONE) return -1;
+    if (kind == 1) c->bcs[i].kind = BC_LID;
+    else if (kind == 2) c->bcs[i].kind = BC_DIRICHLET0;
+    else if (kind == 3) c->bcs[i].kind = BC_SYMMETRY;
+    else return -1;
+    return 0;
+}
+
 void or_set_config(ocase *c, const or_config *cfg) {
     c->cfg = *cfg;
     if (c->rho) for (int e = 1; e <= c->ne; e++) { c->rho[e] = cfg->rho; c->mu[e] = cfg->mu; }

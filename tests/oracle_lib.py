@@ -73,6 +73,7 @@ def lib():
         L.or_subdomain_sizes.argtypes = [vp, C.c_int, vp]
         L.or_subdomain_get.argtypes = [vp, C.c_int, vp, vp]
         L.or_energy_init.argtypes = [vp] + [C.c_double] * 5
+        L.or_set_bc_kind.argtypes = [vp, C.c_int, C.c_int]
         L.or_calc_coef_energy.argtypes = [vp]
         L.or_calc_coef_energy.restype = None
         L.or_solve_energy.argtypes = [vp, C.POINTER(OrStats)]
@@ -161,6 +162,12 @@ class Oracle:
 
     def physics_init(self, cfg):
         lib().or_physics_init(self._h, C.byref(cfg))
+
+    def set_bc_kind(self, i, kind):
+        """Rebind BC i (0-based, eqn%bcs order): 'lid', 'dirichlet0' or 'symmetry'."""
+        k = {"lid": 1, "dirichlet0": 2, "symmetry": 3}[kind]
+        if lib().or_set_bc_kind(self._h, int(i) + 1, k) != 0:
+            raise ValueError("cannot rebind BC %d" % i)
 
     def set_config(self, cfg):
         lib().or_set_config(self._h, C.byref(cfg))

@@ -9,6 +9,7 @@ End to end, both sides run in the tight mode (every inner solve to
 relative L2 after the same number of outer iterations (the target the
 reference comparison is stated in).
 """
+import ctypes as C
 import math
 
 import numpy as np
@@ -271,3 +272,43 @@ def test_step_host_matches_resident(need_gpu, graph):
         assert cfdl.lib().cfdl_step_host(g2._h, C.byref(fl), 1, 0, None) == 0
     for f in ("u", "v", "w", "p", "mip", "gu", "gp", "gpc"):
         assert np.array_equal(g1.get(f), host[f]), f
+
+
+@pytest.mark.parametrize("tet", [False, "prism"])
+def test_symmetry_bc_tight_parity(need_gpu, tet):
+    """A wall rebound to the reference's symmetry procedure (mod_uvwp.f90:517-546,
+    bc_type 'zero_flux'): reflected halo velocity, no wall shear term, the
+    same diffusion coefficient in ap/anb.  Routines and the end-to-end tight
+    run agree with the oracle."""
+    n, jit = 5, 0.2
+    z = cfdl.Zone(n, tet, jit, seed=11)
+    s = cfdl.Setup(z)
+    m = s.mesh(1.0)
+    vel = np.ctypeslib.as_array(C.cast(m.bc_vel, C.POINTER(C.c_double)), (3 * m.nbc,))
+    walls = [i for i in range(m.nbc) if vel[3 * i] == 0.0]
+    sym = {walls[-1]: cfdl.BC_SYMMETRY, walls[0]: cfdl.BC_SYMMETRY}
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    for i in sym:
+        o.set_bc_kind(i, "symmetry")
+    g = cfdl.Solver(s, cfdl.steady(solve_mode=1, tight_rtol=1e-13), bc_kinds=sym)
+    rng = np.random.default_rng(3)
+    seed_state(o, g, rng)
+    o.update_boundaries(); g.update_boundaries()
+    for f in ("u", "v", "w", "p", "mip"):
+        assert rel_max(g.get(f), o.get(f)) < 1e-14, f
+    o.calc_coef_uvw(); g.calc_coef_uvw()
+    for f in ("ap", "anb", "bu", "bv", "bw"):
+        assert rel_max(g.get(f), o.get(f)) < RTOL_KERNEL, f
+    # end to end from the construct state
+    o2 = oracle_lib.Oracle(z, n_subdomains=4)
+    o2.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    for i in sym:
+        o2.set_bc_kind(i, "symmetry")
+    g2 = cfdl.Solver(s, cfdl.steady(solve_mode=1, tight_rtol=1e-13), bc_kinds=sym)
+    o2.run(15, 3)
+    st = g2.step(15, 3)
+    assert st.status == 0
+    for f in ("u", "v", "w", "p"):
+        a, b = g2.get(f)[:o2.ne], o2.get(f)[:o2.ne]
+        assert rel_l2(a, b) < RTOL_FIELD, (f, rel_l2(a, b))

@@ -423,9 +423,12 @@ int cfdl_energy_init(cfdl_ctx *ctx, double cp, double tc, double t_init) {
     for (HostCase *hc : ctx->cases)
         if (hc->h_temp.empty()) return CFDL_ERR_INVALID;   // the mesh carried no energy BCs
     for (HostCase *hc : ctx->cases)
-        if ((st = energy_init_case(ctx, hc, cp, tc, t_init))) return st;
-    destroy_graph(ctx);   // the run graph is captured without the energy launches
-    if ((st = upload_case_table(ctx))) return st;
+        if ((st = energy_init_case(ctx, hc, cp, tc, t_init))) break;
+    // the device table follows the host records even after a failure part way
+    destroy_graph(ctx);   // graphs captured without (or with) the energy launches
+    const int st2 = upload_case_table(ctx);
+    if (st) return st;
+    if (st2) return st2;
     return cuda_status(cudaStreamSynchronize(ctx->stream));
 }
 

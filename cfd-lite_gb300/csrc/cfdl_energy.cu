@@ -236,19 +236,25 @@ int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t
     const size_t ne = hc->ne, nc = ne + hc->nbf;
     int st;
     if (!d.ee) {
+        // allocate everything first: the case's energy pointers are set only
+        // when all of it exists (a null d.ee means "no energy equation")
+        CaseDev e = d;
         void *p;
         struct A { double **dst; size_t n; } list[] = {
-            {&d.et, nc}, {&d.ee, nc}, {&d.ee0, nc}, {&d.egt, 3 * nc}, {&d.ege, 3 * nc}, {&d.ecp, ne}, {&d.etc, ne},
-            {&d.eprop, (size_t)EP_N * hc->nf}};
+            {&e.et, nc}, {&e.ee, nc}, {&e.ee0, nc}, {&e.egt, 3 * nc}, {&e.ege, 3 * nc}, {&e.ecp, ne}, {&e.etc, ne},
+            {&e.eprop, (size_t)EP_N * hc->nf}};
         for (const A &a : list) {
             if ((st = case_alloc(hc, &p, a.n * sizeof(double)))) return st;
             *a.dst = (double *)p;
         }
         if ((st = case_alloc(hc, &p, std::max<size_t>(hc->nbf, 1) * sizeof(double)))) return st;
-        d.eh_t = (const double *)p;
+        e.eh_t = (const double *)p;
         if ((st = cuda_status(cudaMemcpyAsync(p, hc->h_temp.data(), hc->nbf * sizeof(double), cudaMemcpyHostToDevice,
                                               ctx->stream))))
             return st;
+        d.et = e.et; d.ee0 = e.ee0; d.egt = e.egt; d.ege = e.ege; d.ecp = e.ecp; d.etc = e.etc;
+        d.eprop = e.eprop; d.eh_t = e.eh_t;
+        d.ee = e.ee;
     }
     const int tb = 256;
     k_fill<<<(unsigned)((ne + tb - 1) / tb), tb, 0, ctx->stream>>>(d.ecp, ne, cp);

@@ -33,7 +33,8 @@ sys.path.insert(0, PKG)
 
 METRIC = "SIMPLE cell-iters/s"
 DTYPES = {0: "f64", 1: "f64+f32 (mixed pressure solve)",
-          2: "f64+f32 (mixed pressure solve, FP32 momentum corrections)"}
+          2: "f64+f32 (mixed pressure solve, FP32 momentum corrections)",
+          3: "f64+f32 (mixed pressure solve, FP32 momentum corrections, FP32 explicit momentum face terms)"}
 UNIT = "cell-iters/s"
 
 

@@ -22,6 +22,11 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
         # momentum cell gather: ELL nb/fc, 5 face doubles, 13 cell doubles in, 6 out, anb ELL out
         "k_coef_uvw_cell": 2 * ell_i + nf * 40 + ne * (104 + 48) + ell_d + nbf * (24 + 4 + 32),
         "k_grad3": ell_i + 3 * ell_d + 24 * (ne + nbf) + 72 * ne,
+        # precision 3: FP32 stencil, FP32 gradients out and the widened FP64 copies
+        "k_grad3_f32": ell_i + 3 * 4 * W * ne + 24 * (ne + nbf) + 108 * ne,
+        # precision 3: own/nb, 7 FP32 planes, 3 FP32 outputs; FP32 gradients of both cells
+        "k_coef_uvw_face_f32": nfi * (8 + 28 + 12) + ne * 36,
+        "k_narrow_grad": ne * (72 + 36),
         "k_grad1": ell_i + 3 * ell_d + 8 * (ne + nbf) + 24 * ne,
         # Rhie-Chow: own/nb, 8 geometry planes, mip0 in, mip out; 12 cell doubles
         "k_calc_mip": nfi * (8 + 72 + 16) + ne * 80,

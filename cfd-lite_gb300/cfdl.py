@@ -138,6 +138,7 @@ def lib():
     for n in ("cfdl_solve_uvwp", "cfdl_solve_momentum", "cfdl_solve_pc", "cfdl_solve_energy"):
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
     L.cfdl_energy_init.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.cfdl_check_conversions.argtypes = [C.c_int, vp]
     L.cfdl_set_energy_tile.argtypes = [vp, C.c_int]
     L.cfdl_get_energy_tile.argtypes = [vp]
     L.cfdl_calc_coef_energy.argtypes = [vp]
@@ -580,6 +581,14 @@ class Batch(Solver):
         ne, nb = C.c_int(), C.c_size_t()
         _check(lib().cfdl_case_info(self._h, int(cid), C.byref(ne), C.byref(nb)), "case_info")
         return ne.value, nb.value
+
+
+def check_conversions(n=1 << 20):
+    """Mismatches (narrowing, widening) of the precision-3 integer conversions
+    against the hardware ones; both 0 when they agree."""
+    out = np.zeros(2, np.uint32)
+    _check(lib().cfdl_check_conversions(int(n), _p(out)), "check_conversions")
+    return int(out[0]), int(out[1])
 
 
 def case_bytes_estimate(ne, nf, nbf, W=6):

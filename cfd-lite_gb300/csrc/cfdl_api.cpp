@@ -22,8 +22,8 @@ int validate_config(const cfdl_config *c) {
     if (!c) return CFDL_ERR_INVALID;
     if (!(c->rho > 0) || !(c->mu >= 0) || !(c->dt > 0) || !(c->alpha_u > 0 && c->alpha_u <= 1) ||
         !(c->alpha_p > 0 && c->alpha_p <= 1) || c->nit < 0 || c->tight_maxit < 0 ||
-        (c->solve_mode != 0 && c->solve_mode != 1) || c->precision < 0 || c->precision > 2 ||
-        (c->precision == 2 && c->solve_mode != 0) ||
+        (c->solve_mode != 0 && c->solve_mode != 1) || c->precision < 0 || c->precision > 3 ||
+        (c->precision >= 2 && c->solve_mode != 0) ||
         !(c->rtol_u > 0) || !(c->rtol_p > 0) || !(c->tight_rtol > 0) || (c->precond != 0 && c->precond != 1))
         return CFDL_ERR_INVALID;
     return CFDL_OK;
@@ -58,6 +58,7 @@ int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool
     if (!host) return CFDL_ERR_INVALID;
     if (!to_host && (nm.ptr == hc->dev.rho || nm.ptr == hc->dev.mu)) hc->props_dirty = true;
     if (!to_host && nm.ptr && (nm.ptr == hc->dev.ecp || nm.ptr == hc->dev.etc)) hc->eprops_dirty = true;
+    if (!to_host && (nm.ptr == hc->dev.gu || nm.ptr == hc->dev.gv || nm.ptr == hc->dev.gw)) hc->g32_stale = true;
     cudaError_t e;
     if (!nm.ell) {
         e = cudaMemcpyAsync(to_host ? (void *)host : (void *)nm.ptr, to_host ? (const void *)nm.ptr : (const void *)host,
@@ -96,6 +97,7 @@ int transfer_fields(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f, bool to_h
         {f->gu, d.gu, 3 * nc}, {f->gv, d.gv, 3 * nc}, {f->gw, d.gw, 3 * nc}, {f->gp, d.gp, 3 * nc}, {f->gpc, d.gpc, 3 * nc},
         {f->mip, d.mip, nf}, {f->mip0, d.mip0, nf},
     };
+    if (!to_host && (f->gu || f->gv || f->gw)) hc->g32_stale = true;   // precision 3 derives g32 from them
     for (const P &p : list) {
         if (!p.h) continue;
         cudaError_t e = to_host ? cudaMemcpyAsync(p.h, p.dv, p.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream)
@@ -213,6 +215,8 @@ int cfdl_set_config(cfdl_ctx *ctx, const cfdl_config *cfg) {
             if ((st = cuda_status(cudaMemcpy(hc->dev.rho, rho.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
             if ((st = cuda_status(cudaMemcpy(hc->dev.mu, mu.data(), hc->ne * sizeof(double), cudaMemcpyHostToDevice)))) return st;
         }
+        if (cfg->precision == 3 && (st = ensure_f32_assembly(hc, ctx->stream))) return st;
+        if (cfg->precision == 3 && hc->cfg.precision != 3) hc->g32_stale = true;
         apply_config(hc, cfg);
     }
     return upload_case_table(ctx);
@@ -595,6 +599,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 10 * f * 8;                              // property planes
     bytes += 24 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
     bytes += 160 * c;                                 // multigrid hierarchy (bound)
+    bytes += 9 * c * 4 + 3 * w * c * 4 + 7 * f * 4;   // precision 3 FP32 gradients, stencil, face planes
     return bytes;
 }
 

@@ -372,6 +372,7 @@ int upload_case(CasePrep &p, const cfdl_config *cfg, HostCase **out) {
             st = upload_case_amg(hc, p.amg);   // takes the hierarchy
             p.amg = nullptr;
         }
+        if (!st && cfg->precision == 3) st = ensure_f32_assembly(hc, 0);
         if (st) { destroy_case(hc); return st; }
         apply_config(hc, cfg);
     } catch (const std::bad_alloc &) {

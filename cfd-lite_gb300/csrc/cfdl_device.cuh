@@ -146,5 +146,42 @@ __device__ __forceinline__ double flip_sign(double x, bool neg) {
 __device__ __forceinline__ double positive_part(double x) {
     return __double_as_longlong(x) > 0 ? x : 0.0;
 }
+// -x when neg, else x, for FP32
+__device__ __forceinline__ float flip_sign_f(float x, bool neg) {
+    return __uint_as_float(__float_as_uint(x) ^ ((unsigned)neg << 31));
+}
+
+// FP64 <-> FP32 from the IEEE 754 binary64 / binary32 bit layouts, in the
+// integer pipe: GB300 executes the hardware conversion instructions at its
+// FP64 rate (2 per SM per clock), so a kernel that is meant to spend no FP64
+// work converts this way.
+//
+// binary64 -> binary32, rounded to nearest (ties to even) on the 29 dropped
+// mantissa bits; results below the binary32 normal range become a signed
+// zero, overflow gives infinity, NaN stays NaN.
+__device__ __forceinline__ float narrow_f32(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));
+    const int fe = e - 1023 + 127;
+    if (fe <= 0) return __uint_as_float(sign);
+    if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+    unsigned r = ((unsigned)fe << 23) | (unsigned)(m >> 29);
+    const unsigned rem = (unsigned)(m & 0x1fffffffu);
+    if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) r += 1u;   // a carry moves into the exponent
+    return __uint_as_float(sign | r);
+}
+// binary32 -> binary64: exact for normal values; a binary32 subnormal gives a
+// signed zero
+__device__ __forceinline__ double widen_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    const unsigned long long de = e == 0xffu ? 0x7ffull : (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)m << 29)));
+}
 
 }  // namespace cfdl

@@ -393,6 +393,7 @@ int solve_energy_graph(cfdl_ctx *ctx) {
 int run_graph_launch(cfdl_ctx *ctx) {
     int st;
     ensure_face_props(ctx);
+    ensure_g32(ctx);
     ensure_energy_props(ctx);
     if (!ctx->run_exec || ctx->run_form != graph_form(ctx))
         if ((st = build_run_graph(ctx))) return st;
@@ -406,6 +407,7 @@ int run_graph_launch(cfdl_ctx *ctx) {
 int solve_uvwp_graph(cfdl_ctx *ctx) {
     int st;
     ensure_face_props(ctx);
+    ensure_g32(ctx);
     if (!ctx->graph_exec || ctx->graph_form != graph_form(ctx))
         if ((st = build_graph(ctx))) return st;
     ctx->launches += ctx->graph_static_kernels;

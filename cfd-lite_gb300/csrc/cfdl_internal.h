@@ -125,6 +125,10 @@ struct CaseDev {
     // face intermediates of the assemblies
     double *fdiff, *fS;                   // [nf] pressure face coefficient, [3][nf] explicit momentum face terms
     double *fprop;                        // [PR_N][nf] property planes
+    // precision 3 (FP32 explicit momentum face terms); null otherwise:
+    float *g32;                           // [3][ne][3] FP32 gradients of u, v, w
+    float *G32;                           // [3][W][ne] FP32 copy of the gradient stencil hf_G
+    float *fprop32;                       // [7][nf] FP32 weight, mu*area*dr/ds, mu*area*(dr_p/ds_p - dr/ds)
     // Krylov work vectors, [3][ne] each (pressure uses plane 0)
     double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt;
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each
@@ -178,6 +182,7 @@ struct HostCase {
     size_t bytes = 0;                // device bytes held (mesh, fields, solver, hierarchy)
     std::vector<double> h_temp;      // [nbf] energy wall temperature of each halo (empty: none)
     bool eprops_dirty = true;        // eprop must be recomputed (cp or tc changed)
+    bool g32_stale = false;          // g32 must be rebuilt from gu, gv, gw (they were written from outside)
 };
 
 }  // namespace cfdl
@@ -267,6 +272,8 @@ void apply_config(HostCase *hc, const cfdl_config *cfg);
 // kernel launchers (cfdl_kernels.cu): asynchronous on ctx->stream, all cases
 void launch_bc(cfdl_ctx *ctx);
 void ensure_face_props(cfdl_ctx *ctx);   // recompute the property planes of cases whose rho/mu changed
+void ensure_g32(cfdl_ctx *ctx);          // precision 3: rebuild stale FP32 gradients from gu, gv, gw
+int ensure_f32_assembly(HostCase *hc, cudaStream_t stream);   // precision 3 arrays (allocated once)
 void launch_coef_uvw(cfdl_ctx *ctx);
 void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused, 5 = energy t, phi
 void launch_calc_mip(cfdl_ctx *ctx, int rhie_chow);

@@ -107,14 +107,52 @@ __global__ void __launch_bounds__(kTile) k_face_props(const CaseDev *__restrict_
     pr[PR_RHO * nf + i] = rhoip;
     pr[PR_RHOADN * nf + i] = rhoip * adn;
     pr[PR_RHOMADN * nf + i] = (C.rho[o] + C.rho[n]) / 2.0 * adn;
+    if (C.fprop32) {   // precision 3: the planes of the FP32 explicit face terms
+        float *pf = C.fprop32;
+        pf[i] = narrow_f32(wt);
+        for (int m = 0; m < 3; m++) {
+            pf[(1 + m) * nf + i] = narrow_f32(pr[(PR_MAX + m) * nf + i]);
+            pf[(4 + m) * nf + i] = narrow_f32(pr[(PR_MEX + m) * nf + i]);
+        }
+    }
+}
+
+// calc_coef_uvw face part in FP32 (precision 3): the same two explicit terms
+// as k_coef_uvw_face -- sumss and the deferred non-orthogonal correction, the
+// deferred-correction sources of the momentum equations -- from the FP32
+// gradients and planes, with no FP64 instruction; fS holds them as FP32.
+__global__ void __launch_bounds__(kTile) k_coef_uvw_face_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, ne = C.ne, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= ne) return;
+    const float *pf = C.fprop32;
+    const float wt = pf[i], omw = 1.0f - wt;
+    const float A0 = pf[nf + i], A1 = pf[2 * nf + i], A2 = pf[3 * nf + i];
+    const float E0 = pf[4 * nf + i], E1 = pf[5 * nf + i], E2 = pf[6 * nf + i];
+    float gi[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float *g = C.g32 + (size_t)q * 3 * ne;
+#pragma unroll
+        for (int m = 0; m < 3; m++) gi[q][m] = omw * g[3 * o + m] + wt * g[3 * n + m];
+    }
+    float *fS = (float *)C.fS;
+#pragma unroll
+    for (int m = 0; m < 3; m++)
+        fS[m * nf + i] = (gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2) + (gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2);
 }
 
 // calc_coef_uvw, cell part (mod_uvwp.f90:174-284) + implicit relaxation.
+// F32 (precision 3): the explicit face terms are FP32 and summed in FP32.
+template <bool F32>
 __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, nf = C.nf, W = C.W;
     double ap = 0.0, sumf = 0.0, ss0 = 0.0, ss1 = 0.0, ss2 = 0.0;
+    float fs0 = 0.f, fs1 = 0.f, fs2 = 0.f;
+    const float *fS32 = (const float *)C.fS;
     double a[kMaxW];
     int bslot[kMaxW], nb_cnt = 0;
 #pragma unroll
@@ -134,8 +172,13 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         ap += ak;
         // sg * x as a sign-bit flip: no FP64 multiply
         const bool ng = fc < 0;
-        ss0 += flip_sign(C.fS[f], ng); ss1 += flip_sign(C.fS[nf + f], ng); ss2 += flip_sign(C.fS[2 * nf + f], ng);
+        if (F32) {
+            fs0 += flip_sign_f(fS32[f], ng); fs1 += flip_sign_f(fS32[nf + f], ng); fs2 += flip_sign_f(fS32[2 * nf + f], ng);
+        } else {
+            ss0 += flip_sign(C.fS[f], ng); ss1 += flip_sign(C.fS[nf + f], ng); ss2 += flip_sign(C.fS[2 * nf + f], ng);
+        }
     }
+    if (F32) { ss0 = widen_f64(fs0); ss1 = widen_f64(fs1); ss2 = widen_f64(fs2); }
     double asum = ap;                       // sum of the anb of this row so far
     const double vol = C.vol[i];
     const double ue = C.u[i], ve = C.v[i], we = C.w[i];
@@ -226,6 +269,92 @@ __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ case
     }
 #pragma unroll
     for (int q = 0; q < NF; q++) { grad[q][3 * i] = g[q][0]; grad[q][3 * i + 1] = g[q][1]; grad[q][3 * i + 2] = g[q][2]; }
+}
+
+// calc_grad of u, v, w for the FP32 explicit face terms (precision 3): the
+// neighbour differences in FP64, narrowed in the integer pipe, the stencil
+// sums in FP32; the gradients go to g32 and, widened, to gu, gv, gw.
+__global__ void __launch_bounds__(kTile) k_grad3_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, W = C.W;
+    const double *phi[3] = {C.u, C.v, C.w};
+    double *grad[3] = {C.gu, C.gv, C.gw};
+    double pe[3];
+    float g[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) { pe[q] = phi[q][i]; g[q][0] = g[q][1] = g[q][2] = 0.f; }
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= W) break;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb < 0) break;
+        const float G0 = C.G32[(0 * W + k) * ne + i], G1 = C.G32[(1 * W + k) * ne + i], G2 = C.G32[(2 * W + k) * ne + i];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float d = narrow_f32(phi[q][nb] - pe[q]);
+            g[q][0] += G0 * d; g[q][1] += G1 * d; g[q][2] += G2 * d;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        float *g32 = C.g32 + (size_t)q * 3 * ne + 3 * i;
+#pragma unroll
+        for (int m = 0; m < 3; m++) { g32[m] = g[q][m]; grad[q][3 * i + m] = widen_f64(g[q][m]); }
+    }
+}
+
+// precision 3: g32 from gu, gv, gw after they were written from outside
+// (uploads, set_array, a restored snapshot)
+__global__ void __launch_bounds__(kTile) k_narrow_grad(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_PROLOGUE(cells)
+    if (i >= t.last || !C.g32) return;
+    const double *grad[3] = {C.gu, C.gv, C.gw};
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int m = 0; m < 3; m++) C.g32[(size_t)q * 3 * C.ne + 3 * i + m] = narrow_f32(grad[q][3 * i + m]);
+}
+
+__global__ void k_narrow_array(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+    const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j < n) out[j] = narrow_f32(in[j]);
+}
+
+// narrow_f32 / widen_f64 against the hardware conversions on n values drawn
+// from every binary64 exponent (bit patterns from a 64-bit mix of the
+// index) plus signed zeros, infinities and NaN.  Differences are counted
+// except where the definitions differ on purpose: values whose binary32
+// result is subnormal (flushed to a signed zero here).
+__global__ void k_check_conversions(int n, unsigned *bad) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    unsigned long long z = 0x9e3779b97f4a7c15ull * (unsigned long long)(j + 1);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    // exponents concentrated near the binary32 range so that rounding, carries and
+    // the range limits are all exercised
+    const unsigned long long e = 1023 - 140 + (z >> 52) % 290;
+    unsigned long long bits = (z & 0x800fffffffffffffull) | (e << 52);
+    if (j < 8) {
+        const unsigned long long special[8] = {0x0ull, 0x8000000000000000ull, 0x7ff0000000000000ull, 0xfff0000000000000ull,
+                                               0x7ff8000000000000ull, 0x3ff0000010000000ull, 0x3ff0000030000000ull,
+                                               0x47efffffefffffffull};
+        bits = special[j];
+    }
+    const double x = __longlong_as_double((long long)bits);
+    const float mine = narrow_f32(x), ref = __double2float_rn(x);
+    const unsigned mu = __float_as_uint(mine), ru = __float_as_uint(ref);
+    const bool ref_sub = (ru & 0x7f800000u) == 0 && (ru & 0x7fffffu) != 0;
+    const bool nan_both = (ru & 0x7fffffffu) > 0x7f800000u && (mu & 0x7fffffffu) > 0x7f800000u;
+    if (mu != ru && !nan_both && !(ref_sub && (mu & 0x7fffffffu) == 0)) atomicAdd(&bad[0], 1u);
+    // widening: exact for every normal binary32
+    const float f = __uint_as_float((unsigned)(z >> 11));
+    const unsigned fe = (__float_as_uint(f) >> 23) & 0xffu;
+    if (fe != 0 && fe != 0xffu) {
+        if (__double_as_longlong(widen_f64(f)) != __double_as_longlong((double)f)) atomicAdd(&bad[1], 1u);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -384,13 +513,29 @@ void ensure_face_props(cfdl_ctx *ctx) {
     CFDL_LAUNCH("k_face_props", k_face_props, faces);
     for (HostCase *hc : ctx->cases) hc->props_dirty = false;
 }
+static bool f32_assembly(const cfdl_ctx *ctx) { return ctx->cases[0]->cfg.precision == 3; }
+
+void ensure_g32(cfdl_ctx *ctx) {
+    bool stale = false;
+    for (HostCase *hc : ctx->cases) stale |= hc->g32_stale;
+    if (!stale || ctx->capturing || !f32_assembly(ctx)) return;
+    CFDL_LAUNCH("k_narrow_grad", k_narrow_grad, cells);
+    for (HostCase *hc : ctx->cases) hc->g32_stale = false;
+}
 void launch_coef_uvw(cfdl_ctx *ctx) {
     ensure_face_props(ctx);
+    if (f32_assembly(ctx)) {
+        ensure_g32(ctx);
+        CFDL_LAUNCH("k_coef_uvw_face_f32", k_coef_uvw_face_f32, faces);
+        CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell<true>, cells);
+        return;
+    }
     CFDL_LAUNCH("k_coef_uvw_face", k_coef_uvw_face, faces);
-    CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell, cells);
+    CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell<false>, cells);
 }
 void launch_grad(cfdl_ctx *ctx, int field) {
-    if (field == 4) CFDL_LAUNCH("k_grad3", k_grad<3>, cells, 0);
+    if (field == 4 && f32_assembly(ctx)) CFDL_LAUNCH("k_grad3_f32", k_grad3_f32, cells);
+    else if (field == 4) CFDL_LAUNCH("k_grad3", k_grad<3>, cells, 0);
     else if (field == 5) CFDL_LAUNCH("k_grad2", k_grad<2>, cells, 0);
     else CFDL_LAUNCH("k_grad1", k_grad<1>, cells, field);
 }
@@ -426,4 +571,42 @@ void launch_update_time(cfdl_ctx *ctx) {
 }
 void launch_set_mip0(cfdl_ctx *ctx) { CFDL_LAUNCH("k_copy_mip0", k_copy_mip0, faces); }
 
+// precision 3 arrays of a case: FP32 gradients, the FP32 gradient stencil
+// (narrowed from hf_G once) and the FP32 face planes (filled with the
+// property planes, which are marked for recomputation)
+int ensure_f32_assembly(HostCase *hc, cudaStream_t stream) {
+    CaseDev &d = hc->dev;
+    if (d.g32) return CFDL_OK;
+    const size_t ne = hc->ne, nf = hc->nf, nG = 3 * (size_t)hc->W * ne;
+    void *g = nullptr, *G = nullptr, *pf = nullptr;
+    int st;
+    if ((st = case_alloc(hc, &g, 9 * ne * sizeof(float)))) return st;
+    if ((st = case_alloc(hc, &G, nG * sizeof(float)))) return st;
+    if ((st = case_alloc(hc, &pf, 7 * nf * sizeof(float)))) return st;
+    const int tb = 256;
+    k_narrow_array<<<(unsigned)((nG + tb - 1) / tb), tb, 0, stream>>>(d.hf_G, (float *)G, nG);
+    if ((st = cuda_status(cudaGetLastError()))) return st;
+    if ((st = cuda_status(cudaMemsetAsync(pf, 0, 7 * nf * sizeof(float), stream)))) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(stream)))) return st;
+    d.g32 = (float *)g; d.G32 = (float *)G; d.fprop32 = (float *)pf;
+    hc->props_dirty = true;      // k_face_props fills fprop32
+    hc->g32_stale = true;        // k_narrow_grad fills g32 from gu, gv, gw
+    return CFDL_OK;
+}
+
 }  // namespace cfdl
+
+extern "C" int cfdl_check_conversions(int n, unsigned *mismatches) {
+    if (n <= 0 || !mismatches) return CFDL_ERR_INVALID;
+    unsigned *d = nullptr;
+    int st = cfdl::cuda_status(cudaMalloc(&d, 2 * sizeof(unsigned)));
+    if (st) return st;
+    st = cfdl::cuda_status(cudaMemset(d, 0, 2 * sizeof(unsigned)));
+    if (!st) {
+        cfdl::k_check_conversions<<<(n + 255) / 256, 256>>>(n, d);
+        st = cfdl::cuda_status(cudaGetLastError());
+    }
+    if (!st) st = cfdl::cuda_status(cudaMemcpy(mismatches, d, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    cudaFree(d);
+    return st;
+}

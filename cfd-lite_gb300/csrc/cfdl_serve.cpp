@@ -352,7 +352,7 @@ int cfdl_server_create(const cfdl_server_config *cfg, cfdl_server **out) {
     if (!cfg || !out) return CFDL_ERR_INVALID;
     *out = nullptr;
     if (cfg->max_cases <= 0 || cfg->chunk <= 0 || cfg->prep_threads <= 0 || !(cfg->hbm_budget > 0) ||
-        !(cfg->hbm_reserve >= 0) || cfg->precision < 0 || cfg->precision > 2 || (cfg->precond != 0 && cfg->precond != 1) ||
+        !(cfg->hbm_reserve >= 0) || cfg->precision < 0 || cfg->precision > 3 || (cfg->precond != 0 && cfg->precond != 1) ||
         !(cfg->tile == 0 || cfg->tile == 1 || cfg->tile == 2 || cfg->tile == 4 || cfg->tile == 8) ||
         !(cfg->alpha_u > 0 && cfg->alpha_u <= 1) || !(cfg->alpha_p > 0 && cfg->alpha_p <= 1))
         return CFDL_ERR_INVALID;

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
-    const bool m32 = C.precision == 2;
+    const bool m32 = C.precision >= 2;
     if (C.W == 6) { FOR_CELLS(t) mom_init_row<6>(C, i, ne, v, m32); }
     else if (C.W == 4) { FOR_CELLS(t) mom_init_row<4>(C, i, ne, v, m32); }
     else { FOR_CELLS(t) mom_init_row<kMaxW>(C, i, ne, v, m32); }
@@ -580,7 +580,7 @@ void mom_init(cfdl_ctx *ctx) { CFDL_LAUNCH("k_mom_init", k_mom_init, cellsv, RED
 #define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
 
 void mom_iter(cfdl_ctx *ctx) {
-    if (ctx->cases[0]->cfg.precision == 2) {
+    if (ctx->cases[0]->cfg.precision >= 2) {
         CFDL_LAUNCH("k_mom_p", (k_mom_p<float, 3>), cellsv);
         CFDL_LAUNCH("k_mom_v", (k_mom_v<float, 3>), cellsv, RED32);
         CFDL_LAUNCH("k_mom_s", (k_mom_s<float, 3>), cellsv, RED32);
@@ -628,7 +628,7 @@ void energy_iter(cfdl_ctx *ctx) {
 
 // the end of the momentum solve: precision 2 applies its FP32 correction
 void mom_finish(cfdl_ctx *ctx) {
-    if (ctx->cases[0]->cfg.precision == 2) CFDL_LAUNCH("k_mom_apply", k_mom_apply, cellsv);
+    if (ctx->cases[0]->cfg.precision >= 2) CFDL_LAUNCH("k_mom_apply", k_mom_apply, cellsv);
 }
 
 void pcj_init(cfdl_ctx *ctx) {

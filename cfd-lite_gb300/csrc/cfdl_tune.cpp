@@ -70,6 +70,7 @@ struct Snapshot {
                 off += s.n * sizeof(double);
             }
             if ((st = cuda_status(cudaMemcpyAsync(hc->dev.sc, bufs[c] + off, sizeof(SolveScalars), cudaMemcpyDeviceToDevice, ctx->stream)))) return st;
+            hc->g32_stale = true;    // precision 3: the FP32 gradients follow the restored gu, gv, gw
         }
         return cuda_status(cudaStreamSynchronize(ctx->stream));
     }

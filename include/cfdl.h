@@ -138,7 +138,12 @@ typedef struct cfdl_config {
                               preconditioner and inner CG, FP64 residual/refinement);
                               2: as 1, and each momentum solve finds its correction
                               to the FP64 residual with FP32 BiCGStab (solve_mode 0
-                              only: the reference's 10x drop, no refinement needed)   */
+                              only: the reference's 10x drop, no refinement needed);
+                              3: as 2, and the explicit momentum face terms (sumss and
+                              the deferred non-orthogonal correction of calc_coef_uvw)
+                              and the gradients of u, v, w they use are FP32; the
+                              implicit coefficients, fluxes and pressure equation
+                              stay FP64 (solve_mode 0 only)                            */
     int    precond;        /* pressure preconditioner: 0 Jacobi, 1 aggregation AMG      */
 } cfdl_config;
 
@@ -418,6 +423,14 @@ int cfdl_write_vtu(cfdl_ctx *ctx, int case_id, const cfdl_setup *setup, const ch
  * (phi), grad_enthalpy, temperature, grad_temperature; the reference's
  * VTK/output-<iout>/energy.vtu.  Needs cfdl_energy_init. */
 int cfdl_write_vtu_energy(cfdl_ctx *ctx, int case_id, const cfdl_setup *setup, const char *path);
+
+/* Self-check of the integer-pipe FP64 <-> FP32 conversions of the precision-3
+ * kernels against the hardware conversions on n generated values (every
+ * binary64 exponent near the binary32 range, ties, signed zeros, infinities,
+ * NaN).  mismatches[0]: narrowing differences (binary32 subnormal results,
+ * flushed to zero by design, are not counted); mismatches[1]: widening
+ * differences on normal binary32 values. */
+int cfdl_check_conversions(int n, unsigned *mismatches);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t cfdl_launch_count(const cfdl_ctx *ctx);

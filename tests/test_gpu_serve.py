@@ -36,7 +36,7 @@ def solve_alone(req, conv_tol, max_outer, precision, tile=4):
     return out, st
 
 
-@pytest.mark.parametrize("precision", [0, 1, 2])
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
 def test_results_same_alone_and_in_mix(need_gpu, precision):
     conv_tol, max_outer = 1e-4, 80
     srv = cfdl.Server(precision=precision, chunk=7, max_cases=4, prep_threads=3, hbm_budget=8e9, hbm_reserve=1e9)

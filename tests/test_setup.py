@@ -198,11 +198,12 @@ def test_ctx_create_without_device_fails_loudly():
 
 
 def test_case_bytes_estimate_and_server_config():
-    # the estimate grows linearly with the mesh and bounds ~1.6 kB per hex cell
+    # the estimate grows linearly with the mesh and bounds ~2.1 kB per hex cell
+    # (every form's arrays, the precision-3 FP32 copies included)
     e1 = cfdl.case_bytes_estimate(1000, 3300, 600)
     e8 = cfdl.case_bytes_estimate(8000, 26400, 2400)
     assert 0 < e1 < e8 <= 8.5 * e1
-    assert e8 / 8000 < 2000
+    assert e8 / 8000 < 2200
     c = cfdl.server_config()
     assert c.hbm_budget == 150e9 and c.max_cases > 0 and c.chunk > 0 and c.precision in (0, 1)
     with pytest.raises(KeyError):

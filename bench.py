@@ -61,8 +61,8 @@ def parse():
                     help="cavity: one case (default); batched: 64 uneven cases in one run; served: request stream")
     ap.add_argument("--cases", type=int, default=64, help="batched: number of cases")
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
-    ap.add_argument("--forms", default="0,1,2", help="batched/served: precisions to run (0 FP64, 1 mixed pressure, "
-                    "2 mixed pressure + FP32 momentum corrections)")
+    ap.add_argument("--forms", default="0,1,2,3", help="batched/served: precisions to run (0 FP64, 1 mixed pressure, "
+                    "2 mixed pressure + FP32 momentum corrections, 3 also FP32 explicit momentum face terms)")
     ap.add_argument("--rates", default="5,200", help="served: request rates (req/s)")
     ap.add_argument("--requests", type=int, default=16, help="served: requests per rate")
     ap.add_argument("--max-outer", type=int, default=1000, help="served: outer-iteration cap per request")

@@ -121,9 +121,11 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     const double ap = C.ap[i];
     C.rap[i] = kOmega / ap;
     if (C.precision >= 1) {
-        C.fdiag[i] = (float)ap;
-        C.frap[i] = (float)(kOmega / ap);
-        for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = (float)C.anb[k * C.ne + i];
+        // the FP32 copies converted in the integer pipe (GB300 runs the hardware
+        // conversions at its FP64 rate)
+        C.fdiag[i] = narrow_f32(ap);
+        C.frap[i] = narrow_f32(kOmega / ap);
+        for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = narrow_f32(C.anb[k * C.ne + i]);
     }
 }
 
@@ -251,12 +253,12 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
         double v = 0.0;
         for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
         L.a[s] = v;
-        if (mixed) L.a32[s] = (float)v;
+        if (mixed) L.a32[s] = narrow_f32(v);
         dsum += v;
     }
     L.dg[I] = dsum;
     L.rd[I] = kOmega / dsum;
-    if (mixed) { L.dg32[I] = (float)dsum; L.rd32[I] = (float)(kOmega / dsum); }
+    if (mixed) { L.dg32[I] = narrow_f32(dsum); L.rd32[I] = narrow_f32(kOmega / dsum); }
 }
 
 // coarsest: z_L = Minv r_L (one CTA per case, 4 lanes per row)
@@ -431,14 +433,14 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
             double v = 0.0;
             for (int q = L.g_ptr[sl]; q < L.g_ptr[sl + 1]; q++) v += af[L.g_src[q]];
             L.a[sl] = v;
-            if (mixed) L.a32[sl] = (float)v;
+            if (mixed) L.a32[sl] = narrow_f32(v);
             dsum += v;
         }
     dsum = group_sum<G>(dsum);
     if (ok && g == 0) {
         L.dg[i] = dsum;
         L.rd[i] = kOmega / dsum;
-        if (mixed) { L.dg32[i] = (float)dsum; L.rd32[i] = (float)(kOmega / dsum); }
+        if (mixed) { L.dg32[i] = narrow_f32(dsum); L.rd32[i] = narrow_f32(kOmega / dsum); }
     }
 }
 
@@ -877,7 +879,7 @@ __global__ void __launch_bounds__(kTile) k_mx_start(const CaseDev *__restrict__ 
     if (!S->active_p) return;
     float v[1] = {0.f};
     FOR_CELLS(t) {
-        const float r = (float)C.kr[i];
+        const float r = narrow_f32(C.kr[i]);
         C.fr[i] = r; C.fx[i] = 0.f;
         v[0] += r * r;
     }
@@ -994,7 +996,7 @@ __global__ void __launch_bounds__(kTile) k_mx_apply(const CaseDev *__restrict__ 
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (!C.sc->active_p) return;
-    FOR_CELLS(t) C.phic[i] = C.phic[i] + (double)C.fx[i];
+    FOR_CELLS(t) C.phic[i] = C.phic[i] + widen_f64(C.fx[i]);
 }
 
 // FP64 true residual r = (b - mean) - A x and the outer stopping test

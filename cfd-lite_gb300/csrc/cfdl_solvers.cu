@@ -69,11 +69,11 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
     const double api = C.ap[i];
     C.rap[i] = 1.0 / api;                   // the Jacobi scaling of the whole solve, divided once
     if (m32) {                              // the operator in FP32 for the correction solve
-        C.fdiag[i] = (float)api;
-        C.frap[i] = (float)(1.0 / api);
+        C.fdiag[i] = narrow_f32(api);          // integer-pipe conversions (cfdl_device.cuh)
+        C.frap[i] = narrow_f32(1.0 / api);
 #pragma unroll
         for (int k = 0; k < W; k++)
-            if (k < C.W) C.fanb[k * ne + i] = (float)a[k];
+            if (k < C.W) C.fanb[k * ne + i] = narrow_f32(a[k]);
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -92,7 +92,7 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
         // p and v need no clearing: the first iteration sets p = r (k_mom_p)
         if (m32) {
             // FP32 correction solve A d = r from d = 0 (first halves of kr, krh; d after kt's)
-            const float rf = (float)r;
+            const float rf = narrow_f32(r);
             ((float *)C.kr)[q * ne + i] = rf;
             ((float *)C.krh)[q * ne + i] = rf;
             ((float *)C.kt)[3 * (size_t)ne + q * ne + i] = 0.f;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kTile) k_mom_apply(const CaseDev *__restrict__
     double *xs[3] = {C.u, C.v, C.w};
     FOR_CELLS(t) {
 #pragma unroll
-        for (int q = 0; q < 3; q++) xs[q][i] = xs[q][i] + (double)M.x[q][i];
+        for (int q = 0; q < 3; q++) xs[q][i] = xs[q][i] + widen_f64(M.x[q][i]);
     }
 }
 

@@ -113,14 +113,16 @@ __global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ c
     const double *fd = C.eprop + EP_D * C.nf, *fx = C.fS;
     double ap = 0.0, sumf = 0.0, sumdefc = 0.0;
     double a[kMaxW];
-    int bslot[kMaxW], nb_cnt = 0;
+    int nbk[kMaxW], nb_cnt = 0;              // slot neighbours (-1: none), boundary slots
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
         a[k] = 0.0;
+        nbk[k] = -1;
         if (k >= W) continue;
         const int nb = C.hf_nb[k * ne + i];
+        nbk[k] = nb;
         if (nb < 0) continue;
-        if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
+        if (nb >= ne) { nb_cnt++; continue; }
         const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
         const double fl = flip_sign(C.mip[f], fc >= 0);   // -sg * mip
         const double ak = fd[f] + positive_part(fl);
@@ -138,18 +140,22 @@ __global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ c
         ap = ap + ap0;
         b = ap0 * C.ee0[i] + sumf * phi + sumdefc;
     }
-    // walls in BC-loop order (ascending halo index); every bound BC is 'dirichlet'
-    for (int q = 1; q < nb_cnt; q++) {
-        int s = bslot[q], j = q - 1;
-        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
-        bslot[j + 1] = s;
-    }
+    // walls in BC-loop order (ascending halo index), the next boundary slot
+    // picked by comparisons over the unrolled slots (the row stays in
+    // registers); every bound BC is 'dirichlet'
+    int prev = -1;
     for (int q = 0; q < nb_cnt; q++) {
-        const int k = bslot[q], h = C.hf_nb[k * ne + i];
+        int k = 0, h = 0x7fffffff;
+#pragma unroll
+        for (int s = 0; s < kMaxW; s++)
+            if (nbk[s] >= ne && nbk[s] > prev && nbk[s] < h) { h = nbk[s]; k = s; }
+        prev = h;
         if (C.h_kind[h - ne] == 0) continue;
         const double d = fd[face_of(C.hf_fc[k * ne + i])];
         ap = ap + d;
-        a[k] = a[k] + d;
+#pragma unroll
+        for (int s = 0; s < kMaxW; s++)
+            if (s == k) a[s] = a[s] + d;
     }
     C.ap[i] = ap;
     C.b[i] = b;

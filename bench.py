@@ -53,6 +53,8 @@ def parse():
                     "2: also FP32 momentum corrections")
     ap.add_argument("--precond", type=int, default=1, help="pressure preconditioner: 0 Jacobi, 1 AMG")
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of the graph")
+    ap.add_argument("--tile", type=int, default=0, help="solver tile shape (1, 2, 4, 8) instead of the autotuner's "
+                    "choice (fewer launches, e.g. for a profiler's launch list)")
     ap.add_argument("--breakdown", action="store_true", help="print the per-kernel table to stderr")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -214,7 +216,11 @@ def run_ours(a, dist):
 
     for _ in range(a.warmup):
         step()
-    tile, tile_ms = g.autotune(outer=2)     # solver tile shape by measurement (state restored)
+    if a.tile:
+        g.set_tile(a.tile)
+        tile, tile_ms = a.tile, {}
+    else:
+        tile, tile_ms = g.autotune(outer=2)     # solver tile shape by measurement (state restored)
     for _ in range(2):
         step()
     clocks = Clocks(dist.local)
@@ -595,7 +601,12 @@ def run_energy(a, dist):
     g.energy_init()
     for _ in range(a.warmup):                  # developed flow and temperature
         g.step(1, ncoef=0)
-    tile, _ = g.autotune(outer=2)              # solver and energy tile shapes by measurement (state restored)
+    if a.tile:
+        g.set_tile(a.tile)
+        g.set_energy_tile(a.tile)
+        tile = a.tile
+    else:
+        tile, _ = g.autotune(outer=2)          # solver and energy tile shapes by measurement (state restored)
     clocks = Clocks(dist.local)
     e_ms, o_ms, iters = [], [], []
     l0, launches_e = g.launch_count(), 0

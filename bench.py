@@ -666,7 +666,7 @@ def run_energy(a, dist):
     out = {
         "metric": "energy solve cell-updates/s", "value": value, "unit": "cells x solves/s",
         "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPES[a.precision],
         "data": "synthetic (seeded jittered unit-cube hex mesh)",
         "config": {"workload": "energy equation on the lid-driven cavity %d^3 %s, jitter %.2f, Re=100, hot lid "
                                "373 / walls 273, cp=1000, tc=5; solve_energy after each outer pass"

@@ -303,7 +303,7 @@ static int append_energy(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Post 
         return b.capture_into(body_g, [&] { energy_iter(ctx); b.setcond(he, LOOP_EN); }, body);
     });
     if (st) return st;
-    if ((st = b.segment(G, prev, [&] { launch_energy_temp(ctx); post(); }, &k))) return st;
+    if ((st = b.segment(G, prev, [&] { energy_finish(ctx); launch_energy_temp(ctx); post(); }, &k))) return st;
     *static_k += k;
     return CFDL_OK;
 }

@@ -293,6 +293,7 @@ int solve_energy_all(cfdl_ctx *ctx);
 int solve_energy_phi(cfdl_ctx *ctx);          // the phi solve alone (cfdl_solvers.cu)
 void energy_init_solve(cfdl_ctx *ctx);
 void energy_iter(cfdl_ctx *ctx);
+void energy_finish(cfdl_ctx *ctx);
 void launch_energy_temp(cfdl_ctx *ctx);
 int energy_init_case(cfdl_ctx *ctx, HostCase *hc, double cp, double tc, double t_init);
 

@@ -157,6 +157,8 @@ template <> __device__ __forceinline__ MomVec<float> mom_vec<float, 3>(const Cas
 template <> __device__ __forceinline__ MomVec<double> mom_vec<double, 1>(const CaseDev &C) {
     return {C.kr, C.krh, C.kp, C.kph, C.kv, C.ks, C.ksh, C.kt, {C.ee, nullptr, nullptr}, C.anb, C.ap, C.rap};
 }
+// the energy solve's FP32 correction form (precision >= 2): as the momentum one
+template <> __device__ __forceinline__ MomVec<float> mom_vec<float, 1>(const CaseDev &C) { return mom_vec<float, 3>(C); }
 
 // the lanes of the solve: momentum u, v, w or the energy lane
 template <int NC> __device__ __forceinline__ KLanes *lanes(SolveScalars *S) { return NC == 3 ? (KLanes *)S : &S->en; }
@@ -359,11 +361,14 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
 // ------------------------------- energy -----------------------------------
 // init of the phi solve of solve_energy (mod_energy.f90:75): b' = b +
 // sum_bdry anb*phi_halo, r = b' - A phi, rh = r; cases without the energy
-// equation contribute nothing and stay inactive.
+// equation contribute nothing and stay inactive.  m32 (precision >= 2): the
+// solve finds the correction d of A d = r in FP32 from d = 0, as the momentum
+// solve does, on FP32 copies of the operator.
 template <int W>
-__device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, double (&v)[2]) {
+__device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, double (&v)[2], bool m32) {
     const double api = C.ap[i];
     C.rap[i] = 1.0 / api;
+    if (m32) { C.fdiag[i] = narrow_f32(api); C.frap[i] = narrow_f32(1.0 / api); }
     const double *__restrict__ phi = C.ee;
     double bb = C.b[i], s = api * phi[i];
 #pragma unroll
@@ -371,12 +376,20 @@ __device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, dou
         const int j = k < C.W ? C.hf_nb[k * ne + i] : -1;
         if (j < 0) continue;
         const double a = C.anb[k * ne + i];
+        if (m32) C.fanb[k * ne + i] = narrow_f32(a);
         if (j >= ne) bb += a * phi[j];
         else s -= a * phi[j];
     }
     const double r = bb - s;
-    C.kr[i] = r;
-    C.krh[i] = r;
+    if (m32) {
+        const float rf = narrow_f32(r);
+        ((float *)C.kr)[i] = rf;
+        ((float *)C.krh)[i] = rf;
+        ((float *)C.kt)[3 * (size_t)ne + i] = 0.f;
+    } else {
+        C.kr[i] = r;
+        C.krh[i] = r;
+    }
     v[0] += bb * bb;
     v[1] += r * r;
 }
@@ -385,10 +398,11 @@ __global__ void __launch_bounds__(kTile, 3) k_en_init(const CaseDev *__restrict_
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
     TILE_HEAD
     double v[2] = {0, 0};
+    const bool m32 = C.precision >= 2;
     if (C.ee) {
-        if (C.W == 6) { FOR_CELLS(t) en_init_row<6>(C, i, ne, v); }
-        else if (C.W == 4) { FOR_CELLS(t) en_init_row<4>(C, i, ne, v); }
-        else { FOR_CELLS(t) en_init_row<kMaxW>(C, i, ne, v); }
+        if (C.W == 6) { FOR_CELLS(t) en_init_row<6>(C, i, ne, v, m32); }
+        else if (C.W == 4) { FOR_CELLS(t) en_init_row<4>(C, i, ne, v, m32); }
+        else { FOR_CELLS(t) en_init_row<kMaxW>(C, i, ne, v, m32); }
     }
     block_reduce<2>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M1], cnt[t.c])) {
@@ -408,6 +422,14 @@ __global__ void __launch_bounds__(kTile, 3) k_en_init(const CaseDev *__restrict_
             L->active[1] = L->active[2] = 0;
         }
     }
+}
+
+// precision >= 2: phi += the FP32 correction of the energy solve
+__global__ void __launch_bounds__(kTile) k_en_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    TILE_HEAD
+    if (!C.ee) return;
+    const float *x = mom_vec<float, 1>(C).x[0];
+    FOR_CELLS(t) C.ee[i] = C.ee[i] + widen_f64(x[i]);
 }
 
 // precision 2: u, v, w += the FP32 correction of the momentum solve
@@ -614,11 +636,27 @@ int solve_energy_phi(cfdl_ctx *ctx) {
         if (a == 0) break;
     }
     ctx->last_iters_e = maxit;
+    energy_finish(ctx);
     return cuda_status(cudaGetLastError());
 }
 
-// one BiCGStab iteration of the energy solve (one right-hand side, FP64)
+// the end of the energy solve: precision >= 2 applies its FP32 correction
+void energy_finish(cfdl_ctx *ctx) {
+    if (ctx->cases[0]->cfg.precision >= 2) CFDL_LAUNCH("k_en_apply", k_en_apply, cellse);
+}
+
+// one BiCGStab iteration of the energy solve (one right-hand side; FP64, or
+// FP32 on the correction for precision >= 2)
+#define REDE32 ctx->cellse.d_case_first, ctx->cellse.d_case_ntiles, (float *)ctx->d_partials
 void energy_iter(cfdl_ctx *ctx) {
+    if (ctx->cases[0]->cfg.precision >= 2) {
+        CFDL_LAUNCH("k_en_p", (k_mom_p<float, 1>), cellse);
+        CFDL_LAUNCH("k_en_v", (k_mom_v<float, 1>), cellse, REDE32);
+        CFDL_LAUNCH("k_en_s", (k_mom_s<float, 1>), cellse, REDE32);
+        CFDL_LAUNCH("k_en_t", (k_mom_t<float, 1>), cellse, REDE32);
+        CFDL_LAUNCH("k_en_x", (k_mom_x<float, 1>), cellse, REDE32);
+        return;
+    }
     CFDL_LAUNCH("k_en_p", (k_mom_p<double, 1>), cellse);
     CFDL_LAUNCH("k_en_v", (k_mom_v<double, 1>), cellse, REDE);
     CFDL_LAUNCH("k_en_s", (k_mom_s<double, 1>), cellse, REDE);

@@ -115,7 +115,7 @@ def test_energy_converged_default_mode(need_gpu):
     o.physics_init(oracle_lib.steady(mode=0, mu=0.01))
     o.energy_init()
     o.run(700, ncoef=0)
-    for precision in (0, 1):
+    for precision in (0, 1, 2, 3):
         g = cfdl.Solver(s, cfdl.steady(mu=0.01, precision=precision))
         g.energy_init()
         g.set_run(700)
@@ -225,11 +225,13 @@ def test_energy_tile_shapes_and_autotune(need_gpu):
         g.close()
 
 
-def test_energy_graph_equals_eager(need_gpu):
+@pytest.mark.parametrize("precision", [0, 2])
+def test_energy_graph_equals_eager(need_gpu, precision):
     """solve_energy as one graph launch (device-side BiCGStab loop) and as
-    eager launches with host polls give the same fields bit for bit."""
+    eager launches with host polls give the same fields bit for bit (FP64,
+    and the FP32 correction form of precision >= 2)."""
     s = cfdl.Setup(cfdl.Zone(6, False, 0.2, seed=8))
-    cfg = cfdl.default_config(rho=5.0)
+    cfg = cfdl.default_config(rho=5.0, precision=precision)
     a, b = cfdl.Solver(s, cfg), cfdl.Solver(s, cfg)
     b.set_graph_mode(False)
     for g in (a, b):

@@ -136,9 +136,10 @@ typedef struct cfdl_config {
     int    tight_maxit;    /* mode 1 iteration cap                                       */
     int    precision;      /* 0: FP64 throughout; 1: mixed pressure solve (FP32 SpMV,
                               preconditioner and inner CG, FP64 residual/refinement);
-                              2: as 1, and each momentum solve finds its correction
-                              to the FP64 residual with FP32 BiCGStab (solve_mode 0
-                              only: the reference's 10x drop, no refinement needed);
+                              2: as 1, and each momentum solve (and the energy
+                              solve) finds its correction to the FP64 residual with
+                              FP32 BiCGStab (solve_mode 0 only: the reference's 10x
+                              drop, no refinement needed);
                               3: as 2, and the explicit momentum face terms (sumss and
                               the deferred non-orthogonal correction of calc_coef_uvw)
                               and the gradients of u, v, w they use are FP32; the

@@ -139,6 +139,7 @@ def lib():
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
     L.cfdl_energy_init.argtypes = [vp, C.c_double, C.c_double, C.c_double]
     L.cfdl_check_conversions.argtypes = [C.c_int, vp]
+    L.cfdl_set_pdl.argtypes = [vp, C.c_int]
     L.cfdl_set_energy_tile.argtypes = [vp, C.c_int]
     L.cfdl_get_energy_tile.argtypes = [vp]
     L.cfdl_calc_coef_energy.argtypes = [vp]
@@ -436,6 +437,9 @@ class Solver:
         ms = (C.c_double * 4)()
         _check(lib().cfdl_autotune(self._h, int(outer), C.byref(best), ms), "autotune")
         return best.value, dict(zip((1, 2, 4, 8), list(ms)))
+
+    def set_pdl(self, on):
+        _check(lib().cfdl_set_pdl(self._h, int(bool(on))), "set_pdl")
 
     def set_graph_mode(self, on):
         """solve_uvwp as one CUDA graph (True, default) or as individual launches."""

@@ -114,6 +114,7 @@ __device__ __forceinline__ bool mactive(const CaseDev &C) { return C.sc->active3
 
 // level-0 diagonal inverse and the FP32 copies the mixed form needs
 __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const int i = t.first + (int)threadIdx.x;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
 // Dense inverse of A_L + c 11^T at each case's coarsest level (one CTA per
 // case, Gauss-Jordan in shared memory; the matrix is SPD, no pivoting).
 __global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x;
     if (c >= ncases) return;
     const CaseDev &C = cases[c];
@@ -187,6 +189,7 @@ __global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restric
 // t = w D^-1 r
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -199,6 +202,7 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
 // z = t + w D^-1 (r - A t)
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -211,6 +215,7 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -224,6 +229,7 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
 // thread per coarse row: the large levels, where rows outnumber lanes)
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
+    CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -239,6 +245,7 @@ __global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict_
 
 // Galerkin row I, one thread per row (large levels)
 __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const int I = t.first + (int)threadIdx.x;
@@ -264,6 +271,7 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
 // coarsest: z_L = Minv r_L (one CTA per case, 4 lanes per row)
 template <class T>
 __global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x;
     if (c >= ncases) return;
     const CaseDev &C = cases[c];
@@ -306,6 +314,7 @@ __device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__
 
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -363,6 +372,7 @@ template <int G, class T> __device__ __forceinline__ T group_offdiag(const LP<T>
 // z = t + w D^-1 (r - A t)
 template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
@@ -373,6 +383,7 @@ __global__ void __launch_bounds__(kTile) k_vg_jac(const CaseDev *__restrict__ ca
 // t = r - A z
 template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
@@ -383,6 +394,7 @@ __global__ void __launch_bounds__(kTile) k_vg_resid(const CaseDev *__restrict__ 
 // r_{l1}[I] = sum of the residual t_{l1-1} over the members of aggregate I
 template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_restrict(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l1) {
+    CFDL_PDL_WAIT();
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const AmgLevelDev &L = C.lev[l1 - 1];
@@ -398,6 +410,7 @@ __global__ void __launch_bounds__(kTile) k_vg_restrict(const CaseDev *__restrict
 // t = x + w D^-1 (r - A x) with x = z + s P z_{l+1}
 template <class T, int G>
 __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     GROUP_HEAD
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
     const LP<T> P = level<T>(C, l);
@@ -420,6 +433,7 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
 // Galerkin row I of level l: each lane sums the gather lists of its slots
 template <int G>
 __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
     GROUP_HEAD
     if (C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
@@ -448,6 +462,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
 // r = b - mean, x = 0; ||r0||
 __global__ void __launch_bounds__(kTile) k_apc_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -477,6 +492,7 @@ __global__ void __launch_bounds__(kTile) k_apc_init(const CaseDev *__restrict__ 
 // beta = (r,z)/(r,z)_old (0 on the first iteration)
 __global__ void __launch_bounds__(kTile) k_apc_rz(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -497,6 +513,7 @@ __global__ void __launch_bounds__(kTile) k_apc_rz(const CaseDev *__restrict__ ca
 
 // p = z + beta p; q = A p needs every p, so it is the next kernel
 __global__ void __launch_bounds__(kTile) k_apc_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const SolveScalars *S = C.sc;
@@ -507,6 +524,7 @@ __global__ void __launch_bounds__(kTile) k_apc_p(const CaseDev *__restrict__ cas
 // q = A p; alpha = rz / (p, q)
 __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -532,6 +550,7 @@ __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cas
 // x += alpha p; r -= alpha q; ||r||
 __global__ void __launch_bounds__(kTile) k_apc_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -723,7 +742,8 @@ int ensure_amg(cfdl_ctx *ctx) {
         if ((WL).ntiles > 0) {                                                                       \
             const bool p_ = ctx->prof && prof_wants(ctx, name);                                      \
             if (p_) prof_begin(ctx, name);                                                           \
-            kern<<<(WL).ntiles, kTile, 0, ctx->stream>>>(ctx->d_cases, (WL).d_tiles, ##__VA_ARGS__); \
+            launch_k(ctx->pdl, kern, (unsigned)(WL).ntiles, (unsigned)kTile, ctx->stream,                 \
+                     (const CaseDev *)ctx->d_cases, (const Tile *)(WL).d_tiles, ##__VA_ARGS__);          \
             if (p_) prof_end(ctx);                                                                   \
             ctx->launches++;                                                                         \
         }                                                                                            \
@@ -733,7 +753,8 @@ int ensure_amg(cfdl_ctx *ctx) {
         const int nc_ = (int)ctx->cases.size();                                                      \
         const bool p_ = ctx->prof && prof_wants(ctx, name);                                          \
         if (p_) prof_begin(ctx, name);                                                               \
-        kern<<<nc_, threads, 0, ctx->stream>>>(ctx->d_cases, nc_);                                   \
+        launch_k(ctx->pdl, kern, (unsigned)nc_, (unsigned)(threads), ctx->stream,                    \
+                 (const CaseDev *)ctx->d_cases, nc_);                                                \
         if (p_) prof_end(ctx);                                                                       \
         ctx->launches++;                                                                             \
     } while (0)
@@ -845,6 +866,7 @@ enum { CNT_M0 = 15 };   // shares the last counter slot only with itself
 // outer start: r64 = b - mean, x = 0
 __global__ void __launch_bounds__(kTile) k_mx_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -873,6 +895,7 @@ __global__ void __launch_bounds__(kTile) k_mx_init(const CaseDev *__restrict__ c
 // inner start: fr = (float) r64, fx = 0; ||fr|| in FP32
 __global__ void __launch_bounds__(kTile) k_mx_start(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -905,6 +928,7 @@ __global__ void __launch_bounds__(kTile) k_mx_start(const CaseDev *__restrict__ 
 
 // z = M^-1 r for the Jacobi preconditioner (the AMG form uses the V-cycle)
 __global__ void __launch_bounds__(kTile) k_mx_jacobi(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (!C.sc->active32) return;
@@ -913,6 +937,7 @@ __global__ void __launch_bounds__(kTile) k_mx_jacobi(const CaseDev *__restrict__
 
 __global__ void __launch_bounds__(kTile) k_mx_rz(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -932,6 +957,7 @@ __global__ void __launch_bounds__(kTile) k_mx_rz(const CaseDev *__restrict__ cas
 }
 
 __global__ void __launch_bounds__(kTile) k_mx_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     const SolveScalars *S = C.sc;
@@ -941,6 +967,7 @@ __global__ void __launch_bounds__(kTile) k_mx_p(const CaseDev *__restrict__ case
 
 __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -965,6 +992,7 @@ __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ case
 
 __global__ void __launch_bounds__(kTile) k_mx_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -993,6 +1021,7 @@ __global__ void __launch_bounds__(kTile) k_mx_x(const CaseDev *__restrict__ case
 
 // x += (double) fx
 __global__ void __launch_bounds__(kTile) k_mx_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (!C.sc->active_p) return;
@@ -1002,6 +1031,7 @@ __global__ void __launch_bounds__(kTile) k_mx_apply(const CaseDev *__restrict__ 
 // FP64 true residual r = (b - mean) - A x and the outer stopping test
 __global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                   const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;

@@ -628,6 +628,15 @@ int cfdl_run(cfdl_ctx *ctx, int max_outer, int *running) {
     return cuda_status(cudaGetLastError());
 }
 
+int cfdl_set_pdl(cfdl_ctx *ctx, int on) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    ctx->pdl = on != 0;
+    destroy_graph(ctx);   // captured launches carry the launch mode
+    return CFDL_OK;
+}
+
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on) {
     if (!ctx) return CFDL_ERR_INVALID;
     ctx->use_graph = on != 0;

@@ -4,6 +4,12 @@
 
 namespace cfdl {
 
+// First statement of every kernel the launch macros start with programmatic
+// dependent launch: the grid may be scheduled while its predecessor in the
+// stream is finishing, and waits here until that predecessor has completed
+// and its writes are visible (a no-op when launched the ordinary way).
+#define CFDL_PDL_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+
 // Deterministic block reduction of K doubles (kTile threads): a fixed
 // shuffle tree per warp, then warp partials summed in warp order by one
 // thread.  The result lands in out[0..K-1].

@@ -33,6 +33,7 @@ namespace {
 // lid / dirichlet0 of the energy equation (mod_energy.f90:173-212): the halo
 // takes the wall temperature and phi = cp(owner)*t.  One thread per halo.
 __global__ void __launch_bounds__(kTile) k_en_bc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (i >= t.last || C.h_kind[i] == 0) return;
     const int h = C.ne + i;
@@ -45,6 +46,7 @@ __global__ void __launch_bounds__(kTile) k_en_bc(const CaseDev *__restrict__ cas
 // halos (halo = 1); run_due: only the cases whose run cadence is due.
 __global__ void __launch_bounds__(kTile) k_en_time(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    int halo, int run_due) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (run_due && !C.sc->time_due) return;
     if (i >= t.last) return;
@@ -59,6 +61,7 @@ __global__ void __launch_bounds__(kTile) k_en_time(const CaseDev *__restrict__ c
 // tc*area/ds/cp of the BC loop (mod_energy.f90:157), where ds = dr.n (the
 // momentum walls use |dr|).  The divisions are done here, once.
 __global__ void __launch_bounds__(kTile) k_en_props(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -86,6 +89,7 @@ __global__ void __launch_bounds__(kTile) k_en_props(const CaseDev *__restrict__ 
 // (A the area vector; the neighbour sees the opposite normal and the
 // complementary weight, so it takes the negative), into fS[0].
 __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -107,6 +111,7 @@ __global__ void __launch_bounds__(kTile) k_en_face(const CaseDev *__restrict__ c
 // ap = sum anb + rho*vol/dt + the wall coefficients,
 // b = ap0*phi0 + sumf*phi + sumdefc.
 __global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
@@ -166,6 +171,7 @@ __global__ void __launch_bounds__(kTile) k_en_cell(const CaseDev *__restrict__ c
 
 // calc_temperature, mod_properties.f90:214-221: t = phi/cp on the cells
 __global__ void __launch_bounds__(kTile) k_en_temp(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     EN_PROLOGUE
     if (i < t.last) C.et[i] = C.ee[i] / C.ecp[i];
 }
@@ -174,6 +180,7 @@ __global__ void __launch_bounds__(kTile) k_en_temp(const CaseDev *__restrict__ c
 // mod_energy.f90:33-37); the halos take the cp of their owner
 __global__ void k_en_fill(double *t, double *e, double *e0, const double *cp, const int *h_own, int ne, int nbf,
                           double t_init) {
+    CFDL_PDL_WAIT();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= ne + nbf) return;
     const double c = cp[j < ne ? j : h_own[j - ne]];
@@ -183,6 +190,7 @@ __global__ void k_en_fill(double *t, double *e, double *e0, const double *cp, co
 }
 
 __global__ void k_fill(double *x, size_t n, double v) {
+    CFDL_PDL_WAIT();
     const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (j < n) x[j] = v;
 }

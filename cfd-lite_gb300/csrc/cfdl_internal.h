@@ -224,6 +224,7 @@ struct cfdl_ctx {
     int amg_lmax = -1;
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;
+    bool pdl = true;                     // launch with programmatic dependent launch (cfdl_set_pdl)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_form = -1;
@@ -304,6 +305,31 @@ void prof_begin(cfdl_ctx *ctx, const char *name);
 void prof_end(cfdl_ctx *ctx);
 void prof_destroy(cfdl_ctx *ctx);
 
+#ifdef __CUDACC__
+// Launch a kernel whose first statement is CFDL_PDL_WAIT with programmatic
+// stream serialization: it may be scheduled while its predecessor in the
+// stream drains (inside graphs too, as programmatic edges), which hides the
+// gap between dependent launches; or the ordinary way when pdl is off.
+template <class... KArgs, class... Args>
+inline void launch_k(bool pdl, void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    if (!pdl) {
+        k<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+#endif
+
 // Launch a tile kernel over work list WL of the context, with optional
 // event bracketing for the profiler.
 #define CFDL_LAUNCH(name, kern, WL, ...)                                                            \
@@ -311,7 +337,8 @@ void prof_destroy(cfdl_ctx *ctx);
         if (ctx->WL.ntiles > 0) {                                                                   \
             const bool p_ = ctx->prof && cfdl::prof_wants(ctx, name);                               \
             if (p_) cfdl::prof_begin(ctx, name);                                                    \
-            kern<<<ctx->WL.ntiles, cfdl::kTile, 0, ctx->stream>>>(ctx->d_cases, ctx->WL.d_tiles, ##__VA_ARGS__); \
+            cfdl::launch_k(ctx->pdl, kern, (unsigned)ctx->WL.ntiles, (unsigned)cfdl::kTile, ctx->stream, \
+                           (const cfdl::CaseDev *)ctx->d_cases, (const cfdl::Tile *)ctx->WL.d_tiles, ##__VA_ARGS__); \
             if (p_) cfdl::prof_end(ctx);                                                            \
             ctx->launches++;                                                                        \
         }                                                                                           \

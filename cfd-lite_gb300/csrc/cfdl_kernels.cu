@@ -25,6 +25,7 @@ namespace {
 // mod_uvwp.f90:493-570.  One thread per halo.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTile) k_bc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(halos)
     if (i >= t.last) return;
     const int kind = C.h_kind[i];
@@ -58,6 +59,7 @@ __global__ void __launch_bounds__(kTile) k_bc(const CaseDev *__restrict__ cases,
 // diffusion mu*area/ds of the BC loop (mod_uvwp.f90:257).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -85,6 +87,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face(const CaseDev *__restri
 // Property planes of every face (recomputed when rho or mu change): the mesh
 // planes scaled by the interpolated viscosity and density.
 __global__ void __launch_bounds__(kTile) k_face_props(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -122,6 +125,7 @@ __global__ void __launch_bounds__(kTile) k_face_props(const CaseDev *__restrict_
 // deferred-correction sources of the momentum equations -- from the FP32
 // gradients and planes, with no FP64 instruction; fS holds them as FP32.
 __global__ void __launch_bounds__(kTile) k_coef_uvw_face_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, ne = C.ne, o = C.f_own[i], n = C.f_nb[i];
@@ -147,6 +151,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face_f32(const CaseDev *__re
 // F32 (precision 3): the explicit face terms are FP32 and summed in FP32.
 template <bool F32>
 __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, nf = C.nf, W = C.W;
@@ -239,6 +244,7 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
 // ---------------------------------------------------------------------------
 template <int NF>
 __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int field) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
@@ -275,6 +281,7 @@ __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ case
 // neighbour differences in FP64, narrowed in the integer pipe, the stencil
 // sums in FP32; the gradients go to g32 and, widened, to gu, gv, gw.
 __global__ void __launch_bounds__(kTile) k_grad3_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
@@ -307,6 +314,7 @@ __global__ void __launch_bounds__(kTile) k_grad3_f32(const CaseDev *__restrict__
 // precision 3: g32 from gu, gv, gw after they were written from outside
 // (uploads, set_array, a restored snapshot)
 __global__ void __launch_bounds__(kTile) k_narrow_grad(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last || !C.g32) return;
     const double *grad[3] = {C.gu, C.gv, C.gw};
@@ -317,6 +325,7 @@ __global__ void __launch_bounds__(kTile) k_narrow_grad(const CaseDev *__restrict
 }
 
 __global__ void k_narrow_array(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+    CFDL_PDL_WAIT();
     const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (j < n) out[j] = narrow_f32(in[j]);
 }
@@ -327,6 +336,7 @@ __global__ void k_narrow_array(const double *__restrict__ in, float *__restrict_
 // except where the definitions differ on purpose: values whose binary32
 // result is subnormal (flushed to a signed zero here).
 __global__ void k_check_conversions(int n, unsigned *bad) {
+    CFDL_PDL_WAIT();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     unsigned long long z = 0x9e3779b97f4a7c15ull * (unsigned long long)(j + 1);
@@ -362,6 +372,7 @@ __global__ void k_check_conversions(int n, unsigned *bad) {
 // the value their BC set.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int rc) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -393,6 +404,7 @@ __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ 
 // b = net inflow - boundary mass flux.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -402,6 +414,7 @@ __global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict
 }
 
 __global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
@@ -439,11 +452,13 @@ __global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict
 // adjust_pc, mod_uvwp.f90:136-158: pc -= pc(1); halo pc = owner pc.
 // ---------------------------------------------------------------------------
 __global__ void k_save_pref(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < ncases) cases[c].sc->pref = cases[c].phic[0];
 }
 
 __global__ void __launch_bounds__(kTile) k_adjust_pc(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
@@ -462,6 +477,7 @@ __global__ void __launch_bounds__(kTile) k_adjust_pc(const CaseDev *__restrict__
 // cells; mip -= rho_ip*A*dc_ip*(pc_nb-pc_P)/(dr.n) on interior faces.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTile) k_update_cells(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const double a = C.alpha_p;
@@ -477,6 +493,7 @@ __global__ void __launch_bounds__(kTile) k_update_cells(const CaseDev *__restric
 }
 
 __global__ void __launch_bounds__(kTile) k_update_faces(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i >= t.last) return;
     const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
@@ -488,14 +505,17 @@ __global__ void __launch_bounds__(kTile) k_update_faces(const CaseDev *__restric
 
 // update_time, mod_physics.f90:101-112
 __global__ void __launch_bounds__(kTile) k_update_time(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i < t.last) { C.u0[i] = C.u[i]; C.v0[i] = C.v[i]; C.w0[i] = C.w[i]; }
 }
 __global__ void __launch_bounds__(kTile) k_update_time_halo(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(halos)
     if (i < t.last) { const int h = C.ne + i; C.u0[h] = C.u[h]; C.v0[h] = C.v[h]; C.w0[h] = C.w[h]; }
 }
 __global__ void __launch_bounds__(kTile) k_copy_mip0(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_PROLOGUE(faces)
     if (i < t.last) C.mip0[i] = C.mip[i];
 }

@@ -19,6 +19,7 @@ namespace {
 enum { CNT_RUN = 0 };
 
 __global__ void k_run_begin(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncases) return;
     SolveScalars *S = cases[c].sc;
@@ -37,6 +38,7 @@ __global__ void k_run_begin(const CaseDev *__restrict__ cases, int ncases) {
 __global__ void __launch_bounds__(kTile) k_run_end(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt,
                                                    double *partials) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
@@ -63,6 +65,7 @@ __global__ void __launch_bounds__(kTile) k_run_end(const CaseDev *__restrict__ c
 
 // update_time (mod_uvwp.f90:74-93) for the cases whose cadence is due
 __global__ void __launch_bounds__(kTile) k_run_time_cells(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (C.sc->halted || !C.sc->time_due) return;
@@ -70,6 +73,7 @@ __global__ void __launch_bounds__(kTile) k_run_time_cells(const CaseDev *__restr
     if (i < t.last) { C.u0[i] = C.u[i]; C.v0[i] = C.v[i]; C.w0[i] = C.w[i]; }
 }
 __global__ void __launch_bounds__(kTile) k_run_time_halos(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (C.sc->halted || !C.sc->time_due) return;
@@ -77,6 +81,7 @@ __global__ void __launch_bounds__(kTile) k_run_time_halos(const CaseDev *__restr
     if (i < t.last) { const int h = C.ne + i; C.u0[h] = C.u[h]; C.v0[h] = C.v[h]; C.w0[h] = C.w[h]; }
 }
 __global__ void __launch_bounds__(kTile) k_run_time_faces(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (C.sc->halted || !C.sc->time_due) return;
@@ -97,6 +102,7 @@ __device__ __forceinline__ int count_running(const CaseDev *__restrict__ cases, 
 
 __global__ void k_run_cond(const CaseDev *__restrict__ cases, int ncases, cudaGraphConditionalHandle h, int consume,
                            int *ctl, unsigned long long *passes) {
+    CFDL_PDL_WAIT();
     if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     const int running = count_running(cases, ncases);
     if (threadIdx.x != 0) return;
@@ -107,12 +113,14 @@ __global__ void k_run_cond(const CaseDev *__restrict__ cases, int ncases, cudaGr
 
 // eager form of the condition: the same count, no graph handle
 __global__ void k_run_count(const CaseDev *__restrict__ cases, int ncases, int *ctl) {
+    CFDL_PDL_WAIT();
     if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     const int running = count_running(cases, ncases);
     if (threadIdx.x == 0) ctl[1] = running;
 }
 
 __global__ void k_run_finish(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncases) return;
     cases[c].sc->halted = 0;

@@ -107,6 +107,7 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
 
 __global__ void __launch_bounds__(kTile, 3) k_mom_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                     const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     double v[6] = {0, 0, 0, 0, 0, 0};
     const bool m32 = C.precision >= 2;
@@ -172,6 +173,7 @@ template <int NC> __device__ __forceinline__ bool lanes_active(const KLanes *L) 
 // p = r + beta (p - omega v); ph = p / ap
 template <class T, int NC>
 __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     const KLanes *L = lanes<NC>(S);
     if (!lanes_active<NC>(L)) return;
@@ -201,6 +203,7 @@ __global__ void __launch_bounds__(kTile) k_mom_p(const CaseDev *__restrict__ cas
 template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_v(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     KLanes *L = lanes<NC>(S);
     if (!lanes_active<NC>(L)) return;
@@ -238,6 +241,7 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_v(const CaseDev *__restrict__ 
 template <class T, int NC>
 __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     KLanes *L = lanes<NC>(S);
     if (!lanes_active<NC>(L)) return;
@@ -274,6 +278,7 @@ __global__ void __launch_bounds__(kTile) k_mom_s(const CaseDev *__restrict__ cas
 template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_t(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     KLanes *L = lanes<NC>(S);
     if (!lanes_active<NC>(L)) return;
@@ -311,6 +316,7 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_t(const CaseDev *__restrict__ 
 template <class T, int NC>
 __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                  const int *__restrict__ cfirst, const int *__restrict__ cnt, T *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     KLanes *L = lanes<NC>(S);
     if (!lanes_active<NC>(L)) return;
@@ -396,6 +402,7 @@ __device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, dou
 
 __global__ void __launch_bounds__(kTile, 3) k_en_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     double v[2] = {0, 0};
     const bool m32 = C.precision >= 2;
@@ -426,6 +433,7 @@ __global__ void __launch_bounds__(kTile, 3) k_en_init(const CaseDev *__restrict_
 
 // precision >= 2: phi += the FP32 correction of the energy solve
 __global__ void __launch_bounds__(kTile) k_en_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     if (!C.ee) return;
     const float *x = mom_vec<float, 1>(C).x[0];
@@ -434,6 +442,7 @@ __global__ void __launch_bounds__(kTile) k_en_apply(const CaseDev *__restrict__ 
 
 // precision 2: u, v, w += the FP32 correction of the momentum solve
 __global__ void __launch_bounds__(kTile) k_mom_apply(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     const MomVec<float> M = mom_vec<float, 3>(C);
     double *xs[3] = {C.u, C.v, C.w};
@@ -447,6 +456,7 @@ __global__ void __launch_bounds__(kTile) k_mom_apply(const CaseDev *__restrict__
 // mean of b (the singular Neumann system is made consistent)
 __global__ void __launch_bounds__(kTile) k_pc_mean(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     double v[1] = {0.0};
     FOR_CELLS(t) v[0] += C.b[i];
@@ -461,6 +471,7 @@ __global__ void __launch_bounds__(kTile) k_pc_mean(const CaseDev *__restrict__ c
 // r = b - mean, z = r/ap, p = z, x = 0 (set_a_0(phic))
 __global__ void __launch_bounds__(kTile) k_pc_init(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                    const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     double v[3] = {0, 0, 0};
     FOR_CELLS(t) {
@@ -488,6 +499,7 @@ __global__ void __launch_bounds__(kTile) k_pc_init(const CaseDev *__restrict__ c
 // q = A p; alpha = rz / (p, q)
 __global__ void __launch_bounds__(kTile) k_pc_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     if (!S->active_p) return;
     double v[1] = {0};
@@ -510,6 +522,7 @@ __global__ void __launch_bounds__(kTile) k_pc_q(const CaseDev *__restrict__ case
 // x += alpha p; r -= alpha q; z = r/ap; beta = (r,z)'/(r,z)
 __global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, double *partials) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     if (!S->active_p) return;
     double v[2] = {0, 0};
@@ -541,6 +554,7 @@ __global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ case
 
 // p = z + beta p
 __global__ void __launch_bounds__(kTile) k_pc_p(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
     TILE_HEAD
     if (!S->active_p) return;
     FOR_CELLS(t) C.kp[i] = C.ks[i] + S->beta_p * C.kp[i];
@@ -550,6 +564,7 @@ __global__ void __launch_bounds__(kTile) k_pc_p(const CaseDev *__restrict__ case
 // kind 0 momentum, 1 pressure CG, 2 mixed inner CG, 3 mixed outer refinement,
 // 4 energy.
 __global__ void k_poll(const CaseDev *__restrict__ cases, int ncases, int *flags, int kind) {
+    CFDL_PDL_WAIT();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncases) return;
     const SolveScalars *S = cases[c].sc;

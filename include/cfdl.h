@@ -286,6 +286,10 @@ int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_id
  * host polling of the inner convergence when off; the results are the same.
  * Per-kernel profiling always uses the second form. */
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on);
+/* Programmatic dependent launch of the solver kernels (default on): each
+ * kernel may be scheduled while the one before it drains, and waits for it
+ * on the device.  Results do not depend on it. */
+int cfdl_set_pdl(cfdl_ctx *ctx, int on);
 
 /* Multigrid hierarchy of case 0 (built on the first AMG pressure solve):
  * *nlev coarse levels; n[0..nlev] cells and W[0..nlev] ELL widths per level

@@ -1,5 +1,6 @@
 // cfdl_energy.cu -- the energy equation of the reference
-// (src/equations/mod_energy.f90) on the device, FP64.
+// (src/equations/mod_energy.f90) on the device; assembly in FP64 (the solve's
+// FP32 correction form for precision >= 2 is in cfdl_solvers.cu).
 //
 // The equation is for phi = cp*t: upwind advection by the face mass fluxes of
 // solve_uvwp, diffusion tc/cp with a deferred correction carrying the

@@ -224,8 +224,9 @@ int cfdl_update_uvwp(cfdl_ctx *ctx);                     /* mod_uvwp.f90:370-436
  * has the call.  cfdl_solve_energy is solve_energy (:59-80): calc_grad of t
  * and phi, calc_coef_energy (:82-169) into ap/anb/b, the phi solve (mode 0:
  * BiCGStab to the reference's 10x residual drop, mode 1: to tight_rtol), and
- * calc_temperature t = phi/cp (mod_properties.f90:214-221).  FP64 in every
- * precision form. */
+ * calc_temperature t = phi/cp (mod_properties.f90:214-221).  The assembly
+ * is FP64 in every precision form; precision >= 2 solves for the correction
+ * of the FP64 residual in FP32, as the momentum solve does. */
 int cfdl_energy_init(cfdl_ctx *ctx, double cp, double tc, double t_init);
 int cfdl_solve_energy(cfdl_ctx *ctx, cfdl_stats *st);
 int cfdl_calc_coef_energy(cfdl_ctx *ctx);                /* mod_energy.f90:82-169  */

@@ -312,3 +312,21 @@ def test_symmetry_bc_tight_parity(need_gpu, tet):
     for f in ("u", "v", "w", "p"):
         a, b = g2.get(f)[:o2.ne], o2.get(f)[:o2.ne]
         assert rel_l2(a, b) < RTOL_FIELD, (f, rel_l2(a, b))
+
+
+@pytest.mark.parametrize("precision", [0, 3])
+def test_programmatic_launch_does_not_change_results(need_gpu, precision):
+    """Programmatic dependent launch (the default) only overlaps launch
+    latency: the fields equal those of ordinary launches bit for bit, in the
+    graph and in the eager form."""
+    s = cfdl.Setup(cfdl.Zone(7, "mixed", 0.2, seed=9))
+    out = []
+    for pdl, graph in ((True, True), (False, True), (True, False)):
+        g = cfdl.Solver(s, cfdl.steady(precision=precision))
+        g.set_pdl(pdl)
+        g.set_graph_mode(graph)
+        g.step(6, 3)
+        out.append({f: g.get(f) for f in ("u", "v", "w", "p", "mip")})
+        g.close()
+    for f in out[0]:
+        assert np.array_equal(out[0][f], out[1][f]) and np.array_equal(out[0][f], out[2][f]), f

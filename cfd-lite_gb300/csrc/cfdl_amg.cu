@@ -40,12 +40,12 @@ template <class T> struct LP {
 
 template <class T> __device__ __forceinline__ LP<T> level(const CaseDev &C, int l);
 template <> __device__ __forceinline__ LP<double> level<double>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb, C.ap, C.rap, C.kr, C.ks, C.ksh};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb_p, C.ap_p, C.rap_p, C.kr, C.ks, C.ksh};
     const AmgLevelDev &L = C.lev[l - 1];
     return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t};
 }
 template <> __device__ __forceinline__ LP<float> level<float>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb, C.fdiag, C.frap, C.fr, C.fz, C.ft};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb_p, C.fdiag_p, C.frap_p, C.fr, C.fz, C.ft};
     const AmgLevelDev &L = C.lev[l - 1];
     return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32};
 }
@@ -119,14 +119,14 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     const CaseDev &C = cases[t.c];
     const int i = t.first + (int)threadIdx.x;
     if (i >= t.last || C.sc->halted) return;
-    const double ap = C.ap[i];
-    C.rap[i] = kOmega / ap;
+    const double ap = C.ap_p[i];
+    C.rap_p[i] = kOmega / ap;
     if (C.precision >= 1) {
         // the FP32 copies converted in the integer pipe (GB300 runs the hardware
         // conversions at its FP64 rate)
-        C.fdiag[i] = narrow_f32(ap);
-        C.frap[i] = narrow_f32(kOmega / ap);
-        for (int k = 0; k < C.W; k++) C.fanb[k * C.ne + i] = narrow_f32(C.anb[k * C.ne + i]);
+        C.fdiag_p[i] = narrow_f32(ap);
+        C.frap_p[i] = narrow_f32(kOmega / ap);
+        for (int k = 0; k < C.W; k++) C.fanb_p[k * C.ne + i] = narrow_f32(C.anb_p[k * C.ne + i]);
     }
 }
 
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
     const int I = t.first + (int)threadIdx.x;
     if (I >= t.last || C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
-    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    const double *af = l == 1 ? C.anb_p : C.lev[l - 2].a;
     const bool mixed = C.precision >= 1;
     const int n = L.n;
     double dsum = 0.0;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
     GROUP_HEAD
     if (C.sc->halted) return;
     const AmgLevelDev &L = C.lev[l - 1];
-    const double *af = l == 1 ? C.anb : C.lev[l - 2].a;
+    const double *af = l == 1 ? C.anb_p : C.lev[l - 2].a;
     const bool mixed = C.precision >= 1;
     const int n = L.n;
     double dsum = 0.0;
@@ -820,9 +820,18 @@ void launch_pc_mean(cfdl_ctx *ctx);
 #define RED ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, ctx->d_partials
 #define RED32 ctx->cellsv.d_case_first, ctx->cellsv.d_case_ntiles, (float *)ctx->d_partials
 
-// FP64 AMG-PCG: coarse operators, zero-mean right-hand side, x = 0
+// What the pressure solve needs of its matrix, once the matrix exists: the
+// multigrid operators (AMG), or the level-0 FP32 copies and 1/ap (mixed
+// Jacobi); the FP64 Jacobi form needs nothing.  In solve_uvwp this runs
+// beside the momentum solve (cfdl_graph.cu): it depends on dc only.
+void pressure_operators(cfdl_ctx *ctx) {
+    const cfdl_config &c = ctx->cases[0]->cfg;
+    if (c.precond == 1) amg_setup_operators(ctx);
+    else if (c.precision >= 1) ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
+}
+
+// FP64 AMG-PCG: zero-mean right-hand side, x = 0 (operators already built)
 void apc_init(cfdl_ctx *ctx) {
-    amg_setup_operators(ctx);
     launch_pc_mean(ctx);
     ALAUNCH("k_apc_init", k_apc_init, ctx->cellsv, RED);
 }
@@ -932,7 +941,7 @@ __global__ void __launch_bounds__(kTile) k_mx_jacobi(const CaseDev *__restrict__
     const Tile t = tiles[blockIdx.x];
     const CaseDev &C = cases[t.c];
     if (!C.sc->active32) return;
-    FOR_CELLS(t) C.fz[i] = C.fr[i] * C.frap[i];
+    FOR_CELLS(t) C.fz[i] = C.fr[i] * C.frap_p[i];
 }
 
 __global__ void __launch_bounds__(kTile) k_mx_rz(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
@@ -1064,8 +1073,6 @@ __global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ ca
 
 // mixed form: FP32 operator copies (+ coarse operators), FP64 start
 void mx_init(cfdl_ctx *ctx) {
-    if (ctx->cases[0]->cfg.precond == 1) amg_setup_operators(ctx);
-    else ALAUNCH("k_amg_prep0", k_amg_prep0, ctx->cells);
     launch_pc_mean(ctx);
     ALAUNCH("k_mx_init", k_mx_init, ctx->cellsv, RED);
 }

@@ -41,14 +41,17 @@ Named lookup(HostCase *hc, const char *name) {
         {"u0", d.u0, nc}, {"v0", d.v0, nc}, {"w0", d.w0, nc}, {"phic", d.phic, nc},
         {"gu", d.gu, 3 * nc}, {"gv", d.gv, 3 * nc}, {"gw", d.gw, 3 * nc}, {"gp", d.gp, 3 * nc}, {"gpc", d.gpc, 3 * nc},
         {"mip", d.mip, nf}, {"mip0", d.mip0, nf},
-        {"ap", d.ap, ne}, {"b", d.b, ne}, {"bu", d.bu, ne}, {"bv", d.bv, ne}, {"bw", d.bw, ne},
+        {"b", d.b, ne}, {"bu", d.bu, ne}, {"bv", d.bv, ne}, {"bw", d.bw, ne},
         {"d", d.d, ne}, {"dc", d.dc, ne}, {"rho", d.rho, ne}, {"mu", d.mu, ne},
         // energy equation (null until cfdl_energy_init)
         {"t", d.et, nc}, {"e", d.ee, nc}, {"e0", d.ee0, nc}, {"gt", d.egt, 3 * nc}, {"ge", d.ege, 3 * nc},
         {"cp", d.ecp, ne}, {"tc", d.etc, ne},
     };
     for (const E &e : tab) if (s == e.nm) return {e.p, e.n, false};
-    if (s == "anb") return {d.anb, (size_t)hc->H, true};
+    // ap/anb as the reference's phys_t holds them: the last assembly's (the
+    // pressure matrix after calc_coef_p / solve_uvwp)
+    if (s == "anb") return {hc->coef_is_pressure ? d.anb_p : d.anb, (size_t)hc->H, true};
+    if (s == "ap") return {hc->coef_is_pressure ? d.ap_p : d.ap, ne, false};
     return {nullptr, 0, false};
 }
 
@@ -133,16 +136,22 @@ cfdl_ctx *ctx_new() {
 
 int solve_uvwp_all(cfdl_ctx *ctx) {
     // solve_uvwp, src/equations/mod_uvwp.f90:95-134: as one graph launch unless
-    // graphs are off or launches are being profiled one by one
+    // graphs are off or launches are being profiled one by one.  The pressure
+    // matrix needs only dc of calc_coef_uvw, so it and the pressure solve's
+    // operators are built right after it (in the graph: beside the momentum
+    // solve); the right-hand side follows calc_mip.
     if (ctx->use_graph && !prof_active(ctx)) return solve_uvwp_graph(ctx);
+    int st;
+    if (ctx->cases[0]->cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
     launch_coef_uvw(ctx);
-    int st = solve_momentum(ctx);
-    if (st) return st;
+    launch_coef_p_matrix(ctx);
+    pressure_operators(ctx);
+    if ((st = solve_momentum(ctx))) return st;
     launch_grad(ctx, 4);
     if (ctx->ev_mom) cudaEventRecord(ctx->ev_mom, ctx->stream);
     launch_calc_mip(ctx, 1);
-    launch_coef_p(ctx);
-    st = solve_pressure(ctx);
+    launch_coef_p_rhs(ctx);
+    st = solve_pressure_prepared(ctx);
     if (st) return st;
     launch_adjust_pc(ctx);
     launch_grad(ctx, 3);
@@ -600,6 +609,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 24 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
     bytes += 160 * c;                                 // multigrid hierarchy (bound)
     bytes += 9 * c * 4 + 3 * w * c * 4 + 7 * f * 4;   // precision 3 FP32 gradients, stencil, face planes
+    bytes += w * c * 12 + c * 24;                     // the pressure matrix's own storage and FP32 copies
     return bytes;
 }
 

@@ -172,6 +172,12 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
     double **ef[] = {&d.bu, &d.bv, &d.bw, &d.d, &d.dc, &d.rho, &d.mu, &d.ap, &d.b};
     for (double **pp : ef) if ((st = zeros(hc, pp, (size_t)ne))) return st;
     if ((st = zeros(hc, &d.anb, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.anb_p, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.ap_p, (size_t)ne))) return st;
+    if ((st = zeros(hc, &d.rap_p, (size_t)ne))) return st;
+    if ((st = zeros(hc, &d.fanb_p, (size_t)W * ne))) return st;
+    if ((st = zeros(hc, &d.fdiag_p, (size_t)ne))) return st;
+    if ((st = zeros(hc, &d.frap_p, (size_t)ne))) return st;
     if ((st = zeros(hc, &d.fdiff, (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fS, 3 * (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fprop, (size_t)PR_N * nf))) return st;

@@ -224,6 +224,8 @@ void ensure_energy_props(cfdl_ctx *ctx) {
 
 void launch_coef_energy(cfdl_ctx *ctx) {
     ensure_energy_props(ctx);
+    if (!ctx->capturing)
+        for (HostCase *hc : ctx->cases) hc->coef_is_pressure = false;   // ap/anb hold the energy matrix
     CFDL_LAUNCH("k_en_face", k_en_face, faces);
     CFDL_LAUNCH("k_en_cell", k_en_cell, cells);
 }

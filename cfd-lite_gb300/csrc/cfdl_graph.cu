@@ -94,14 +94,20 @@ struct Builder {
     }
     // append a captured segment as a child-graph node after *prev
     template <class F> int segment(cudaGraph_t G, cudaGraphNode_t *prev, F f, int64_t *count) {
+        cudaGraphNode_t dep[1] = {*prev};
+        return segment_after(G, dep, *prev ? 1 : 0, f, count, prev);
+    }
+    // a captured segment as a child-graph node depending on deps[0..ndep)
+    template <class F>
+    int segment_after(cudaGraph_t G, const cudaGraphNode_t *deps, int ndep, F f, int64_t *count, cudaGraphNode_t *out) {
         cudaGraph_t child = nullptr;
         int st = capture(f, &child, count);
         if (st) return st;
         cudaGraphNode_t n;
-        cudaError_t e = cudaGraphAddChildGraphNode(&n, G, *prev ? prev : nullptr, *prev ? 1 : 0, child);
+        cudaError_t e = cudaGraphAddChildGraphNode(&n, G, ndep ? deps : nullptr, ndep, child);
         cudaGraphDestroy(child);
         if (e != cudaSuccess) return cuda_status(e);
-        *prev = n;
+        *out = n;
         return CFDL_OK;
     }
     // append a while node; fill(body) builds its body graph
@@ -194,6 +200,18 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
          }, &k)))
         return st;
     *static_k += k;
+    // beside the momentum solve: the pressure matrix (it needs only dc of
+    // calc_coef_uvw) and the pressure solve's operators, in their own storage
+    cudaGraphNode_t branch = nullptr;
+    {
+        const cudaGraphNode_t dep[1] = {*prev};
+        if ((st = b.segment_after(G, dep, 1, [&] {
+                 launch_coef_p_matrix(ctx);
+                 pressure_operators(ctx);
+             }, &k, &branch)))
+            return st;
+        *static_k += k;
+    }
     st = b.loop(G, prev, hm, [&](cudaGraph_t body_g) {
         return b.capture_into(body_g, [&] { mom_iter(ctx); b.setcond(hm, LOOP_MOM); }, &body[LOOP_MOM]);
     });
@@ -209,16 +227,19 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
         if (e != cudaSuccess) return cuda_status(e);
         *prev = n;
     }
-    if ((st = b.segment(G, prev, [&] {
-             launch_calc_mip(ctx, 1);
-             launch_coef_p(ctx);
-             if (cfg.precision >= 1) mx_init(ctx);
-             else if (cfg.precond == 1) apc_init(ctx);
-             else pcj_init(ctx);
-             b.setone(hp);
-         }, &k)))
-        return st;
-    *static_k += k;
+    {
+        const cudaGraphNode_t deps[2] = {*prev, branch};
+        if ((st = b.segment_after(G, deps, 2, [&] {
+                 launch_calc_mip(ctx, 1);
+                 launch_coef_p_rhs(ctx);
+                 if (cfg.precision >= 1) mx_init(ctx);
+                 else if (cfg.precond == 1) apc_init(ctx);
+                 else pcj_init(ctx);
+                 b.setone(hp);
+             }, &k, prev)))
+            return st;
+        *static_k += k;
+    }
     if (cfg.precision == 0) {
         st = b.loop(G, prev, hp, [&](cudaGraph_t body_g) {
             return b.capture_into(body_g, [&] {
@@ -399,6 +420,8 @@ int run_graph_launch(cfdl_ctx *ctx) {
         if ((st = build_run_graph(ctx))) return st;
     ctx->launches += ctx->run_static_kernels;
     ctx->graph_launches++;
+    const bool pressure_last = !energy_on(ctx);
+    for (HostCase *hc : ctx->cases) hc->coef_is_pressure = pressure_last;
     return cuda_status(cudaGraphLaunch(ctx->run_exec, ctx->stream));
 }
 
@@ -412,6 +435,7 @@ int solve_uvwp_graph(cfdl_ctx *ctx) {
         if ((st = build_graph(ctx))) return st;
     ctx->launches += ctx->graph_static_kernels;
     ctx->graph_launches++;
+    for (HostCase *hc : ctx->cases) hc->coef_is_pressure = true;
     return cuda_status(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
 }
 

@@ -122,6 +122,11 @@ struct CaseDev {
     double *mip, *mip0;
     double *bu, *bv, *bw, *d, *dc, *rho, *mu;
     double *ap, *anb, *b, *phic;          // phys_t scratch: ap[ne], anb ELL [W][ne], b[ne], phic[ne+nbf]
+    // the pressure-correction matrix in its own storage (the reference shares
+    // ap/anb): it depends only on dc, so it and the multigrid set-up are built
+    // beside the momentum solve; its 1/ap scaling and FP32 copies likewise
+    double *ap_p, *anb_p, *rap_p;
+    float *fdiag_p, *fanb_p, *frap_p;
     // face intermediates of the assemblies
     double *fdiff, *fS;                   // [nf] pressure face coefficient, [3][nf] explicit momentum face terms
     double *fprop;                        // [PR_N][nf] property planes
@@ -183,6 +188,7 @@ struct HostCase {
     std::vector<double> h_temp;      // [nbf] energy wall temperature of each halo (empty: none)
     bool eprops_dirty = true;        // eprop must be recomputed (cp or tc changed)
     bool g32_stale = false;          // g32 must be rebuilt from gu, gv, gw (they were written from outside)
+    bool coef_is_pressure = false;   // ap/anb as the reference's phys_t holds them: the pressure matrix last
 };
 
 }  // namespace cfdl
@@ -278,7 +284,9 @@ int ensure_f32_assembly(HostCase *hc, cudaStream_t stream);   // precision 3 arr
 void launch_coef_uvw(cfdl_ctx *ctx);
 void launch_grad(cfdl_ctx *ctx, int field);     // 0 u, 1 v, 2 w, 3 phic, 4 = u,v,w fused, 5 = energy t, phi
 void launch_calc_mip(cfdl_ctx *ctx, int rhie_chow);
-void launch_coef_p(cfdl_ctx *ctx);
+void launch_coef_p(cfdl_ctx *ctx);             // matrix and right-hand side
+void launch_coef_p_matrix(cfdl_ctx *ctx);      // face coefficients, ap_p/anb_p (needs dc only)
+void launch_coef_p_rhs(cfdl_ctx *ctx);         // b (needs the fluxes of calc_mip)
 void launch_adjust_pc(cfdl_ctx *ctx);
 void launch_update_uvwp(cfdl_ctx *ctx);
 void launch_update_time(cfdl_ctx *ctx);
@@ -346,7 +354,9 @@ inline void launch_k(bool pdl, void (*k)(KArgs...), unsigned grid, unsigned bloc
 
 // solvers (cfdl_solvers.cu)
 int solve_momentum(cfdl_ctx *ctx);
-int solve_pressure(cfdl_ctx *ctx);
+int solve_pressure(cfdl_ctx *ctx);              // operators (multigrid / FP32 copies) + solve
+int solve_pressure_prepared(cfdl_ctx *ctx);     // the solve, operators already built
+void pressure_operators(cfdl_ctx *ctx);         // what the pressure solve needs of its matrix
 // AMG-preconditioned pressure solve (cfdl_amg.cu)
 int ensure_amg(cfdl_ctx *ctx);
 int solve_pressure_amg(cfdl_ctx *ctx);

@@ -413,26 +413,46 @@ __global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict
     C.fdiff[i] = (omw * C.dc[o] + wt * C.dc[n]) * C.fprop[PR_RHOADN * nf + i];
 }
 
-__global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+// the matrix: anb = the face coefficient on interior slots (0 on walls,
+// mod_uvwp.f90:354-363), ap = their sum
+__global__ void __launch_bounds__(kTile) k_coef_p_mat(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
-    double ap = 0.0, sumf = 0.0;
-    int bslot[kMaxW], nb_cnt = 0;
+    double ap = 0.0;
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
         if (k >= W) continue;
         const int nb = C.hf_nb[k * ne + i];
         double a = 0.0;
-        if (nb >= ne) bslot[nb_cnt++] = k;
-        else if (nb >= 0) {
-            const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
-            sumf += flip_sign(C.mip[f], fc >= 0);   // -sg * mip
-            a = C.fdiff[f];
+        if (nb >= 0 && nb < ne) {
+            a = C.fdiff[face_of(C.hf_fc[k * ne + i])];
             ap += a;
         }
-        C.anb[k * ne + i] = a;
+        C.anb_p[k * ne + i] = a;
+    }
+    C.ap_p[i] = ap;
+}
+
+// the right-hand side: b = net inflow over the interior faces, minus the
+// boundary mass fluxes in BC-loop order
+__global__ void __launch_bounds__(kTile) k_coef_p_rhs(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
+    TILE_PROLOGUE(cells)
+    if (i >= t.last) return;
+    const int ne = C.ne, W = C.W;
+    double sumf = 0.0;
+    int bslot[kMaxW], nb_cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (k >= W) continue;
+        const int nb = C.hf_nb[k * ne + i];
+        if (nb >= ne) bslot[nb_cnt++] = k;
+        else if (nb >= 0) {
+            const int fc = C.hf_fc[k * ne + i];
+            sumf += flip_sign(C.mip[face_of(fc)], fc >= 0);   // -sg * mip
+        }
     }
     for (int q = 1; q < nb_cnt; q++) {
         int s = bslot[q], j = q - 1;
@@ -444,7 +464,6 @@ __global__ void __launch_bounds__(kTile) k_coef_p_cell(const CaseDev *__restrict
         if (C.h_kind[C.hf_nb[k * ne + i] - ne] == 0) continue;
         sumf = sumf - C.mip[face_of(C.hf_fc[k * ne + i])];
     }
-    C.ap[i] = ap;
     C.b[i] = sumf;
 }
 
@@ -544,6 +563,7 @@ void ensure_g32(cfdl_ctx *ctx) {
 }
 void launch_coef_uvw(cfdl_ctx *ctx) {
     ensure_face_props(ctx);
+    for (HostCase *hc : ctx->cases) hc->coef_is_pressure = false;
     if (f32_assembly(ctx)) {
         ensure_g32(ctx);
         CFDL_LAUNCH("k_coef_uvw_face_f32", k_coef_uvw_face_f32, faces);
@@ -563,10 +583,18 @@ void launch_calc_mip(cfdl_ctx *ctx, int rc) {
     ensure_face_props(ctx);
     CFDL_LAUNCH("k_calc_mip", k_calc_mip, faces, rc);
 }
-void launch_coef_p(cfdl_ctx *ctx) {
+void launch_coef_p_matrix(cfdl_ctx *ctx) {
     ensure_face_props(ctx);
     CFDL_LAUNCH("k_coef_p_face", k_coef_p_face, faces);
-    CFDL_LAUNCH("k_coef_p_cell", k_coef_p_cell, cells);
+    CFDL_LAUNCH("k_coef_p_mat", k_coef_p_mat, cells);
+}
+void launch_coef_p_rhs(cfdl_ctx *ctx) {
+    CFDL_LAUNCH("k_coef_p_rhs", k_coef_p_rhs, cells);
+    for (HostCase *hc : ctx->cases) hc->coef_is_pressure = true;
+}
+void launch_coef_p(cfdl_ctx *ctx) {
+    launch_coef_p_matrix(ctx);
+    launch_coef_p_rhs(ctx);
 }
 void launch_adjust_pc(cfdl_ctx *ctx) {
     int n = (int)ctx->cases.size();

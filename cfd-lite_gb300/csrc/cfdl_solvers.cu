@@ -31,10 +31,10 @@ enum { CNT_M1 = 0, CNT_M2, CNT_M3, CNT_M4, CNT_M5, CNT_P0, CNT_P1, CNT_P2, CNT_P
 __device__ __forceinline__ double *comp_field(const CaseDev &C, int q) { return q == 0 ? C.u : q == 1 ? C.v : C.w; }
 __device__ __forceinline__ const double *comp_rhs(const CaseDev &C, int q) { return q == 0 ? C.bu : q == 1 ? C.bv : C.bw; }
 
-// (A x)_i for the interior operator: ap_i x_i - sum_{interior nb} anb x_nb
+// (A x)_i for the pressure-correction operator: ap_i x_i - sum_{interior nb} anb x_nb
 __device__ __forceinline__ double amul_row(const CaseDev &C, const double *x, int i) {
     double y[1];
-    ell_row<1, double>(C.hf_nb, C.anb, C.ap[i], x, 0, C.ne, C.W, i, y);
+    ell_row<1, double>(C.hf_nb, C.anb_p, C.ap_p[i], x, 0, C.ne, C.W, i, y);
     return y[0];
 }
 
@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(kTile) k_pc_init(const CaseDev *__restrict__ c
     TILE_HEAD
     double v[3] = {0, 0, 0};
     FOR_CELLS(t) {
-        const double r = C.b[i] - S->mean_b, z = r / C.ap[i];
+        const double r = C.b[i] - S->mean_b, z = r / C.ap_p[i];
         C.kr[i] = r; C.ks[i] = z; C.kp[i] = z; C.phic[i] = 0.0;
         v[0] += r * r; v[1] += r * z; v[2] += C.b[i] * C.b[i];
     }
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(kTile) k_pc_x(const CaseDev *__restrict__ case
     FOR_CELLS(t) {
         const double a = S->alpha_p;
         C.phic[i] = C.phic[i] + a * C.kp[i];
-        const double r = C.kr[i] - a * C.kv[i], z = r / C.ap[i];
+        const double r = C.kr[i] - a * C.kv[i], z = r / C.ap_p[i];
         C.kr[i] = r; C.ks[i] = z;
         v[0] += r * r; v[1] += r * z;
     }
@@ -714,7 +714,16 @@ int solve_momentum(cfdl_ctx *ctx) {
 
 void launch_pc_mean(cfdl_ctx *ctx) { CFDL_LAUNCH("k_pc_mean", k_pc_mean, cellsv, RED); }
 
+// the pressure solve with its operators (the per-routine entry point)
 int solve_pressure(cfdl_ctx *ctx) {
+    if (ctx->cells.ntiles == 0) return CFDL_OK;
+    int st;
+    if (ctx->cases[0]->cfg.precond == 1 && (st = ensure_amg(ctx))) return st;
+    pressure_operators(ctx);
+    return solve_pressure_prepared(ctx);
+}
+
+int solve_pressure_prepared(cfdl_ctx *ctx) {
     if (ctx->cells.ntiles == 0) return CFDL_OK;
     if (ctx->cases[0]->cfg.precision >= 1) return solve_pressure_mixed(ctx);
     if (ctx->cases[0]->cfg.precond == 1) return solve_pressure_amg(ctx);

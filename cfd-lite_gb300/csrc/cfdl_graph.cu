@@ -216,17 +216,27 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
         return b.capture_into(body_g, [&] { mom_iter(ctx); b.setcond(hm, LOOP_MOM); }, &body[LOOP_MOM]);
     });
     if (st) return st;
-    // gradients, Rhie-Chow fluxes, pressure assembly, pressure-solve start
-    if ((st = b.segment(G, prev, [&] { mom_finish(ctx); launch_grad(ctx, 4); }, &k))) return st;
-    *static_k += k;
+    // the FP32 correction of precision >= 2 completes u, v, w
+    if (cfg.precision >= 2) {
+        if ((st = b.segment(G, prev, [&] { mom_finish(ctx); }, &k))) return st;
+        *static_k += k;
+    }
+    // the gradients of u, v, w are read only by the next outer iteration's
+    // face terms, so they run beside the whole pressure part
+    cudaGraphNode_t gradn = nullptr;
+    {
+        const cudaGraphNode_t dep[1] = {*prev};
+        if ((st = b.segment_after(G, dep, 1, [&] { launch_grad(ctx, 4); }, &k, &gradn))) return st;
+        *static_k += k;
+    }
     if (ctx->ev_mom && mark) {
         // u, v, w and their gradients are final here (cfdl_solve_uvwp_host
         // starts their download on this record)
         cudaGraphNode_t n;
-        cudaError_t e = cudaGraphAddEventRecordNode(&n, G, prev, 1, ctx->ev_mom);
+        cudaError_t e = cudaGraphAddEventRecordNode(&n, G, &gradn, 1, ctx->ev_mom);
         if (e != cudaSuccess) return cuda_status(e);
-        *prev = n;
     }
+    // Rhie-Chow fluxes, the pressure right-hand side, the pressure-solve start
     {
         const cudaGraphNode_t deps[2] = {*prev, branch};
         if ((st = b.segment_after(G, deps, 2, [&] {

@@ -442,8 +442,11 @@ class Solver:
         _check(lib().cfdl_set_pdl(self._h, int(bool(on))), "set_pdl")
 
     def set_graph_mode(self, on):
-        """solve_uvwp as one CUDA graph (True, default) or as individual launches."""
-        _check(lib().cfdl_set_graph_mode(self._h, int(bool(on))), "set_graph_mode")
+        """solve_uvwp as one CUDA graph (True or 1, default), as individual
+        launches (False or 0), or as the graph in one chain without its
+        parallel branches (2)."""
+        mode = on if (isinstance(on, int) and not isinstance(on, bool)) else int(bool(on))
+        _check(lib().cfdl_set_graph_mode(self._h, mode), "set_graph_mode")
 
     def set_config(self, cfg):
         _check(lib().cfdl_set_config(self._h, C.byref(cfg)), "set_config")

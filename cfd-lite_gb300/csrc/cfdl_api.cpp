@@ -648,8 +648,15 @@ int cfdl_set_pdl(cfdl_ctx *ctx, int on) {
 }
 
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on) {
-    if (!ctx) return CFDL_ERR_INVALID;
+    if (!ctx || on < 0 || on > 2) return CFDL_ERR_INVALID;
+    const bool branches = on != 2;
+    if (branches != ctx->graph_branches) {
+        int st = cuda_status(cudaStreamSynchronize(ctx->stream));
+        if (st) return st;
+        destroy_graph(ctx);
+    }
     ctx->use_graph = on != 0;
+    ctx->graph_branches = branches;
     return CFDL_OK;
 }
 

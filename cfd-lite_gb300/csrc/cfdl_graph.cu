@@ -211,6 +211,7 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
              }, &k, &branch)))
             return st;
         *static_k += k;
+        if (!ctx->graph_branches) *prev = branch;   // one chain: the momentum solve after it
     }
     st = b.loop(G, prev, hm, [&](cudaGraph_t body_g) {
         return b.capture_into(body_g, [&] { mom_iter(ctx); b.setcond(hm, LOOP_MOM); }, &body[LOOP_MOM]);
@@ -228,6 +229,7 @@ static int append_uvwp(Builder &b, cudaGraph_t G, cudaGraphNode_t *prev, Pre pre
         const cudaGraphNode_t dep[1] = {*prev};
         if ((st = b.segment_after(G, dep, 1, [&] { launch_grad(ctx, 4); }, &k, &gradn))) return st;
         *static_k += k;
+        if (!ctx->graph_branches) *prev = gradn;
     }
     if (ctx->ev_mom && mark) {
         // u, v, w and their gradients are final here (cfdl_solve_uvwp_host

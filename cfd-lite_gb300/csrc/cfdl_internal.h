@@ -230,6 +230,7 @@ struct cfdl_ctx {
     int amg_lmax = -1;
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;
+    bool graph_branches = true;          // the outer-iteration graph's parallel branches (off: one chain)
     bool pdl = true;                     // launch with programmatic dependent launch (cfdl_set_pdl)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;

@@ -283,9 +283,12 @@ int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_id
                           int *iters, double *rnorm);
 
 /* solve_uvwp runs as one CUDA graph (inner solve loops as device-side while
- * nodes) when on (the default), or as individually launched kernels with
- * host polling of the inner convergence when off; the results are the same.
- * Per-kernel profiling always uses the second form. */
+ * nodes) when on (1, the default), or as individually launched kernels with
+ * host polling of the inner convergence when off (0); 2 is the graph with
+ * its nodes in one chain instead of the parallel branches (the pressure
+ * matrix and multigrid set-up beside the momentum solve, the velocity
+ * gradients beside the pressure part).  The results are the same in every
+ * mode.  Per-kernel profiling always uses the eager form. */
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on);
 /* Programmatic dependent launch of the solver kernels (default on): each
  * kernel may be scheduled while the one before it drains, and waits for it

@@ -10,7 +10,10 @@
  * of all host arrays.  Every entry point returns a status code (CFDL_OK = 0).
  *
  * Threading: one CUDA stream per context; a context is not thread-safe;
- * different contexts may be used from different threads.
+ * different contexts may be used from different threads.  A set-up object is
+ * read-only after creation except for cfdl_setup_mesh, which fills the
+ * boundary-condition tables the returned cfdl_mesh points into: call it from
+ * one thread at a time per set-up.
  */
 #ifndef CFDL_H
 #define CFDL_H

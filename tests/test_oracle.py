@@ -75,8 +75,12 @@ def test_golden_runs():
         z = cfdl.Zone(rec["n"], rec["tet"], rec["jitter"], seed=rec["seed"])
         o = oracle_lib.Oracle(z, n_subdomains=4)
         o.physics_init(oracle_lib.config(**kw))
+        if rec.get("energy"):
+            o.energy_init()
         st = o.run(rec["n_outer"], 3)
         assert [st.it_u, st.it_v, st.it_w, st.it_p] == rec["iters"], key
+        if rec.get("energy"):
+            assert st.it_e == rec["iters_e"], key
         for f, h in rec["hash"].items():
             assert sha(o.get(f)) == h, (key, f)
 

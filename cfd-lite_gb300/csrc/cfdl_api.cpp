@@ -253,6 +253,7 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     for (WorkList *wl : wls) free_worklist(*wl);
     free_worklist(ctx->cellsv);
     free_worklist(ctx->cellse);
+    free_worklist(ctx->facesv);
     for (auto &wl : ctx->amg_cells) free_worklist(wl);
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);

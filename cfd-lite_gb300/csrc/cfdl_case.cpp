@@ -406,6 +406,7 @@ int rebuild_worklists(cfdl_ctx *ctx) {
     int st;
     if ((st = build_worklist(ctx, ctx->cells, nc))) return st;
     if ((st = build_worklist(ctx, ctx->faces, nfc))) return st;
+    if ((st = build_worklist(ctx, ctx->facesv, nfc, kTile * kFaceVec))) return st;
     if ((st = build_worklist(ctx, ctx->halos, nh))) return st;
     if ((st = build_worklist(ctx, ctx->cellsv, nc, kTile * ctx->vec))) return st;
     if ((st = build_worklist(ctx, ctx->cellse, nc, kTile * ctx->en_vec))) return st;

@@ -32,6 +32,7 @@ constexpr int kTile = 256;        // cells / faces / halos per CTA
 constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
 constexpr int kNPart = 16;        // partial slots per tile
 constexpr int kVec = 4;           // default cells per thread in the solver kernels
+constexpr int kFaceVec = 8;       // faces per thread in the face reductions (their FP64 tree amortised)
 constexpr int kMixedMaxOuter = 60;   // FP64 refinement cycles of the mixed pressure solve
 // loop-pass counters: [0,4) loops of the solve_uvwp graph, [4,8) the same
 // loops inside the run graph, [8] the run graph's outer loop, [9] its energy
@@ -210,6 +211,7 @@ struct cfdl_ctx {
     cfdl::WorkList cellsv;               // wide tiles (kTile*vec cells) for the solver kernels
     int vec = cfdl::kVec;                // cells per thread in those tiles (autotuned)
     cfdl::WorkList cellse;               // tiles of the energy solve (kTile*en_vec cells)
+    cfdl::WorkList facesv;               // wide face tiles (kTile*kFaceVec faces) for face reductions
     int en_vec = 1;                      // cells per thread in those tiles (autotuned with the energy equation)
     int last_iters_m = 0, last_iters_p = 0, last_iters_e = 0;   // previous inner iteration counts (poll scheduling)
     double *d_partials = nullptr;        // [max tiles][kNPart]

@@ -43,9 +43,10 @@ __global__ void __launch_bounds__(kTile) k_run_end(const CaseDev *__restrict__ c
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (S->halted) return;
+    // several faces per thread (wide tiles), then one block tree: the FP64
+    // reduction tree is paid once per kTile*kFaceVec faces
     double v[1] = {0.0};
-    const int f = t.first + (int)threadIdx.x;
-    if (f < t.last) v[0] = fabs(C.mip[f]);
+    FOR_CELLS(t) v[0] += fabs(C.mip[i]);
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_RUN], cnt[t.c])) {
         __shared__ double s[1];
@@ -135,7 +136,7 @@ void launch_run_begin(cfdl_ctx *ctx) {
 }
 
 void launch_run_end(cfdl_ctx *ctx) {
-    CFDL_LAUNCH("k_run_end", k_run_end, faces, ctx->faces.d_case_first, ctx->faces.d_case_ntiles, ctx->d_partials);
+    CFDL_LAUNCH("k_run_end", k_run_end, facesv, ctx->facesv.d_case_first, ctx->facesv.d_case_ntiles, ctx->d_partials);
     CFDL_LAUNCH("k_run_time_cells", k_run_time_cells, cells);
     CFDL_LAUNCH("k_run_time_halos", k_run_time_halos, halos);
     CFDL_LAUNCH("k_run_time_faces", k_run_time_faces, faces);

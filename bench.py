@@ -309,9 +309,27 @@ def run_ours(a, dist):
         wall = time.perf_counter() - t0
         ms_e = max(ms_e, wall * 1e3)
         ms_e = dist.max(ms_e)
+        # the host link alone: the upload, and the part of the download that
+        # cannot overlap the pressure correction (p, gp, gpc, mip)
+        def wall_ms(fn, reps=5):
+            fn()
+            t = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            return (time.perf_counter() - t) * 1e3 / reps
+        up = cfdl.Fields(**{k: v.ctypes.data_as(C.c_void_p) for k, v in host.items() if k != "gpc"})
+        late_keys = ("p", "gp", "gpc", "mip")
+        late = cfdl.Fields(**{k: host[k].ctypes.data_as(C.c_void_p) for k in late_keys})
+        ms_up = wall_ms(lambda: cfdl._check(L.cfdl_upload_fields(g._h, C.byref(up)), "upload"))
+        ms_dn = wall_ms(lambda: cfdl._check(L.cfdl_download_fields(g._h, C.byref(fl)), "download"))
+        ms_late = ms_dn * sum(host[k].nbytes for k in late_keys) / d2h
         e2e = {"value": dist.sum(ne * a.steps) / (ms_e / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "api": "cfdl_step_host (upload, update_boundaries + solve_uvwp, overlapped download)"}
+               "api": "cfdl_step_host (upload, update_boundaries + solve_uvwp, overlapped download)",
+               "ms_per_step": ms_e / a.steps,
+               "link": {"h2d_gbs": h2d / ms_up / 1e6, "d2h_gbs": d2h / ms_dn / 1e6,
+                        "floor_ms_per_step": ms_max / a.steps + ms_up + ms_late,
+                        "floor": "device step + upload + non-overlapped download (p, gp, gpc, mip)"}}
 
     cpu = None
     if not a.no_cpu and dist.rank == 0 and dist.world == 1:

@@ -57,26 +57,67 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
     return y[0];
 }
 
-// sum_j a_ij x_j over the row's couplings inside the level (the ELL values
-// are the off-diagonal magnitudes: A = D - offdiag)
-template <int W, class T> __device__ __forceinline__ T offsum_w(const LP<T> &P, const T *x, int i) {
-    int j[W];
-    T c[W];
+// The first W slots of row i: neighbour j[k] (i itself for a slot outside
+// [0, n)) and coefficient c[k] (0 there).  The coefficient's address does not
+// depend on the index, so both loads are issued together: a load guarded by
+// the index would wait for it, a second memory latency in the row's chain.
+// kGuard: the row has P.W <= W slots (the mesh level, W = kMaxW); slots past
+// P.W are not read.  kEager false: the coefficient load waits for the index
+// (the coarse levels' kernels, where that form measured faster).
+template <int W, class T, bool kGuard, bool kEager = true>
+__device__ __forceinline__ void row_slots(const LP<T> &P, int i, int (&j)[W], T (&c)[W]) {
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        const int jj = P.nb[k * P.n + i];
+        const bool in = !kGuard || k < P.W;
+        const int jj = in ? P.nb[k * P.n + i] : -1;
         const bool ok = (unsigned)jj < (unsigned)P.n;
         j[k] = ok ? jj : i;
-        c[k] = ok ? P.a[k * P.n + i] : (T)0;
+        if (kEager) {
+            const T ak = in ? P.a[k * P.n + i] : (T)0;
+            c[k] = ok ? ak : (T)0;
+        } else {
+            c[k] = ok ? P.a[k * P.n + i] : (T)0;
+        }
     }
+}
+
+// sum_j a_ij x_j over the row's couplings inside the level (the ELL values
+// are the off-diagonal magnitudes: A = D - offdiag)
+template <int W, class T, bool kGuard = false, bool kEager = true>
+__device__ __forceinline__ T offsum_w(const LP<T> &P, const T *x, int i) {
+    int j[W];
+    T c[W];
+    row_slots<W, T, kGuard, kEager>(P, i, j, c);
     T s = 0;
 #pragma unroll
     for (int k = 0; k < W; k++) s += c[k] * x[j[k]];
     return s;
 }
-template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
+
+// The mesh level (level 0): at most kMaxW slots a row, every width on the
+// short fixed-width paths (no wide-row code in the kernels that use these)
+template <class T> __device__ __forceinline__ T offsum_mesh(const LP<T> &P, const T *x, int i) {
     if (P.W == 6) return offsum_w<6, T>(P, x, i);
     if (P.W == 4) return offsum_w<4, T>(P, x, i);
+    return offsum_w<kMaxW, T, true>(P, x, i);
+}
+template <int W, class T, bool kGuard = false> __device__ __forceinline__ T amul_w(const LP<T> &P, const T *x, int i) {
+    int j[W];
+    T c[W];
+    row_slots<W, T, kGuard>(P, i, j, c);
+    T s = P.dg[i] * x[i];
+#pragma unroll
+    for (int k = 0; k < W; k++) s -= c[k] * x[j[k]];
+    return s;
+}
+template <class T> __device__ __forceinline__ T amul_mesh(const LP<T> &P, const T *x, int i) {
+    if (P.W == 6) return amul_w<6, T>(P, x, i);
+    if (P.W == 4) return amul_w<4, T>(P, x, i);
+    return amul_w<kMaxW, T, true>(P, x, i);
+}
+template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
+    if (P.W == 6) return offsum_w<6, T, false, false>(P, x, i);
+    if (P.W == 4) return offsum_w<4, T, false, false>(P, x, i);
     // wide coarse rows: four slots per step, loads issued together
     T s = 0;
     for (int k0 = 0; k0 < P.W; k0 += 4) {
@@ -199,8 +240,8 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
     P.t[i] = P.rd[i] * P.r[i];
 }
 
-// z = t + w D^-1 (r - A t)
-template <class T>
+// z = t + w D^-1 (r - A t).  kMesh: launched on the mesh level only
+template <class T, bool kMesh>
 __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
@@ -209,11 +250,17 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
+    if (kMesh) {
+        const T off = offsum_mesh<T>(P, P.t, i);
+        P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], off);
+    } else {
+        // the row's own values first: measured faster on the coarse levels
+        P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
+    }
 }
 
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
-template <class T>
+template <class T, bool kMesh>
 __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
@@ -222,7 +269,7 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.t[i] = P.r[i] - amul<T>(P, P.z, i);
+    P.t[i] = P.r[i] - (kMesh ? amul_mesh<T>(P, P.z, i) : amul<T>(P, P.z, i));
 }
 
 // r_{l1}[I] = sum of the residual t over the members of aggregate I (one
@@ -292,14 +339,17 @@ __global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ ca
 // t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly),
 // on the mesh level: the W neighbour indices, then their aggregates, then the
 // values are loaded as three independent batches (no per-slot load chain)
-template <int W, class T>
+template <int W, class T, bool kGuard = false, bool kEager = true>
 __device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__ agg, const T *__restrict__ zc, T sc,
                                          int i) {
     int j[W], ag[W];
     bool ok[W];
+    T c[W];
 #pragma unroll
     for (int k = 0; k < W; k++) {
-        j[k] = P.nb[k * P.n + i];
+        const bool in = !kGuard || k < P.W;
+        j[k] = in ? P.nb[k * P.n + i] : -1;
+        if (kEager) c[k] = in ? P.a[k * P.n + i] : (T)0;     // not waiting for the index
         ok[k] = (unsigned)j[k] < (unsigned)P.n;
         if (!ok[k]) j[k] = i;
     }
@@ -308,11 +358,11 @@ __device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__
     T s = 0;
 #pragma unroll
     for (int k = 0; k < W; k++)
-        if (ok[k]) s += P.a[k * P.n + i] * (P.z[j[k]] + sc * zc[ag[k]]);
+        if (ok[k]) s += (kEager ? c[k] : P.a[k * P.n + i]) * (P.z[j[k]] + sc * zc[ag[k]]);
     return s;
 }
 
-template <class T>
+template <class T, bool kMesh>
 __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
@@ -326,8 +376,9 @@ __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__
     const T sc = (T)kOverCorrect;
     const T xi = P.z[i] + sc * zc[L.agg[i]];
     T off;
-    if (P.W == 6) off = prolong_row<6, T>(P, L.agg, zc, sc, i);
-    else if (P.W == 4) off = prolong_row<4, T>(P, L.agg, zc, sc, i);
+    if (P.W == 6) off = prolong_row<6, T, false, kMesh>(P, L.agg, zc, sc, i);
+    else if (P.W == 4) off = prolong_row<4, T, false, kMesh>(P, L.agg, zc, sc, i);
+    else if (kMesh) off = prolong_row<kMaxW, T, true>(P, L.agg, zc, sc, i);
     else {
         off = 0;
         for (int k = 0; k < P.W; k++) {
@@ -795,8 +846,13 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
             GROUPED("k_v_resid_c", k_vg_resid, ctx->amg_gsmooth[l], 0, l)
         } else {
-            ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
-            ALAUNCH(l ? "k_v_resid_c" : "k_v_resid_f", k_v_resid<T>, ctx->amg_smooth[l], l);
+            if (l == 0) {
+                ALAUNCH("k_v_jac_f", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid<T, true>), ctx->amg_smooth[l], l);
+            } else {
+                ALAUNCH("k_v_jac_c", (k_v_jac<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_c", (k_v_resid<T, false>), ctx->amg_smooth[l], l);
+            }
         }
         G = ctx->amg_grouped[l + 1];
         if (G > 1) { GROUPED(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict, ctx->amg_gcells[l + 1], 0, l + 1) }
@@ -809,8 +865,13 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             GROUPED("k_v_prolong_c", k_vg_prolong, ctx->amg_gsmooth[l], 0, l)
             GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
         } else {
-            ALAUNCH(l ? "k_v_prolong_c" : "k_v_prolong_f", k_v_prolong<T>, ctx->amg_smooth[l], l);
-            ALAUNCH(l ? "k_v_jac_c" : "k_v_jac_f", k_v_jac<T>, ctx->amg_smooth[l], l);
+            if (l == 0) {
+                ALAUNCH("k_v_prolong_f", (k_v_prolong<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
+            } else {
+                ALAUNCH("k_v_prolong_c", (k_v_prolong<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_c", (k_v_jac<T, false>), ctx->amg_smooth[l], l);
+            }
         }
     }
 }

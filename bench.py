@@ -376,6 +376,29 @@ def oracle_case(zone, setup):
     return o, oracle_lib
 
 
+def host_cpu():
+    """The host's CPU model and logical core count, for the CPU baselines."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for line in fh:
+                    if line.lower().startswith("model name"):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"cpu": model or "unknown", "nproc": os.cpu_count()}
+
+
 def cpu_baseline(zone, setup, budget_s=20.0):
     """The reference algorithm (CPU oracle, ref mode: Gauss-Seidel / 4-block
     SSOR inner solves, nsubd = 4), single thread like the serial reference,
@@ -389,7 +412,7 @@ def cpu_baseline(zone, setup, budget_s=20.0):
     o.run(k, 3)
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": o.ne * k / dt, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": o.ne * k / dt, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
             "sample": "%d outer iteration(s) of the full %d-cell mesh after 1 warm-up iteration, %.1f s" % (k, o.ne, dt)}
 
 
@@ -417,7 +440,7 @@ def run_reference(a, dist):
            "data": "synthetic (seeded jittered unit-cube hex mesh)",
            "config": {"workload": "lid-driven cavity %d^3 %s, jitter %.2f, Re=100, SIMPLE alpha 0.7/0.3, FP64"
                                   % (a.n, "tet-split" if a.tet else "hex", a.jitter), "cells": o.ne},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                             "sample": "%d outer iterations of the full mesh (reference algorithm, serial), %.1f s"
                                       % (steps, dt)},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -741,7 +764,7 @@ def cpu_energy_baseline(a, budget_s=15.0):
         k += 1
     ne = o.ne
     o.close()
-    return {"value": ne * k / dt, "unit": "cells x solves/s", "cores": 1, "kind": "port",
+    return {"value": ne * k / dt, "unit": "cells x solves/s", "cores": 1, "kind": "port", "host": host_cpu(),
             "sample": "%d solve_energy calls on a %d^3 mesh (%d cells) after 3 outer passes, %.1f s of solves"
                       % (k, n, ne, dt)}
 

@@ -117,6 +117,77 @@ def test_mass_conservation_improves():
     assert np.linalg.norm(o.get("b")) < 0.2 * b0
 
 
+@pytest.mark.parametrize("kind,jit", [(False, 0.2), (True, 0.1), ("prism", 0.2), ("mixed", 0.2)])
+def test_rhie_chow_term_vanishes_for_linear_pressure(kind, jit):
+    """calc_mip's pressure-smoothing term -rho A d_ip/(dr.n) (p_nb - p_P -
+    gp_ip.dr) (mod_uvwp.f90:438-490) is zero when p is linear and gp its exact
+    gradient, on any mesh: the fluxes with and without the term agree to
+    rounding, and differ at O(1) for a non-linear p."""
+    z = cfdl.Zone(5, kind, jit, seed=7)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1))       # dt = inf: no transient term
+    o.run(3)
+    o.update_boundaries()
+    o.calc_coef_uvw()                                # d = vol / ap, the term's weight
+    assert np.abs(o.get("d")).max() > 0
+    xc, yc, zc = o.get("xc"), o.get("yc"), o.get("zc")
+    p = 0.4 + 2.0 * xc - 1.0 * yc + 3.0 * zc
+    o.set("p", p)
+    o.set("gp", np.tile([2.0, -1.0, 3.0], len(xc)))
+    o.calc_mip(False)
+    plain = o.get("mip").copy()
+    o.calc_mip(True)
+    assert np.abs(o.get("mip") - plain).max() < 1e-13 * np.abs(plain).max()
+    o.set("p", p + 0.5 * xc ** 2)
+    o.calc_mip(True)
+    assert np.abs(o.get("mip") - plain).max() > 1e-2 * np.abs(plain).max()
+
+
+def test_cavity_is_mirror_symmetric_across_the_lid_direction():
+    """The lid moves in x on the top face, so on an unjittered hex mesh the
+    discrete solution is symmetric under y -> 1 - y with v -> -v; the two
+    other reflections are not symmetries of the flow."""
+    z = cfdl.Zone(6, False, 0.0, seed=1)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    o.run(15)
+    ne = o.ne
+    xyz = np.stack([o.get(c)[:ne] for c in ("xc", "yc", "zc")], axis=1)
+    where = {tuple(np.round(r, 9)): i for i, r in enumerate(xyz)}
+    u, v, w, p = (o.get(f)[:ne] for f in "uvwp")
+    scale = np.abs(u).max()
+    for axis in range(3):
+        r = xyz.copy()
+        r[:, axis] = 1.0 - r[:, axis]
+        m = np.array([where[tuple(np.round(q, 9))] for q in r])
+        sign = [1.0, 1.0, 1.0]
+        sign[axis] = -1.0
+        err = max(np.abs(f - s * f[m]).max() for f, s in zip((u, v, w), sign)) / scale
+        if axis == 1:
+            assert err < 1e-12
+            assert np.abs(p - p[m]).max() < 1e-12 * np.abs(p).max()
+        else:
+            assert err > 1e-2
+
+
+@pytest.mark.parametrize("kind", [False, True, "pyramid"])
+def test_momentum_matrix_is_an_m_matrix(kind):
+    """calc_coef_uvw (mod_uvwp.f90:161-286): upwind convection max(-mip, 0)
+    plus diffusion mu A/ds gives non-negative neighbour coefficients, and the
+    under-relaxed diagonal ap/alpha_u exceeds the row's neighbour sum."""
+    z = cfdl.Zone(5, kind, 0.2, seed=3)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1))
+    o.run(5)
+    o.update_boundaries()
+    o.calc_coef_uvw()
+    ap, anb = o.get("ap"), o.get("anb")
+    idx = o.get_int("ef2nb_idx")
+    assert anb.min() >= 0.0
+    rows = np.add.reduceat(anb, idx[:-1] - 1)
+    assert (ap - rows > 0).all()
+
+
 # ---- energy equation (src/equations/mod_energy.f90) ----------------------------
 
 def test_energy_pure_diffusion_matrix():

@@ -170,6 +170,28 @@ def test_cavity_is_mirror_symmetric_across_the_lid_direction():
             assert err > 1e-2
 
 
+@pytest.mark.parametrize("kind,jit", [(False, 0.2), (True, 0.1), ("pyramid", 0.1)])
+def test_corrected_fluxes_satisfy_continuity(kind, jit):
+    """calc_coef_p's face coefficient rho_ip dc_ip A/(dr.n) (mod_uvwp.f90:289-368)
+    is the one update_uvwp corrects mip with (:370-436): after a tight
+    pressure-correction solve, every cell's net face flux is the solve's
+    residual, ~1e-13 of the imbalance before the correction."""
+    z = cfdl.Zone(5, kind, jit, seed=7)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    o.run(4)
+    o.update_boundaries(); o.calc_coef_uvw(); o.calc_mip(True); o.calc_coef_p()
+    b0 = o.get("b").copy()
+    o.solve_pc(); o.adjust_pc(); o.update_uvwp()
+    mip = o.get("mip")
+    ef2, idx = o.get_int("ef2nb2"), o.get_int("ef2nb_idx")
+    owner = np.repeat(np.arange(o.ne), np.diff(idx))
+    net = np.zeros(o.ne)
+    np.add.at(net, owner, np.sign(ef2) * mip[np.abs(ef2) - 1])
+    assert np.linalg.norm(b0) > 1e-3 * np.abs(mip).sum() / o.ne ** 0.5
+    assert np.linalg.norm(net) < 1e-11 * np.linalg.norm(b0)
+
+
 @pytest.mark.parametrize("kind", [False, True, "pyramid"])
 def test_momentum_matrix_is_an_m_matrix(kind):
     """calc_coef_uvw (mod_uvwp.f90:161-286): upwind convection max(-mip, 0)

@@ -123,50 +123,50 @@ extern "C" int cfdl_box_zone_fill(int n, int tet, double jitter, uint64_t seed,
     };
     int vol_stop[2] = {0, 0};
     for (int pass = 0; pass < (kind == K_MIXED ? 2 : 1); pass++) {
-    for (int k = 0; k < n; k++)
-        for (int j = 0; j < n; j++)
-            for (int i = 0; i < n; i++) {
-                int c[8];
-                corners(i, j, k, c);
-                const bool py = pyra_cube(kind, i, j, k);
-                if (kind == K_MIXED && py != (pass == 1)) continue;
-                if (kind == K_HEX || (kind == K_MIXED && !py)) { put(c, 8); continue; }
-                if (kind == K_PRISM) {
-                    // bottom triangles (0,0)(1,0)(1,1) and (0,0)(1,1)(0,1), counterclockwise seen from +z
-                    const int a[6] = {c[0], c[1], c[2], c[4], c[5], c[6]}, b[6] = {c[0], c[2], c[3], c[4], c[6], c[7]};
-                    put(a, 6); put(b, 6);
-                    continue;
-                }
-                if (py) {
-                    // one pyramid per cube face: base = the face in reverse of its outward
-                    // (faces_hexa8) order, so the pyramid's own base face points outward
-                    static const int hf[6][4] = {{1, 4, 3, 2}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {1, 5, 8, 4}, {5, 6, 7, 8}};
-                    const int ap = apex[(size_t)i + (size_t)n * (j + (size_t)n * k)];
-                    for (int f = 0; f < 6; f++) {
-                        const int q[5] = {c[hf[f][0] - 1], c[hf[f][3] - 1], c[hf[f][2] - 1], c[hf[f][1] - 1], ap};
-                        put(q, 5);
+        for (int k = 0; k < n; k++)
+            for (int j = 0; j < n; j++)
+                for (int i = 0; i < n; i++) {
+                    int c[8];
+                    corners(i, j, k, c);
+                    const bool py = pyra_cube(kind, i, j, k);
+                    if (kind == K_MIXED && py != (pass == 1)) continue;
+                    if (kind == K_HEX || (kind == K_MIXED && !py)) { put(c, 8); continue; }
+                    if (kind == K_PRISM) {
+                        // bottom triangles (0,0)(1,0)(1,1) and (0,0)(1,1)(0,1), counterclockwise seen from +z
+                        const int a[6] = {c[0], c[1], c[2], c[4], c[5], c[6]}, b[6] = {c[0], c[2], c[3], c[4], c[6], c[7]};
+                        put(a, 6); put(b, 6);
+                        continue;
                     }
-                    continue;
-                }
-                // Kuhn split along (i,j,k)-(i+1,j+1,k+1): one tet per axis order.
-                static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-                for (int t = 0; t < 6; t++) {
-                    int o[3] = {0, 0, 0}, p[4][3];
-                    for (int q = 0; q < 3; q++) p[0][q] = 0;
-                    for (int s = 0; s < 3; s++) {
-                        o[perm[t][s]] = 1;
-                        for (int q = 0; q < 3; q++) p[s + 1][q] = o[q];
+                    if (py) {
+                        // one pyramid per cube face: base = the face in reverse of its outward
+                        // (faces_hexa8) order, so the pyramid's own base face points outward
+                        static const int hf[6][4] = {{1, 4, 3, 2}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {1, 5, 8, 4}, {5, 6, 7, 8}};
+                        const int ap = apex[(size_t)i + (size_t)n * (j + (size_t)n * k)];
+                        for (int f = 0; f < 6; f++) {
+                            const int q[5] = {c[hf[f][0] - 1], c[hf[f][3] - 1], c[hf[f][2] - 1], c[hf[f][1] - 1], ap};
+                            put(q, 5);
+                        }
+                        continue;
                     }
-                    // orientation from the lattice: (p1-p0)x(p2-p0).(p3-p0) > 0
-                    int a[3], b[3], cc[3];
-                    for (int q = 0; q < 3; q++) { a[q] = p[1][q] - p[0][q]; b[q] = p[2][q] - p[0][q]; cc[q] = p[3][q] - p[0][q]; }
-                    int det = (a[1] * b[2] - a[2] * b[1]) * cc[0] + (a[2] * b[0] - a[0] * b[2]) * cc[1] + (a[0] * b[1] - a[1] * b[0]) * cc[2];
-                    int vv[4];
-                    for (int s = 0; s < 4; s++) vv[s] = vid(n, i + p[s][0], j + p[s][1], k + p[s][2]);
-                    if (det < 0) { int t2 = vv[1]; vv[1] = vv[2]; vv[2] = t2; }
-                    put(vv, 4);
+                    // Kuhn split along (i,j,k)-(i+1,j+1,k+1): one tet per axis order.
+                    static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+                    for (int t = 0; t < 6; t++) {
+                        int o[3] = {0, 0, 0}, p[4][3];
+                        for (int q = 0; q < 3; q++) p[0][q] = 0;
+                        for (int s = 0; s < 3; s++) {
+                            o[perm[t][s]] = 1;
+                            for (int q = 0; q < 3; q++) p[s + 1][q] = o[q];
+                        }
+                        // orientation from the lattice: (p1-p0)x(p2-p0).(p3-p0) > 0
+                        int a[3], b[3], cc[3];
+                        for (int q = 0; q < 3; q++) { a[q] = p[1][q] - p[0][q]; b[q] = p[2][q] - p[0][q]; cc[q] = p[3][q] - p[0][q]; }
+                        int det = (a[1] * b[2] - a[2] * b[1]) * cc[0] + (a[2] * b[0] - a[0] * b[2]) * cc[1] + (a[0] * b[1] - a[1] * b[0]) * cc[2];
+                        int vv[4];
+                        for (int s = 0; s < 4; s++) vv[s] = vid(n, i + p[s][0], j + p[s][1], k + p[s][2]);
+                        if (det < 0) { int t2 = vv[1]; vv[1] = vv[2]; vv[2] = t2; }
+                        put(vv, 4);
+                    }
                 }
-            }
         vol_stop[pass] = (int)e;
     }
     const int ne = (int)e;

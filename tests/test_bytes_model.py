@@ -1,0 +1,47 @@
+"""The algorithmic-bytes model behind bench.py's roofline.achieved, pinned to
+hand counts for the kernels the benchmark reports as dominant.  CPU only."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "cfd-lite_gb300"))
+
+from bytes_model import amg_kernel_bytes, kernel_bytes  # noqa: E402
+
+
+def hex_sizes(n):
+    ne, nbf = n ** 3, 6 * n * n
+    nf = 3 * n * n * (n - 1) + nbf
+    return ne, nf, nbf
+
+
+def test_mesh_level_jacobi_sweep_is_104_bytes_per_hex_cell():
+    # t, r, w/D in and z out (4 doubles), 6 ELL coefficients (doubles) and
+    # 6 ELL indices (int32): 32 + 48 + 24 = 104 B per cell
+    ne, _, _ = hex_sizes(128)
+    levels = [(ne, 6), (ne // 8, 26), (ne // 64, 26)]
+    assert amg_kernel_bytes("k_v_jac_f", levels, 8) == 104 * ne
+    assert amg_kernel_bytes("k_v_resid_f", levels, 8) == 104 * ne
+    # the FP32 form of the mixed solve halves the values, not the indices
+    assert amg_kernel_bytes("k_v_jac_f", levels, 4) == (16 + 24 + 24) * ne
+    assert amg_kernel_bytes("k_v_jac0_f", levels, 8) == 24 * ne
+    assert 218103808 == amg_kernel_bytes("k_v_jac_f", levels, 8)   # the 128^3 bench figure
+
+
+def test_cg_and_bicgstab_spmv_counts():
+    ne, nf, nbf = hex_sizes(64)
+    levels = [(ne, 6), (ne // 8, 26)]
+    # q = A p and (p, q): p in (own), q out, diagonal, ELL values and indices
+    assert amg_kernel_bytes("k_apc_q", levels, 8) == (24 + 48 + 24) * ne
+    # momentum t = A s for three components: diagonal, ELL, and per component s in, t out, t.s partial
+    assert kernel_bytes("k_mom_t", ne, nf, nbf, 6) == (8 + 48 + 24 + 3 * 24) * ne
+    # the energy solve's single right-hand side
+    assert kernel_bytes("k_en_t", ne, nf, nbf, 6) == (8 + 48 + 24 + 24) * ne
+
+
+def test_counts_grow_linearly_with_the_mesh():
+    for name in ("k_coef_uvw_face", "k_coef_uvw_cell", "k_calc_mip", "k_grad3", "k_mom_init", "k_en_cell"):
+        a = kernel_bytes(name, *hex_sizes(32), 6)
+        b = kernel_bytes(name, *hex_sizes(64), 6)
+        assert 7.5 < b / a < 8.2, name     # interior faces 3n^2(n-1) grow a little faster than n^3
+    assert kernel_bytes("no_such_kernel", *hex_sizes(8), 6) is None

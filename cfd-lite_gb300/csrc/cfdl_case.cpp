@@ -133,7 +133,7 @@ double vec_weight(const double *r0, const double *r1, const double *r2) {
     return la + lb > 0. ? la / (la + lb) : 0.5;
 }
 
-template <class T> int upload(HostCase *hc, T **dptr, const std::vector<T> &h) {
+template <class T, class A> int upload(HostCase *hc, T **dptr, const std::vector<T, A> &h) {
     int st = case_alloc(hc, (void **)dptr, h.size() * sizeof(T));
     if (st) return st;
     return cuda_status(cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -145,8 +145,8 @@ template <class T> int zeros(HostCase *hc, T **dptr, size_t n) {
 }
 
 int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_nb, const std::vector<int> &hf_fc,
-               const std::vector<double> &hf_G, const std::vector<int> &f_own, const std::vector<int> &f_nb,
-               const std::vector<double> &fgeo, const std::vector<int> &h_own, const std::vector<int> &h_face,
+               const FillVec<double> &hf_G, const std::vector<int> &f_own, const std::vector<int> &f_nb,
+               const FillVec<double> &fgeo, const std::vector<int> &h_own, const std::vector<int> &h_face,
                const std::vector<int> &h_kind, const std::vector<double> &h_vel, const std::vector<double> &vol) {
     CaseDev &d = hc->dev;
     const int ne = hc->ne, nf = hc->nf, nbf = hc->nbf, W = hc->W, nc = ne + nbf;
@@ -202,7 +202,7 @@ void CasePrep::release_tables() {
     std::vector<int>().swap(ef2nb_idx); std::vector<int>().swap(hf_nb); std::vector<int>().swap(hf_fc);
     std::vector<int>().swap(f_own); std::vector<int>().swap(f_nb); std::vector<int>().swap(h_own);
     std::vector<int>().swap(h_face); std::vector<int>().swap(h_kind);
-    std::vector<double>().swap(hf_G); std::vector<double>().swap(fgeo); std::vector<double>().swap(h_vel);
+    FillVec<double>().swap(hf_G); FillVec<double>().swap(fgeo); std::vector<double>().swap(h_vel);
     std::vector<double>().swap(vol); std::vector<double>().swap(h_temp);
     delete amg;
     amg = nullptr;
@@ -290,8 +290,8 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
                 for (int el = m->bc_esec[2 * bc]; el <= m->bc_esec[2 * bc + 1]; el++) p->h_temp[el - ne - 1] = m->bc_temp[bc];
         }
         // ---- face geometry planes ----
-        std::vector<double> &fgeo = p->fgeo;
-        fgeo.assign((size_t)FG_N * nf, 0.0);
+        FillVec<double> &fgeo = p->fgeo;
+        fgeo.resize((size_t)FG_N * nf);       // every plane of every face is written below
         auto G = [&](int plane, int f) -> double & { return fgeo[(size_t)plane * nf + f]; };
         parallel_for(nf, [&](long fb, long fe) {
         for (int f = (int)fb; f < (int)fe; f++) {
@@ -309,7 +309,11 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
             // boundary faces too: the energy equation's wall coefficient uses it
             const double dn = dr[0]*nrm[0] + dr[1]*nrm[1] + dr[2]*nrm[2];
             G(FG_ADN, f) = area / dn;
-            if (n < ne) {
+            if (n >= ne) {
+                // boundary faces: no interpolation weight, no non-orthogonal terms
+                G(FG_WT, f) = 0.0;
+                for (int q = 0; q < 3; q++) G(FG_ADRX + q, f) = G(FG_EX + q, f) = 0.0;
+            } else {
                 G(FG_WT, f) = vec_weight(ri, rp, rn);
                 double drip[3], t, rpp[3], rnp[3], drp[3];
                 for (int q = 0; q < 3; q++) drip[q] = ri[q] - rp[q];
@@ -328,8 +332,8 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
         }
         });
         // ---- least-squares gradient stencil ----
-        std::vector<double> &hf_G = p->hf_G;
-        hf_G.assign(3 * (size_t)W * ne, 0.0);
+        FillVec<double> &hf_G = p->hf_G;
+        hf_G.resize(3 * (size_t)W * ne);      // every slot written below (0 past a cell's faces)
         parallel_for(ne, [&](long cb, long ce) {
         for (int e = (int)cb; e < (int)ce; e++) {
             double A[3][3] = {{0}}, Ai[3][3], wdr[kMaxW][3];
@@ -348,9 +352,10 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
             }
             A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
             matinv3(A, Ai);
-            for (int k = 0; k < cnt; k++)
+            for (int k = 0; k < W; k++)
                 for (int q = 0; q < 3; q++)
-                    hf_G[((size_t)q * W + k) * ne + e] = Ai[q][0]*wdr[k][0] + Ai[q][1]*wdr[k][1] + Ai[q][2]*wdr[k][2];
+                    hf_G[((size_t)q * W + k) * ne + e] =
+                        k < cnt ? Ai[q][0]*wdr[k][0] + Ai[q][1]*wdr[k][1] + Ai[q][2]*wdr[k][2] : 0.0;
         }
         });
         p->vol.assign(m->vol, m->vol + ne);

@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(kTile) k_apc_x(const CaseDev *__restrict__ cas
 // ------------------------------------------------------------------ host
 namespace {
 
-template <class T> int dupload(HostCase *hc, T **d, const std::vector<T> &h) {
+template <class T, class A> int dupload(HostCase *hc, T **d, const std::vector<T, A> &h) {
     size_t bytes = std::max<size_t>(1, h.size()) * sizeof(T);
     cudaError_t e = cudaMalloc((void **)d, bytes);
     if (e != cudaSuccess) { cudaGetLastError(); return cuda_status(e); }
@@ -655,14 +655,16 @@ template <class T> int dzeros(HostCase *hc, T **d, size_t n) {
 
 // strength of each ELL slot = |area/(dr.n)| of its face; -1 marks the slots
 // that are not interior couplings
-void amg_strength(int ne, int W, const int *nb_in, const int *fc, const double *adn, std::vector<int> &nb,
-                  std::vector<double> &strength) {
-    nb.assign(nb_in, nb_in + (size_t)W * ne);
-    strength.assign((size_t)W * ne, 0.0);
+void amg_strength(int ne, int W, const int *nb_in, const int *fc, const double *adn, FillVec<int> &nb,
+                  FillVec<double> &strength) {
+    nb.resize((size_t)W * ne);          // every slot written below (first touch in parallel)
+    strength.resize((size_t)W * ne);
     parallel_for((long)nb.size(), [&](long b, long e) {
         for (long s = b; s < e; s++) {
-            if (nb[s] < 0 || nb[s] >= ne) { nb[s] = -1; continue; }
+            const int j = nb_in[s];
+            if (j < 0 || j >= ne) { nb[s] = -1; strength[s] = 0.0; continue; }
             const int f = fc[s] >= 0 ? fc[s] : ~fc[s];
+            nb[s] = j;
             strength[s] = std::fabs(adn[f]);
         }
     });
@@ -680,8 +682,8 @@ int build_case_amg(HostCase *hc) {
     if ((st = cuda_status(cudaMemcpy(nb0.data(), d.hf_nb, nb0.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
     if ((st = cuda_status(cudaMemcpy(fc.data(), d.hf_fc, fc.size() * sizeof(int), cudaMemcpyDeviceToHost)))) return st;
     if ((st = cuda_status(cudaMemcpy(adn.data(), d.fgeo + (size_t)FG_ADN * nf, nf * sizeof(double), cudaMemcpyDeviceToHost)))) return st;
-    std::vector<int> nb;
-    std::vector<double> strength;
+    FillVec<int> nb;
+    FillVec<double> strength;
     amg_strength(ne, W, nb0.data(), fc.data(), adn.data(), nb, strength);
     AmgHierarchy *H = new AmgHierarchy;
     AmgFineView fv{ne, W, nb.data(), strength.data()};
@@ -693,8 +695,8 @@ int build_case_amg(HostCase *hc) {
 
 int prepare_case_amg(CasePrep *p) {
     if (!p || p->amg) return p ? CFDL_OK : CFDL_ERR_INVALID;
-    std::vector<int> nb;
-    std::vector<double> strength;
+    FillVec<int> nb;
+    FillVec<double> strength;
     amg_strength(p->ne, p->W, p->hf_nb.data(), p->hf_fc.data(), p->fgeo.data() + (size_t)FG_ADN * p->nf, nb, strength);
     AmgHierarchy *H = new (std::nothrow) AmgHierarchy;
     if (!H) return CFDL_ERR_OOM;

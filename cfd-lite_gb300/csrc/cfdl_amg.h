@@ -19,10 +19,10 @@ struct AmgFineView {
 // finer level; "fine" means the level just above.
 struct AmgHostLevel {
     int n_fine = 0, n = 0, W_fine = 0, W = 0;
-    std::vector<int> agg;              // [n_fine] coarse cell of each fine cell
-    std::vector<int> mem_ptr, mem;     // members of each coarse cell
-    std::vector<int> nb;               // [W][n] coarse neighbours, -1 padded
-    std::vector<int> g_ptr, g_src;     // fine slots summed into coarse slot s = k*n + c
+    FillVec<int> agg;                  // [n_fine] coarse cell of each fine cell
+    FillVec<int> mem_ptr, mem;         // members of each coarse cell
+    FillVec<int> nb;                   // [W][n] coarse neighbours, -1 padded
+    FillVec<int> g_ptr, g_src;         // fine slots summed into coarse slot s = k*n + c
 };
 
 struct AmgHierarchy {

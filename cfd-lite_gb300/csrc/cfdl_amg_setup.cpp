@@ -22,14 +22,16 @@
 namespace cfdl {
 namespace {
 
+// The large arrays below are sized without a fill (FillVec) and written in
+// full by the parallel loops that follow, which first-touch their pages.
 struct Graph {
     int n = 0, W = 0;
-    std::vector<int> nb;        // [W][n] neighbour or -1
-    std::vector<double> w;      // [W][n] strength
+    FillVec<int> nb;            // [W][n] neighbour or -1
+    FillVec<double> w;          // [W][n] strength
 };
 
 // greedy aggregation of one level
-int aggregate(const Graph &g, std::vector<int> &agg) {
+int aggregate(const Graph &g, FillVec<int> &agg) {
     const int n = g.n, W = g.W;
     agg.assign(n, -1);
     int nagg = 0;
@@ -76,26 +78,29 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
     H.levels.clear();
     Graph g;
     g.n = fine.n; g.W = fine.W;
-    g.nb.assign((size_t)g.W * g.n, -1);
-    g.w.assign((size_t)g.W * g.n, 0.0);
+    g.nb.resize((size_t)g.W * g.n);
+    g.w.resize((size_t)g.W * g.n);
     parallel_for((long)g.W * g.n, [&](long b, long e) {
         for (long s = b; s < e; s++) {
             const int j = fine.nb[s];
-            if (j >= 0 && j < g.n) { g.nb[s] = j; g.w[s] = fine.strength[s]; }
+            const bool in = j >= 0 && j < g.n;
+            g.nb[s] = in ? j : -1;
+            g.w[s] = in ? fine.strength[s] : 0.0;
         }
     });
     while (g.n > kAmgCoarsest && (int)H.levels.size() < kAmgMaxLevels) {
-        std::vector<int> agg;
-        int nc = aggregate(g, agg);
+        FillVec<int> agg_new;
+        int nc = aggregate(g, agg_new);
         if (nc >= g.n) break;                           // no coarsening possible
         AmgHostLevel L;
         L.n_fine = g.n; L.n = nc; L.W_fine = g.W;
-        L.agg = agg;
+        L.agg = std::move(agg_new);
+        const FillVec<int> &agg = L.agg;
         // members CSR (fine cells in increasing order per aggregate)
         L.mem_ptr.assign(nc + 1, 0);
         for (int i = 0; i < g.n; i++) L.mem_ptr[agg[i] + 1]++;
         for (int c = 0; c < nc; c++) L.mem_ptr[c + 1] += L.mem_ptr[c];
-        L.mem.assign(g.n, 0);
+        L.mem.resize(g.n);                              // each fine cell filed once below
         {
             std::vector<int> fill(L.mem_ptr.begin(), L.mem_ptr.end() - 1);
             for (int i = 0; i < g.n; i++) L.mem[fill[agg[i]]++] = i;
@@ -108,8 +113,8 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
         // slots once the coarse slot offsets are known.
         std::vector<long> cap(nc + 1, 0);
         for (int c = 0; c < nc; c++) cap[c + 1] = cap[c] + (long)(L.mem_ptr[c + 1] - L.mem_ptr[c]) * g.W;
-        std::vector<int> nbr(cap[nc]), cntq(cap[nc]), ncnb(nc);
-        std::vector<double> wq(cap[nc]);
+        FillVec<int> nbr(cap[nc]), cntq(cap[nc]), ncnb(nc);   // read only where pass 1 wrote
+        FillVec<double> wq(cap[nc]);
         parallel_for(nc, [&](long cb, long ce) {
             for (int c = (int)cb; c < (int)ce; c++) {
                 int *nb_c = &nbr[cap[c]], *cn_c = &cntq[cap[c]];
@@ -135,8 +140,9 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
         int Wc = 1;
         for (int c = 0; c < nc; c++) Wc = std::max(Wc, ncnb[c]);
         L.W = Wc;
-        L.nb.assign((size_t)Wc * nc, -1);
-        L.g_ptr.assign((size_t)Wc * nc + 1, 0);
+        L.nb.resize((size_t)Wc * nc);                   // every slot written below
+        L.g_ptr.resize((size_t)Wc * nc + 1);
+        L.g_ptr[0] = 0;
         // slot-major offsets: each slot plane k scanned on its own, then the
         // planes' totals carried over in order
         std::vector<long> plane_total(Wc + 1, 0);
@@ -148,7 +154,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
                     const bool has = k < ncnb[c];
                     run += has ? cntq[cap[c] + k] : 0;
                     L.g_ptr[sl + 1] = (int)run;
-                    if (has) L.nb[sl] = nbr[cap[c] + k];
+                    L.nb[sl] = has ? nbr[cap[c] + k] : -1;
                 }
                 plane_total[k + 1] = run;
             }
@@ -158,7 +164,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
             for (int k = (int)kb; k < (int)ke; k++)
                 for (int c = 0; c < nc; c++) L.g_ptr[(size_t)k * nc + c + 1] += (int)plane_total[k];
         }, 1);
-        L.g_src.assign(L.g_ptr.back(), 0);
+        L.g_src.resize(L.g_ptr.back());                 // each fine slot filed once below
         parallel_for(nc, [&](long cb, long ce) {
             std::vector<int> fill;
             for (int c = (int)cb; c < (int)ce; c++) {
@@ -181,11 +187,15 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H) {
         // next graph
         Graph ng;
         ng.n = nc; ng.W = Wc;
-        ng.nb = L.nb;
-        ng.w.assign((size_t)Wc * nc, 0.0);
+        ng.nb.resize((size_t)Wc * nc);
+        ng.w.resize((size_t)Wc * nc);
         parallel_for(nc, [&](long cb, long ce) {
             for (int c = (int)cb; c < (int)ce; c++)
-                for (int k = 0; k < ncnb[c]; k++) ng.w[(size_t)k * nc + c] = wq[cap[c] + k];
+                for (int k = 0; k < Wc; k++) {
+                    const size_t sl = (size_t)k * nc + c;
+                    ng.nb[sl] = L.nb[sl];
+                    ng.w[sl] = k < ncnb[c] ? wq[cap[c] + k] : 0.0;
+                }
         });
         H.levels.push_back(std::move(L));
         g = std::move(ng);

@@ -132,6 +132,7 @@ def lib():
     L.cfdl_upload_fields.argtypes = [vp, C.POINTER(Fields)]
     L.cfdl_download_fields.argtypes = [vp, C.POINTER(Fields)]
     L.cfdl_ctx_destroy.argtypes = [vp]
+    L.cfdl_mesh_check.argtypes = [C.POINTER(Mesh)]
     for n in ("cfdl_update_boundaries", "cfdl_update_time", "cfdl_calc_coef_uvw", "cfdl_calc_coef_p",
               "cfdl_adjust_pc", "cfdl_update_uvwp"):
         getattr(L, n).argtypes = [vp]
@@ -276,6 +277,10 @@ class Setup:
         m = Mesh()
         _check(lib().cfdl_setup_mesh(self._h, float(u_lid), C.byref(m)), "mesh")
         return m
+
+    def check(self):
+        """cfdl_mesh_check of this set-up's mesh: 0 when valid (no GPU needed)."""
+        return lib().cfdl_mesh_check(C.byref(self.mesh()))
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:

@@ -189,6 +189,11 @@ const char *cfdl_status_string(int s) {
     }
 }
 
+int cfdl_mesh_check(const cfdl_mesh *mesh) {
+    cfdl::CasePrep p;
+    return cfdl::prepare_case(mesh, &p);
+}
+
 int cfdl_ctx_create(const cfdl_mesh *mesh, const cfdl_config *cfg, cfdl_ctx **out) {
     if (!out) return CFDL_ERR_INVALID;
     *out = nullptr;

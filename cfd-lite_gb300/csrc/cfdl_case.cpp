@@ -16,6 +16,7 @@
 #include "cfdl_amg.h"
 #include "cfdl_par.h"
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cfloat>
 #include <cstring>
@@ -144,8 +145,8 @@ template <class T> int zeros(HostCase *hc, T **dptr, size_t n) {
     return cuda_status(cudaMemset(*dptr, 0, n * sizeof(T)));
 }
 
-int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_nb, const std::vector<int> &hf_fc,
-               const FillVec<double> &hf_G, const std::vector<int> &f_own, const std::vector<int> &f_nb,
+int upload_all(HostCase *hc, const cfdl_config *cfg, const FillVec<int> &hf_nb, const FillVec<int> &hf_fc,
+               const FillVec<double> &hf_G, const FillVec<int> &f_own, const FillVec<int> &f_nb,
                const FillVec<double> &fgeo, const std::vector<int> &h_own, const std::vector<int> &h_face,
                const std::vector<int> &h_kind, const std::vector<double> &h_vel, const std::vector<double> &vol) {
     CaseDev &d = hc->dev;
@@ -199,8 +200,8 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const std::vector<int> &hf_
 CasePrep::~CasePrep() { delete amg; }
 
 void CasePrep::release_tables() {
-    std::vector<int>().swap(ef2nb_idx); std::vector<int>().swap(hf_nb); std::vector<int>().swap(hf_fc);
-    std::vector<int>().swap(f_own); std::vector<int>().swap(f_nb); std::vector<int>().swap(h_own);
+    std::vector<int>().swap(ef2nb_idx); FillVec<int>().swap(hf_nb); FillVec<int>().swap(hf_fc);
+    FillVec<int>().swap(f_own); FillVec<int>().swap(f_nb); std::vector<int>().swap(h_own);
     std::vector<int>().swap(h_face); std::vector<int>().swap(h_kind);
     FillVec<double>().swap(hf_G); FillVec<double>().swap(fgeo); std::vector<double>().swap(h_vel);
     std::vector<double>().swap(vol); std::vector<double>().swap(h_temp);
@@ -232,26 +233,52 @@ int prepare_case(const cfdl_mesh *m, CasePrep *p) {
         }
         p->W = W;
         // ---- ELL half-faces + validation of every index ----
-        std::vector<int> &hf_nb = p->hf_nb, &hf_fc = p->hf_fc, &f_own = p->f_own, &f_nb = p->f_nb;
-        hf_nb.assign((size_t)W * ne, -1); hf_fc.assign((size_t)W * ne, 0);
-        f_own.assign(nf, -1); f_nb.assign(nf, -1);
-        for (int e = 0; e < ne; e++) {
-            for (int idx = m->ef2nb_idx[e]; idx < m->ef2nb_idx[e + 1]; idx++) {
-                int k = idx - m->ef2nb_idx[e];
-                int enb, lfnb;
-                get_idx(m->ef2nb1[idx - 1], enb, lfnb);
-                int fg = m->ef2nb2[idx - 1];
-                int fa = fg >= 0 ? fg : -fg;
-                if (enb < 1 || enb > nc || fa < 1 || fa > nf) return CFDL_ERR_INVALID;
-                if ((lfnb == 0) != (enb > ne)) return CFDL_ERR_INVALID;
-                hf_nb[(size_t)k * ne + e] = enb - 1;
-                hf_fc[(size_t)k * ne + e] = fg > 0 ? fa - 1 : ~(fa - 1);
-                if (fg > 0) {
-                    if (f_own[fa - 1] != -1) return CFDL_ERR_INVALID;
-                    f_own[fa - 1] = e; f_nb[fa - 1] = enb - 1;
+        // In parallel over cells: each cell writes its own slots, and the
+        // owner side of each face records (owner, neighbour).  Two owner
+        // claims on one face (an invalid mesh) are found by the second pass:
+        // every owner-side half-face must be the one recorded.
+        FillVec<int> &hf_nb = p->hf_nb, &hf_fc = p->hf_fc, &f_own = p->f_own, &f_nb = p->f_nb;
+        hf_nb.resize((size_t)W * ne); hf_fc.resize((size_t)W * ne);
+        f_own.resize(nf); f_nb.resize(nf);
+        parallel_for(nf, [&](long fb, long fe) {
+            for (long f = fb; f < fe; f++) { f_own[f] = -1; f_nb[f] = -1; }
+        });
+        std::atomic<int> bad{0};
+        parallel_for(ne, [&](long cb, long ce) {
+            for (int e = (int)cb; e < (int)ce; e++) {
+                const int b0 = m->ef2nb_idx[e], cnt = m->ef2nb_idx[e + 1] - b0;
+                for (int k = 0; k < W; k++) {
+                    const size_t sl = (size_t)k * ne + e;
+                    hf_nb[sl] = -1; hf_fc[sl] = 0;          // padding past the cell's faces
+                    if (k >= cnt) continue;
+                    int enb, lfnb;
+                    get_idx(m->ef2nb1[b0 + k - 1], enb, lfnb);
+                    const int fg = m->ef2nb2[b0 + k - 1];
+                    const int fa = fg >= 0 ? fg : -fg;
+                    if (enb < 1 || enb > nc || fa < 1 || fa > nf || (lfnb == 0) != (enb > ne)) {
+                        bad.store(1, std::memory_order_relaxed);
+                        continue;
+                    }
+                    hf_nb[sl] = enb - 1;
+                    hf_fc[sl] = fg > 0 ? fa - 1 : ~(fa - 1);
+                    if (fg > 0) {
+                        __atomic_store_n(&f_own[fa - 1], e, __ATOMIC_RELAXED);
+                        __atomic_store_n(&f_nb[fa - 1], enb - 1, __ATOMIC_RELAXED);
+                    }
                 }
             }
-        }
+        });
+        if (bad.load()) return CFDL_ERR_INVALID;
+        parallel_for(ne, [&](long cb, long ce) {
+            for (int e = (int)cb; e < (int)ce; e++)
+                for (int idx = m->ef2nb_idx[e]; idx < m->ef2nb_idx[e + 1]; idx++) {
+                    const int fg = m->ef2nb2[idx - 1];
+                    const int k = idx - m->ef2nb_idx[e];
+                    if (fg > 0 && (f_own[fg - 1] != e || f_nb[fg - 1] != hf_nb[(size_t)k * ne + e]))
+                        bad.store(1, std::memory_order_relaxed);
+                }
+        });
+        if (bad.load()) return CFDL_ERR_INVALID;
         for (int f = 0; f < nf; f++) {
             if (f_own[f] < 0) return CFDL_ERR_INVALID;
             int e, lf;

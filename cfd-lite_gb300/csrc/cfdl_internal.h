@@ -282,8 +282,9 @@ template <class T> using FillVec = std::vector<T, NoInitAlloc<T>>;
 
 struct CasePrep {
     int ne = 0, nf = 0, nbf = 0, W = 0, H = 0;
-    std::vector<int> ef2nb_idx, hf_nb, hf_fc, f_own, f_nb, h_own, h_face, h_kind;
-    FillVec<double> hf_G, fgeo;      // every element written by prepare_case's parallel loops
+    std::vector<int> ef2nb_idx, h_own, h_face, h_kind;
+    FillVec<int> hf_nb, hf_fc, f_own, f_nb;   // every element written by prepare_case's parallel loops
+    FillVec<double> hf_G, fgeo;
     std::vector<double> h_vel, vol;
     std::vector<double> h_temp;      // energy wall temperatures (empty when the mesh has none)
     AmgHierarchy *amg = nullptr;     // optional, built on the host by prepare_case_amg

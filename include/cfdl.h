@@ -179,6 +179,12 @@ void cfdl_config_default(cfdl_config *cfg);
  * upload the mesh, zero the fields, set rho/mu, bind BCs, mip = calc_mip(.false.),
  * mip0 = mip. */
 int cfdl_ctx_create(const cfdl_mesh *mesh, const cfdl_config *cfg, cfdl_ctx **out);
+/* The host-side checks cfdl_ctx_create makes of a mesh before it touches the
+ * device (sizes, CSR offsets, every neighbour and face index, one owner per
+ * face agreeing with s2g, halos against bs, boundary-condition ranges and
+ * kinds): CFDL_OK, CFDL_ERR_INVALID or CFDL_ERR_OOM.  Needs no GPU.  The
+ * reference trusts its mesh reader (cell_input.f90) and checks nothing. */
+int cfdl_mesh_check(const cfdl_mesh *mesh);
 int cfdl_set_config(cfdl_ctx *ctx, const cfdl_config *cfg);
 int cfdl_upload_fields(cfdl_ctx *ctx, const cfdl_fields *f);
 int cfdl_download_fields(cfdl_ctx *ctx, cfdl_fields *f);

@@ -208,3 +208,58 @@ def test_case_bytes_estimate_and_server_config():
     assert c.hbm_budget == 150e9 and c.max_cases > 0 and c.chunk > 0 and c.precision in (0, 1)
     with pytest.raises(KeyError):
         cfdl.server_config(no_such_field=1)
+
+
+# ---- cfdl_mesh_check: the host-side validation of cfdl_ctx_create -----------
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "prism", "pyramid", "mixed"])
+def test_mesh_check_accepts_every_kind(kind):
+    s = cfdl.Setup(cfdl.Zone(4, kind if kind != "hex" else False, 0.2, seed=5))
+    assert s.check() == 0
+
+
+def _corrupted(s, **arrays):
+    """s's mesh with some arrays replaced (the replacements kept alive on the struct)."""
+    import ctypes as C
+    m = s.mesh()
+    keep = []
+    for name, arr in arrays.items():
+        arr = np.ascontiguousarray(arr)
+        keep.append(arr)
+        setattr(m, name, arr.ctypes.data_as(C.c_void_p))
+    return m, keep
+
+
+def test_mesh_check_refuses_corrupted_meshes():
+    import ctypes as C
+    s = cfdl.Setup(cfdl.Zone(4, True, 0.1, seed=5))
+    L = cfdl.lib()
+    ef1, ef2, idx = s.get_int("ef2nb1"), s.get_int("ef2nb2"), s.get_int("ef2nb_idx")
+    s2g = s.get_int("s2g")
+    ne, nbf = s.ne, s.nbf
+    own0 = next(h for h in range(idx[0] - 1, idx[1] - 1) if ef2[h] > 0)
+    other = next(h for h in range(idx[1] - 1, len(ef2)) if ef2[h] > 0)
+    interior = next(h for h in range(len(ef1)) if 0 < (ef1[h] >> 5) <= ne and (ef1[h] & 31))
+
+    def refused(**arrays):
+        m, keep = _corrupted(s, **arrays)
+        return L.cfdl_mesh_check(C.byref(m)) == 1
+
+    a = ef2.copy(); a[own0] = ef2[other]                     # two owners of one face
+    assert refused(ef2nb2=a)
+    a = ef1.copy(); a[5] = ((ne + nbf + 3) << 5) | 1         # neighbour past the halos
+    assert refused(ef2nb1=a)
+    a = ef1.copy(); a[interior] = (ef1[interior] >> 5) << 5  # interior neighbour marked as boundary
+    assert refused(ef2nb1=a)
+    a = idx.copy(); a[0] = 2                                 # CSR offsets not 1-based
+    assert refused(ef2nb_idx=a)
+    a = s2g.copy(); a[0] = ((((s2g[0] >> 5) % ne) + 1) << 5) | (s2g[0] & 31)   # s2g names another owner
+    assert refused(s2g=a)
+    m = s.mesh()
+    kinds = np.array([7] * m.nbc, np.int32)                  # no such boundary kind
+    assert refused(bc_kind=kinds)
+    esec = np.array(C.cast(m.bc_esec, C.POINTER(C.c_int))[:2 * m.nbc], np.int32)
+    esec[0] = 1                                              # a boundary range over interior cells
+    assert refused(bc_esec=esec)
+    assert s.check() == 0                                    # the originals are untouched
+    assert L.cfdl_mesh_check(None) == 1

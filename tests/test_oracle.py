@@ -278,3 +278,19 @@ def test_energy_ref_and_tight_reach_the_same_steady_state():
     a, b = runs[0].get("t")[:runs[0].ne], runs[1].get("t")[:runs[1].ne]
     assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
     assert b.min() > 273.0 - 1e-6 and b.max() < 373.0 and b.max() > 280.0
+
+
+@pytest.mark.parametrize("kind,jit", [(False, 0.0), (False, 0.2), (True, 0.0)])
+def test_energy_discrete_maximum_principle(kind, jit):
+    """Upwind convection plus diffusion gives calc_coef_energy an M-matrix
+    (mod_energy.f90:82-169), so the temperature stays between the wall
+    temperatures (273 K walls, 373 K lid) at every outer pass."""
+    z = cfdl.Zone(6, kind, jit, seed=3)
+    o = oracle_lib.Oracle(z, n_subdomains=4)
+    o.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    o.energy_init(t_init=300.0)
+    for _ in range(4):
+        o.run(10)
+        t = o.get("t")[:o.ne]
+        assert t.min() >= 273.0 - 1e-9 and t.max() <= 373.0 + 1e-9
+    assert t.max() > 300.0 and t.min() < 300.0      # heated by the lid, cooled by the walls

@@ -100,9 +100,20 @@ cfdl_config request_config(const cfdl_server_config &s, const cfdl_request &r) {
     return c;
 }
 
+// The host threads this preparation's parallel loops may use: the cores
+// shared by the requests being prepared now (a lone request gets them all).
+// Re-read before each parallel phase, so a request that started during a
+// burst takes the cores back once the others are done; the loops give the
+// same result on any number of threads.
+void share_cores(cfdl_server *S) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::lock_guard<std::mutex> lk(S->mu);
+    host_threads() = std::max(1, hw / std::max(1, S->preparing));
+}
+
 // Host preparation of one request: zone, mesh set-up, device-layout tables,
 // multigrid hierarchy.
-int prepare(const cfdl_server_config &s, Request &q) {
+int prepare(cfdl_server *S, const cfdl_server_config &s, Request &q) {
     const cfdl_request &r = q.r;
     int nvx, nelem, nsec, m;
     int st = cfdl_box_zone_sizes(r.n, r.tet, &nvx, &nelem, &nsec, &m);
@@ -121,9 +132,11 @@ int prepare(const cfdl_server_config &s, Request &q) {
             return st;
         cfdl_mesh mesh;
         st = cfdl_setup_mesh(su, 1.0, &mesh);
+        share_cores(S);
         if (!st) st = prepare_case(&mesh, &q.prep);
         cfdl_setup_destroy(su);
         if (st) return st;
+        share_cores(S);
         if (s.precond == 1 && (st = prepare_case_amg(&q.prep))) return st;
     } catch (const std::bad_alloc &) {
         return CFDL_ERR_OOM;
@@ -133,7 +146,6 @@ int prepare(const cfdl_server_config &s, Request &q) {
 }
 
 void prep_loop(cfdl_server *S) {
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
     if (S->cfg.device_setup) cudaSetDevice(S->cfg.device);   // the set-up kernels' device
     for (;;) {
         std::unique_ptr<Request> q;
@@ -144,11 +156,9 @@ void prep_loop(cfdl_server *S) {
             q = std::move(S->pending.front());
             S->pending.pop_front();
             S->preparing++;
-            // the requests being prepared share the host cores for their
-            // parallel loops: a lone request gets them all
-            host_threads() = std::max(1, hw / S->preparing);
         }
-        q->status = prepare(S->cfg, *q);
+        share_cores(S);
+        q->status = prepare(S, S->cfg, *q);
         std::lock_guard<std::mutex> lk(S->mu);
         S->preparing--;
         q->t_ready = S->now();

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -87,7 +88,8 @@ int match_faces_host(cfdl_setup &S) {
     const int ng = S.ne, m = S.m, H = S.ef2nb_idx[ng] - 1;
     // one key per element face: volume element e's faces at its CSR slots,
     // each 2D element's single face after them (disjoint writes, any order)
-    std::vector<FaceKey> keys((size_t)H + (S.nelem - ng));
+    const size_t nk = (size_t)H + (S.nelem - ng);
+    std::unique_ptr<FaceKey[]> keys(new FaceKey[nk]);   // every key written below
     std::atomic<int> bad{0};
     cfdl::parallel_for(S.nelem, [&](long b, long e_end) {
         for (long e0 = b; e0 < e_end; e0++) {
@@ -109,25 +111,57 @@ int match_faces_host(cfdl_setup &S) {
         }
     });
     if (bad) return CFDL_ERR_MESH;
-    cfdl::parallel_sort(keys, [](const FaceKey &a, const FaceKey &b) { return a < b; });
-    struct Pair { int minv, e1, f1, e2, f2; };
-    std::vector<Pair> pairs;
-    pairs.reserve(S.nf);
-    for (size_t i = 0; i < keys.size();) {
-        size_t j = i + 1;
-        while (j < keys.size() && std::equal(keys[j].v, keys[j].v + 4, keys[i].v)) j++;
-        if (j - i != 2) return CFDL_ERR_MESH;  // non-conforming or unmatched face
-        const FaceKey &a = keys[i], &b = keys[i + 1];   // a.e < b.e
-        if (a.e > ng) return CFDL_ERR_MESH;            // two 2D elements
-        pairs.push_back({a.minv, a.e, a.f, b.e, b.f});
-        i = j;
-    }
-    if ((int)pairs.size() != S.nf) return CFDL_ERR_MESH;
-    cfdl::parallel_sort(pairs, [](const Pair &p, const Pair &q) {
-        if (p.minv != q.minv) return p.minv < q.minv;
-        if (p.e1 != q.e1) return p.e1 < q.e1;
-        return p.f1 < q.f1;
+    // The two keys of a face share its smallest vertex.  The keys are
+    // bucketed by it (a counting sort), and each bucket is sorted and paired
+    // on its own: pairs of (lower, higher) element, each bucket's pairs in
+    // (element, local face) order.  Buckets in vertex order then give the
+    // faces in (smallest vertex, element, local face) order, the numbering of
+    // find_element_nb, with no global sort.
+    const int nv = S.nvx;
+    if (nk % 2 != 0 || (long long)(nk / 2) != S.nf) return CFDL_ERR_MESH;   // some face unmatched
+    std::vector<int> start((size_t)nv + 2, 0);     // bucket v: keys order[start[v] .. start[v+1])
+    cfdl::parallel_for((long)nk, [&](long b, long e_end) {
+        for (long i = b; i < e_end; i++) {
+            const int v = keys[i].minv;
+            if (v < 1 || v > nv) { bad = 1; continue; }
+            __atomic_fetch_add(&start[v + 1], 1, __ATOMIC_RELAXED);
+        }
     });
+    if (bad) return CFDL_ERR_MESH;
+    for (int v = 0; v <= nv; v++) start[v + 1] += start[v];
+    std::vector<int> order(nk);
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        cfdl::parallel_for((long)nk, [&](long b, long e_end) {
+            for (long i = b; i < e_end; i++) order[__atomic_fetch_add(&fill[keys[i].minv], 1, __ATOMIC_RELAXED)] = (int)i;
+        });
+    }
+    struct Pair { int minv, e1, f1, e2, f2; };
+    std::unique_ptr<Pair[]> pairs(new Pair[nk / 2]);   // every pair written below
+    cfdl::parallel_for((long)nv + 1, [&](long vb, long ve) {
+        for (long v = vb; v < ve && !bad; v++) {
+            const int a = start[v], cnt = start[v + 1] - a;
+            if (cnt == 0) continue;
+            if (cnt % 2 != 0 || a % 2 != 0) { bad = 1; return; }
+            int *o = &order[a];
+            std::sort(o, o + cnt, [&](int p, int q) { return keys[p] < keys[q]; });
+            Pair *out = &pairs[a / 2];
+            for (int i = 0; i < cnt; i += 2) {
+                const FaceKey &k1 = keys[o[i]], &k2 = keys[o[i + 1]];   // k1.e < k2.e
+                // exactly two keys per face: non-conforming or unmatched otherwise
+                if (!std::equal(k1.v, k1.v + 4, k2.v) ||
+                    (i + 2 < cnt && std::equal(k2.v, k2.v + 4, keys[o[i + 2]].v)) || k1.e > ng) {   // k1.e > ng: two 2D elements
+                    bad = 1;
+                    return;
+                }
+                out[i / 2] = {k1.minv, k1.e, k1.f, k2.e, k2.f};
+            }
+            std::sort(out, out + cnt / 2, [](const Pair &p, const Pair &q) {
+                return p.e1 != q.e1 ? p.e1 < q.e1 : p.f1 < q.f1;
+            });
+        }
+    }, 4096);
+    if (bad) return CFDL_ERR_MESH;
     S.ef2nb1.assign(H, 0); S.ef2nb2.assign(H, 0); S.s2g.assign(S.nf, 0); S.bs.assign(S.nbf, 0);
     cfdl::parallel_for(S.nf, [&](long b, long e_end) {
     for (int fg = (int)b + 1; fg <= (int)e_end; fg++) {

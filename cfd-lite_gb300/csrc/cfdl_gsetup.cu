@@ -279,7 +279,7 @@ template <class T> int upload(DevBufs &B, T **d, const std::vector<T> &h) {
     return cuda_st(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
 }
 
-template <class T> int download(std::vector<T> &h, const T *d, size_t n) {
+template <class T, class A> int download(std::vector<T, A> &h, const T *d, size_t n) {
     h.resize(n);
     return cuda_st(cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost));
 }

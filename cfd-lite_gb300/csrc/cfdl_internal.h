@@ -23,11 +23,8 @@
 #pragma once
 #include "cfdl.h"
 #include <cuda_runtime.h>
+#include "cfdl_par.h"
 #include <cstdint>
-#include <memory>
-#include <new>
-#include <type_traits>
-#include <utility>
 #include <vector>
 
 namespace cfdl {
@@ -263,23 +260,6 @@ int rebuild_worklists(cfdl_ctx *ctx);
 int upload_case_table(cfdl_ctx *ctx);
 int create_case(cfdl_ctx *ctx, const cfdl_mesh *mesh, const cfdl_config *cfg, HostCase **out);
 // create_case in two halves: host tables (any thread), then device upload
-// An allocator that leaves elements default-initialised (no zero-fill) when a
-// vector is sized: a large table is then first touched, and its pages
-// faulted in, by the parallel loop that fills every element, instead of by a
-// serial fill that the loop overwrites.
-template <class T> struct NoInitAlloc : std::allocator<T> {
-    template <class U> struct rebind { using other = NoInitAlloc<U>; };
-    NoInitAlloc() = default;
-    template <class U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
-    template <class U> void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) {
-        ::new (static_cast<void *>(p)) U;
-    }
-    template <class U, class... A> void construct(U *p, A &&...a) {
-        ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
-    }
-};
-template <class T> using FillVec = std::vector<T, NoInitAlloc<T>>;
-
 struct CasePrep {
     int ne = 0, nf = 0, nbf = 0, W = 0, H = 0;
     std::vector<int> ef2nb_idx, h_own, h_face, h_kind;

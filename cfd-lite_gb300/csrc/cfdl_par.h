@@ -7,10 +7,31 @@
 // serving loop lowers on its preparation threads so that they share the cores.
 #pragma once
 #include <algorithm>
+#include <memory>
+#include <new>
 #include <thread>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace cfdl {
+
+// An allocator that leaves elements default-initialised (no zero-fill) when a
+// vector is sized: a large table is then first touched, and its pages
+// faulted in, by the parallel loop that fills every element, instead of by a
+// serial fill that the loop overwrites.
+template <class T> struct NoInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = NoInitAlloc<U>; };
+    NoInitAlloc() = default;
+    template <class U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+    template <class U> void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <class U, class... A> void construct(U *p, A &&...a) {
+        ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+    }
+};
+template <class T> using FillVec = std::vector<T, NoInitAlloc<T>>;
 
 // threads a parallel loop on this thread may use (0: all hardware threads)
 inline int &host_threads() {

@@ -242,7 +242,7 @@ int finish_topology(cfdl_setup &S) {
 int geometry_host(cfdl_setup &S) {
     const int ng = S.ne, m = S.m;
     // calc_aip_xyzip_uns (calc_aip_xyzip.f90:7-74)
-    S.aip.assign(3 * (size_t)S.nf, 0.0); S.rip.assign(3 * (size_t)S.nf, 0.0);
+    S.aip.resize(3 * (size_t)S.nf); S.rip.resize(3 * (size_t)S.nf);   // every face written below
     cfdl::parallel_for(S.nf, [&](long b, long e_end) {
     for (int fg = (int)b + 1; fg <= (int)e_end; fg++) {
         int e, fl; get_idx(S.s2g[fg - 1], e, fl);
@@ -269,7 +269,8 @@ int geometry_host(cfdl_setup &S) {
     }
     });
     // calc_vol_cv_centers_uns (calc_vol_cv_centers.f90:4-61)
-    S.xc.assign(S.nelem, 0.0); S.yc.assign(S.nelem, 0.0); S.zc.assign(S.nelem, 0.0); S.vol.assign(ng, 0.0);
+    // every cell below, every halo through its one boundary face
+    S.xc.resize(S.nelem); S.yc.resize(S.nelem); S.zc.resize(S.nelem); S.vol.resize(ng);
     std::atomic<int> flat{0};
     cfdl::parallel_for(ng, [&](long b, long e_end) {
     for (int e = (int)b + 1; e <= (int)e_end; e++) {
@@ -425,7 +426,7 @@ extern "C" int cfdl_setup_get_int(const cfdl_setup *s, const char *name, int *ou
 
 extern "C" int cfdl_setup_get_dbl(const cfdl_setup *s, const char *name, double *out) {
     if (!s || !name || !out) return CFDL_ERR_INVALID;
-    const std::vector<double> *v = nullptr;
+    const cfdl::FillVec<double> *v = nullptr;
     std::string n(name);
     if (n == "aip") v = &s->aip;
     else if (n == "rip") v = &s->rip;

@@ -3,6 +3,7 @@
 // set-up object and its build phases.
 #pragma once
 #include "cfdl.h"
+#include "cfdl_par.h"
 #include <string>
 #include <vector>
 
@@ -64,7 +65,7 @@ struct cfdl_setup {
     std::vector<int> e2vx, esec, etype, sec2intf, intf2sec;
     std::vector<std::string> names;          // file order, as mg%sectionName
     std::vector<int> ef2nb1, ef2nb2, ef2nb_idx, s2g, bs, red;
-    std::vector<double> aip, rip, xc, yc, zc, vol;
+    cfdl::FillVec<double> aip, rip, xc, yc, zc, vol;   // written in full by the geometry phase
     // boundary-condition binding produced by cfdl_setup_mesh
     mutable std::vector<int> bc_esec, bc_kind;
     mutable std::vector<double> bc_vel, bc_temp;

@@ -22,11 +22,12 @@ LIB_PATH = os.path.join(HERE, "libcfdgpu.so")
 
 CFDL_OK = 0
 (CFDL_ERR_INVALID, CFDL_ERR_OOM, CFDL_ERR_NONFINITE, CFDL_ERR_ITER_CAP, CFDL_ERR_CUDA, CFDL_ERR_MESH,
- CFDL_ERR_NO_DEVICE, CFDL_ERR_NAME, CFDL_ERR_TOO_LARGE) = range(1, 10)
+ CFDL_ERR_NO_DEVICE, CFDL_ERR_NAME, CFDL_ERR_TOO_LARGE, CFDL_ERR_BREAKDOWN) = range(1, 11)
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "non-finite value in a solve",
           4: "inner solve reached its iteration cap", 5: "CUDA runtime error", 6: "mesh connectivity error",
           7: "no CUDA device", 8: "unknown array name",
-          9: "problem larger than the fixed scratch of the allocation-free entry point"}
+          9: "problem larger than the fixed scratch of the allocation-free entry point",
+          10: "Krylov breakdown: p.Ap <= 0 above the tolerance (matrix not positive definite)"}
 BC_WALL, BC_SYMMETRY = 1, 2
 HEXA_8, TETRA_4, QUAD_4, TRI_3 = 17, 10, 7, 5
 

@@ -592,7 +592,11 @@ __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cas
         __shared__ double s[1];
         sum_partials<1>(partials, cfirst[t.c], cnt[t.c], s);
         if (threadIdx.x == 0) {
-            if (!(s[0] > 0.0) || !isfinite(s[0])) { S->active_p = 0; if (!isfinite(s[0])) S->status_p = CFDL_ERR_NONFINITE; }
+            if (!(s[0] > 0.0) || !isfinite(s[0])) {
+                // runs only while ||r|| is above the tolerance, where p.Ap > 0 for the SPD system
+                S->active_p = 0;
+                S->status_p = isfinite(s[0]) ? CFDL_ERR_BREAKDOWN : CFDL_ERR_NONFINITE;
+            }
             else S->alpha_p = S->rz / s[0];
         }
     }

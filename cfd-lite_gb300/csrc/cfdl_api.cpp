@@ -185,6 +185,7 @@ const char *cfdl_status_string(int s) {
     case CFDL_ERR_NO_DEVICE: return "no CUDA device";
     case CFDL_ERR_NAME: return "unknown array name";
     case CFDL_ERR_TOO_LARGE: return "problem larger than the fixed scratch of the allocation-free entry point";
+    case CFDL_ERR_BREAKDOWN: return "Krylov breakdown: p.Ap <= 0 above the tolerance (matrix not positive definite)";
     default: return "unknown status";
     }
 }

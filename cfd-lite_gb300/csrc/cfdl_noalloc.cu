@@ -13,7 +13,7 @@
 // the CSR rows, deterministic tile reductions.
 #include "cfdl_internal.h"
 #include "cfdl_device.cuh"
-#include <mutex>
+#include <cstddef>
 
 namespace cfdl {
 namespace {
@@ -27,6 +27,7 @@ struct NoAllocScratch {
     double mean, rz, alpha, beta, rnorm, r0, tol;
     int counter[4];
     int active, iters, bad;
+    int fail;           // why CG stopped early: 0 it did not, 1 a non-finite value, 2 p.Ap <= 0
 };
 
 // Shared by every call on a device and kept between calls.
@@ -82,7 +83,9 @@ __global__ void __launch_bounds__(kTile) k_na_init(NoAllocScratch *S, int ne, co
             S->tol = rtol * S->r0;
             S->iters = 0;
             S->bad = 0;
-            S->active = S->r0 > S->tol && maxit > 0 && isfinite(S->r0);
+            // a zero or non-finite diagonal entry makes z = r/ap, and so (r, z), non-finite
+            S->fail = isfinite(S->r0) && isfinite(S->rz) ? 0 : 1;
+            S->active = S->r0 > S->tol && maxit > 0 && !S->fail;
         }
     }
 }
@@ -102,7 +105,10 @@ __global__ void __launch_bounds__(kTile) k_na_q(NoAllocScratch *S, int ne, int n
         __shared__ double s[1];
         sum_partials<1>(S->partials, 0, gridDim.x, s);
         if (threadIdx.x == 0) {
-            if (!(s[0] > 0.0) || !isfinite(s[0]) || S->bad) S->active = 0;
+            // only runs while ||r|| is above the tolerance, where an SPD system has p.Ap > 0
+            if (S->bad) S->active = 0;
+            else if (!isfinite(s[0])) { S->active = 0; S->fail = 1; }
+            else if (!(s[0] > 0.0)) { S->active = 0; S->fail = 2; }
             else S->alpha = S->rz / s[0];
         }
     }
@@ -128,7 +134,8 @@ __global__ void __launch_bounds__(kTile) k_na_x(NoAllocScratch *S, int ne, const
             S->iters += 1;
             S->beta = S->rz != 0.0 ? s[1] / S->rz : 0.0;
             S->rz = s[1];
-            S->active = S->rnorm > S->tol && S->iters < maxit && isfinite(S->rnorm);
+            if (!isfinite(S->rnorm) || !isfinite(S->rz)) S->fail = 1;
+            S->active = S->rnorm > S->tol && S->iters < maxit && !S->fail;
         }
     }
 }
@@ -139,25 +146,21 @@ __global__ void __launch_bounds__(kTile) k_na_p(NoAllocScratch *S, int ne) {
     if (i < ne) S->p[i] = S->z[i] + S->beta * S->p[i];
 }
 
-std::mutex g_na_mutex;
-NoAllocScratch *g_na_ptr[64] = {nullptr};
-
-// Device address of the scratch array on the current device, looked up once
-// per device with that device current (the host-side symbol is only a
-// stand-in, not a device address).
+// Device address of the scratch array on the current device.  The host-side
+// symbol is only a stand-in, not a device address, so the address is asked
+// of the runtime with the device current.  The first call on a device loads
+// the library's device code there (make it before any stream capture); later
+// calls only read the runtime's table.  Asking on every call, rather than
+// keeping the first answer, keeps the address right after a cudaDeviceReset,
+// which gives the device a new context and may place the array elsewhere.
 int na_scratch(NoAllocScratch **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_status(e);
-    if (dev < 0 || dev >= 64) return CFDL_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        void *ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_na_scratch);
-        if (e != cudaSuccess) return cuda_status(e);
-        g_na_ptr[dev] = static_cast<NoAllocScratch *>(ptr);
-    }
-    *out = g_na_ptr[dev];
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_na_scratch);
+    if (e != cudaSuccess) return cuda_status(e);
+    *out = static_cast<NoAllocScratch *>(ptr);
     return CFDL_OK;
 }
 
@@ -197,16 +200,23 @@ extern "C" int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const in
         if (!active) break;
         chunk = chunk < 64 ? chunk * 2 : 64;
     }
-    int it_dev = 0, bad = 0;
-    double rn = 0.0;
-    e = cudaMemcpyAsync(&it_dev, &S->iters, sizeof(int), cudaMemcpyDeviceToHost, s0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, &S->bad, sizeof(int), cudaMemcpyDeviceToHost, s0);
+    // iters, bad and fail are adjacent ints; rnorm and tol are read alone
+    int flags[3] = {0, 0, 0};
+    double rn = 0.0, tol = 0.0;
+    static_assert(offsetof(NoAllocScratch, bad) == offsetof(NoAllocScratch, iters) + sizeof(int) &&
+                  offsetof(NoAllocScratch, fail) == offsetof(NoAllocScratch, bad) + sizeof(int),
+                  "iters, bad, fail must be adjacent");
+    e = cudaMemcpyAsync(flags, &S->iters, sizeof(flags), cudaMemcpyDeviceToHost, s0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&rn, &S->rnorm, sizeof(double), cudaMemcpyDeviceToHost, s0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tol, &S->tol, sizeof(double), cudaMemcpyDeviceToHost, s0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) return cuda_status(e);
+    const int it_dev = flags[0], bad = flags[1], fail = flags[2];
     if (iters) *iters = it_dev;
     if (rnorm) *rnorm = rn;
     if (bad) return CFDL_ERR_INVALID;
-    if (!isfinite(rn)) return CFDL_ERR_NONFINITE;
+    if (fail == 1 || !isfinite(rn)) return CFDL_ERR_NONFINITE;
+    if (fail == 2) return CFDL_ERR_BREAKDOWN;
+    if (rn > tol) return CFDL_ERR_ITER_CAP;       // stopped at maxit above the tolerance
     return CFDL_OK;
 }

@@ -34,6 +34,8 @@ extern "C" {
 #define CFDL_ERR_MESH       6   /* connectivity could not be built           */
 #define CFDL_ERR_NO_DEVICE  7   /* no CUDA device                            */
 #define CFDL_ERR_NAME       8   /* unknown array name                        */
+#define CFDL_ERR_BREAKDOWN 10   /* CG breakdown: p.Ap <= 0 above the tolerance
+                                   (the matrix is not positive definite)     */
 
 /* CGNS element type codes (src/modules/mod_util.f90:18-39) */
 #define CFDL_TRI_3    5
@@ -278,13 +280,19 @@ int cfdl_profile_get(cfdl_ctx *ctx, int i, char *name64, int64_t *launches, doub
  * reduction partials and scalars live in one file-scope device array sized
  * for CFDL_NOALLOC_MAX_CELLS cells (about 4.2 MB), which every GPU that loads
  * the library holds until the process exits.  Larger systems are rejected
- * with CFDL_ERR_TOO_LARGE.  The first call on a device looks up that array's
- * device address with the device current; make that first call before any
- * stream capture.  Every call shares the one array (the call clears what must
- * start at zero), so calls that overlap on the GPU -- from several host
- * threads, or on one device at the same time -- race.  Work is queued on the
- * legacy default stream and the call returns after synchronising it; iters
- * and rnorm (optional) receive the CG iterations and the final ||r||2. */
+ * with CFDL_ERR_TOO_LARGE.  Each call asks the runtime for that array's
+ * device address with the device current (so a cudaDeviceReset between calls
+ * is harmless); the first call on a device also loads the library's device
+ * code there, so make it before any stream capture.  Every call shares the
+ * one array (the call clears what must start at zero), so calls that overlap
+ * on the GPU -- from several host threads, or on one device at the same time
+ * -- race.  Work is queued on the legacy default stream and the call returns
+ * after synchronising it; iters and rnorm (optional) receive the CG
+ * iterations and the final ||r||2.  Status: CFDL_OK when ||r||2 <= rtol*||r0||2;
+ * CFDL_ERR_ITER_CAP when CG stopped at maxit above it (as cfdl_solve_pc in
+ * tight mode); CFDL_ERR_BREAKDOWN when p.Ap <= 0 above it; CFDL_ERR_NONFINITE
+ * for a non-finite value (a zero diagonal entry, say); CFDL_ERR_INVALID for an
+ * index outside the arrays (that access is skipped on the device). */
 #define CFDL_ERR_TOO_LARGE      9
 #define CFDL_NOALLOC_MAX_CELLS  131072
 int cfdl_solve_pc_noalloc(int ne, int nh, const int *ef2nb1, const int *ef2nb_idx, const double *ap,

@@ -132,6 +132,8 @@ void or_solve_energy(ocase *c, or_stats *st);        /* mod_energy.f90:59-80  */
 
 /* Timing helper for the CPU baseline: monotonic seconds. */
 double or_wtime(void);
+int or_num_threads(void);
+void or_set_num_threads(int n);
 
 #ifdef __cplusplus
 }

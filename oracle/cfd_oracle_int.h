@@ -84,6 +84,18 @@ static inline void o_get_idx(int idx, int *g, int *s) {
 /* sgn, mod_util.f90:832-843 */
 static inline int o_sgn(int x) { return x >= 0 ? 1 : -1; }
 
+/* Host threads.  Loops whose iterations write only their own cell or face
+ * (the assembly, gradient, flux and correction loops, the per-subdomain
+ * sweeps of the 4-block pressure solve, the Krylov vector updates) run in
+ * parallel: each element's arithmetic is unchanged, so results do not depend
+ * on the thread count.  The reference's sequential Gauss-Seidel sweeps stay
+ * serial.  Built without OpenMP, O_PAR is empty and everything is serial. */
+#ifdef _OPENMP
+#define O_PAR _Pragma("omp parallel for schedule(static)")
+#else
+#define O_PAR
+#endif
+
 void *o_alloc(size_t n, size_t sz);
 /* shared with the energy equation (cfd_oracle_energy.c) */
 double o_vec_weight(const double *r0, const double *r1, const double *r2);

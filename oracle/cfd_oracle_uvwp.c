@@ -36,6 +36,27 @@
 #include <math.h>
 #include <float.h>
 #include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* host threads the parallel loops use (1 when built without OpenMP) */
+int or_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* threads for the parallel loops from now on (no effect without OpenMP) */
+void or_set_num_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
 
 double or_wtime(void) {
     struct timespec ts;
@@ -391,6 +412,7 @@ static void matinv3(const double A[3][3], double B[3][3]) {
 
 static void calc_grad(ocase *c, const double *phi, double *grad) {
     /* phi [1..ne+nbf], grad [1..3(ne+nbf)] */
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         double A[3][3] = {{0}}, Ai[3][3], g[3] = {0, 0, 0};
         for (int idx = c->ef2nb_idx[e]; idx <= c->ef2nb_idx[e+1] - 1; idx++) {
@@ -429,6 +451,7 @@ void or_calc_grad(ocase *c, const double *phi0, double *grad0) {
 void or_calc_coef_uvw(ocase *c) {
     const double dt = c->cfg.dt;
     double *ap = c->ap, *anb = c->anb;
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         double rp[3] = {c->xc[e], c->yc[e], c->zc[e]};
         double sumf = 0., sumss[3] = {0, 0, 0}, sumdefc[3] = {0, 0, 0};
@@ -520,6 +543,7 @@ void or_calc_coef_uvw(ocase *c) {
     /* implicit under-relaxation (extension) */
     if (c->cfg.alpha_u != 1.0) {
         const double a = c->cfg.alpha_u;
+        O_PAR
         for (int e = 1; e <= c->ne; e++) {
             double apr = ap[e] / a;
             c->bu[e] = c->bu[e] + (1.0 - a)*apr*c->u[e];
@@ -529,6 +553,7 @@ void or_calc_coef_uvw(ocase *c) {
         }
     }
     /* Rhie-Chow and SIMPLEC coefficients, mod_uvwp.f90:275-284 */
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         c->d[e] = c->vol[e]/ap[e];
         double dc = ap[e];
@@ -542,6 +567,7 @@ void or_calc_coef_uvw(ocase *c) {
  * ---------------------------------------------------------------------- */
 void or_calc_coef_p(ocase *c) {
     double *ap = c->ap, *anb = c->anb, *b = c->b;
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         double sumf = 0., rp[3] = {c->xc[e], c->yc[e], c->zc[e]};
         ap[e] = 0.;
@@ -592,6 +618,7 @@ void or_calc_coef_p(ocase *c) {
  * ---------------------------------------------------------------------- */
 void or_calc_mip(ocase *c, int lRhieChow) {
     const double dt = c->cfg.dt;
+    O_PAR
     for (int fg = 1; fg <= c->nf; fg++) {
         int e, lf, idx, enb, lfnb, i;
         o_get_idx(c->s2g[fg], &e, &lf);
@@ -629,6 +656,7 @@ void or_calc_mip(ocase *c, int lRhieChow) {
  * ---------------------------------------------------------------------- */
 static void update_uvwp(ocase *c, const double *pc) {
     const double ap_ = c->cfg.alpha_p;
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         if (ap_ == 1.0) {
             c->p[e] = c->p[e] + pc[e];
@@ -638,6 +666,7 @@ static void update_uvwp(ocase *c, const double *pc) {
             for (int k = 0; k < 3; k++) c->gp[3*e-2+k] = c->gp[3*e-2+k] + ap_*c->gpc[3*e-2+k];
         }
     }
+    O_PAR
     for (int fg = 1; fg <= c->nf; fg++) {
         int e, lf, idx, enb, lfnb, i;
         o_get_idx(c->s2g[fg], &e, &lf);
@@ -662,7 +691,9 @@ void or_update_uvwp(ocase *c) { update_uvwp(c, c->phic); }
 
 /* adjust_pc, mod_uvwp.f90:136-158 */
 static void adjust_pc(ocase *c, double *pc, double pref) {
+    O_PAR
     for (int e = 1; e <= c->ne; e++) pc[e] = pc[e] - pref;
+    O_PAR
     for (int enb = c->ne + 1; enb <= c->ne + c->nbf; enb++) {
         int e, lf;
         o_get_idx(abs(BS(c, enb)), &e, &lf);
@@ -772,6 +803,7 @@ static void solve_gs(int is_pc, double *phi, const double *ap, const double *anb
 
 /* assemble_coef, update_halos, update_phi: mod_subdomains.f90:162-229 */
 static void assemble_coef(ocase *c, const double *ap, const double *anb, const double *b, const double *phi) {
+    O_PAR
     for (int cc = 1; cc <= c->nsubd; cc++) {
         osubd *S = &c->sd[cc];
         for (int e = 1; e <= S->ne; e++) {
@@ -810,10 +842,15 @@ static void multi_subdomain_solver(ocase *c, const double *ap, const double *anb
                                    int nit, int *it_out, double *ri, double *rf, double *rmax) {
     const int nsd = c->nsubd;
     double res, res_max, res_i_tot = 0., res_f_tot = 0., res_max_tot = 0., res_target;
+    double *sres = o_alloc((size_t)nsd + 1, sizeof(double)), *sres_max = o_alloc((size_t)nsd + 1, sizeof(double));
     assemble_coef(c, ap, anb, b, phi);
+    O_PAR
     for (int cc = 1; cc <= nsd; cc++) {
         osubd *S = &c->sd[cc];
-        calc_residual(S->phic, S->ap, S->anb, S->b, S->ef2nb_idx, S->ef2nb, S->ne, &res, &res_max);
+        calc_residual(S->phic, S->ap, S->anb, S->b, S->ef2nb_idx, S->ef2nb, S->ne, &sres[cc], &sres_max[cc]);
+    }
+    for (int cc = 1; cc <= nsd; cc++) {
+        res = sres[cc]; res_max = sres_max[cc];
         res_i_tot = res_i_tot + res*res;
         res_max_tot = fmax(res_max_tot, res_max);
     }
@@ -822,6 +859,8 @@ static void multi_subdomain_solver(ocase *c, const double *ap, const double *anb
     res_f_tot = res_i_tot;
     res_target = res_i_tot / 10.;
     while (it < nit && res_f_tot > res_target) {
+        /* each block sweeps its own cells and reads only its own halo copies */
+        O_PAR
         for (int cc = 1; cc <= nsd; cc++) {
             osubd *S = &c->sd[cc];
             smoother_gs(1, S->phic, S->ap, S->anb, S->b, S->ef2nb_idx, S->ef2nb, S->ne, 2);
@@ -831,9 +870,13 @@ static void multi_subdomain_solver(ocase *c, const double *ap, const double *anb
             for (int j = i + 1; j <= nsd; j++)
                 update_halos(&c->intf[(j-1)*nsd + i-1], &c->sd[i], &c->sd[j]);
         if (it % 10 == 0) {
+            O_PAR
             for (int cc = 1; cc <= nsd; cc++) {
                 osubd *S = &c->sd[cc];
-                calc_residual(S->phic, S->ap, S->anb, S->b, S->ef2nb_idx, S->ef2nb, S->ne, &res, &res_max);
+                calc_residual(S->phic, S->ap, S->anb, S->b, S->ef2nb_idx, S->ef2nb, S->ne, &sres[cc], &sres_max[cc]);
+            }
+            for (int cc = 1; cc <= nsd; cc++) {
+                res = sres[cc]; res_max = sres_max[cc];
                 res_f_tot = res_f_tot + res*res;    /* not reset: reference quirk */
                 res_max_tot = fmax(res_max_tot, res_max);
             }
@@ -844,12 +887,14 @@ static void multi_subdomain_solver(ocase *c, const double *ap, const double *anb
         osubd *S = &c->sd[cc];
         for (int e = 1; e <= S->ne; e++) phi[c->g2gf[c->g2gf_idx[cc] + e - 1]] = S->phic[e];
     }
+    free(sres); free(sres_max);
     *it_out = it; *ri = res_i_tot; *rf = res_f_tot; *rmax = res_max_tot;
 }
 
 /* ---- tight mode: Krylov inner solves (parity mode) -------------------- */
 /* y = A x for the interior operator: (A x)_e = ap_e x_e - sum_interior anb x_nb */
 static void amul(const ocase *c, const double *ap, const double *anb, const double *x, double *y) {
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         double s = ap[e]*x[e];
         for (int idx = c->ef2nb_idx[e]; idx <= c->ef2nb_idx[e+1] - 1; idx++) {
@@ -859,13 +904,33 @@ static void amul(const ocase *c, const double *ap, const double *anb, const doub
         y[e] = s;
     }
 }
+/* Dot product over fixed blocks of O_DOT_BLOCK elements: each block is summed
+ * in order, then the block sums in order, so the result does not depend on
+ * the number of threads (a single block is the plain serial sum). */
+#define O_DOT_BLOCK 4096
 static double vdot(int n, const double *a, const double *b) {
+    const int nb = (n + O_DOT_BLOCK - 1) / O_DOT_BLOCK;
+    if (nb <= 1) {
+        double s = 0.;
+        for (int e = 1; e <= n; e++) s = s + a[e]*b[e];
+        return s;
+    }
+    double *part = o_alloc((size_t)nb, sizeof(double));
+    O_PAR
+    for (int k = 0; k < nb; k++) {
+        const int e1 = 1 + k*O_DOT_BLOCK, e2 = (k + 1)*O_DOT_BLOCK < n ? (k + 1)*O_DOT_BLOCK : n;
+        double s = 0.;
+        for (int e = e1; e <= e2; e++) s = s + a[e]*b[e];
+        part[k] = s;
+    }
     double s = 0.;
-    for (int e = 1; e <= n; e++) s = s + a[e]*b[e];
+    for (int k = 0; k < nb; k++) s = s + part[k];
+    free(part);
     return s;
 }
 /* RHS including the known halo terms: b'_e = b_e + sum_boundary anb*phi_halo */
 static void full_rhs(const ocase *c, const double *anb, const double *b, const double *phi, double *bb) {
+    O_PAR
     for (int e = 1; e <= c->ne; e++) {
         double s = b[e];
         for (int idx = c->ef2nb_idx[e]; idx <= c->ef2nb_idx[e+1] - 1; idx++) {
@@ -884,6 +949,7 @@ static int bicgstab(const ocase *c, const double *ap, const double *anb, const d
     double *t = o_alloc(n + 1, 8);
     full_rhs(c, anb, b, phi, bb);
     amul(c, ap, anb, phi, t);
+    O_PAR
     for (int e = 1; e <= n; e++) { r[e] = bb[e] - t[e]; rh[e] = r[e]; }
     double bn = sqrt(vdot(n, bb, bb)), rn = sqrt(vdot(n, r, r));
     double rho = 1., alpha = 1., omega = 1., rho1;
@@ -894,26 +960,35 @@ static int bicgstab(const ocase *c, const double *ap, const double *anb, const d
         it++;
         rho1 = vdot(n, rh, r);
         if (rho1 == 0.) break;
-        if (it == 1) for (int e = 1; e <= n; e++) pp[e] = r[e];
-        else {
+        if (it == 1) {
+            O_PAR
+            for (int e = 1; e <= n; e++) pp[e] = r[e];
+        } else {
             double beta = (rho1/rho)*(alpha/omega);
+            O_PAR
             for (int e = 1; e <= n; e++) pp[e] = r[e] + beta*(pp[e] - omega*vv[e]);
         }
+        O_PAR
         for (int e = 1; e <= n; e++) ph[e] = pp[e]/ap[e];
         amul(c, ap, anb, ph, vv);
         alpha = rho1 / vdot(n, rh, vv);
+        O_PAR
         for (int e = 1; e <= n; e++) s[e] = r[e] - alpha*vv[e];
         double sn = sqrt(vdot(n, s, s));
         if (sn <= tol) {
+            O_PAR
             for (int e = 1; e <= n; e++) phi[e] = phi[e] + alpha*ph[e];
             rn = sn;
             break;
         }
+        O_PAR
         for (int e = 1; e <= n; e++) sh[e] = s[e]/ap[e];
         amul(c, ap, anb, sh, t);
         double tt = vdot(n, t, t);
         omega = tt > 0. ? vdot(n, t, s)/tt : 0.;
+        O_PAR
         for (int e = 1; e <= n; e++) phi[e] = phi[e] + alpha*ph[e] + omega*sh[e];
+        O_PAR
         for (int e = 1; e <= n; e++) r[e] = s[e] - omega*t[e];
         rn = sqrt(vdot(n, r, r));
         rho = rho1;
@@ -932,11 +1007,13 @@ static int pcg(const ocase *c, const double *ap, const double *anb, const double
     double mean = 0.;
     for (int e = 1; e <= n; e++) mean = mean + b[e];
     mean = mean / n;
+    O_PAR
     for (int e = 1; e <= n; e++) { r[e] = b[e] - mean; x[e] = 0.; }
     double bn = sqrt(vdot(n, r, r)), rn = bn, rz, rz1, alpha, beta;
     *r0n = bn;
     double tol = rtol * bn;
     int it = 0;
+    O_PAR
     for (int e = 1; e <= n; e++) { z[e] = r[e]/ap[e]; pp[e] = z[e]; }
     rz = vdot(n, r, z);
     while (rn > tol && it < maxit) {
@@ -945,12 +1022,15 @@ static int pcg(const ocase *c, const double *ap, const double *anb, const double
         double pq = vdot(n, pp, q);
         if (pq <= 0.) break;
         alpha = rz / pq;
+        O_PAR
         for (int e = 1; e <= n; e++) { x[e] = x[e] + alpha*pp[e]; r[e] = r[e] - alpha*q[e]; }
         rn = sqrt(vdot(n, r, r));
+        O_PAR
         for (int e = 1; e <= n; e++) z[e] = r[e]/ap[e];
         rz1 = vdot(n, r, z);
         beta = rz1 / rz;
         rz = rz1;
+        O_PAR
         for (int e = 1; e <= n; e++) pp[e] = z[e] + beta*pp[e];
     }
     *rfn = rn;

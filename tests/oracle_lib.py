@@ -4,6 +4,7 @@ Test infrastructure only: the oracle is the checker, never the code under
 test.  It restates the reference Fortran line by line (see oracle/*.c).
 """
 import ctypes as C
+import hashlib
 import math
 import os
 import subprocess
@@ -79,6 +80,9 @@ def lib():
         L.or_solve_energy.argtypes = [vp, C.POINTER(OrStats)]
         L.or_solve_energy.restype = None
         L.or_wtime.restype = C.c_double
+        L.or_num_threads.restype = C.c_int
+        L.or_set_num_threads.argtypes = [C.c_int]
+        L.or_set_num_threads.restype = None
         _lib = L
     return _lib
 
@@ -254,3 +258,18 @@ class Oracle:
 
 def wtime():
     return lib().or_wtime()
+
+
+def sha256(a):
+    """SHA-256 of an array's bytes (the golden fixtures' hash)."""
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def num_threads():
+    """Host threads the oracle's parallel loops use."""
+    return int(lib().or_num_threads())
+
+
+def set_num_threads(n):
+    """Threads for the oracle's parallel loops from now on."""
+    lib().or_set_num_threads(int(n))

@@ -85,6 +85,31 @@ def test_golden_runs():
             assert sha(o.get(f)) == h, (key, f)
 
 
+def test_cavity_fixture_checkpoints_reproduce():
+    """The 32^3 cavity fixture (tests/golden/make_cavity_runs.py) is
+    reproduced by the oracle here, bit for bit, at its first two checkpoints,
+    with the thread count halved: the tight-mode oracle does not depend on
+    how many threads run it."""
+    with open(os.path.join(ROOT, "tests", "golden", "cavity_runs.json")) as fh:
+        rec = json.load(fh)["cases"]["cavity32"]
+    z = cfdl.Zone(rec["n"], rec["tet"], rec["jitter"], seed=rec["seed"])
+    o = oracle_lib.Oracle(z, n_subdomains=1)
+    o.physics_init(oracle_lib.steady(mode=1, tight_rtol=1e-13))
+    threads = oracle_lib.num_threads()
+    oracle_lib.set_num_threads(max(1, threads // 2))
+    try:
+        done = 0
+        for k in sorted(int(c) for c in rec["checkpoints"])[:2]:
+            st = o.run(k - done, 3)
+            done = k
+            cp = rec["checkpoints"][str(k)]
+            assert [st.it_u, st.it_v, st.it_w, st.it_p] == cp["iters"], k
+            for f, h in cp["hash"].items():
+                assert sha(o.get(f)) == h, (k, f)
+    finally:
+        oracle_lib.set_num_threads(threads)
+
+
 def test_reference_pressure_quirk_runs_full_nit():
     """multi_subdomain_solver never resets res_f_tot (mod_solver.f90:175-178),
     so for small residuals the 4-block pressure solve runs all nit sweeps."""

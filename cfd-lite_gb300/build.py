@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 SOURCES = ["cfdl_zone.cpp", "cfdl_setup.cpp", "cfdl_case.cpp", "cfdl_api.cpp",
-           "cfdl_prof.cpp", "cfdl_tune.cpp", "cfdl_serve.cpp", "cfdl_amg_setup.cpp", "cfdl_kernels.cu", "cfdl_amg.cu", "cfdl_solvers.cu", "cfdl_graph.cu", "cfdl_run.cu", "cfdl_noalloc.cu", "cfdl_gsetup.cu", "cfdl_vtu.cpp", "cfdl_energy.cu"]
+           "cfdl_prof.cpp", "cfdl_tune.cpp", "cfdl_serve.cpp", "cfdl_amg_setup.cpp", "cfdl_kernels.cu", "cfdl_amg.cu", "cfdl_solvers.cu", "cfdl_graph.cu", "cfdl_run.cu", "cfdl_noalloc.cu", "cfdl_gsetup.cu", "cfdl_vtu.cpp", "cfdl_energy.cu", "cfdl_probe.cu"]
 # the device mesh set-up reproduces the host builder's doubles: no FMA contraction
 EXTRA = {"cfdl_gsetup.cu": ["-fmad=false"]}
 

@@ -29,6 +29,9 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "non-finite val
           9: "problem larger than the fixed scratch of the allocation-free entry point",
           10: "Krylov breakdown: p.Ap <= 0 above the tolerance (matrix not positive definite)"}
 BC_WALL, BC_SYMMETRY = 1, 2
+# cfdl_fields members as CFDL_F_* bits (cfdl_step_host_keep)
+FIELD_BITS = {f: 1 << k for k, f in enumerate(("u", "v", "w", "p", "u0", "v0", "w0", "gu", "gv", "gw", "gp", "gpc",
+                                                "mip", "mip0"))}
 HEXA_8, TETRA_4, QUAD_4, TRI_3 = 17, 10, 7, 5
 
 
@@ -141,6 +144,7 @@ def lib():
         getattr(L, n).argtypes = [vp, C.POINTER(Stats)]
     L.cfdl_energy_init.argtypes = [vp, C.c_double, C.c_double, C.c_double]
     L.cfdl_check_conversions.argtypes = [C.c_int, vp]
+    L.cfdl_probe_fp64.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cfdl_set_pdl.argtypes = [vp, C.c_int]
     L.cfdl_set_energy_tile.argtypes = [vp, C.c_int]
     L.cfdl_get_energy_tile.argtypes = [vp]
@@ -148,6 +152,7 @@ def lib():
     L.cfdl_step.argtypes = [vp, C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_solve_uvwp_host.argtypes = [vp, C.POINTER(Fields), C.POINTER(Stats)]
     L.cfdl_step_host.argtypes = [vp, C.POINTER(Fields), C.c_int, C.c_int, C.POINTER(Stats)]
+    L.cfdl_step_host_keep.argtypes = [vp, C.POINTER(Fields), C.c_uint, C.c_int, C.c_int, C.POINTER(Stats)]
     L.cfdl_calc_grad.argtypes = [vp, C.c_int]
     L.cfdl_calc_mip.argtypes = [vp, C.c_int]
     L.cfdl_get_array.argtypes = [vp, C.c_char_p, vp]
@@ -291,6 +296,13 @@ class Setup:
 
 def select_device(device):
     _check(lib().cfdl_select_device(int(device)), "select_device")
+
+
+def probe_fp64():
+    """The current device's measured FP64 FMA rate: (FMA instructions/s, probe ms)."""
+    rate, ms = C.c_double(), C.c_double()
+    _check(lib().cfdl_probe_fp64(C.byref(rate), C.byref(ms)), "probe_fp64")
+    return rate.value, ms.value
 
 
 def default_config(**kw):

@@ -29,6 +29,8 @@ constexpr double kOmega = 0.8;     // damped Jacobi weight
 constexpr double kOverCorrect = 3.0;   // scaling of the prolongated coarse correction
 constexpr int kG = 8;                  // lanes per row on the small coarse levels
 constexpr int kGroupedRows = 65536;    // levels below this many rows (per case) run grouped
+constexpr int kTailRows = 2048;        // a case's levels at or below this many rows run in its V-cycle tail
+constexpr int kTailThreads = 1024;     // threads of the tail's one CTA per case
 enum { CNT_A0 = 9, CNT_A1, CNT_A2, CNT_A3, CNT_A4, CNT_A5 };
 
 template <class T> struct LP {
@@ -36,18 +38,19 @@ template <class T> struct LP {
     const int *nb;
     const T *a, *dg, *rd;   // rd = omega / diagonal (the damped Jacobi scaling)
     T *r, *z, *t;
+    const int *len;         // coarse levels: valid slots of each row, packed first (null on the mesh level)
 };
 
 template <class T> __device__ __forceinline__ LP<T> level(const CaseDev &C, int l);
 template <> __device__ __forceinline__ LP<double> level<double>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb_p, C.ap_p, C.rap_p, C.kr, C.ks, C.ksh};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb_p, C.ap_p, C.rap_p, C.kr, C.ks, C.ksh, nullptr};
     const AmgLevelDev &L = C.lev[l - 1];
-    return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t};
+    return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t, L.len};
 }
 template <> __device__ __forceinline__ LP<float> level<float>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb_p, C.fdiag_p, C.frap_p, C.fr, C.fz, C.ft};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb_p, C.fdiag_p, C.frap_p, C.fr, C.fz, C.ft, nullptr};
     const AmgLevelDev &L = C.lev[l - 1];
-    return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32};
+    return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32, L.len};
 }
 
 // (A x)_i at a level; neighbours outside [0, n) (halos, padding) are skipped
@@ -55,6 +58,30 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
     T y[1];
     ell_row<1, T>(P.nb, P.a, P.dg[i], x, 0, P.n, P.W, i, y);
     return y[0];
+}
+// the same on a coarse level, over the row's valid slots only (the padding
+// slots would subtract zero terms): four slots per step, loads issued together
+template <class T> __device__ __forceinline__ T amul_coarse(const LP<T> &P, const T *x, int i) {
+    if (P.W == 6 || P.W == 4 || !P.len) return amul<T>(P, x, i);
+    const int len = P.len[i];
+    T y = P.dg[i] * x[i];
+    for (int k0 = 0; k0 < len; k0 += 4) {
+        int jj[4];
+        T ak[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ok = (unsigned)jj[u] < (unsigned)P.n;
+            ak[u] = ok ? P.a[(k0 + u) * P.n + i] : (T)0;
+            if (!ok) jj[u] = i;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[u] = x[jj[u]];
+#pragma unroll
+        for (int u = 0; u < 4; u++) y -= ak[u] * xv[u];
+    }
+    return y;
 }
 
 // The first W slots of row i: neighbour j[k] (i itself for a slot outside
@@ -115,16 +142,24 @@ template <class T> __device__ __forceinline__ T amul_mesh(const LP<T> &P, const 
     if (P.W == 4) return amul_w<4, T>(P, x, i);
     return amul_w<kMaxW, T, true>(P, x, i);
 }
+// Valid slots of row i: a coarse row's couplings are packed in its first
+// len[i] slots (the rest is padding up to the level's widest row, W).
+template <class T> __device__ __forceinline__ int row_len(const LP<T> &P, int i) {
+    return P.len ? P.len[i] : P.W;
+}
+
 template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
     if (P.W == 6) return offsum_w<6, T, false, false>(P, x, i);
     if (P.W == 4) return offsum_w<4, T, false, false>(P, x, i);
-    // wide coarse rows: four slots per step, loads issued together
+    // wide coarse rows: four slots per step, loads issued together, up to the
+    // row's own length (the padding would add zero terms)
     T s = 0;
-    for (int k0 = 0; k0 < P.W; k0 += 4) {
+    const int len = row_len(P, i);
+    for (int k0 = 0; k0 < len; k0 += 4) {
         int jj[4];
         T c[4], xv[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < P.W ? P.nb[(k0 + u) * P.n + i] : -1;
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const bool ok = (unsigned)jj[u] < (unsigned)P.n;
@@ -172,25 +207,36 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
 }
 
 // Dense inverse of A_L + c 11^T at each case's coarsest level (one CTA per
-// case, Gauss-Jordan in shared memory; the matrix is SPD, no pivoting).
-__global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restrict__ cases, int ncases) {
+// case, Gauss-Jordan in shared memory; the matrix is SPD, no pivoting).  Per
+// pivot k, the first n threads scale the pivot row into R (R[k] = 1/p, one
+// division per column: FP64 division is a long instruction sequence on a
+// single SM's FP64 pipe) and save the pivot column into Q; after a barrier
+// every thread updates its own entries (up to four: n <= 64, so
+// n^2 <= 4 * kInvThreads) from M, Q and R alone, so the update is in place;
+// a second barrier ends the pivot.
+constexpr int kInvThreads = 1024;
+__global__ void __launch_bounds__(kInvThreads) k_amg_coarse_inv(const CaseDev *__restrict__ cases, int ncases) {
     CFDL_PDL_WAIT();
     const int c = blockIdx.x;
     if (c >= ncases) return;
     const CaseDev &C = cases[c];
     if (C.precond != 1 || C.sc->halted) return;
     __shared__ double M[kAmgCoarsest * kAmgCoarsest];
-    __shared__ double piv;
+    __shared__ double R[kAmgCoarsest], Q[kAmgCoarsest];
     const LP<double> P = level<double>(C, C.nlev);
     const int n = P.n;
     if (n > kAmgCoarsest) return;   // cannot happen: the builder coarsens to <= kAmgCoarsest
     double dmax = 0.0;
     for (int i = 0; i < n; i++) dmax = fmax(dmax, fabs(P.dg[i]));
     const double cc = dmax > 0.0 ? dmax / n : 1.0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int i = e / n, j = e % n;
-        double v = cc + (i == j ? P.dg[i] : 0.0);
-        M[e] = v;
+    constexpr int kPer = kAmgCoarsest * kAmgCoarsest / kInvThreads;
+    int ei[kPer], ej[kPer];
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        const int e = (int)threadIdx.x + q * kInvThreads;
+        ei[q] = e < n * n ? e / n : -1;
+        ej[q] = e < n * n ? e % n : -1;
+        if (ei[q] >= 0) M[e] = cc + (ei[q] == ej[q] ? P.dg[ei[q]] : 0.0);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += blockDim.x) {
@@ -201,26 +247,28 @@ __global__ void __launch_bounds__(256) k_amg_coarse_inv(const CaseDev *__restric
     }
     __syncthreads();
     for (int k = 0; k < n; k++) {
-        if (threadIdx.x == 0) piv = M[k * n + k];
-        __syncthreads();
-        const double p = piv;
-        // scale row k
-        for (int j = threadIdx.x; j < n; j += blockDim.x) M[k * n + j] = (j == k ? 1.0 : M[k * n + j]) / p;
-        __syncthreads();
-        // eliminate column k from the other rows
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-            const int i = e / n, j = e % n;
-            if (i == k) continue;
-            const double f = M[i * n + k];
-            if (j == k) continue;
-            M[e] -= f * M[k * n + j];
+        const int t = (int)threadIdx.x;
+        if (t < n) {
+            const double p = M[k * n + k];
+            R[t] = (t == k ? 1.0 : M[k * n + t]) / p;     // the pivot row, scaled
+            Q[t] = M[t * n + k];                          // the pivot column, before the update
         }
         __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-            if (i != k) M[i * n + k] = -M[i * n + k] * M[k * n + k];
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int i = ei[q], j = ej[q];
+            if (i < 0) continue;
+            double &m = M[i * n + j];
+            if (i == k) m = R[j];
+            else if (j == k) m = -Q[i] * R[k];
+            else m -= Q[i] * R[j];
+        }
         __syncthreads();
     }
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        if (ei[q] < 0) continue;
+        const int e = ei[q] * n + ej[q];
         C.cinv[e] = M[e];
         if (C.precision >= 1) C.cinv32[e] = (float)M[e];
     }
@@ -269,7 +317,7 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.t[i] = P.r[i] - (kMesh ? amul_mesh<T>(P, P.z, i) : amul<T>(P, P.z, i));
+    P.t[i] = P.r[i] - (kMesh ? amul_mesh<T>(P, P.z, i) : amul_coarse<T>(P, P.z, i));
 }
 
 // r_{l1}[I] = sum of the residual t over the members of aggregate I (one
@@ -302,7 +350,9 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
     const bool mixed = C.precision >= 1;
     const int n = L.n;
     double dsum = 0.0;
-    for (int k = 0; k < L.W; k++) {
+    // padding slots (k >= len) keep the zeros they were created with
+    const int len = L.len[I];
+    for (int k = 0; k < len; k++) {
         const int s = k * n + I;
         double v = 0.0;
         for (int q = L.g_ptr[s]; q < L.g_ptr[s + 1]; q++) v += af[L.g_src[q]];
@@ -313,27 +363,6 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
     L.dg[I] = dsum;
     L.rd[I] = kOmega / dsum;
     if (mixed) { L.dg32[I] = narrow_f32(dsum); L.rd32[I] = narrow_f32(kOmega / dsum); }
-}
-
-// coarsest: z_L = Minv r_L (one CTA per case, 4 lanes per row)
-template <class T>
-__global__ void __launch_bounds__(256) k_v_coarse(const CaseDev *__restrict__ cases, int ncases) {
-    CFDL_PDL_WAIT();
-    const int c = blockIdx.x;
-    if (c >= ncases) return;
-    const CaseDev &C = cases[c];
-    if (C.precond != 1 || (sizeof(T) == 8 ? !pactive(C) : !mactive(C))) return;
-    const LP<T> P = level<T>(C, C.nlev);
-    const T *Mi = sizeof(T) == 8 ? (const T *)C.cinv : (const T *)C.cinv32;
-    const int n = P.n, q = (int)threadIdx.x & 3;
-    for (int i0 = (int)threadIdx.x >> 2; i0 < ((n + 63) & ~63); i0 += 64) {
-        T s = 0;
-        if (i0 < n)
-            for (int j = q; j < n; j += 4) s += Mi[i0 * n + j] * P.r[j];
-        s += __shfl_xor_sync(0xffffffffu, s, 1);
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (i0 < n && q == 0) P.z[i0] = s;
-    }
 }
 
 // t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly),
@@ -381,12 +410,78 @@ __global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__
     else if (kMesh) off = prolong_row<kMaxW, T, true>(P, L.agg, zc, sc, i);
     else {
         off = 0;
-        for (int k = 0; k < P.W; k++) {
+        const int len = row_len(P, i);
+        for (int k = 0; k < len; k++) {
             const int j = P.nb[k * P.n + i];
             if (j >= 0 && j < P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
         }
     }
     P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
+}
+
+// ------------------------------------------------- the V-cycle's tail
+// The small coarse levels of a case, from its tail level (the first level of
+// at most kTailRows rows) down to the coarsest and back, in one CTA: the
+// steps of k_v_jac0 / k_v_jac / k_v_resid / k_v_restrict, the coarsest solve
+// and k_v_prolong / k_v_jac, one row per thread per pass, with a block
+// barrier between steps.  Each step is a few microseconds of dependent loads
+// from L2; launched one by one, every step costs a kernel launch instead.
+// The CTA waits only at __syncthreads, on its own threads.
+template <class T>
+__global__ void __launch_bounds__(kTailThreads) k_v_tail(const CaseDev *__restrict__ cases, int ncases) {
+    CFDL_PDL_WAIT();
+    const int c = blockIdx.x;
+    if (c >= ncases) return;
+    const CaseDev &C = cases[c];
+    if (C.precond != 1 || (sizeof(T) == 8 ? !pactive(C) : !mactive(C))) return;
+    const int L = C.nlev, lt = C.amg_tail, nt = (int)blockDim.x;
+    for (int l = lt; l < L; l++) {
+        const LP<T> P = level<T>(C, l);
+        for (int i = threadIdx.x; i < P.n; i += nt) P.t[i] = P.rd[i] * P.r[i];
+        __syncthreads();
+        for (int i = threadIdx.x; i < P.n; i += nt) P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
+        __syncthreads();
+        for (int i = threadIdx.x; i < P.n; i += nt) P.t[i] = P.r[i] - amul_coarse<T>(P, P.z, i);
+        __syncthreads();
+        const AmgLevelDev &Lc = C.lev[l];                  // level l + 1
+        T *rc = sizeof(T) == 8 ? (T *)Lc.r : (T *)Lc.r32;
+        for (int I = threadIdx.x; I < Lc.n; I += nt) {
+            T sum = 0;
+            for (int m = Lc.mem_ptr[I]; m < Lc.mem_ptr[I + 1]; m++) sum += P.t[Lc.mem[m]];
+            rc[I] = sum;
+        }
+        __syncthreads();
+    }
+    {   // coarsest: z_L = Minv r_L
+        const LP<T> P = level<T>(C, L);
+        const T *Mi = sizeof(T) == 8 ? (const T *)C.cinv : (const T *)C.cinv32;
+        const int n = P.n;
+        for (int i = threadIdx.x; i < n; i += nt) {
+            T sum = 0;
+            for (int j = 0; j < n; j++) sum += Mi[i * n + j] * P.r[j];
+            P.z[i] = sum;
+        }
+        __syncthreads();
+    }
+    const T sc = (T)kOverCorrect;
+    for (int l = L - 1; l >= lt; l--) {
+        const LP<T> P = level<T>(C, l);
+        const AmgLevelDev &Lc = C.lev[l];
+        const T *zc = sizeof(T) == 8 ? (const T *)Lc.z : (const T *)Lc.z32;
+        for (int i = threadIdx.x; i < P.n; i += nt) {
+            const T xi = P.z[i] + sc * zc[Lc.agg[i]];
+            T off = 0;
+            const int len = row_len(P, i);
+            for (int k = 0; k < len; k++) {
+                const int j = P.nb[k * P.n + i];
+                if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[Lc.agg[j]]);
+            }
+            P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < P.n; i += nt) P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------- coarse levels, grouped
@@ -412,11 +507,13 @@ template <int G, class T> __device__ __forceinline__ T group_sum(T v) {
 // sum_k a_ik x_j over the row's couplings inside the level, split over the group
 template <int G, class T> __device__ __forceinline__ T group_offdiag(const LP<T> &P, const T *x, int i, bool ok, int g) {
     T s = 0;
-    if (ok)
-        for (int k = g; k < P.W; k += G) {
+    if (ok) {
+        const int len = row_len(P, i);
+        for (int k = g; k < len; k += G) {
             const int j = P.nb[k * P.n + i];
             if ((unsigned)j < (unsigned)P.n) s += P.a[k * P.n + i] * x[j];
         }
+    }
     return group_sum<G>(s);
 }
 
@@ -469,11 +566,13 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
     const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
     const T sc = (T)kOverCorrect;
     T off = 0;
-    if (ok)
-        for (int k = g; k < P.W; k += G) {
+    if (ok) {
+        const int len = row_len(P, i);
+        for (int k = g; k < len; k += G) {
             const int j = P.nb[k * P.n + i];
             if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
         }
+    }
     off = group_sum<G>(off);
     if (ok && g == 0) {
         const T xi = P.z[i] + sc * zc[L.agg[i]];
@@ -493,7 +592,7 @@ __global__ void __launch_bounds__(kTile) k_amg_galg(const CaseDev *__restrict__ 
     const int n = L.n;
     double dsum = 0.0;
     if (ok)
-        for (int k = g; k < L.W; k += G) {
+        for (int k = g, len = L.len[i]; k < len; k += G) {
             const int sl = k * n + i;
             double v = 0.0;
             for (int q = L.g_ptr[sl]; q < L.g_ptr[sl + 1]; q++) v += af[L.g_src[q]];
@@ -729,6 +828,14 @@ int upload_case_amg(HostCase *hc, AmgHierarchy *H) {
         if ((st = dupload(hc, (int **)&D.mem, L.mem))) return st;
         if ((st = dupload(hc, (int **)&D.g_ptr, L.g_ptr))) return st;
         if ((st = dupload(hc, (int **)&D.g_src, L.g_src))) return st;
+        {
+            // valid slots of each row: the builder packs a row's couplings first
+            std::vector<int> len((size_t)L.n, 0);
+            for (int k = 0; k < L.W; k++)
+                for (int c = 0; c < L.n; c++)
+                    if (L.nb[(size_t)k * L.n + c] >= 0) len[c] = k + 1;
+            if ((st = dupload(hc, (int **)&D.len, len))) return st;
+        }
         if ((st = dzeros(hc, &D.a, (size_t)L.W * L.n))) return st;
         if ((st = dzeros(hc, &D.a32, (size_t)L.W * L.n))) return st;
         double **v64[] = {&D.dg, &D.rd, &D.r, &D.z, &D.t};
@@ -765,21 +872,36 @@ int ensure_amg(cfdl_ctx *ctx) {
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);
     for (auto &wl : ctx->amg_gsmooth) free_worklist(wl);
+    for (auto &wl : ctx->amg_restr) free_worklist(wl);
+    for (auto &wl : ctx->amg_grestr) free_worklist(wl);
     ctx->amg_cells.assign(lmax + 1, WorkList());
     ctx->amg_smooth.assign(lmax + 1, WorkList());
     ctx->amg_gcells.assign(lmax + 1, WorkList());
     ctx->amg_gsmooth.assign(lmax + 1, WorkList());
+    ctx->amg_restr.assign(lmax + 1, WorkList());
+    ctx->amg_grestr.assign(lmax + 1, WorkList());
     ctx->amg_grouped.assign(lmax + 1, 0);
+    // each case's tail level: its first coarse level of at most kTailRows rows
+    // (the coarsest always qualifies); a case without coarse levels solves its
+    // mesh level directly (tail level 0)
+    for (HostCase *hc : ctx->cases) {
+        int lt = 0;
+        for (int l = 1; l <= hc->dev.nlev; l++)
+            if (hc->amg->levels[l - 1].n <= kTailRows) { lt = l; break; }
+        hc->dev.amg_tail = lt;
+    }
     for (int l = 0; l <= lmax; l++) {
-        std::vector<int> cells, smooth;
+        std::vector<int> cells, smooth, restr;
         for (HostCase *hc : ctx->cases) {
             int n = l == 0 ? hc->ne : (l <= hc->dev.nlev ? hc->amg->levels[l - 1].n : 0);
             cells.push_back(l <= hc->dev.nlev ? n : 0);
-            smooth.push_back(l < hc->dev.nlev ? n : 0);
+            smooth.push_back(l < hc->dev.amg_tail ? n : 0);
+            restr.push_back(l >= 1 && l <= hc->dev.amg_tail ? n : 0);
         }
         int st;
         if ((st = build_worklist(ctx, ctx->amg_cells[l], cells))) return st;
         if ((st = build_worklist(ctx, ctx->amg_smooth[l], smooth))) return st;
+        if ((st = build_worklist(ctx, ctx->amg_restr[l], restr))) return st;
         // lanes per row: 8 when every case's level is small, else the tuned
         // cgroup (1 = one thread per row); the mesh level is always 1
         const int nmax = *std::max_element(cells.begin(), cells.end());
@@ -788,6 +910,7 @@ int ensure_amg(cfdl_ctx *ctx) {
         if (G > 1) {
             if ((st = build_worklist(ctx, ctx->amg_gcells[l], cells, kTile / G))) return st;
             if ((st = build_worklist(ctx, ctx->amg_gsmooth[l], smooth, kTile / G))) return st;
+            if ((st = build_worklist(ctx, ctx->amg_grestr[l], restr, kTile / G))) return st;
         }
     }
     ctx->amg_lmax = lmax;
@@ -827,7 +950,7 @@ static void amg_setup_operators(cfdl_ctx *ctx) {
         default: ALAUNCH("k_amg_gal", k_amg_gal, ctx->amg_cells[l], l);
         }
     }
-    CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, 256);
+    CLAUNCH("k_amg_coarse_inv", k_amg_coarse_inv, kInvThreads);
 }
 
 // One V-cycle z_0 = M^-1 r_0 on every active case.
@@ -861,10 +984,11 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             }
         }
         G = ctx->amg_grouped[l + 1];
-        if (G > 1) { GROUPED(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict, ctx->amg_gcells[l + 1], 0, l + 1) }
-        else ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_cells[l + 1], l + 1);
+        if (G > 1) { GROUPED(l ? "k_v_restrict_c" : "k_v_restrict_f", k_vg_restrict, ctx->amg_grestr[l + 1], 0, l + 1) }
+        else ALAUNCH(l ? "k_v_restrict_c" : "k_v_restrict_f", k_v_restrict<T>, ctx->amg_restr[l + 1], l + 1);
     }
-    CLAUNCH("k_v_coarse", k_v_coarse<T>, 256);
+    // each case's small levels and its coarsest solve, one CTA per case
+    CLAUNCH("k_v_tail", k_v_tail<T>, kTailThreads);
     for (int l = L - 1; l >= 0; l--) {
         const int G = ctx->amg_grouped[l];
         if (G > 1) {

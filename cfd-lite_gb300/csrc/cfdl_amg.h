@@ -35,6 +35,7 @@ int build_amg_hierarchy(const AmgFineView &fine, AmgHierarchy &H);
 struct AmgLevelDev {
     int n, W, n_fine, W_fine;
     const int *nb, *agg, *mem_ptr, *mem, *g_ptr, *g_src;
+    const int *len;                           // [n] couplings of each row (its slots k < len are the valid ones)
     double *a, *dg, *rd, *r, *z, *t;          // FP64 operator and V-cycle vectors
     float *a32, *dg32, *rd32, *r32, *z32, *t32; // FP32 copies (mixed-precision form)
 };

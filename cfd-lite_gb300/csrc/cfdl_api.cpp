@@ -59,6 +59,7 @@ int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool
     Named nm = lookup(hc, name);
     if (!nm.ptr) return CFDL_ERR_NAME;
     if (!host) return CFDL_ERR_INVALID;
+    if (!to_host) ctx->host_writes++;
     if (!to_host && (nm.ptr == hc->dev.rho || nm.ptr == hc->dev.mu)) hc->props_dirty = true;
     if (!to_host && nm.ptr && (nm.ptr == hc->dev.ecp || nm.ptr == hc->dev.etc)) hc->eprops_dirty = true;
     if (!to_host && (nm.ptr == hc->dev.gu || nm.ptr == hc->dev.gv || nm.ptr == hc->dev.gw)) hc->g32_stale = true;
@@ -103,6 +104,7 @@ int transfer_fields(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f, bool to_h
     if (!to_host && (f->gu || f->gv || f->gw)) hc->g32_stale = true;   // precision 3 derives g32 from them
     for (const P &p : list) {
         if (!p.h) continue;
+        if (!to_host) ctx->host_writes++;
         cudaError_t e = to_host ? cudaMemcpyAsync(p.h, p.dv, p.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream)
                                 : cudaMemcpyAsync(p.dv, p.h, p.n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
         if (e != cudaSuccess) return cuda_status(e);
@@ -264,6 +266,8 @@ int cfdl_ctx_destroy(cfdl_ctx *ctx) {
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);
     for (auto &wl : ctx->amg_gsmooth) free_worklist(wl);
+    for (auto &wl : ctx->amg_restr) free_worklist(wl);
+    for (auto &wl : ctx->amg_grestr) free_worklist(wl);
     cudaFree(ctx->d_cases);
     cudaFree(ctx->d_partials);
     cudaFree(ctx->d_flags);
@@ -349,6 +353,35 @@ static int download_overlapped(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f
     return cuda_status(cudaStreamSynchronize(ctx->stream));
 }
 
+// The members of a cfdl_fields in CFDL_F_* bit order.
+static double **field_slot(cfdl_fields *f, int k) {
+    double **m[14] = {&f->u, &f->v, &f->w, &f->p, &f->u0, &f->v0, &f->w0,
+                      &f->gu, &f->gv, &f->gw, &f->gp, &f->gpc, &f->mip, &f->mip0};
+    return m[k];
+}
+
+// The host drop-in's upload: every non-NULL member of f, except those the
+// caller declares unchanged (keep) whose host array is the one the last
+// drop-in download filled while nothing has written the device since.
+static int upload_changed(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f, unsigned keep) {
+    const bool clean = ctx->launches == ctx->synced_launches && ctx->graph_launches == ctx->synced_graphs &&
+                       ctx->host_writes == ctx->synced_writes;
+    cfdl_fields up = *f;
+    for (int k = 0; k < 14; k++) {
+        double **slot = field_slot(&up, k);
+        if (clean && (keep >> k & 1u) && *slot && *slot == ctx->synced_ptr[k]) *slot = nullptr;
+    }
+    return transfer_fields(ctx, hc, &up, false);
+}
+
+// After the drop-in's download: which host arrays now equal the device's.
+static void mark_synced(cfdl_ctx *ctx, cfdl_fields *f) {
+    for (int k = 0; k < 14; k++) ctx->synced_ptr[k] = *field_slot(f, k);
+    ctx->synced_launches = ctx->launches;
+    ctx->synced_graphs = ctx->graph_launches;
+    ctx->synced_writes = ctx->host_writes;
+}
+
 int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *stats) {
     int st = check_ctx(ctx);
     if (st) return st;
@@ -358,16 +391,17 @@ int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *stats) {
     if ((st = transfer_fields(ctx, hc, f, false))) return st;
     if ((st = solve_uvwp_all(ctx))) return st;
     if ((st = download_overlapped(ctx, hc, f))) return st;
+    mark_synced(ctx, f);
     return finish(ctx, stats);
 }
 
-int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_stats *stats) {
+int cfdl_step_host_keep(cfdl_ctx *ctx, cfdl_fields *f, unsigned keep, int n_outer, int ncoef, cfdl_stats *stats) {
     int st = check_ctx(ctx);
     if (st) return st;
-    if (!f || n_outer < 1) return CFDL_ERR_INVALID;
+    if (!f || n_outer < 1 || (keep >> 14) != 0u) return CFDL_ERR_INVALID;
     HostCase *hc = ctx->cases[0];
     if ((st = ensure_copy_stream(ctx))) return st;
-    if ((st = transfer_fields(ctx, hc, f, false))) return st;
+    if ((st = upload_changed(ctx, hc, f, keep))) return st;
     for (int k = 1; k <= n_outer; k++) {
         launch_bc(ctx);
         if ((st = solve_uvwp_all(ctx))) return st;
@@ -375,7 +409,12 @@ int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_s
         if (ncoef > 0 && k % ncoef == 0) launch_update_time(ctx);
     }
     if ((st = download_overlapped(ctx, hc, f))) return st;
+    mark_synced(ctx, f);
     return finish(ctx, stats);
+}
+
+int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_stats *stats) {
+    return cfdl_step_host_keep(ctx, f, 0u, n_outer, ncoef, stats);
 }
 
 int cfdl_calc_coef_uvw(cfdl_ctx *ctx) {

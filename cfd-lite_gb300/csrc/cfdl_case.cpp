@@ -446,7 +446,10 @@ int rebuild_worklists(cfdl_ctx *ctx) {
     for (auto &wl : ctx->amg_smooth) free_worklist(wl);
     for (auto &wl : ctx->amg_gcells) free_worklist(wl);
     for (auto &wl : ctx->amg_gsmooth) free_worklist(wl);
-    ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_gcells.clear(); ctx->amg_gsmooth.clear(); ctx->amg_lmax = -1;
+    for (auto &wl : ctx->amg_restr) free_worklist(wl);
+    for (auto &wl : ctx->amg_grestr) free_worklist(wl);
+    ctx->amg_cells.clear(); ctx->amg_smooth.clear(); ctx->amg_gcells.clear(); ctx->amg_gsmooth.clear();
+    ctx->amg_restr.clear(); ctx->amg_grestr.clear(); ctx->amg_lmax = -1;
     destroy_graph(ctx);   // captured launch arguments refer to the old lists
     int need = std::max({ctx->cells.ntiles, ctx->faces.ntiles, ctx->halos.ntiles, 1});
     if (need > ctx->partials_cap) {

@@ -144,6 +144,7 @@ struct CaseDev {
     // 1/ap of the operator being solved (momentum, then pressure), AMG levels, coarsest inverse
     double *rap;
     int nlev, ncoarse;                    // coarse levels; cells of the coarsest level
+    int amg_tail;                         // first level the one-CTA V-cycle tail runs (k_v_tail)
     const AmgLevelDev *lev;               // [nlev] device array
     double *cinv;                         // [ncoarse^2] dense inverse of the coarsest operator
     float *cinv32;
@@ -218,16 +219,28 @@ struct cfdl_ctx {
     double *d_partials = nullptr;        // [max tiles][kNPart]
     int partials_cap = 0;                // tiles
     int64_t launches = 0;
+    int64_t host_writes = 0;             // host-to-device copies into the fields (uploads, set_array)
+    // the host drop-in's last download (cfdl_step_host*): the host array each
+    // field went to, and the launch and write counters at that moment; a
+    // field whose host array the caller declares unchanged is not uploaded
+    // again while nothing has touched the device since (cfdl_step_host_keep)
+    double *synced_ptr[14] = {};
+    int64_t synced_launches = -1, synced_graphs = -1, synced_writes = -1;
     void *h_pinned = nullptr;            // pinned staging for host transfers
     size_t h_pinned_bytes = 0;
     int *h_flags = nullptr;              // pinned, per-case convergence flags
     int h_flags_cap = 0;
     int *d_flags = nullptr;
     void *prof = nullptr;                // event profiler state (cfdl_prof.cpp)
-    // AMG work lists: amg_cells[l] = level-l cells of cases with nlev >= l,
-    // amg_smooth[l] = level-l cells of cases with nlev > l; amg_lmax = max nlev
+    // AMG work lists: amg_cells[l] = level-l cells of cases with nlev >= l
+    // (the Galerkin operators), amg_smooth[l] = level-l cells of cases whose
+    // V-cycle tail starts below level l (smoothed by per-level kernels);
+    // amg_lmax = max nlev
     std::vector<cfdl::WorkList> amg_cells, amg_smooth;      // per level, kTile rows per tile
     std::vector<cfdl::WorkList> amg_gcells, amg_gsmooth;    // per small coarse level, kTile/8 rows per tile
+    // restriction targets of the V-cycle's per-level kernels: level-l rows of
+    // cases whose tail starts at level l or below (amg_restr), and grouped
+    std::vector<cfdl::WorkList> amg_restr, amg_grestr;
     std::vector<int> amg_grouped;                           // lanes per row of each level (1: one thread per row)
     int cgroup = 1;                                          // lanes per row on the large coarse levels (autotuned)
     int amg_lmax = -1;

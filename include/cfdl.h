@@ -208,6 +208,32 @@ int cfdl_solve_uvwp_host(cfdl_ctx *ctx, cfdl_fields *f, cfdl_stats *st);
 /* cfdl_step with host arrays: upload, n_outer passes of update_boundaries +
  * solve_uvwp (+ update_time every ncoef), download as above. */
 int cfdl_step_host(cfdl_ctx *ctx, cfdl_fields *f, int n_outer, int ncoef, cfdl_stats *st);
+/* cfdl_step_host for a host that leaves some fields alone between calls:
+ * keep is a set of CFDL_F_* bits naming the members of f whose host arrays
+ * the caller has not modified since the previous cfdl_step_host* call
+ * downloaded into them.  Such a member is not uploaded again -- the device
+ * copy already equals it -- provided its pointer is the one that call
+ * downloaded into and nothing has written the context's device state since
+ * (no kernel launch, upload or set_array in between); otherwise it is
+ * uploaded as usual.  Every non-NULL member is still downloaded.  A Fortran
+ * host whose gradients and face fluxes are only the solver's own state
+ * (solve_uvwp's callees write them, the host reads them for output) keeps
+ * CFDL_F_GU|GV|GW|GP|GPC|MIP and uploads only u, v, w, p. */
+#define CFDL_F_U    (1u << 0)
+#define CFDL_F_V    (1u << 1)
+#define CFDL_F_W    (1u << 2)
+#define CFDL_F_P    (1u << 3)
+#define CFDL_F_U0   (1u << 4)
+#define CFDL_F_V0   (1u << 5)
+#define CFDL_F_W0   (1u << 6)
+#define CFDL_F_GU   (1u << 7)
+#define CFDL_F_GV   (1u << 8)
+#define CFDL_F_GW   (1u << 9)
+#define CFDL_F_GP   (1u << 10)
+#define CFDL_F_GPC  (1u << 11)
+#define CFDL_F_MIP  (1u << 12)
+#define CFDL_F_MIP0 (1u << 13)
+int cfdl_step_host_keep(cfdl_ctx *ctx, cfdl_fields *f, unsigned keep, int n_outer, int ncoef, cfdl_stats *st);
 
 /* ---- individual routines, for per-routine replacement and parity ---- */
 int cfdl_calc_coef_uvw(cfdl_ctx *ctx);                   /* mod_uvwp.f90:161-286   */
@@ -263,6 +289,12 @@ int cfdl_timer_end(cfdl_ctx *ctx, double *ms);      /* synchronises */
 int cfdl_profile_start(cfdl_ctx *ctx, const char *kernel);
 int cfdl_profile_stop(cfdl_ctx *ctx, int *nkernels);
 int cfdl_profile_get(cfdl_ctx *ctx, int i, char *name64, int64_t *launches, double *total_ms);
+/* The current device's FP64 FMA rate (thread-instructions per second;
+ * multiply by 2 for flop/s), measured by a probe kernel of independent DFMA
+ * chains on every SM, timed with CUDA events; *ms (optional) receives the
+ * probe's duration.  No counterpart in the reference: it is the ceiling of
+ * the FP64-bound kernels' roofline. */
+int cfdl_probe_fp64(double *fma_per_s, double *ms);
 
 /* ---- allocation-free pressure-correction solve --------------------------
  * No counterpart in the reference.  For callers that cannot allocate GPU

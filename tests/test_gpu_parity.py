@@ -265,6 +265,43 @@ def test_step_host_matches_resident(need_gpu, graph):
         assert np.array_equal(g1.get(f), host[f]), f
 
 
+def test_step_host_keep_skips_only_safe_uploads(need_gpu):
+    """cfdl_step_host_keep with the gradients and face fluxes declared
+    unchanged equals the resident path bit for bit; when something else wrote
+    the device in between (a kernel, set_array), the kept fields are uploaded
+    again, so the result equals cfdl_step_host's."""
+    import ctypes as C
+    z = cfdl.Zone(7, False, 0.2, seed=6)
+    s = cfdl.Setup(z)
+    g1 = cfdl.Solver(s, cfdl.steady())
+    g2 = cfdl.Solver(s, cfdl.steady())
+    g3 = cfdl.Solver(s, cfdl.steady())
+    nc = s.ne + s.nbf
+    keep = sum(cfdl.FIELD_BITS[f] for f in ("gu", "gv", "gw", "gp", "gpc", "mip"))
+
+    def host_for(g):
+        h = {f: np.zeros(nc) for f in ("u", "v", "w", "p")}
+        h.update({f: np.zeros(3 * nc) for f in ("gu", "gv", "gw", "gp", "gpc")})
+        h["mip"] = g.get("mip")
+        return h, cfdl.Fields(**{k: v.ctypes.data_as(C.c_void_p) for k, v in h.items()})
+
+    h2, f2 = host_for(g2)
+    h3, f3 = host_for(g3)
+    L = cfdl.lib()
+    for k in range(5):
+        g1.step(1, ncoef=0)
+        assert L.cfdl_step_host_keep(g2._h, C.byref(f2), keep, 1, 0, None) == 0
+        if k == 2:
+            # a device write between calls: the kept host arrays are stale for the
+            # device now (here: its mip moved on), so they must be uploaded again
+            g3.update_boundaries()
+            g3.set("gp", h3["gp"] * 0.0)
+        assert L.cfdl_step_host_keep(g3._h, C.byref(f3), keep, 1, 0, None) == 0
+    for f in ("u", "v", "w", "p", "mip", "gu", "gp", "gpc"):
+        assert np.array_equal(g1.get(f), h2[f]), f
+        assert np.array_equal(h2[f], h3[f]), f
+
+
 @pytest.mark.parametrize("tet", [False, "prism"])
 def test_symmetry_bc_tight_parity(need_gpu, tet):
     """A wall rebound to the reference's symmetry procedure (mod_uvwp.f90:517-546,

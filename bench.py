@@ -65,8 +65,10 @@ def parse():
     ap.add_argument("--outer", type=int, default=300, help="batched: outer iterations per case")
     ap.add_argument("--forms", default="0,1,2,3", help="batched/served: precisions to run (0 FP64, 1 mixed pressure, "
                     "2 mixed pressure + FP32 momentum corrections, 3 also FP32 explicit momentum face terms)")
-    ap.add_argument("--rates", default="5,200", help="served: request rates (req/s)")
-    ap.add_argument("--requests", type=int, default=16, help="served: requests per rate")
+    ap.add_argument("--rates", default="5,20,50,100,200", help="served: request rates (req/s)")
+    ap.add_argument("--requests", type=int, default=200, help="served: requests per rate")
+    ap.add_argument("--err-sample", type=int, default=16, help="served: requests checked against FP64 converged "
+                    "references")
     ap.add_argument("--max-outer", type=int, default=1000, help="served: outer-iteration cap per request")
     ap.add_argument("--conv-tol", type=float, default=1e-6, help="served/converged: mass-ratio tolerance")
     ap.add_argument("--ref-tol", type=float, default=1e-11, help="converged: mass ratio of the FP64 reference")
@@ -270,6 +272,10 @@ def run_ours(a, dist):
         nbytes = amg_kernel_bytes(dominant, levels, val)
     achieved = nbytes / avg_s / 1e9 if nbytes else None
     traffic = ncu_traffic(dominant, a.n)
+    # the FP64 pipe's ceiling: the probe's DFMA rate on this device, and each
+    # FP64-bound kernel's FP64 instructions per launch (flops_model) over its
+    # average launch time from the profile pass above
+    fp64 = fp64_roofline(cfdl, prof, ne, nf, nbf, W, peaks)
     breakdown = {k: {"launches": c, "ms": round(t, 3), "share": round(t / sum(v[1] for v in prof.values()), 4)}
                  for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
     if a.breakdown and dist.rank == 0:
@@ -364,6 +370,8 @@ def run_ours(a, dist):
         "inner_iterations": {"u": stl.it_u, "v": stl.it_v, "w": stl.it_w, "pc": stl.it_p},
         "kernel_shares": {k: v["share"] for k, v in list(breakdown.items())[:8]},
     }
+    if fp64:
+        out["fp64_roofline"] = fp64
     if clk:
         out["clocks"] = clk
     if e2e:
@@ -372,6 +380,31 @@ def run_ours(a, dist):
         out["cpu_baseline"] = cpu
     g.close()
     return out
+
+
+def fp64_roofline(cfdl, prof, ne, nf, nbf, W, peaks):
+    """FP64-pipe roofline of the kernels the flops model covers: FP64
+    thread-instructions per launch / average launch time (the profile pass's
+    CUDA events) against the probe's measured DFMA rate, beside each kernel's
+    HBM fraction (its algorithmic bytes over the same time)."""
+    from bytes_model import kernel_bytes
+    try:
+        from flops_model import fp64_inst
+        rate, probe_ms = cfdl.probe_fp64()
+    except Exception as e:          # no model or no probe: no FP64 ceiling in the line
+        return {"unavailable": str(e)[:200]}
+    rows = {}
+    for k, (launches, ms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+        inst = fp64_inst(k, ne, nf, nbf, W)
+        if not inst or not launches:
+            continue
+        t = ms / launches / 1e3
+        nb = kernel_bytes(k, ne, nf, nbf, W)
+        rows[k] = {"fp64_inst_per_launch": inst, "avg_launch_us": round(t * 1e6, 2),
+                   "fp64_frac": round(inst / t / rate, 3),
+                   "hbm_frac": round(nb / t / 1e9 / peaks["hbm_gbs"], 3) if nb else None}
+    return {"peak_fp64_inst_per_s": rate, "peak_fp64_tflops": 2 * rate / 1e12, "probe_ms": probe_ms,
+            "peak_source": "measured (cfdl_probe_fp64: DFMA chains on every SM)", "kernels": rows}
 
 
 # ---------------------------------------------------------- CPU reference
@@ -930,7 +963,11 @@ def run_setup(a, dist):
 # ------------------------------------------------------------ served stream
 def run_served(a, dist):
     """A Poisson stream of cavity requests through the serving loop; one JSON
-    line per (form, rate) with p50/p99 latency and throughput."""
+    line per (form, rate) with p50/p99 latency and throughput.  The first
+    --err-sample requests of every stream are the same cases (the stream draws
+    each request's mesh and Reynolds number before its arrival time), so their
+    FP64 converged states are computed once (converged_reference) and each
+    line reports those requests' relative L2 error against them."""
     import threading
     import numpy as np
     import cfdl
@@ -942,19 +979,31 @@ def run_served(a, dist):
         lo, hi = (int(x) for x in a.n_range.split(","))
         kw = dict(n_lo=lo, n_hi=hi)
     lines = []
+    ref, t_ref = None, 0.0
+    nerr = min(a.err_sample, a.requests)
+    if nerr > 0:
+        sample = workloads.served_requests(seed=a.seed, count=a.requests, rate=1.0, **kw)[:nerr]
+        setups = [cfdl.Setup(cfdl.Zone(r["n"], r["tet"], 0.0, seed=a.seed)) for r in sample]
+        t0 = time.perf_counter()
+        ref, ref_stats, _ = converged_reference(setups, sample, a.ref_tol, 4 * a.max_outer)
+        t_ref = time.perf_counter() - t0
+        ref_ne = [s_.ne for s_ in setups]
+        ref_conv = int(sum(st.converged for st in ref_stats))
+        del setups
     for prec in [int(x) for x in a.forms.split(",")]:
         for rate in [float(x) for x in a.rates.split(",")]:
             reqs = workloads.served_requests(seed=a.seed, count=a.requests, rate=rate, **kw)
             srv = cfdl.Server(precision=prec, hbm_budget=150e9)
             t_start = srv.now()
+            rids = []
 
             def feeder():
-                for r in reqs:
+                for k, r in enumerate(reqs):
                     delay = t_start + r["t"] - srv.now()
                     if delay > 0:
                         time.sleep(delay)
-                    srv.submit(n=r["n"], tet=r["tet"], jitter=0.0, seed=a.seed, re=r["re"],
-                               conv_tol=a.conv_tol, max_outer=a.max_outer)
+                    rids.append(srv.submit(n=r["n"], tet=r["tet"], jitter=0.0, seed=a.seed, re=r["re"],
+                                           conv_tol=a.conv_tol, max_outer=a.max_outer, keep_fields=k < nerr))
 
             clocks = Clocks(dist.local)
             clocks.start()
@@ -965,6 +1014,13 @@ def run_served(a, dist):
             clk = clocks.stop()
             res = srv.poll(max_results=4 * len(reqs))
             info = srv.info()
+            errs = []
+            for k in range(nerr):
+                e = {}
+                for f in ("u", "v", "w", "p"):
+                    x, r_ = srv.fields(rids[k], f)[:ref_ne[k]], ref[k][f][:ref_ne[k]]
+                    e[f] = float(np.linalg.norm(x - r_) / max(np.linalg.norm(r_), 1e-300))
+                errs.append(max(e.values()))
             srv.close()
             lat = np.array([r.t_done - r.t_submit for r in res])
             dev = np.array([r.t_done - r.t_admit for r in res])
@@ -991,6 +1047,11 @@ def run_served(a, dist):
                                      "max": int(max(r.outer_done for r in res))},
                 "launches": info["launches"], "makespan_s": span,
             }
+            if nerr:
+                out["rel_l2_vs_fp64_converged"] = {
+                    "requests": nerr, "max": max(errs), "median": float(np.median(errs)),
+                    "reference": "each request's case, FP64, to mass ratio <= %.0e (%d of %d converged, %.0f s)"
+                                 % (a.ref_tol, ref_conv, nerr, t_ref)}
             if clk:
                 out["clocks"] = clk
             lines.append(out)

@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--max-outer", type=int, default=1000, help="served: outer-iteration cap per request")
     ap.add_argument("--conv-tol", type=float, default=1e-6, help="served/converged: mass-ratio tolerance")
     ap.add_argument("--ref-tol", type=float, default=1e-11, help="converged: mass ratio of the FP64 reference")
+    ap.add_argument("--field-tol", type=float, default=1e-6, help="converged: rel L2 target against the reference")
+    ap.add_argument("--chunk", type=int, default=20, help="converged: outer iterations between field checks")
     ap.add_argument("--n-range", default="", help="batched/served: override the mesh-edge range lo,hi")
     return ap.parse_args()
 
@@ -613,13 +615,19 @@ def converged_reference(setups, cases, tol, cap):
 
 
 def run_converged(a, dist):
-    """The mixed forms against plain FP64 on the same converged target: the
+    """The mixed forms against plain FP64 on one converged target: the
     batched cases (64 uneven cavities, N~U{16..64}, half tet-split, Re
-    log-U[10,1000]) each run until their mass ratio reaches --conv-tol, all in
-    one graph launch (cfdl_run); the time of that launch is the time to
-    solution.  Per case, the relative L2 of u, v, w, p against the FP64
-    converged state (converged_reference) is reported, its maximum over the
-    cases in the line.  One JSON line per form."""
+    log-U[10,1000]) until each case's u, v, w and p are within --field-tol
+    (relative L2, default 1e-6) of its FP64 converged state
+    (converged_reference).  A first, untimed pass runs each form in chunks of
+    --chunk outer iterations and records per case the first chunk end at
+    which its fields are within the tolerance (the case is then stopped).  The
+    timed pass runs a fresh batch of the form with exactly those per-case
+    iteration counts in one graph launch (cfdl_run): its device time is the
+    form's time to solution.  A case's arithmetic does not depend on the
+    other cases in the batch, so the timed pass ends on the fields the first
+    pass checked; the line reports their errors again from the timed pass.
+    One JSON line per form."""
     import numpy as np
     import cfdl
     import workloads
@@ -631,67 +639,90 @@ def run_converged(a, dist):
         kw = dict(n_lo=lo, n_hi=hi)
     cases = workloads.batched_cases(seed=a.seed, count=a.cases, **kw)
     setups = workloads.build_setups(cases)
-    total_cells = sum(s.ne for s in setups)
+    total_cells = sum(s_.ne for s_ in setups)
     cap = a.max_outer
     t0 = time.perf_counter()
     ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, 4 * cap)
     t_ref = time.perf_counter() - t0
+
+    def errors(b, ids, which):
+        out = {}
+        for k in which:
+            e = 0.0
+            for f in ("u", "v", "w", "p"):
+                x, r = b.case_get(ids[k], f)[:setups[k].ne], ref[k][f][:setups[k].ne]
+                e = max(e, float(np.linalg.norm(x - r) / max(np.linalg.norm(r), 1e-300)))
+            out[k] = e
+        return out
+
     lines, t_fp64 = [], None
     for prec in [int(x) for x in a.forms.split(",")]:
         cfgs = [cfdl.steady(mu=1.0 / c["re"], precision=prec) for c in cases]
         b = cfdl.Batch(setups, cfgs)
         best, _ = b.autotune(outer=2)
-        # fresh state after the tuner's trial passes, then the warm-up pass
-        # that builds the run graph is not needed: the timed launch builds it
-        # once outside the timing (set_run + run(0) primes it)
         b.close()
+        # pass 1: iterations each case needs (chunk granularity), untimed
         b = cfdl.Batch(setups, cfgs)
         b.set_tile(best)
-        b.set_run(cap, 0, a.conv_tol)
-        b.run(0)
+        ids = b.ids()
+        need, last_err, done_it = {}, {}, 0
+        todo = list(range(len(ids)))
+        while todo and done_it < cap:
+            step = min(a.chunk, cap - done_it)
+            for k in range(len(ids)):
+                b.set_run(step if k in todo else 0, 0, 0.0, cid=ids[k])
+            b.run(step)
+            done_it += step
+            errs = errors(b, ids, todo)
+            last_err.update(errs)
+            for k, e in errs.items():
+                if e <= a.field_tol:
+                    need[k] = done_it
+            todo = [k for k in todo if k not in need]
+        b.close()
+        for k in todo:                   # not within the tolerance by the cap: run to the cap
+            need[k] = cap
+        # pass 2: the timed run with those iteration counts
+        b = cfdl.Batch(setups, cfgs)
+        b.set_tile(best)
+        ids = b.ids()
+        for k in range(len(ids)):
+            b.set_run(need[k], 0, 0.0, cid=ids[k])
+        b.run(0)                         # builds the run graph outside the timing
         clocks = Clocks(dist.local)
         dist.barrier()
         clocks.start()
         l0 = b.launch_count()
         b.timer_begin()
-        left = b.run(cap)
+        left = b.run(max(need.values()))
         ms = b.timer_end()
         launches = b.launch_count() - l0
         clk = clocks.stop()
         ms = dist.max(ms)
-        ids = b.ids()
-        stats = [b.case_stats(c) for c in ids]
-        errs = []
-        for k, c in enumerate(ids):
-            e = {}
-            for f in ("u", "v", "w", "p"):
-                x, r = b.case_get(c, f)[:setups[k].ne], ref[k][f][:setups[k].ne]
-                e[f] = float(np.linalg.norm(x - r) / max(np.linalg.norm(r), 1e-300))
-            errs.append(e)
+        final = errors(b, ids, range(len(ids)))
         b.close()
-        iters = [st.outer_done for st in stats]
-        cell_iters = sum(s.ne * n for s, n in zip(setups, iters))
-        worst = {f: max(e[f] for e in errs) for f in ("u", "v", "w", "p")}
+        iters = [need[k] for k in range(len(ids))]
+        cell_iters = sum(s_.ne * n for s_, n in zip(setups, iters))
+        errs = list(final.values())
         if prec == 0:
             t_fp64 = ms
         out = {
-            "metric": "batched time to the converged state", "value": ms / 1e3, "unit": "s",
-            "higher_is_better": False, "n_gpus": dist.world, "dtype": DTYPES[prec],
+            "metric": "batched time to the FP64 converged fields within %.0e" % a.field_tol, "value": ms / 1e3,
+            "unit": "s", "higher_is_better": False, "n_gpus": dist.world, "dtype": DTYPES[prec],
             "data": "synthetic (seeded cavity meshes)",
             "config": {"workload": "batched to convergence: %d lid-driven cavity cases, N~U{%d..%d} (seed %d), half "
-                                   "tet-split, Re log-U[10,1000], each run until mass ratio <= %.0e (cap %d), "
-                                   "one graph launch" %
+                                   "tet-split, Re log-U[10,1000], each run until u, v, w, p are within %.0e (rel L2) "
+                                   "of its FP64 converged state, one graph launch" %
                                    (len(cases), min(c["n"] for c in cases), max(c["n"] for c in cases), a.seed,
-                                    a.conv_tol, cap),
-                       "cases": len(cases), "cells": total_cells, "tile": best, "conv_tol": a.conv_tol,
-                       "reference": "FP64 GPU batch to mass ratio <= %.0e (%d cases converged, %.0f s)" %
-                                    (a.ref_tol, sum(st.converged for st in ref_stats), t_ref)},
+                                    a.field_tol),
+                       "cases": len(cases), "cells": total_cells, "tile": best, "chunk": a.chunk, "cap": cap,
+                       "reference": "the FP64 form to mass ratio <= %.0e (%d of %d cases reached it, %.0f s)" %
+                                    (a.ref_tol, sum(st.converged for st in ref_stats), len(cases), t_ref)},
             "cell_iters_per_s": cell_iters / (ms / 1e3),
-            "converged": int(sum(st.converged for st in stats)), "not_finished": left,
+            "cases_within_tol": int(sum(e <= a.field_tol for e in errs)), "not_finished": left,
             "outer_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters)),
                                  "total_cell_iters": cell_iters},
-            "rel_l2_vs_fp64_converged_max_over_cases": worst,
-            "all_cases_within_1e-6": bool(max(worst.values()) <= 1e-6),
+            "rel_l2_vs_fp64_converged": {"max": max(errs), "median": float(np.median(errs))},
             "gpu_launches": launches,
         }
         if t_fp64 is not None and prec != 0:

@@ -84,11 +84,12 @@ def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
         "jac": 4 * s * n + W * s * n + ell_i,               # t, r, w/D in; z out; ELL values and indices
         "resid": 4 * s * n + W * s * n + ell_i,             # z, r, D in; t out
         "prolong": (4 * s + 4) * n + W * s * n + ell_i + n_next * s,   # z, r, w/D, agg in; t out; coarse z
+        "lift": (2 * s + 4) * n + n_next * s,               # z in and out, agg in; coarse z
         "restrict": n_prev * (s + 4) + n * (4 + s),     # into this level from the finer one
     }[kind]
 
 
-def amg_kernel_bytes(name, levels, s):
+def amg_kernel_bytes(name, levels, s, tail_rows=2048):
     """Multigrid and CG-around-multigrid kernels.  levels = [(n_l, W_l)] for
     l = 0 (mesh) .. L (coarsest); s = value size (8 for the FP64 form, 4 for
     the FP32 inner solve of the mixed form).  Kernels suffixed _f run on the
@@ -104,6 +105,19 @@ def amg_kernel_bytes(name, levels, s):
     }
     if name in fixed:
         return fixed[name]
+    if name == "k_v_tail":
+        # a case's levels of at most tail_rows rows, down and back up, and its
+        # coarsest solve (dense inverse times the residual)
+        lt = next((l for l in range(1, L + 1) if levels[l][0] <= tail_rows), L) if L >= 1 else 0
+        b = 0
+        for l in range(lt, L):
+            n, w = levels[l]
+            nn = levels[l + 1][0]
+            b += _vcycle_level_bytes("jac0", n, w, s) + 3 * _vcycle_level_bytes("jac", n, w, s)
+            b += _vcycle_level_bytes("resid", n, w, s) + _vcycle_level_bytes("restrict", nn, 0, s, n_prev=n)
+            b += _vcycle_level_bytes("lift", n, w, s, n_next=nn)
+        nL = levels[L][0]
+        return b + nL * nL * s + 2 * nL * s
     if not name.startswith("k_v_") or L < 1:
         return None
     kind, where = name[4:].rsplit("_", 1)

@@ -11,8 +11,10 @@
 //                    over each aggregate (P^T, P piecewise constant);
 //   coarsest level   dense inverse of (A_L + c 11^T), which is A_L's
 //                    pseudo-inverse on zero-sum right-hand sides;
-//   level l+1 -> l   prolongation (injection) fused into the first of two
-//                    damped-Jacobi sweeps.
+//   level l+1 -> l   prolongation (injection, scaled by kOverCorrect) added
+//                    in place, then two damped-Jacobi sweeps;
+//   small levels     a case's levels of at most kTailRows rows and its
+//                    coarsest solve run in one CTA (k_v_tail).
 // Pre- and post-smoothing match, so the preconditioner is symmetric and
 // positive semi-definite, as CG requires.  The coarse operators are rebuilt
 // at every pressure solve from the current coefficients (A_c = P^T A P).
@@ -288,8 +290,10 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
     P.t[i] = P.rd[i] * P.r[i];
 }
 
-// z = t + w D^-1 (r - A t).  kMesh: launched on the mesh level only
-template <class T, bool kMesh>
+// z = t + w D^-1 (r - A t).  kMesh: launched on the mesh level only.
+// kToT: the sweep from z into t instead (the first post-smoothing sweep,
+// after k_v_lift has added the prolongated coarse correction to z)
+template <class T, bool kMesh, bool kToT = false>
 __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
     const Tile tl = tiles[blockIdx.x];
@@ -298,13 +302,33 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
+    const T *x = kToT ? P.z : P.t;
+    T *y = kToT ? P.t : P.z;
     if (kMesh) {
-        const T off = offsum_mesh<T>(P, P.t, i);
-        P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], off);
+        const T off = offsum_mesh<T>(P, x, i);
+        y[i] = jacobi_step<T>(x[i], P.r[i], P.rd[i], off);
     } else {
         // the row's own values first: measured faster on the coarse levels
-        P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
+        y[i] = jacobi_step<T>(x[i], P.r[i], P.rd[i], offsum<T>(P, x, i));
     }
+}
+
+// z = z + s P z_{l+1}: the prolongated coarse correction, added in place.
+// With it as its own streaming pass, the sweep after it gathers each
+// neighbour's corrected value once instead of the neighbour's aggregate and
+// then the coarse value: the same values, a shorter load chain.
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_lift(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
+    const Tile tl = tiles[blockIdx.x];
+    const CaseDev &C = cases[tl.c];
+    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
+    const int i = tl.first + (int)threadIdx.x;
+    if (i >= tl.last) return;
+    const LP<T> P = level<T>(C, l);
+    const AmgLevelDev &L = C.lev[l];
+    const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
+    P.z[i] = P.z[i] + (T)kOverCorrect * zc[L.agg[i]];
 }
 
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
@@ -365,65 +389,11 @@ __global__ void __launch_bounds__(kTile) k_amg_gal(const CaseDev *__restrict__ c
     if (mixed) { L.dg32[I] = narrow_f32(dsum); L.rd32[I] = narrow_f32(kOmega / dsum); }
 }
 
-// t = x + w D^-1 (r - A x) with x = z + P z_{l+1} (prolongation on the fly),
-// on the mesh level: the W neighbour indices, then their aggregates, then the
-// values are loaded as three independent batches (no per-slot load chain)
-template <int W, class T, bool kGuard = false, bool kEager = true>
-__device__ __forceinline__ T prolong_row(const LP<T> &P, const int *__restrict__ agg, const T *__restrict__ zc, T sc,
-                                         int i) {
-    int j[W], ag[W];
-    bool ok[W];
-    T c[W];
-#pragma unroll
-    for (int k = 0; k < W; k++) {
-        const bool in = !kGuard || k < P.W;
-        j[k] = in ? P.nb[k * P.n + i] : -1;
-        if (kEager) c[k] = in ? P.a[k * P.n + i] : (T)0;     // not waiting for the index
-        ok[k] = (unsigned)j[k] < (unsigned)P.n;
-        if (!ok[k]) j[k] = i;
-    }
-#pragma unroll
-    for (int k = 0; k < W; k++) ag[k] = agg[j[k]];
-    T s = 0;
-#pragma unroll
-    for (int k = 0; k < W; k++)
-        if (ok[k]) s += (kEager ? c[k] : P.a[k * P.n + i]) * (P.z[j[k]] + sc * zc[ag[k]]);
-    return s;
-}
-
-template <class T, bool kMesh>
-__global__ void __launch_bounds__(kTile) k_v_prolong(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
-    CFDL_PDL_WAIT();
-    const Tile tl = tiles[blockIdx.x];
-    const CaseDev &C = cases[tl.c];
-    if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
-    const int i = tl.first + (int)threadIdx.x;
-    if (i >= tl.last) return;
-    const LP<T> P = level<T>(C, l);
-    const AmgLevelDev &L = C.lev[l];
-    const T *zc = sizeof(T) == 8 ? (const T *)L.z : (const T *)L.z32;
-    const T sc = (T)kOverCorrect;
-    const T xi = P.z[i] + sc * zc[L.agg[i]];
-    T off;
-    if (P.W == 6) off = prolong_row<6, T, false, kMesh>(P, L.agg, zc, sc, i);
-    else if (P.W == 4) off = prolong_row<4, T, false, kMesh>(P, L.agg, zc, sc, i);
-    else if (kMesh) off = prolong_row<kMaxW, T, true>(P, L.agg, zc, sc, i);
-    else {
-        off = 0;
-        const int len = row_len(P, i);
-        for (int k = 0; k < len; k++) {
-            const int j = P.nb[k * P.n + i];
-            if (j >= 0 && j < P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[L.agg[j]]);
-        }
-    }
-    P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
-}
-
 // ------------------------------------------------- the V-cycle's tail
 // The small coarse levels of a case, from its tail level (the first level of
 // at most kTailRows rows) down to the coarsest and back, in one CTA: the
 // steps of k_v_jac0 / k_v_jac / k_v_resid / k_v_restrict, the coarsest solve
-// and k_v_prolong / k_v_jac, one row per thread per pass, with a block
+// and k_v_lift / k_v_jac, one row per thread per pass, with a block
 // barrier between steps.  Each step is a few microseconds of dependent loads
 // from L2; launched one by one, every step costs a kernel launch instead.
 // The CTA waits only at __syncthreads, on its own threads.
@@ -995,11 +965,13 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             GROUPED("k_v_prolong_c", k_vg_prolong, ctx->amg_gsmooth[l], 0, l)
             GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
         } else {
+            // z += s P z_{l+1}; t = J(z); z = J(t)
+            ALAUNCH(l ? "k_v_lift_c" : "k_v_lift_f", k_v_lift<T>, ctx->amg_smooth[l], l);
             if (l == 0) {
-                ALAUNCH("k_v_prolong_f", (k_v_prolong<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac<T, true, true>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_jac_f", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
             } else {
-                ALAUNCH("k_v_prolong_c", (k_v_prolong<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_c", (k_v_jac<T, false, true>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_jac_c", (k_v_jac<T, false>), ctx->amg_smooth[l], l);
             }
         }

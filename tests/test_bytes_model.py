@@ -45,3 +45,14 @@ def test_counts_grow_linearly_with_the_mesh():
         b = kernel_bytes(name, *hex_sizes(64), 6)
         assert 7.5 < b / a < 8.2, name     # interior faces 3n^2(n-1) grow a little faster than n^3
     assert kernel_bytes("no_such_kernel", *hex_sizes(8), 6) is None
+
+
+def test_lift_and_tail_counts():
+    """k_v_lift reads and writes z and reads the aggregate map (plus the coarse
+    vector); the tail sums its levels' passes and the dense coarsest solve."""
+    lv = [(4096, 6), (520, 20), (30, 12)]
+    assert amg_kernel_bytes("k_v_lift_f", lv, 8) == (16 + 4) * 4096 + 520 * 8
+    n, w, nn = 520, 20, 30
+    per_level = (3 * 8 * n + 3 * (4 * 8 * n + w * 8 * n + 4 * w * n) + (4 * 8 * n + w * 8 * n + 4 * w * n)
+                 + (n * (8 + 4) + nn * (4 + 8)) + ((16 + 4) * n + nn * 8))
+    assert amg_kernel_bytes("k_v_tail", lv, 8) == per_level + nn * nn * 8 + 2 * nn * 8

@@ -348,7 +348,7 @@ def run_ours(a, dist):
 
     cpu = None
     if not a.no_cpu and dist.rank == 0 and dist.world == 1:
-        cpu = cpu_baseline(zone, setup, budget_s=20.0)
+        cpu = cpu_baseline(a, budget_s=20.0)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": a.steps,
@@ -410,10 +410,20 @@ def fp64_roofline(cfdl, prof, ne, nf, nbf, W, peaks):
 
 
 # ---------------------------------------------------------- CPU reference
-def oracle_case(zone, setup):
+def oracle_case(a):
+    """The reference algorithm's case, built entirely by the oracle: its own
+    hex cavity zone (the same zone as the product's generator, tests/
+    test_setup.py) and its own restatement of the reference's set-up, four
+    subdomains, mode 0.  A tet-split mesh takes the product's zone as input
+    (the oracle has no tet generator) and still the oracle's own set-up."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    o = oracle_lib.Oracle(zone, n_subdomains=4, setup=setup)
+    if a.tet:
+        import cfdl
+        zone = cfdl.Zone(a.n, a.tet, a.jitter, seed=a.seed)
+    else:
+        zone = oracle_lib.BoxZone(a.n, a.jitter, a.seed)
+    o = oracle_lib.Oracle(zone, n_subdomains=4)
     o.physics_init(oracle_lib.steady(mode=0))
     return o, oracle_lib
 
@@ -441,14 +451,14 @@ def host_cpu():
     return {"cpu": model or "unknown", "nproc": os.cpu_count()}
 
 
-def cpu_baseline(zone, setup, budget_s=20.0):
+def cpu_baseline(a, budget_s=20.0):
     """The reference algorithm (CPU oracle, ref mode: Gauss-Seidel / 4-block
     SSOR inner solves, nsubd = 4) on the host's cores: its Gauss-Seidel
     sweeps are sequential, as in the reference; the loops whose iterations are
     independent (assembly, gradients, fluxes, corrections, the four pressure
     blocks) run on all host threads.  Timed over a bounded number of outer
     iterations of the same mesh."""
-    o, oracle_lib = oracle_case(zone, setup)
+    o, oracle_lib = oracle_case(a)
     t0 = time.perf_counter()
     o.run(1, 3)                       # untimed warm iteration
     t1 = time.perf_counter() - t0
@@ -465,10 +475,7 @@ def cpu_baseline(zone, setup, budget_s=20.0):
 def run_reference(a, dist):
     if dist.rank != 0:
         return None
-    import cfdl
-    zone = cfdl.Zone(a.n, a.tet, a.jitter, seed=a.seed)
-    setup = cfdl.Setup(zone)
-    o, oracle_lib = oracle_case(zone, setup)
+    o, oracle_lib = oracle_case(a)
     threads = oracle_lib.num_threads()
     t0 = time.perf_counter()
     o.run(1, 3)
@@ -928,16 +935,18 @@ def run_energy(a, dist):
 
 
 def cpu_energy_baseline(a, budget_s=15.0):
-    """The reference's solve_energy (CPU oracle, Gauss-Seidel to a 10x drop),
-    single thread, on a 32^3 sample of the same cavity after a few outer
-    passes; cells x solves / s."""
-    import cfdl
+    """The reference's solve_energy (CPU oracle, Gauss-Seidel to a 10x drop,
+    sequential like the reference), on a 32^3 sample of the same cavity
+    after a few outer passes; cells x solves / s."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     n = min(a.n, 32)
-    zone = cfdl.Zone(n, a.tet, a.jitter, seed=a.seed)
-    setup = cfdl.Setup(zone)
-    o = oracle_lib.Oracle(zone, n_subdomains=4, setup=setup)
+    if a.tet:
+        import cfdl
+        zone = cfdl.Zone(n, a.tet, a.jitter, seed=a.seed)
+    else:
+        zone = oracle_lib.BoxZone(n, a.jitter, a.seed)
+    o = oracle_lib.Oracle(zone, n_subdomains=4)
     o.physics_init(oracle_lib.steady(mode=0))
     o.energy_init()
     o.run(3, 0)

@@ -27,7 +27,16 @@
 namespace cfdl {
 namespace {
 
-constexpr double kOmega = 0.8;     // damped Jacobi weight
+// Damped-Jacobi weights of a level's two smoothing sweeps.  Pre-smoothing
+// runs the kOmega sweep from zero (k_v_jac0) and then the kOmega2 sweep;
+// post-smoothing runs the kOmega sweep from the prolongated value and then
+// the kOmega2 sweep.  Either way the error propagator is
+// (I - kOmega2 D^-1 A)(I - kOmega D^-1 A), the same polynomial in D^-1 A
+// before and after the coarse correction, so the V-cycle stays symmetric.
+// rd = kOmega / D is stored per level; the second sweep scales it by
+// kOmega2 / kOmega.
+constexpr double kOmega = 0.8;     // first sweep
+constexpr double kOmega2 = 0.8;    // second sweep
 constexpr double kOverCorrect = 3.0;   // scaling of the prolongated coarse correction
 constexpr int kG = 8;                  // lanes per row on the small coarse levels
 constexpr int kGroupedRows = 65536;    // levels below this many rows (per case) run grouped
@@ -174,9 +183,11 @@ template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *
     return s;
 }
 
-// damped Jacobi sweep from x: x + w D^-1 (r - A x) = (1 - w) x + (w/D)(r + offsum)
-template <class T> __device__ __forceinline__ T jacobi_step(T x, T r, T wrd, T off) {
-    return (T)(1.0 - kOmega) * x + wrd * (r + off);
+// damped Jacobi sweep from x: x + w D^-1 (r - A x) = (1 - w) x + (w/D)(r + offsum);
+// kSweep 1 with w = kOmega (wrd = rd as stored), 2 with w = kOmega2
+template <class T, int kSweep = 2> __device__ __forceinline__ T jacobi_step(T x, T r, T wrd, T off) {
+    if (kSweep == 1) return (T)(1.0 - kOmega) * x + wrd * (r + off);
+    return (T)(1.0 - kOmega2) * x + (wrd * (T)(kOmega2 / kOmega)) * (r + off);
 }
 
 __device__ __forceinline__ bool pactive(const CaseDev &C) { return C.sc->active_p != 0; }
@@ -306,10 +317,10 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
     T *y = kToT ? P.t : P.z;
     if (kMesh) {
         const T off = offsum_mesh<T>(P, x, i);
-        y[i] = jacobi_step<T>(x[i], P.r[i], P.rd[i], off);
+        y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], off);
     } else {
         // the row's own values first: measured faster on the coarse levels
-        y[i] = jacobi_step<T>(x[i], P.r[i], P.rd[i], offsum<T>(P, x, i));
+        y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], offsum<T>(P, x, i));
     }
 }
 
@@ -446,7 +457,7 @@ __global__ void __launch_bounds__(kTailThreads) k_v_tail(const CaseDev *__restri
                 const int j = P.nb[k * P.n + i];
                 if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[Lc.agg[j]]);
             }
-            P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
+            P.t[i] = jacobi_step<T, 1>(xi, P.r[i], P.rd[i], off);
         }
         __syncthreads();
         for (int i = threadIdx.x; i < P.n; i += nt) P.z[i] = jacobi_step<T>(P.t[i], P.r[i], P.rd[i], offsum<T>(P, P.t, i));
@@ -546,7 +557,7 @@ __global__ void __launch_bounds__(kTile) k_vg_prolong(const CaseDev *__restrict_
     off = group_sum<G>(off);
     if (ok && g == 0) {
         const T xi = P.z[i] + sc * zc[L.agg[i]];
-        P.t[i] = jacobi_step<T>(xi, P.r[i], P.rd[i], off);
+        P.t[i] = jacobi_step<T, 1>(xi, P.r[i], P.rd[i], off);
     }
 }
 

@@ -131,6 +131,10 @@ void or_calc_coef_energy(ocase *c);                  /* mod_energy.f90:82-169 */
 void or_solve_energy(ocase *c, or_stats *st);        /* mod_energy.f90:59-80  */
 
 /* Timing helper for the CPU baseline: monotonic seconds. */
+/* the hex cavity zone in CGNS shape (cfd_oracle_zone.c); sizes = nvx, nelem, nsec, ne2vxmax */
+int or_box_zone_sizes(int n, int *sizes);
+int or_box_zone_fill(int n, double jitter, uint64_t seed, double *x, double *y, double *z, int *e2vx,
+                     int *etype, int *esec, char *names);
 double or_wtime(void);
 int or_num_threads(void);
 void or_set_num_threads(int n);

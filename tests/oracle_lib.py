@@ -81,6 +81,8 @@ def lib():
         L.or_solve_energy.restype = None
         L.or_wtime.restype = C.c_double
         L.or_num_threads.restype = C.c_int
+        L.or_box_zone_sizes.argtypes = [C.c_int, vp]
+        L.or_box_zone_fill.argtypes = [C.c_int, C.c_double, C.c_uint64] + [vp] * 6 + [C.c_char_p]
         L.or_set_num_threads.argtypes = [C.c_int]
         L.or_set_num_threads.restype = None
         _lib = L
@@ -258,6 +260,28 @@ class Oracle:
 
 def wtime():
     return lib().or_wtime()
+
+
+class BoxZone:
+    """The hex cavity zone made by the oracle (cfd_oracle_zone.c): the same
+    attributes as the product's Zone, so an Oracle can be built from it
+    without the GPU library."""
+
+    def __init__(self, n, jitter=0.0, seed=0):
+        L = lib()
+        sz = np.zeros(4, np.int32)
+        if L.or_box_zone_sizes(int(n), _p(sz)) != 0:
+            raise ValueError("zone size out of range")
+        self.nvx, self.nelem, self.nsec, self.ne2vxmax = (int(v) for v in sz)
+        self.x, self.y, self.z = (np.zeros(self.nvx) for _ in range(3))
+        self.e2vx = np.zeros(self.ne2vxmax * self.nelem, np.int32)
+        self.etype = np.zeros(self.nsec, np.int32)
+        self.esec = np.zeros(2 * self.nsec, np.int32)
+        buf = C.create_string_buffer(33 * self.nsec)
+        if L.or_box_zone_fill(int(n), float(jitter), int(seed), _p(self.x), _p(self.y), _p(self.z), _p(self.e2vx),
+                              _p(self.etype), _p(self.esec), buf) != 0:
+            raise RuntimeError("or_box_zone_fill failed")
+        self.names = buf.raw
 
 
 def sha256(a):

@@ -263,3 +263,15 @@ def test_mesh_check_refuses_corrupted_meshes():
     assert refused(bc_esec=esec)
     assert s.check() == 0                                    # the originals are untouched
     assert L.cfdl_mesh_check(None) == 1
+
+
+@pytest.mark.parametrize("n,jit,seed", [(1, 0.0, 0), (5, 0.2, 7), (8, 0.0, 0), (12, 0.2, 3)])
+def test_oracle_zone_equals_product_zone(n, jit, seed):
+    """The oracle's own hex cavity zone (used where an oracle run must not
+    load the GPU library, as the benchmark's reference arm) is the product's
+    synthetic zone, bit for bit."""
+    a, b = cfdl.Zone(n, False, jit, seed=seed), oracle_lib.BoxZone(n, jit, seed)
+    assert (a.nvx, a.nelem, a.nsec, a.ne2vxmax) == (b.nvx, b.nelem, b.nsec, b.ne2vxmax)
+    for f in ("x", "y", "z", "e2vx", "etype", "esec"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    assert a.names.raw == b.names

@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--ref-tol", type=float, default=1e-11, help="converged: mass ratio of the FP64 reference")
     ap.add_argument("--field-tol", type=float, default=1e-6, help="converged: rel L2 target against the reference")
     ap.add_argument("--chunk", type=int, default=20, help="converged: outer iterations between field checks")
+    ap.add_argument("--conv-cap", type=int, default=16000, help="converged: outer-iteration cap per case")
     ap.add_argument("--n-range", default="", help="batched/served: override the mesh-edge range lo,hi")
     return ap.parse_args()
 
@@ -647,9 +648,9 @@ def run_converged(a, dist):
     cases = workloads.batched_cases(seed=a.seed, count=a.cases, **kw)
     setups = workloads.build_setups(cases)
     total_cells = sum(s_.ne for s_ in setups)
-    cap = a.max_outer
+    cap = a.conv_cap
     t0 = time.perf_counter()
-    ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, 4 * cap)
+    ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, cap)
     t_ref = time.perf_counter() - t0
 
     def errors(b, ids, which):
@@ -668,6 +669,8 @@ def run_converged(a, dist):
         b = cfdl.Batch(setups, cfgs)
         best, _ = b.autotune(outer=2)
         b.close()
+        # check every --chunk outer iterations, then every 5% of those done:
+        # a case's count is at most that much above the least it needs
         # pass 1: iterations each case needs (chunk granularity), untimed
         b = cfdl.Batch(setups, cfgs)
         b.set_tile(best)
@@ -675,7 +678,7 @@ def run_converged(a, dist):
         need, last_err, done_it = {}, {}, 0
         todo = list(range(len(ids)))
         while todo and done_it < cap:
-            step = min(a.chunk, cap - done_it)
+            step = min(max(a.chunk, done_it // 20), cap - done_it)
             for k in range(len(ids)):
                 b.set_run(step if k in todo else 0, 0, 0.0, cid=ids[k])
             b.run(step)

@@ -1,33 +1,49 @@
-"""FP64 thread-instructions per launch of the FP64-bound kernels.
+"""FP64 thread-instructions per launch of the kernels that do FP64 arithmetic.
 
-GB300 issues about two FP64 thread-instructions per SM per clock, so the
-assembly kernels of the outer iteration (one face or cell term after another,
-each a handful of FP64 multiplies and adds) are bound by the FP64 pipe before
-they are bound by HBM.  Each figure counts DADD, DMUL and DFMA (one pipe slot
-each) and the FP64 instructions of the compiler's division sequence, per
-unit of work, as the kernel source does them; W = faces per cell, ne cells,
-nf faces, nbf boundary faces (steady form, W = 6 or 4).
+GB300 issues about two FP64 thread-instructions per SM per clock (the
+cfdl_probe_fp64 DFMA probe measures 0.63 T instructions/s, 1.25 TFLOP/s), so
+the assembly kernels of the outer iteration are bound by the FP64 pipe before
+they are bound by HBM.  The per-unit figures are the FP64 instructions the
+kernels execute (DADD, DMUL, DFMA and the rest of the double-precision
+class, each one pipe slot), as ncu counted them
+(sm__sass_thread_inst_executed_op_fp64_pred_on) on the 48^3 hex cavity
+(profiles/fp64_instructions_cavity48.md); the source of each kernel accounts
+for them:
+
+  k_coef_uvw_face  40 per interior face: 1 - wt, nine gradient
+                   interpolations (2 each), three components of
+                   G^T A + G E (7 each)
+  k_calc_mip       21 per interior face: velocity and pressure-gradient
+                   interpolation, the flux and the Rhie-Chow correction
+  k_coef_uvw_cell  70 per cell (6 per slot, the three right-hand sides, the
+                   relaxation, the divisions of d and dc) and about 50 per
+                   wall face (unit normal, tangential slip, wall terms)
+  k_grad<N>        4 per slot and field (a difference and three FMAs)
+  k_mom_*          BiCGStab with three active right-hand sides
+  k_v_* , k_apc_q  the pressure solve's mesh-level rows
+
+W = faces per cell; per-cell figures of the W-slot rows are scaled from the
+hex counts by W / 6.
 """
-
-DIV = 9          # FP64 instructions of one IEEE division sequence (reciprocal seed and Newton steps)
 
 
 def fp64_inst(name, ne, nf, nbf, W):
     nfi = nf - nbf
+    w = W / 6.0
     table = {
-        # per interior face: 1 - wt, nine gradient interpolations (2 each), three
-        # components of (G^T A + G E) (3 + 3 + 1 each)
-        "k_coef_uvw_face": nfi * (1 + 18 + 21),
-        # per cell: 6 per interior slot (upwind sum, ap, sumf, three explicit sums),
-        # bu/bv/bw (3 each), relaxation (6), d and dc (two divisions and a subtraction);
-        # per wall face of a cell: unit normal (3 divisions), tangential slip and the
-        # wall terms (about 20)
-        "k_coef_uvw_cell": ne * (6 * W + 9 + 6 + 2 * DIV + 1) + nbf * (3 * DIV + 20),
-        # per interior face: 1 - wt, velocity interpolation (6), flux (4), Rhie-Chow:
-        # pressure-gradient interpolation (6), d_ip (2), the correction (8)
-        "k_calc_mip": nfi * (1 + 6 + 4 + 6 + 2 + 8),
-        # per cell and slot: a difference and three FMAs for each of the three fields
-        "k_grad3": ne * W * 12,
-        "k_grad1": ne * W * 4,
+        "k_coef_uvw_face": 40 * nfi,
+        "k_calc_mip": 21 * nfi,
+        "k_coef_uvw_cell": 70 * ne + 50 * nbf,
+        "k_grad3": 12 * W * ne,
+        "k_grad1": 4 * W * ne,
+        "k_mom_init": 42.7 * w * ne,
+        "k_mom_v": 26.5 * w * ne,
+        "k_mom_t": 31.3 * w * ne,
+        "k_mom_x": 17.3 * ne,
+        "k_mom_s": 8.8 * ne,
+        "k_v_jac_f": 9.0 * w * ne,
+        "k_v_resid_f": 8.0 * w * ne,
+        "k_apc_q": 9.3 * w * ne,
     }
-    return table.get(name)
+    v = table.get(name)
+    return int(round(v)) if v is not None else None

@@ -56,3 +56,18 @@ def test_lift_and_tail_counts():
     per_level = (3 * 8 * n + 3 * (4 * 8 * n + w * 8 * n + 4 * w * n) + (4 * 8 * n + w * 8 * n + 4 * w * n)
                  + (n * (8 + 4) + nn * (4 + 8)) + ((16 + 4) * n + nn * 8))
     assert amg_kernel_bytes("k_v_tail", lv, 8) == per_level + nn * nn * 8 + 2 * nn * 8
+
+
+def test_flops_model_matches_the_counted_instructions():
+    """The FP64 model against ncu's counted FP64 instructions on the 48^3 hex
+    cavity (profiles/fp64_instructions_cavity48.md): within 2% for each
+    kernel the model covers."""
+    from flops_model import fp64_inst
+    ne, nf, nbf = hex_sizes(48)
+    counted = {"k_coef_uvw_face": 12994560, "k_coef_uvw_cell": 8432640, "k_grad3": 7962624,
+               "k_calc_mip": 6822144, "k_mom_init": 4718392, "k_mom_t": 3464964, "k_mom_v": 2930573,
+               "k_grad1": 2654208, "k_mom_x": 1916710, "k_apc_q": 1026012, "k_v_jac_f": 995328,
+               "k_mom_s": 976779, "k_v_resid_f": 884736}
+    for k, c in counted.items():
+        m = fp64_inst(k, ne, nf, nbf, 6)
+        assert abs(m - c) <= 0.02 * c, (k, m, c)

@@ -34,9 +34,15 @@ namespace {
 // (I - kOmega2 D^-1 A)(I - kOmega D^-1 A), the same polynomial in D^-1 A
 // before and after the coarse correction, so the V-cycle stays symmetric.
 // rd = kOmega / D is stored per level; the second sweep scales it by
-// kOmega2 / kOmega.
-constexpr double kOmega = 0.8;     // first sweep
-constexpr double kOmega2 = 0.8;    // second sweep
+// kOmega2 / kOmega.  The two weights are the reciprocals of the roots of the
+// degree-2 Chebyshev polynomial on [0.6, 2] (D^-1 A of these zero-row-sum
+// M-matrices has its spectrum in [0, 2]): the pair damps the upper part of
+// the spectrum more than two sweeps of one weight.  Measured on the 128^3
+// cavity against 0.8 / 0.8: 2% less time per outer iteration, FP64 and
+// mixed alike (Chebyshev on [0.5, 2] 1%, [0.4, 2] 1% more; a coarse
+// over-correction of 2 instead of 3: 22% more).
+constexpr double kOmega = 0.557;   // first sweep
+constexpr double kOmega2 = 1.242;  // second sweep
 constexpr double kOverCorrect = 3.0;   // scaling of the prolongated coarse correction
 constexpr int kG = 8;                  // lanes per row on the small coarse levels
 constexpr int kGroupedRows = 65536;    // levels below this many rows (per case) run grouped

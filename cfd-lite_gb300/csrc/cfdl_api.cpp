@@ -649,6 +649,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 2 * w * c * 4 + 3 * w * c * 8;          // ELL connectivity, gradient stencil
     bytes += 2 * f * 4 + 16 * f * 8;                 // face tables, geometry planes
     bytes += 3 * b * 4 + 3 * b * 8 + c * 8;          // halo tables, volume
+    bytes += 4 * b * 8;                               // the BC loop's per-halo terms
     bytes += 8 * nc * 8 + 15 * nc * 8 + 2 * f * 8;   // cell fields, gradients, mip/mip0
     bytes += 9 * c * 8 + w * c * 8 + 4 * f * 8;      // coefficients, face intermediates
     bytes += 10 * f * 8;                              // property planes

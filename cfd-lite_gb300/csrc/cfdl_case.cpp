@@ -181,6 +181,7 @@ int upload_all(HostCase *hc, const cfdl_config *cfg, const FillVec<int> &hf_nb, 
     if ((st = zeros(hc, &d.frap_p, (size_t)ne))) return st;
     if ((st = zeros(hc, &d.fdiff, (size_t)nf))) return st;
     if ((st = zeros(hc, &d.fS, 3 * (size_t)nf))) return st;
+    if ((st = zeros(hc, &d.hbc, 4 * (size_t)nbf))) return st;
     if ((st = zeros(hc, &d.fprop, (size_t)PR_N * nf))) return st;
     double **kv[] = {&d.kr, &d.krh, &d.kp, &d.kph, &d.kv, &d.ks, &d.ksh, &d.kt};
     for (double **pp : kv) if ((st = zeros(hc, pp, 3 * (size_t)ne))) return st;

@@ -131,6 +131,8 @@ struct CaseDev {
     float *fdiag_p, *fanb_p, *frap_p;
     // face intermediates of the assemblies
     double *fdiff, *fS;                   // [nf] pressure face coefficient, [3][nf] explicit momentum face terms
+    double *hbc;                          // [4][nbf] per halo: the wall diffusion added to ap and anb, and the
+                                          // three momentum sources of the BC loop (k_coef_uvw_halo)
     double *fprop;                        // [PR_N][nf] property planes
     // precision 3 (FP32 explicit momentum face terms); null otherwise:
     float *g32;                           // [3][ne][3] FP32 gradients of u, v, w

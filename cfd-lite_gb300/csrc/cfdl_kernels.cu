@@ -147,26 +147,69 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_face_f32(const CaseDev *__re
         fS[m * nf + i] = (gi[0][m] * A0 + gi[1][m] * A1 + gi[2][m] * A2) + (gi[m][0] * E0 + gi[m][1] * E1 + gi[m][2] * E2);
 }
 
+// calc_coef_uvw, boundary-condition loop (mod_uvwp.f90:242-273), one thread
+// per halo: the wall diffusion mu*area/ds it adds to the owner's ap and to
+// the slot's anb, and for a wall ('dirichlet') the momentum source
+// d*(u_wall - u_tangential) - d*u of each component; a symmetry plane
+// ('zero_flux') adds the diffusion only.  The cell kernel gathers them.
+__global__ void __launch_bounds__(kTile) k_coef_uvw_halo(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+    CFDL_PDL_WAIT();
+    TILE_PROLOGUE(halos)
+    if (i >= t.last) return;
+    const int nbf = C.nbf, nf = C.nf, kind = C.h_kind[i];
+    double dbc = 0.0, s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    if (kind != 0) {
+        const int e = C.h_own[i], f = C.h_face[i], h = C.ne + i;
+        dbc = C.fprop[PR_FDIFF * nf + f];
+        if (kind == CFDL_BC_WALL) {
+            const double ue = C.u[e], ve = C.v[e], we = C.w[e];
+            const double area = C.fgeo[FG_AREA * nf + f];
+            const double n0 = C.fgeo[FG_AX * nf + f] / area, n1 = C.fgeo[FG_AY * nf + f] / area,
+                         n2 = C.fgeo[FG_AZ * nf + f] / area;
+            const double tn = ue * n0 + ve * n1 + we * n2;
+            const double r0 = C.u[h] - (ue - tn * n0), r1 = C.v[h] - (ve - tn * n1), r2 = C.w[h] - (we - tn * n2);
+            s0 = dbc * r0 - dbc * ue;
+            s1 = dbc * r1 - dbc * ve;
+            s2 = dbc * r2 - dbc * we;
+        }
+    }
+    C.hbc[i] = dbc;
+    C.hbc[nbf + i] = s0;
+    C.hbc[2 * nbf + i] = s1;
+    C.hbc[3 * nbf + i] = s2;
+}
+
 // calc_coef_uvw, cell part (mod_uvwp.f90:174-284) + implicit relaxation.
+// Interior slots first (their faces' terms), then the boundary slots' terms
+// of k_coef_uvw_halo, summed apart and added after the right-hand sides as
+// the reference's BC loop adds them after its cell loop.  Every slot is
+// indexed by an unrolled loop counter, so the row stays in registers.
 // F32 (precision 3): the explicit face terms are FP32 and summed in FP32.
 template <bool F32>
 __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
-    const int ne = C.ne, nf = C.nf, W = C.W;
+    const int ne = C.ne, nf = C.nf, nbf = C.nbf, W = C.W;
     double ap = 0.0, sumf = 0.0, ss0 = 0.0, ss1 = 0.0, ss2 = 0.0;
+    double bap = 0.0, bs0 = 0.0, bs1 = 0.0, bs2 = 0.0;   // the boundary slots' terms
     float fs0 = 0.f, fs1 = 0.f, fs2 = 0.f;
     const float *fS32 = (const float *)C.fS;
     double a[kMaxW];
-    int bslot[kMaxW], nb_cnt = 0;
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
         a[k] = 0.0;
         if (k >= W) continue;
         const int nb = C.hf_nb[k * ne + i];
         if (nb < 0) continue;
-        if (nb >= ne) { bslot[nb_cnt++] = k; continue; }
+        if (nb >= ne) {
+            const int q = nb - ne;
+            const double dbc = C.hbc[q];
+            a[k] = dbc;                 // anb of a boundary slot is 0 before the BC loop: 0 + d = d
+            bap += dbc;
+            bs0 += C.hbc[nbf + q]; bs1 += C.hbc[2 * nbf + q]; bs2 += C.hbc[3 * nbf + q];
+            continue;
+        }
         const int fc = C.hf_fc[k * ne + i], f = face_of(fc);
         // inward flux f = -sg*mip and upwind max(f,0): sign and comparison on
         // the bit pattern, so they cost no FP64 instruction
@@ -199,30 +242,10 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
         bv = ap0 * C.v0[i] + sumf * ve - vol * C.gp[3 * i + 1] + ss1;
         bw = ap0 * C.w0[i] + sumf * we - vol * C.gp[3 * i + 2] + ss2;
     }
-    // boundary conditions in BC-loop order (ascending halo index)
-    for (int q = 1; q < nb_cnt; q++) {
-        int s = bslot[q], j = q - 1;
-        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
-        bslot[j + 1] = s;
-    }
-    for (int q = 0; q < nb_cnt; q++) {
-        const int k = bslot[q], h = C.hf_nb[k * ne + i], f = face_of(C.hf_fc[k * ne + i]);
-        const int kind = C.h_kind[h - ne];
-        if (kind == 0) continue;
-        const double dbc = C.fprop[PR_FDIFF * nf + f];
-        if (kind == CFDL_BC_WALL) {
-            const double area = C.fgeo[FG_AREA * nf + f];
-            const double n0 = C.fgeo[FG_AX * nf + f] / area, n1 = C.fgeo[FG_AY * nf + f] / area, n2 = C.fgeo[FG_AZ * nf + f] / area;
-            const double tn = ue * n0 + ve * n1 + we * n2;
-            const double r0 = C.u[h] - (ue - tn * n0), r1 = C.v[h] - (ve - tn * n1), r2 = C.w[h] - (we - tn * n2);
-            bu = bu + dbc * r0 - dbc * ue;
-            bv = bv + dbc * r1 - dbc * ve;
-            bw = bw + dbc * r2 - dbc * we;
-        }
-        ap = ap + dbc;
-        asum = asum + dbc;
-        a[k] = a[k] + dbc;
-    }
+    // the boundary-condition loop's additions
+    ap = ap + bap;
+    asum = asum + bap;
+    bu = bu + bs0; bv = bv + bs1; bw = bw + bs2;
     if (C.alpha_u != 1.0) {
         const double apr = ap * C.ralpha_u, f1 = (1.0 - C.alpha_u) * apr;
         bu = bu + f1 * ue; bv = bv + f1 * ve; bw = bw + f1 * we;
@@ -566,10 +589,12 @@ void launch_coef_uvw(cfdl_ctx *ctx) {
     for (HostCase *hc : ctx->cases) hc->coef_is_pressure = false;
     if (f32_assembly(ctx)) {
         ensure_g32(ctx);
+        CFDL_LAUNCH("k_coef_uvw_halo", k_coef_uvw_halo, halos);
         CFDL_LAUNCH("k_coef_uvw_face_f32", k_coef_uvw_face_f32, faces);
         CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell<true>, cells);
         return;
     }
+    CFDL_LAUNCH("k_coef_uvw_halo", k_coef_uvw_halo, halos);
     CFDL_LAUNCH("k_coef_uvw_face", k_coef_uvw_face, faces);
     CFDL_LAUNCH("k_coef_uvw_cell", k_coef_uvw_cell<false>, cells);
 }

@@ -67,13 +67,18 @@ __device__ __forceinline__ void mom_init_row(const CaseDev &C, int i, int ne, do
         a[k] = j >= 0 ? C.anb[k * ne + i] : 0.0;
     }
     const double api = C.ap[i];
-    C.rap[i] = 1.0 / api;                   // the Jacobi scaling of the whole solve, divided once
     if (m32) {                              // the operator in FP32 for the correction solve
-        C.fdiag[i] = narrow_f32(api);          // integer-pipe conversions (cfdl_device.cuh)
-        C.frap[i] = narrow_f32(1.0 / api);
+        // integer-pipe conversion (cfdl_device.cuh); the FP32 solve's Jacobi
+        // scaling is divided in FP32 (the FP64 1/ap would be one of the
+        // kernel's costliest FP64 sequences, for a preconditioner)
+        const float fa = narrow_f32(api);
+        C.fdiag[i] = fa;
+        C.frap[i] = 1.0f / fa;
 #pragma unroll
         for (int k = 0; k < W; k++)
             if (k < C.W) C.fanb[k * ne + i] = narrow_f32(a[k]);
+    } else {
+        C.rap[i] = 1.0 / api;               // the Jacobi scaling of the whole FP64 solve, divided once
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) {
@@ -373,8 +378,8 @@ __global__ void __launch_bounds__(kTile, 4) k_mom_x(const CaseDev *__restrict__ 
 template <int W>
 __device__ __forceinline__ void en_init_row(const CaseDev &C, int i, int ne, double (&v)[2], bool m32) {
     const double api = C.ap[i];
-    C.rap[i] = 1.0 / api;
-    if (m32) { C.fdiag[i] = narrow_f32(api); C.frap[i] = narrow_f32(1.0 / api); }
+    if (m32) { const float fa = narrow_f32(api); C.fdiag[i] = fa; C.frap[i] = 1.0f / fa; }
+    else C.rap[i] = 1.0 / api;
     const double *__restrict__ phi = C.ee;
     double bb = C.b[i], s = api * phi[i];
 #pragma unroll

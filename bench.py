@@ -278,7 +278,7 @@ def run_ours(a, dist):
     # the FP64 pipe's ceiling: the probe's DFMA rate on this device, and each
     # FP64-bound kernel's FP64 instructions per launch (flops_model) over its
     # average launch time from the profile pass above
-    fp64 = fp64_roofline(cfdl, prof, ne, nf, nbf, W, peaks)
+    fp64 = fp64_roofline(cfdl, prof, ne, nf, nbf, W, peaks) if a.precision == 0 else None
     breakdown = {k: {"launches": c, "ms": round(t, 3), "share": round(t / sum(v[1] for v in prof.values()), 4)}
                  for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
     if a.breakdown and dist.rank == 0:

@@ -62,7 +62,9 @@ int copy_named(cfdl_ctx *ctx, HostCase *hc, const char *name, double *host, bool
     if (!to_host) ctx->host_writes++;
     if (!to_host && (nm.ptr == hc->dev.rho || nm.ptr == hc->dev.mu)) hc->props_dirty = true;
     if (!to_host && nm.ptr && (nm.ptr == hc->dev.ecp || nm.ptr == hc->dev.etc)) hc->eprops_dirty = true;
-    if (!to_host && (nm.ptr == hc->dev.gu || nm.ptr == hc->dev.gv || nm.ptr == hc->dev.gw)) hc->g32_stale = true;
+    if (!to_host && (nm.ptr == hc->dev.gu || nm.ptr == hc->dev.gv || nm.ptr == hc->dev.gw || nm.ptr == hc->dev.gp ||
+                     nm.ptr == hc->dev.d))
+        hc->g32_stale = true;
     cudaError_t e;
     if (!nm.ell) {
         e = cudaMemcpyAsync(to_host ? (void *)host : (void *)nm.ptr, to_host ? (const void *)nm.ptr : (const void *)host,
@@ -101,7 +103,7 @@ int transfer_fields(cfdl_ctx *ctx, HostCase *hc, const cfdl_fields *f, bool to_h
         {f->gu, d.gu, 3 * nc}, {f->gv, d.gv, 3 * nc}, {f->gw, d.gw, 3 * nc}, {f->gp, d.gp, 3 * nc}, {f->gpc, d.gpc, 3 * nc},
         {f->mip, d.mip, nf}, {f->mip0, d.mip0, nf},
     };
-    if (!to_host && (f->gu || f->gv || f->gw)) hc->g32_stale = true;   // precision 3 derives g32 from them
+    if (!to_host && (f->gu || f->gv || f->gw || f->gp)) hc->g32_stale = true;   // precision 3 derives g32, gp32 from them
     for (const P &p : list) {
         if (!p.h) continue;
         if (!to_host) ctx->host_writes++;

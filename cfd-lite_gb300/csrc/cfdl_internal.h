@@ -137,7 +137,10 @@ struct CaseDev {
     // precision 3 (FP32 explicit momentum face terms); null otherwise:
     float *g32;                           // [3][ne][3] FP32 gradients of u, v, w
     float *G32;                           // [3][W][ne] FP32 copy of the gradient stencil hf_G
-    float *fprop32;                       // [7][nf] FP32 weight, mu*area*dr/ds, mu*area*(dr_p/ds_p - dr/ds)
+    float *fprop32;                       // [11][nf] FP32 weight, mu*area*dr/ds, mu*area*(dr_p/ds_p - dr/ds),
+                                          // dr, rho_ip*area/(dr.n) (the Rhie-Chow term's planes)
+    float *gp32;                          // [ne][3] FP32 copy of gp, and d32 [ne] of d (the FP32 Rhie-Chow term)
+    float *d32;
     // Krylov work vectors, [3][ne] each (pressure uses plane 0)
     double *kr, *krh, *kp, *kph, *kv, *ks, *ksh, *kt;
     // FP32 work vectors for the mixed-precision pressure solve, [ne] each

@@ -110,13 +110,15 @@ __global__ void __launch_bounds__(kTile) k_face_props(const CaseDev *__restrict_
     pr[PR_RHO * nf + i] = rhoip;
     pr[PR_RHOADN * nf + i] = rhoip * adn;
     pr[PR_RHOMADN * nf + i] = (C.rho[o] + C.rho[n]) / 2.0 * adn;
-    if (C.fprop32) {   // precision 3: the planes of the FP32 explicit face terms
+    if (C.fprop32) {   // precision 3: the planes of the FP32 explicit face terms and Rhie-Chow term
         float *pf = C.fprop32;
         pf[i] = narrow_f32(wt);
         for (int m = 0; m < 3; m++) {
             pf[(1 + m) * nf + i] = narrow_f32(pr[(PR_MAX + m) * nf + i]);
             pf[(4 + m) * nf + i] = narrow_f32(pr[(PR_MEX + m) * nf + i]);
+            pf[(7 + m) * nf + i] = narrow_f32(g[(FG_DRX + m) * nf + i]);
         }
+        pf[10 * nf + i] = narrow_f32(pr[PR_RHOADN * nf + i]);
     }
 }
 
@@ -253,7 +255,9 @@ __global__ void __launch_bounds__(kTile) k_coef_uvw_cell(const CaseDev *__restri
     }
     C.ap[i] = ap;
     C.bu[i] = bu; C.bv[i] = bv; C.bw[i] = bw;
-    C.d[i] = vol / ap;
+    const double dd = vol / ap;
+    C.d[i] = dd;
+    if (F32) C.d32[i] = narrow_f32(dd);
 #pragma unroll
     for (int k = 0; k < kMaxW; k++)
         if (k < W) C.anb[k * ne + i] = a[k];
@@ -345,6 +349,9 @@ __global__ void __launch_bounds__(kTile) k_narrow_grad(const CaseDev *__restrict
     for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int m = 0; m < 3; m++) C.g32[(size_t)q * 3 * C.ne + 3 * i + m] = narrow_f32(grad[q][3 * i + m]);
+#pragma unroll
+    for (int m = 0; m < 3; m++) C.gp32[3 * i + m] = narrow_f32(C.gp[3 * i + m]);
+    C.d32[i] = narrow_f32(C.d[i]);
 }
 
 __global__ void k_narrow_array(const double *__restrict__ in, float *__restrict__ out, size_t n) {
@@ -416,6 +423,45 @@ __global__ void __launch_bounds__(kTile) k_calc_mip(const CaseDev *__restrict__ 
         if (!C.steady) {   // the transient term carries 1/dt and vanishes when steady
             const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
             mip = mip - rhoip * dip * C.rdt * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
+        }
+    }
+    C.mip[i] = mip;
+}
+
+// calc_mip in precision 3: the flux (rho_ip v_ip . A) in FP64, the Rhie-Chow
+// pressure-smoothing term -rho_ip A/(dr.n) d_ip ((p_nb - p_P) - gp_ip . dr)
+// in FP32 from the FP64 pressure difference and FP32 copies of gp, d and the
+// planes (it is a correction to the flux, well inside FP32's range and
+// relative precision), widened and subtracted in FP64.  The transient term
+// of an unsteady case stays FP64.
+__global__ void __launch_bounds__(kTile) k_calc_mip_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int rc) {
+    CFDL_PDL_WAIT();
+    TILE_PROLOGUE(faces)
+    if (i >= t.last) return;
+    const int nf = C.nf, o = C.f_own[i], n = C.f_nb[i];
+    if (n >= C.ne) return;
+    const double *g = C.fgeo;
+    const double wt = g[FG_WT * nf + i], omw = 1.0 - wt;
+    const double A0 = g[FG_AX * nf + i], A1 = g[FG_AY * nf + i], A2 = g[FG_AZ * nf + i];
+    const double vx = omw * C.u[o] + wt * C.u[n], vy = omw * C.v[o] + wt * C.v[n], vz = omw * C.w[o] + wt * C.w[n];
+    const double rhoip = C.fprop[PR_RHO * nf + i];
+    double mip = (vx * A0 + vy * A1 + vz * A2) * rhoip;
+    if (rc) {
+        const float *pf = C.fprop32;
+        const float wf = pf[i], omf = 1.0f - wf;
+        const float D0 = pf[7 * nf + i], D1 = pf[8 * nf + i], D2 = pf[9 * nf + i];
+        const float *gp = C.gp32;
+        const float gx = omf * gp[3 * o] + wf * gp[3 * n];
+        const float gy = omf * gp[3 * o + 1] + wf * gp[3 * n + 1];
+        const float gz = omf * gp[3 * o + 2] + wf * gp[3 * n + 2];
+        const float dip = omf * C.d32[o] + wf * C.d32[n];
+        const float dp = narrow_f32(C.p[n] - C.p[o]);
+        const float corr = dip * pf[10 * nf + i] * (dp - (gx * D0 + gy * D1 + gz * D2));
+        mip = mip - widen_f64(corr);
+        if (!C.steady) {
+            const double dip64 = omw * C.d[o] + wt * C.d[n];
+            const double ux = omw * C.u0[o] + wt * C.u0[n], uy = omw * C.v0[o] + wt * C.v0[n], uz = omw * C.w0[o] + wt * C.w0[n];
+            mip = mip - rhoip * dip64 * C.rdt * (C.mip0[i] - (ux * A0 + uy * A1 + uz * A2) * rhoip);
         }
     }
     C.mip[i] = mip;
@@ -532,6 +578,10 @@ __global__ void __launch_bounds__(kTile) k_update_cells(const CaseDev *__restric
 #pragma unroll
         for (int q = 0; q < 3; q++) C.gp[3 * i + q] = C.gp[3 * i + q] + a * C.gpc[3 * i + q];
     }
+    if (C.gp32) {   // precision 3: the FP32 copy the Rhie-Chow term reads
+#pragma unroll
+        for (int q = 0; q < 3; q++) C.gp32[3 * i + q] = narrow_f32(C.gp[3 * i + q]);
+    }
 }
 
 __global__ void __launch_bounds__(kTile) k_update_faces(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
@@ -606,6 +656,11 @@ void launch_grad(cfdl_ctx *ctx, int field) {
 }
 void launch_calc_mip(cfdl_ctx *ctx, int rc) {
     ensure_face_props(ctx);
+    if (rc && f32_assembly(ctx)) {
+        ensure_g32(ctx);
+        CFDL_LAUNCH("k_calc_mip", k_calc_mip_f32, faces, rc);
+        return;
+    }
     CFDL_LAUNCH("k_calc_mip", k_calc_mip, faces, rc);
 }
 void launch_coef_p_matrix(cfdl_ctx *ctx) {
@@ -653,17 +708,19 @@ int ensure_f32_assembly(HostCase *hc, cudaStream_t stream) {
     const size_t ne = hc->ne, nf = hc->nf, nG = 3 * (size_t)hc->W * ne;
     void *g = nullptr, *G = nullptr, *pf = nullptr;
     int st;
-    if ((st = case_alloc(hc, &g, 9 * ne * sizeof(float)))) return st;
+    // g32: the FP32 gradients of u, v, w [9 ne], then gp32 [3 ne] and d32 [ne]
+    if ((st = case_alloc(hc, &g, 13 * ne * sizeof(float)))) return st;
     if ((st = case_alloc(hc, &G, nG * sizeof(float)))) return st;
-    if ((st = case_alloc(hc, &pf, 7 * nf * sizeof(float)))) return st;
+    if ((st = case_alloc(hc, &pf, 11 * nf * sizeof(float)))) return st;
     const int tb = 256;
     k_narrow_array<<<(unsigned)((nG + tb - 1) / tb), tb, 0, stream>>>(d.hf_G, (float *)G, nG);
     if ((st = cuda_status(cudaGetLastError()))) return st;
-    if ((st = cuda_status(cudaMemsetAsync(pf, 0, 7 * nf * sizeof(float), stream)))) return st;
+    if ((st = cuda_status(cudaMemsetAsync(pf, 0, 11 * nf * sizeof(float), stream)))) return st;
     if ((st = cuda_status(cudaStreamSynchronize(stream)))) return st;
     d.g32 = (float *)g; d.G32 = (float *)G; d.fprop32 = (float *)pf;
+    d.gp32 = d.g32 + 9 * ne; d.d32 = d.g32 + 12 * ne;
     hc->props_dirty = true;      // k_face_props fills fprop32
-    hc->g32_stale = true;        // k_narrow_grad fills g32 from gu, gv, gw
+    hc->g32_stale = true;        // k_narrow_grad fills g32, gp32, d32 from gu, gv, gw, gp, d
     return CFDL_OK;
 }
 

@@ -147,9 +147,10 @@ typedef struct cfdl_config {
                               drop, no refinement needed);
                               3: as 2, and the explicit momentum face terms (sumss and
                               the deferred non-orthogonal correction of calc_coef_uvw)
-                              and the gradients of u, v, w they use are FP32; the
-                              implicit coefficients, fluxes and pressure equation
-                              stay FP64 (solve_mode 0 only)                            */
+                              and the gradients of u, v, w they use are FP32, as is
+                              the Rhie-Chow term of calc_mip; the implicit
+                              coefficients, the fluxes themselves and the pressure
+                              equation stay FP64 (solve_mode 0 only)                   */
     int    precond;        /* pressure preconditioner: 0 Jacobi, 1 aggregation AMG      */
 } cfdl_config;
 

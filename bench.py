@@ -627,15 +627,10 @@ def run_converged(a, dist):
     batched cases (64 uneven cavities, N~U{16..64}, half tet-split, Re
     log-U[10,1000]) until each case's u, v, w and p are within --field-tol
     (relative L2, default 1e-6) of its FP64 converged state
-    (converged_reference).  A first, untimed pass runs each form in chunks of
-    --chunk outer iterations and records per case the first chunk end at
-    which its fields are within the tolerance (the case is then stopped).  The
-    timed pass runs a fresh batch of the form with exactly those per-case
-    iteration counts in one graph launch (cfdl_run): its device time is the
-    form's time to solution.  A case's arithmetic does not depend on the
-    other cases in the batch, so the timed pass ends on the fields the first
-    pass checked; the line reports their errors again from the timed pass.
-    One JSON line per form."""
+    (converged_reference).  Each form runs from the initial state in timed
+    graph launches of a few outer iterations; after each the cases within
+    the tolerance are stopped.  The summed device time of the launches is the
+    form's time to solution.  One JSON line per form, printed as it ends."""
     import numpy as np
     import cfdl
     import workloads
@@ -663,54 +658,46 @@ def run_converged(a, dist):
             out[k] = e
         return out
 
-    lines, t_fp64 = [], None
+    t_fp64 = None
     for prec in [int(x) for x in a.forms.split(",")]:
         cfgs = [cfdl.steady(mu=1.0 / c["re"], precision=prec) for c in cases]
         b = cfdl.Batch(setups, cfgs)
         best, _ = b.autotune(outer=2)
         b.close()
-        # check every --chunk outer iterations, then every 5% of those done:
-        # a case's count is at most that much above the least it needs
-        # pass 1: iterations each case needs (chunk granularity), untimed
+        # one pass from the initial state: runs of --chunk outer iterations,
+        # then of 5% of those done, each one graph launch timed on the device;
+        # after each run the cases within the tolerance are stopped (their
+        # count is at most one run above the least they need).  The host's
+        # checks between runs are outside the timed launches.
         b = cfdl.Batch(setups, cfgs)
         b.set_tile(best)
         ids = b.ids()
-        need, last_err, done_it = {}, {}, 0
+        b.set_run(0, 0, 0.0)
+        b.run(0)                         # builds the run graph outside the timing
+        need, done_it, ms, launches = {}, 0, 0.0, 0
         todo = list(range(len(ids)))
+        clocks = Clocks(dist.local)
+        clocks.start()
         while todo and done_it < cap:
             step = min(max(a.chunk, done_it // 20), cap - done_it)
             for k in range(len(ids)):
                 b.set_run(step if k in todo else 0, 0, 0.0, cid=ids[k])
+            l0 = b.launch_count()
+            b.timer_begin()
             b.run(step)
+            ms += b.timer_end()
+            launches += b.launch_count() - l0
             done_it += step
-            errs = errors(b, ids, todo)
-            last_err.update(errs)
-            for k, e in errs.items():
+            for k, e in errors(b, ids, todo).items():
                 if e <= a.field_tol:
                     need[k] = done_it
             todo = [k for k in todo if k not in need]
-        b.close()
-        for k in todo:                   # not within the tolerance by the cap: run to the cap
-            need[k] = cap
-        # pass 2: the timed run with those iteration counts
-        b = cfdl.Batch(setups, cfgs)
-        b.set_tile(best)
-        ids = b.ids()
-        for k in range(len(ids)):
-            b.set_run(need[k], 0, 0.0, cid=ids[k])
-        b.run(0)                         # builds the run graph outside the timing
-        clocks = Clocks(dist.local)
-        dist.barrier()
-        clocks.start()
-        l0 = b.launch_count()
-        b.timer_begin()
-        left = b.run(max(need.values()))
-        ms = b.timer_end()
-        launches = b.launch_count() - l0
         clk = clocks.stop()
-        ms = dist.max(ms)
+        for k in todo:
+            need[k] = cap
         final = errors(b, ids, range(len(ids)))
         b.close()
+        ms = dist.max(ms)
         iters = [need[k] for k in range(len(ids))]
         cell_iters = sum(s_.ne * n for s_, n in zip(setups, iters))
         errs = list(final.values())
@@ -722,16 +709,16 @@ def run_converged(a, dist):
             "data": "synthetic (seeded cavity meshes)",
             "config": {"workload": "batched to convergence: %d lid-driven cavity cases, N~U{%d..%d} (seed %d), half "
                                    "tet-split, Re log-U[10,1000], each run until u, v, w, p are within %.0e (rel L2) "
-                                   "of its FP64 converged state, one graph launch" %
+                                   "of its FP64 converged state" %
                                    (len(cases), min(c["n"] for c in cases), max(c["n"] for c in cases), a.seed,
                                     a.field_tol),
                        "cases": len(cases), "cells": total_cells, "tile": best, "chunk": a.chunk, "cap": cap,
                        "reference": "the FP64 form to mass ratio <= %.0e (%d of %d cases reached it, %.0f s)" %
                                     (a.ref_tol, sum(st.converged for st in ref_stats), len(cases), t_ref)},
             "cell_iters_per_s": cell_iters / (ms / 1e3),
-            "cases_within_tol": int(sum(e <= a.field_tol for e in errs)), "not_finished": left,
+            "cases_within_tol": int(sum(e <= a.field_tol for e in errs)),
             "outer_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters)),
-                                 "total_cell_iters": cell_iters},
+                                 "total_cell_iters": cell_iters, "runs": "%d outer iterations in total" % done_it},
             "rel_l2_vs_fp64_converged": {"max": max(errs), "median": float(np.median(errs))},
             "gpu_launches": launches,
         }
@@ -739,8 +726,7 @@ def run_converged(a, dist):
             out["speedup_vs_fp64_time_to_solution"] = t_fp64 / ms
         if clk:
             out["clocks"] = clk
-        lines.append(out)
-    return lines
+        yield out
 
 
 # ------------------------------------------------------- pressure solve
@@ -1021,14 +1007,13 @@ def run_served(a, dist):
     if a.n_range:
         lo, hi = (int(x) for x in a.n_range.split(","))
         kw = dict(n_lo=lo, n_hi=hi)
-    lines = []
     ref, t_ref = None, 0.0
     nerr = min(a.err_sample, a.requests)
     if nerr > 0:
         sample = workloads.served_requests(seed=a.seed, count=a.requests, rate=1.0, **kw)[:nerr]
         setups = [cfdl.Setup(cfdl.Zone(r["n"], r["tet"], 0.0, seed=a.seed)) for r in sample]
         t0 = time.perf_counter()
-        ref, ref_stats, _ = converged_reference(setups, sample, a.ref_tol, 4 * a.max_outer)
+        ref, ref_stats, _ = converged_reference(setups, sample, a.ref_tol, a.conv_cap)
         t_ref = time.perf_counter() - t0
         ref_ne = [s_.ne for s_ in setups]
         ref_conv = int(sum(st.converged for st in ref_stats))
@@ -1097,8 +1082,7 @@ def run_served(a, dist):
                                  % (a.ref_tol, ref_conv, nerr, t_ref)}
             if clk:
                 out["clocks"] = clk
-            lines.append(out)
-    return lines
+            yield out
 
 
 def main():
@@ -1121,10 +1105,12 @@ def main():
             out = run_setup(a, dist)
         else:
             out = run_ours(a, dist)
-        if out is not None and dist.rank == 0:
-            for line in (out if isinstance(out, list) else [out]):
-                print(json.dumps(line))
-                sys.stdout.flush()
+        if out is not None:
+            # lists print at the end, generators (the long workloads) as each line is ready
+            for line in ([out] if isinstance(out, dict) else out):
+                if dist.rank == 0:
+                    print(json.dumps(line))
+                    sys.stdout.flush()
     finally:
         dist.close()
 

@@ -603,7 +603,7 @@ def run_batched(a, dist):
 
 
 # ------------------------------------------- batched, to the converged state
-def converged_reference(setups, cases, tol, cap):
+def converged_reference(setups, cases, tol, cap, tile=0):
     """The FP64 converged state of each case: the plain FP64 form run in one
     batch until every case's mass ratio (mass imbalance / sum |mip|) is at or
     below tol.  These fields stand in for the oracle's converged fields: the
@@ -613,6 +613,8 @@ def converged_reference(setups, cases, tol, cap):
     the oracle itself needs hours per case at these sizes."""
     import cfdl
     b = cfdl.Batch(setups, [cfdl.steady(mu=1.0 / c["re"], precision=0) for c in cases])
+    if tile:
+        b.set_tile(tile)
     b.set_run(cap, 0, tol)
     left = b.run(cap)
     ids = b.ids()
@@ -644,8 +646,13 @@ def run_converged(a, dist):
     setups = workloads.build_setups(cases)
     total_cells = sum(s_.ne for s_ in setups)
     cap = a.conv_cap
+    # the FP64 form's tile shape first: the reference runs with it, so that the
+    # FP64 form's timed run repeats the reference's arithmetic exactly
+    b = cfdl.Batch(setups, [cfdl.steady(mu=1.0 / c["re"], precision=0) for c in cases])
+    tile0, _ = b.autotune(outer=2)
+    b.close()
     t0 = time.perf_counter()
-    ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, cap)
+    ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, cap, tile=tile0)
     t_ref = time.perf_counter() - t0
 
     def errors(b, ids, which):
@@ -696,6 +703,7 @@ def run_converged(a, dist):
         for k in todo:
             need[k] = cap
         final = errors(b, ids, range(len(ids)))
+        ratios = [b.case_stats(c).mass_ratio for c in ids]
         b.close()
         ms = dist.max(ms)
         iters = [need[k] for k in range(len(ids))]
@@ -720,6 +728,9 @@ def run_converged(a, dist):
             "outer_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters)),
                                  "total_cell_iters": cell_iters, "runs": "%d outer iterations in total" % done_it},
             "rel_l2_vs_fp64_converged": {"max": max(errs), "median": float(np.median(errs))},
+            "not_within_tol": [{"case": k, "n": cases[k]["n"], "tet": cases[k]["tet"], "re": round(cases[k]["re"], 1),
+                                "rel_l2": final[k], "mass_ratio_last_pass": ratios[k]}
+                               for k in range(len(ids)) if final[k] > a.field_tol],
             "gpu_launches": launches,
         }
         if t_fp64 is not None and prec != 0:

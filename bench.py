@@ -605,8 +605,9 @@ def run_batched(a, dist):
 # ------------------------------------------- batched, to the converged state
 def converged_reference(setups, cases, tol, cap, tile=0):
     """The FP64 converged state of each case: the plain FP64 form run in one
-    batch until every case's mass ratio (mass imbalance / sum |mip|) is at or
-    below tol.  These fields stand in for the oracle's converged fields: the
+    batch for cap outer iterations, a case stopping early once its mass ratio
+    (mass imbalance / sum |mip|) is at or below tol (tol 0: never).  These
+    fields stand in for the oracle's converged fields: the
     FP64 GPU path reproduces the oracle within 1e-9 per outer iteration in
     tight mode (tests/test_gpu_configs.py, test_gpu_parity.py) and the
     converged states agree within 1e-6 (tests/test_gpu_converged.py), while
@@ -651,9 +652,14 @@ def run_converged(a, dist):
     b = cfdl.Batch(setups, [cfdl.steady(mu=1.0 / c["re"], precision=0) for c in cases])
     tile0, _ = b.autotune(outer=2)
     b.close()
+    # the reference runs every case the whole cap, with no early stop: a mass
+    # ratio of 1e-11 can still leave the fields 1e-4 from their limit on the
+    # slowest cases (measured), while after the cap the mass ratio is at
+    # rounding level (1e-15 and below)
     t0 = time.perf_counter()
-    ref, ref_stats, ref_left = converged_reference(setups, cases, a.ref_tol, cap, tile=tile0)
+    ref, ref_stats, ref_left = converged_reference(setups, cases, 0.0, cap, tile=tile0)
     t_ref = time.perf_counter() - t0
+    ref_ratio = max(st.mass_ratio for st in ref_stats)
 
     def errors(b, ids, which):
         out = {}
@@ -724,8 +730,8 @@ def run_converged(a, dist):
                                    (len(cases), min(c["n"] for c in cases), max(c["n"] for c in cases), a.seed,
                                     a.field_tol),
                        "cases": len(cases), "cells": total_cells, "tile": best, "chunk": a.chunk, "cap": cap,
-                       "reference": "the FP64 form to mass ratio <= %.0e (%d of %d cases reached it, %.0f s)" %
-                                    (a.ref_tol, sum(st.converged for st in ref_stats), len(cases), t_ref)},
+                       "reference": "the FP64 form, %d outer iterations of every case (largest mass ratio after "
+                                    "them %.1e, %.0f s)" % (cap, ref_ratio, t_ref)},
             "cell_iters_per_s": cell_iters / (ms / 1e3),
             "cases_within_tol": int(sum(e <= a.field_tol for e in errs)),
             "outer_iterations": {"min": int(min(iters)), "median": float(np.median(iters)), "max": int(max(iters)),

@@ -666,16 +666,12 @@ __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
-    // one row per thread over the kTile-row tiles of the cells list, the
-    // coefficient loads issued with the index loads (the mesh-level V-cycle
-    // kernels' row form), not a loop of rows per thread
     double v[1] = {0};
-    const int i = t.first + (int)threadIdx.x;
-    if (i < t.last) {
+    FOR_CELLS(t) {
         const LP<double> P = level<double>(C, 0);
-        const double q = amul_mesh<double>(P, C.kp, i);
+        const double q = amul<double>(P, C.kp, i);
         C.kv[i] = q;
-        v[0] = C.kp[i] * q;
+        v[0] += C.kp[i] * q;
     }
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
@@ -1025,7 +1021,7 @@ void apc_iter(cfdl_ctx *ctx) {
     vcycle<double>(ctx);
     ALAUNCH("k_apc_rz", k_apc_rz, ctx->cellsv, RED);
     ALAUNCH("k_apc_p", k_apc_p, ctx->cellsv);
-    ALAUNCH("k_apc_q", k_apc_q, ctx->cells, ctx->cells.d_case_first, ctx->cells.d_case_ntiles, ctx->d_partials);
+    ALAUNCH("k_apc_q", k_apc_q, ctx->cellsv, RED);
     ALAUNCH("k_apc_x", k_apc_x, ctx->cellsv, RED);
 }
 
@@ -1166,12 +1162,11 @@ __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ case
     SolveScalars *S = C.sc;
     if (!S->active32) return;
     float v[1] = {0.f};
-    const int i = t.first + (int)threadIdx.x;   // one row per thread, as k_apc_q
-    if (i < t.last) {
+    FOR_CELLS(t) {
         const LP<float> P = level<float>(C, 0);
-        const float q = amul_mesh<float>(P, C.fp, i);
+        const float q = amul<float>(P, C.fp, i);
         C.fq[i] = q;
-        v[0] = C.fp[i] * q;
+        v[0] += C.fp[i] * q;
     }
     block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A3], cnt[t.c])) {
@@ -1267,7 +1262,7 @@ void mx_inner_iter(cfdl_ctx *ctx) {
     else ALAUNCH("k_mx_jacobi", k_mx_jacobi, ctx->cellsv);
     ALAUNCH("k_mx_rz", k_mx_rz, ctx->cellsv, RED32);
     ALAUNCH("k_mx_p", k_mx_p, ctx->cellsv);
-    ALAUNCH("k_mx_q", k_mx_q, ctx->cells, ctx->cells.d_case_first, ctx->cells.d_case_ntiles, (float *)ctx->d_partials);
+    ALAUNCH("k_mx_q", k_mx_q, ctx->cellsv, RED32);
     ALAUNCH("k_mx_x", k_mx_x, ctx->cellsv, RED32);
 }
 void mx_finish(cfdl_ctx *ctx) {

@@ -76,6 +76,24 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
     ell_row<1, T>(P.nb, P.a, P.dg[i], x, 0, P.n, P.W, i, y);
     return y[0];
 }
+// CG's q = A p over a thread's rows of a wide tile, returning its share of
+// (p, q).  Two rows per step, both rows' loads issued before either store (a
+// store holds back the loads after it, since it may alias them), the
+// products summed in row order exactly as one row per step would.
+template <class T>
+__device__ __forceinline__ T cg_aq_rows(const LP<T> &P, const T *p, T *q, const Tile &t) {
+    T v = 0;
+    for (int j_ = 0, i = t.first + (int)threadIdx.x; j_ < t.pad; j_ += 2, i += 2 * kTile) {
+        const int i1 = i + kTile;
+        const bool ok0 = i < t.last, ok1 = j_ + 1 < t.pad && i1 < t.last;
+        T q0 = 0, q1 = 0, p0 = 0, p1 = 0;
+        if (ok0) { q0 = amul<T>(P, p, i); p0 = p[i]; }
+        if (ok1) { q1 = amul<T>(P, p, i1); p1 = p[i1]; }
+        if (ok0) { q[i] = q0; v += p0 * q0; }
+        if (ok1) { q[i1] = q1; v += p1 * q1; }
+    }
+    return v;
+}
 // the same on a coarse level, over the row's valid slots only (the padding
 // slots would subtract zero terms): four slots per step, loads issued together
 template <class T> __device__ __forceinline__ T amul_coarse(const LP<T> &P, const T *x, int i) {
@@ -310,9 +328,8 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
 // z = t + w D^-1 (r - A t).  kMesh: launched on the mesh level only.
 // kToT: the sweep from z into t instead (the first post-smoothing sweep,
 // after k_v_lift has added the prolongated coarse correction to z)
-template <class T, bool kMesh, bool kToT = false>
-__global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
-    CFDL_PDL_WAIT();
+template <class T, bool kMesh, bool kToT>
+__device__ __forceinline__ void v_jac_row(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -328,6 +345,23 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
         // the row's own values first: measured faster on the coarse levels
         y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], offsum<T>(P, x, i));
     }
+}
+template <class T, bool kToT = false>
+__global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
+    v_jac_row<T, false, kToT>(cases, tiles, l);
+}
+// The mesh-level sweeps (one row per thread, two dependent trips to memory
+// a row) are kernels of their own, so that their register cap, and with it
+// the resident warps and the loads in flight, is set apart from the coarse
+// levels' sweeps: 32 registers, 8 CTAs per SM (the FP64 forms keep one
+// 8-byte spill slot), measured 2-4% faster at 128^3 than the 40 registers
+// and 6 CTAs the compiler picks unbounded; the coarse sweeps would spill
+// 100+ bytes under the same cap.
+template <class T, bool kToT = false>
+__global__ void __launch_bounds__(kTile, 8) k_v_jac_mesh(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
+    v_jac_row<T, true, kToT>(cases, tiles, l);
 }
 
 // z = z + s P z_{l+1}: the prolongated coarse correction, added in place.
@@ -350,8 +384,7 @@ __global__ void __launch_bounds__(kTile) k_v_lift(const CaseDev *__restrict__ ca
 
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
 template <class T, bool kMesh>
-__global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
-    CFDL_PDL_WAIT();
+__device__ __forceinline__ void v_resid_row(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
     if (sizeof(T) == 8 ? !pactive(C) : !mactive(C)) return;
@@ -359,6 +392,17 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
     P.t[i] = P.r[i] - (kMesh ? amul_mesh<T>(P, P.z, i) : amul_coarse<T>(P, P.z, i));
+}
+template <class T>
+__global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
+    v_resid_row<T, false>(cases, tiles, l);
+}
+// the mesh level's residual, with the mesh sweeps' register cap
+template <class T>
+__global__ void __launch_bounds__(kTile, 8) k_v_resid_mesh(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
+    CFDL_PDL_WAIT();
+    v_resid_row<T, true>(cases, tiles, l);
 }
 
 // r_{l1}[I] = sum of the residual t over the members of aggregate I (one
@@ -666,13 +710,7 @@ __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
-    double v[1] = {0};
-    FOR_CELLS(t) {
-        const LP<double> P = level<double>(C, 0);
-        const double q = amul<double>(P, C.kp, i);
-        C.kv[i] = q;
-        v[0] += C.kp[i] * q;
-    }
+    double v[1] = {cg_aq_rows<double>(level<double>(C, 0), C.kp, C.kv, t)};
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
         __shared__ double s[1];
@@ -963,11 +1001,11 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             GROUPED("k_v_resid_c", k_vg_resid, ctx->amg_gsmooth[l], 0, l)
         } else {
             if (l == 0) {
-                ALAUNCH("k_v_jac_f", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_resid_f", (k_v_resid<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T>), ctx->amg_smooth[l], l);
             } else {
-                ALAUNCH("k_v_jac_c", (k_v_jac<T, false>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_resid_c", (k_v_resid<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_c", (k_v_jac<T>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_c", (k_v_resid<T>), ctx->amg_smooth[l], l);
             }
         }
         G = ctx->amg_grouped[l + 1];
@@ -985,11 +1023,11 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             // z += s P z_{l+1}; t = J(z); z = J(t)
             ALAUNCH(l ? "k_v_lift_c" : "k_v_lift_f", k_v_lift<T>, ctx->amg_smooth[l], l);
             if (l == 0) {
-                ALAUNCH("k_v_jac_f", (k_v_jac<T, true, true>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_jac_f", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T>), ctx->amg_smooth[l], l);
             } else {
-                ALAUNCH("k_v_jac_c", (k_v_jac<T, false, true>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_jac_c", (k_v_jac<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_c", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_c", (k_v_jac<T>), ctx->amg_smooth[l], l);
             }
         }
     }
@@ -1161,13 +1199,7 @@ __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ case
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active32) return;
-    float v[1] = {0.f};
-    FOR_CELLS(t) {
-        const LP<float> P = level<float>(C, 0);
-        const float q = amul<float>(P, C.fp, i);
-        C.fq[i] = q;
-        v[0] += C.fp[i] * q;
-    }
+    float v[1] = {cg_aq_rows<float>(level<float>(C, 0), C.fp, C.fq, t)};
     block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A3], cnt[t.c])) {
         __shared__ float s[1];

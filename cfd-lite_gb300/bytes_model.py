@@ -82,6 +82,7 @@ def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
     return {
         "jac0": 3 * s * n,                                  # r, w/D in; t out
         "jac": 4 * s * n + W * s * n + ell_i,               # t, r, w/D in; z out; ELL values and indices
+        "jacr": 3 * s * n + W * s * n + ell_i,              # r, w/D in (t = w/D r formed); z out; ELL
         "resid": 4 * s * n + W * s * n + ell_i,             # z, r, D in; t out
         "prolong": (4 * s + 4) * n + W * s * n + ell_i + n_next * s,   # z, r, w/D, agg in; t out; coarse z
         "lift": (2 * s + 4) * n + n_next * s,               # z in and out, agg in; coarse z

@@ -76,45 +76,95 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
     ell_row<1, T>(P.nb, P.a, P.dg[i], x, 0, P.n, P.W, i, y);
     return y[0];
 }
+// A thread's rows of a wide tile, two per step: rows i0 and i1, with ok0 and
+// ok1 false past the tile's end.  The CG kernels issue both rows' loads
+// before either row's stores: a store holds back every load after it (the
+// compiler cannot tell that they do not alias), so one row per step made
+// each row its own trip to memory.  Sums still run in row order.
+#define FOR_ROW_PAIRS(t)                                                                            \
+    for (int j_ = 0, i0 = (t).first + (int)threadIdx.x; j_ < (t).pad; j_ += 2, i0 += 2 * kTile)     \
+        if (const int i1 = i0 + kTile, ok0 = i0 < (t).last, ok1 = j_ + 1 < (t).pad && i1 < (t).last; \
+            true)
+
 // CG's q = A p over a thread's rows of a wide tile, returning its share of
-// (p, q).  Two rows per step, both rows' loads issued before either store (a
-// store holds back the loads after it, since it may alias them), the
-// products summed in row order exactly as one row per step would.
+// (p, q), two rows per step
 template <class T>
 __device__ __forceinline__ T cg_aq_rows(const LP<T> &P, const T *p, T *q, const Tile &t) {
     T v = 0;
-    for (int j_ = 0, i = t.first + (int)threadIdx.x; j_ < t.pad; j_ += 2, i += 2 * kTile) {
-        const int i1 = i + kTile;
-        const bool ok0 = i < t.last, ok1 = j_ + 1 < t.pad && i1 < t.last;
+    FOR_ROW_PAIRS(t) {
         T q0 = 0, q1 = 0, p0 = 0, p1 = 0;
-        if (ok0) { q0 = amul<T>(P, p, i); p0 = p[i]; }
+        if (ok0) { q0 = amul<T>(P, p, i0); p0 = p[i0]; }
         if (ok1) { q1 = amul<T>(P, p, i1); p1 = p[i1]; }
-        if (ok0) { q[i] = q0; v += p0 * q0; }
+        if (ok0) { q[i0] = q0; v += p0 * q0; }
         if (ok1) { q[i1] = q1; v += p1 * q1; }
     }
     return v;
 }
+// CG's (r, z), two rows per step
+template <class T>
+__device__ __forceinline__ T cg_rz_rows(const T *r, const T *z, const Tile &t) {
+    T v = 0;
+    FOR_ROW_PAIRS(t) {
+        T r0 = 0, z0 = 0, r1 = 0, z1 = 0;
+        if (ok0) { r0 = r[i0]; z0 = z[i0]; }
+        if (ok1) { r1 = r[i1]; z1 = z[i1]; }
+        if (ok0) v += r0 * z0;
+        if (ok1) v += r1 * z1;
+    }
+    return v;
+}
+// CG's p = z (first iteration) or z + beta p, two rows per step
+template <class T>
+__device__ __forceinline__ void cg_p_rows(const T *z, T *p, bool first, T beta, const Tile &t) {
+    FOR_ROW_PAIRS(t) {
+        T z0 = 0, p0 = 0, z1 = 0, p1 = 0;
+        if (ok0) { z0 = z[i0]; if (!first) p0 = p[i0]; }
+        if (ok1) { z1 = z[i1]; if (!first) p1 = p[i1]; }
+        if (ok0) p[i0] = first ? z0 : z0 + beta * p0;
+        if (ok1) p[i1] = first ? z1 : z1 + beta * p1;
+    }
+}
+// CG's x += alpha p; r -= alpha q, returning the share of (r, r), two rows
+// per step
+template <class T>
+__device__ __forceinline__ T cg_x_rows(T *x, const T *p, T *r, const T *q, T a, const Tile &t) {
+    T v = 0;
+    FOR_ROW_PAIRS(t) {
+        T x0 = 0, p0 = 0, r0 = 0, q0 = 0, x1 = 0, p1 = 0, r1 = 0, q1 = 0;
+        if (ok0) { x0 = x[i0]; p0 = p[i0]; r0 = r[i0]; q0 = q[i0]; }
+        if (ok1) { x1 = x[i1]; p1 = p[i1]; r1 = r[i1]; q1 = q[i1]; }
+        if (ok0) { x[i0] = x0 + a * p0; const T rr = r0 - a * q0; r[i0] = rr; v += rr * rr; }
+        if (ok1) { x[i1] = x1 + a * p1; const T rr = r1 - a * q1; r[i1] = rr; v += rr * rr; }
+    }
+    return v;
+}
+// Slots of a wide coarse row taken per step, their index, coefficient and
+// vector loads issued together (sums stay in slot order): 8 for the FP32
+// levels, 4 for FP64, where 8 took the sweeps from 48 to 64 registers and
+// measured slower (the FP32 sweeps and tail measured 5-15% faster at 8)
+template <class T> __host__ __device__ constexpr int coarse_chunk() { return sizeof(T) == 4 ? 8 : 4; }
 // the same on a coarse level, over the row's valid slots only (the padding
-// slots would subtract zero terms): four slots per step, loads issued together
+// slots would subtract zero terms): kCh slots per step
 template <class T> __device__ __forceinline__ T amul_coarse(const LP<T> &P, const T *x, int i) {
     if (P.W == 6 || P.W == 4 || !P.len) return amul<T>(P, x, i);
+    constexpr int kCh = coarse_chunk<T>();
     const int len = P.len[i];
     T y = P.dg[i] * x[i];
-    for (int k0 = 0; k0 < len; k0 += 4) {
-        int jj[4];
-        T ak[4], xv[4];
+    for (int k0 = 0; k0 < len; k0 += kCh) {
+        int jj[kCh];
+        T ak[kCh], xv[kCh];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
+        for (int u = 0; u < kCh; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < kCh; u++) {
             const bool ok = (unsigned)jj[u] < (unsigned)P.n;
             ak[u] = ok ? P.a[(k0 + u) * P.n + i] : (T)0;
             if (!ok) jj[u] = i;
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) xv[u] = x[jj[u]];
+        for (int u = 0; u < kCh; u++) xv[u] = x[jj[u]];
 #pragma unroll
-        for (int u = 0; u < 4; u++) y -= ak[u] * xv[u];
+        for (int u = 0; u < kCh; u++) y -= ak[u] * xv[u];
     }
     return y;
 }
@@ -143,22 +193,37 @@ __device__ __forceinline__ void row_slots(const LP<T> &P, int i, int (&j)[W], T 
     }
 }
 
+// The vector a sweep reads: a stored one, or t = w D^-1 r formed on the fly
+// for the first pre-smoothing sweep (the product k_v_jac0 would store; the
+// same multiplication, so the same values)
+template <class T> struct VecIn {
+    const T *x;
+    __device__ __forceinline__ T operator()(int j) const { return x[j]; }
+};
+template <class T> struct VecRdR {
+    const T *rd, *r;
+    __device__ __forceinline__ T operator()(int j) const { return rd[j] * r[j]; }
+};
+
 // sum_j a_ij x_j over the row's couplings inside the level (the ELL values
 // are the off-diagonal magnitudes: A = D - offdiag)
-template <int W, class T, bool kGuard = false, bool kEager = true>
-__device__ __forceinline__ T offsum_w(const LP<T> &P, const T *x, int i) {
+template <int W, class T, bool kGuard = false, bool kEager = true, class X>
+__device__ __forceinline__ T offsum_w(const LP<T> &P, const X &xv, int i) {
     int j[W];
     T c[W];
     row_slots<W, T, kGuard, kEager>(P, i, j, c);
+    T xj[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) xj[k] = xv(j[k]);
     T s = 0;
 #pragma unroll
-    for (int k = 0; k < W; k++) s += c[k] * x[j[k]];
+    for (int k = 0; k < W; k++) s += c[k] * xj[k];
     return s;
 }
 
 // The mesh level (level 0): at most kMaxW slots a row, every width on the
 // short fixed-width paths (no wide-row code in the kernels that use these)
-template <class T> __device__ __forceinline__ T offsum_mesh(const LP<T> &P, const T *x, int i) {
+template <class T, class X> __device__ __forceinline__ T offsum_mesh(const LP<T> &P, const X &x, int i) {
     if (P.W == 6) return offsum_w<6, T>(P, x, i);
     if (P.W == 4) return offsum_w<4, T>(P, x, i);
     return offsum_w<kMaxW, T, true>(P, x, i);
@@ -183,28 +248,32 @@ template <class T> __device__ __forceinline__ int row_len(const LP<T> &P, int i)
     return P.len ? P.len[i] : P.W;
 }
 
-template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
+template <class T, class X> __device__ __forceinline__ T offsum_x(const LP<T> &P, const X &x, int i) {
     if (P.W == 6) return offsum_w<6, T, false, false>(P, x, i);
     if (P.W == 4) return offsum_w<4, T, false, false>(P, x, i);
-    // wide coarse rows: four slots per step, loads issued together, up to the
-    // row's own length (the padding would add zero terms)
+    constexpr int kCh = coarse_chunk<T>();
+    // wide coarse rows: kCh slots per step, loads issued together,
+    // up to the row's own length (the padding would add zero terms)
     T s = 0;
     const int len = row_len(P, i);
-    for (int k0 = 0; k0 < len; k0 += 4) {
-        int jj[4];
-        T c[4], xv[4];
+    for (int k0 = 0; k0 < len; k0 += kCh) {
+        int jj[kCh];
+        T c[kCh], xv[kCh];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
+        for (int u = 0; u < kCh; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < kCh; u++) {
             const bool ok = (unsigned)jj[u] < (unsigned)P.n;
             c[u] = ok ? P.a[(k0 + u) * P.n + i] : (T)0;
-            xv[u] = x[ok ? jj[u] : i];
+            xv[u] = x(ok ? jj[u] : i);
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) s += c[u] * xv[u];
+        for (int u = 0; u < kCh; u++) s += c[u] * xv[u];
     }
     return s;
+}
+template <class T> __device__ __forceinline__ T offsum(const LP<T> &P, const T *x, int i) {
+    return offsum_x<T>(P, VecIn<T>{x}, i);
 }
 
 // damped Jacobi sweep from x: x + w D^-1 (r - A x) = (1 - w) x + (w/D)(r + offsum);
@@ -327,8 +396,11 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
 
 // z = t + w D^-1 (r - A t).  kMesh: launched on the mesh level only.
 // kToT: the sweep from z into t instead (the first post-smoothing sweep,
-// after k_v_lift has added the prolongated coarse correction to z)
-template <class T, bool kMesh, bool kToT>
+// after k_v_lift has added the prolongated coarse correction to z).
+// kFromR: the first pre-smoothing sweep, from t = w D^-1 r formed on the fly
+// for the row and its neighbours instead of read from k_v_jac0's pass (the
+// same products, so the same z; one pass over the level fewer)
+template <class T, bool kMesh, bool kToT, bool kFromR = false>
 __device__ __forceinline__ void v_jac_row(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
@@ -336,20 +408,27 @@ __device__ __forceinline__ void v_jac_row(const CaseDev *__restrict__ cases, con
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
+    if (kFromR) {
+        const VecRdR<T> tv{P.rd, P.r};
+        const T ri = P.r[i], rdi = P.rd[i];
+        const T off = kMesh ? offsum_mesh<T>(P, tv, i) : offsum_x<T>(P, tv, i);
+        P.z[i] = jacobi_step<T, 2>(rdi * ri, ri, rdi, off);
+        return;
+    }
     const T *x = kToT ? P.z : P.t;
     T *y = kToT ? P.t : P.z;
     if (kMesh) {
-        const T off = offsum_mesh<T>(P, x, i);
+        const T off = offsum_mesh<T>(P, VecIn<T>{x}, i);
         y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], off);
     } else {
         // the row's own values first: measured faster on the coarse levels
         y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], offsum<T>(P, x, i));
     }
 }
-template <class T, bool kToT = false>
+template <class T, bool kToT = false, bool kFromR = false>
 __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
-    v_jac_row<T, false, kToT>(cases, tiles, l);
+    v_jac_row<T, false, kToT, kFromR>(cases, tiles, l);
 }
 // The mesh-level sweeps (one row per thread, two dependent trips to memory
 // a row) are kernels of their own, so that their register cap, and with it
@@ -358,10 +437,10 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
 // 8-byte spill slot), measured 2-4% faster at 128^3 than the 40 registers
 // and 6 CTAs the compiler picks unbounded; the coarse sweeps would spill
 // 100+ bytes under the same cap.
-template <class T, bool kToT = false>
+template <class T, bool kToT = false, bool kFromR = false>
 __global__ void __launch_bounds__(kTile, 8) k_v_jac_mesh(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
-    v_jac_row<T, true, kToT>(cases, tiles, l);
+    v_jac_row<T, true, kToT, kFromR>(cases, tiles, l);
 }
 
 // z = z + s P z_{l+1}: the prolongated coarse correction, added in place.
@@ -405,6 +484,28 @@ __global__ void __launch_bounds__(kTile, 8) k_v_resid_mesh(const CaseDev *__rest
     v_resid_row<T, true>(cases, tiles, l);
 }
 
+// sum of t over the members of aggregate I of the level below L: four
+// members per step, their indices and then their values loaded side by side,
+// summed in member order (one member per step made every member two
+// dependent trips to memory)
+template <class T>
+__device__ __forceinline__ T restrict_row(const AmgLevelDev &L, const T *t, int I) {
+    const int m0 = L.mem_ptr[I], m1 = L.mem_ptr[I + 1];
+    T s = 0;
+    for (int m = m0; m < m1; m += 4) {
+        int j[4];
+        T x[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) j[u] = m + u < m1 ? L.mem[m + u] : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) x[u] = j[u] >= 0 ? t[j[u]] : (T)0;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (j[u] >= 0) s += x[u];
+    }
+    return s;
+}
+
 // r_{l1}[I] = sum of the residual t over the members of aggregate I (one
 // thread per coarse row: the large levels, where rows outnumber lanes)
 template <class T>
@@ -417,10 +518,8 @@ __global__ void __launch_bounds__(kTile) k_v_restrict(const CaseDev *__restrict_
     if (I >= tl.last) return;
     const AmgLevelDev &L = C.lev[l1 - 1];
     const LP<T> F = level<T>(C, l1 - 1);
-    T s = 0;
-    for (int m = L.mem_ptr[I]; m < L.mem_ptr[I + 1]; m++) s += F.t[L.mem[m]];
     T *rc = sizeof(T) == 8 ? (T *)L.r : (T *)L.r32;
-    rc[I] = s;
+    rc[I] = restrict_row<T>(L, F.t, I);
 }
 
 // Galerkin row I, one thread per row (large levels)
@@ -476,11 +575,7 @@ __global__ void __launch_bounds__(kTailThreads) k_v_tail(const CaseDev *__restri
         __syncthreads();
         const AmgLevelDev &Lc = C.lev[l];                  // level l + 1
         T *rc = sizeof(T) == 8 ? (T *)Lc.r : (T *)Lc.r32;
-        for (int I = threadIdx.x; I < Lc.n; I += nt) {
-            T sum = 0;
-            for (int m = Lc.mem_ptr[I]; m < Lc.mem_ptr[I + 1]; m++) sum += P.t[Lc.mem[m]];
-            rc[I] = sum;
-        }
+        for (int I = threadIdx.x; I < Lc.n; I += nt) rc[I] = restrict_row<T>(Lc, P.t, I);
         __syncthreads();
     }
     {   // coarsest: z_L = Minv r_L
@@ -495,17 +590,33 @@ __global__ void __launch_bounds__(kTailThreads) k_v_tail(const CaseDev *__restri
         __syncthreads();
     }
     const T sc = (T)kOverCorrect;
+    constexpr int kCh = coarse_chunk<T>();
     for (int l = L - 1; l >= lt; l--) {
         const LP<T> P = level<T>(C, l);
         const AmgLevelDev &Lc = C.lev[l];
         const T *zc = sizeof(T) == 8 ? (const T *)Lc.z : (const T *)Lc.z32;
         for (int i = threadIdx.x; i < P.n; i += nt) {
             const T xi = P.z[i] + sc * zc[Lc.agg[i]];
+            // the neighbours' lifted values, kCh slots per step with
+            // each step's loads issued together, summed in slot order
             T off = 0;
             const int len = row_len(P, i);
-            for (int k = 0; k < len; k++) {
-                const int j = P.nb[k * P.n + i];
-                if ((unsigned)j < (unsigned)P.n) off += P.a[k * P.n + i] * (P.z[j] + sc * zc[Lc.agg[j]]);
+            for (int k0 = 0; k0 < len; k0 += kCh) {
+                int jj[kCh], ag[kCh];
+                bool ok[kCh];
+                T ak[kCh], zj[kCh];
+#pragma unroll
+                for (int u = 0; u < kCh; u++) jj[u] = k0 + u < len ? P.nb[(k0 + u) * P.n + i] : -1;
+#pragma unroll
+                for (int u = 0; u < kCh; u++) {
+                    ok[u] = (unsigned)jj[u] < (unsigned)P.n;
+                    ak[u] = ok[u] ? P.a[(k0 + u) * P.n + i] : (T)0;
+                    zj[u] = ok[u] ? P.z[jj[u]] : (T)0;
+                    ag[u] = ok[u] ? Lc.agg[jj[u]] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < kCh; u++)
+                    if (ok[u]) off += ak[u] * (zj[u] + sc * zc[ag[u]]);
             }
             P.t[i] = jacobi_step<T, 1>(xi, P.r[i], P.rd[i], off);
         }
@@ -678,6 +789,8 @@ __global__ void __launch_bounds__(kTile) k_apc_rz(const CaseDev *__restrict__ ca
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
+    // one row per step in FP64: the paired form (cg_rz_rows) measured slower
+    // here (21.4 against 18.8 us a launch at 128^3)
     double v[1] = {0.0};
     FOR_CELLS(t) v[0] += C.kr[i] * C.ks[i];
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
@@ -699,7 +812,7 @@ __global__ void __launch_bounds__(kTile) k_apc_p(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     const SolveScalars *S = C.sc;
     if (!S->active_p) return;
-    FOR_CELLS(t) C.kp[i] = S->iters_p == 0 ? C.ks[i] : C.ks[i] + S->beta_p * C.kp[i];
+    cg_p_rows<double>(C.ks, C.kp, S->iters_p == 0, S->beta_p, t);
 }
 
 // q = A p; alpha = rz / (p, q)
@@ -734,6 +847,8 @@ __global__ void __launch_bounds__(kTile) k_apc_x(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
+    // one row per step in FP64: the paired form (cg_x_rows, 48 registers
+    // against 32) measured slower here (31.9 against 28.5 us a launch)
     double v[1] = {0};
     FOR_CELLS(t) {
         const double a = S->alpha_p;
@@ -994,12 +1109,20 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
     // shortens each thread's chain of loads (amg_grouped[l] = G).
     const int L = ctx->amg_lmax;
     for (int l = 0; l < L; l++) {
-        ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
         int G = ctx->amg_grouped[l];
         if (G > 1) {
+            ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
             GROUPED("k_v_jac_c", k_vg_jac, ctx->amg_gsmooth[l], 0, l)
             GROUPED("k_v_resid_c", k_vg_resid, ctx->amg_gsmooth[l], 0, l)
+        } else if (l == 0 && sizeof(T) == 4) {
+            // FP32 mesh level: t = w D^-1 r and the first sweep from it in one
+            // pass (46.6 -> 33.2 us at 128^3).  The FP64 form keeps the two
+            // passes: there the fused sweep measured slower (65.0 -> 74.7 us),
+            // and so did the coarse levels' in both forms.
+            ALAUNCH("k_v_jacr_f", (k_v_jac_mesh<T, false, true>), ctx->amg_smooth[l], l);
+            ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T>), ctx->amg_smooth[l], l);
         } else {
+            ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
             if (l == 0) {
                 ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T>), ctx->amg_smooth[l], l);
@@ -1169,8 +1292,7 @@ __global__ void __launch_bounds__(kTile) k_mx_rz(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active32) return;
-    float v[1] = {0.f};
-    FOR_CELLS(t) v[0] += C.fr[i] * C.fz[i];
+    float v[1] = {cg_rz_rows<float>(C.fr, C.fz, t)};
     block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
         __shared__ float s[1];
@@ -1189,7 +1311,7 @@ __global__ void __launch_bounds__(kTile) k_mx_p(const CaseDev *__restrict__ case
     const CaseDev &C = cases[t.c];
     const SolveScalars *S = C.sc;
     if (!S->active32) return;
-    FOR_CELLS(t) C.fp[i] = S->iters32 == 0 ? C.fz[i] : C.fz[i] + S->beta32 * C.fp[i];
+    cg_p_rows<float>(C.fz, C.fp, S->iters32 == 0, S->beta32, t);
 }
 
 __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
@@ -1218,14 +1340,7 @@ __global__ void __launch_bounds__(kTile) k_mx_x(const CaseDev *__restrict__ case
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active32) return;
-    float v[1] = {0.f};
-    FOR_CELLS(t) {
-        const float a = S->alpha32;
-        C.fx[i] = C.fx[i] + a * C.fp[i];
-        const float r = C.fr[i] - a * C.fq[i];
-        C.fr[i] = r;
-        v[0] += r * r;
-    }
+    float v[1] = {cg_x_rows<float>(C.fx, C.fp, C.fr, C.fq, S->alpha32, t)};
     block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A4], cnt[t.c])) {
         __shared__ float s[1];

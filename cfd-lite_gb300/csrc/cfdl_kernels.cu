@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kTile) k_grad(const CaseDev *__restrict__ case
 // calc_grad of u, v, w for the FP32 explicit face terms (precision 3): the
 // neighbour differences in FP64, narrowed in the integer pipe, the stencil
 // sums in FP32; the gradients go to g32 and, widened, to gu, gv, gw.
-__global__ void __launch_bounds__(kTile) k_grad3_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
+__global__ void __launch_bounds__(kTile, 3) k_grad3_f32(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
@@ -318,16 +318,36 @@ __global__ void __launch_bounds__(kTile) k_grad3_f32(const CaseDev *__restrict__
     float g[3][3];
 #pragma unroll
     for (int q = 0; q < 3; q++) { pe[q] = phi[q][i]; g[q][0] = g[q][1] = g[q][2] = 0.f; }
+    // Every slot's loads are issued before the first is used: a loop that
+    // stopped at the first padding slot had to wait for each slot's index
+    // before it could load the next slot, six dependent trips to memory.  A
+    // row's slots end at its first padding slot (live), as that loop did.
+    // With 3 CTAs per SM (80 registers) this measured 203 -> 151 us at 128^3.
+    int nb[kMaxW];
+    bool live[kMaxW];
+    float G[3][kMaxW];
+    bool on = true;
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
-        if (k >= W) break;
-        const int nb = C.hf_nb[k * ne + i];
-        if (nb < 0) break;
-        const float G0 = C.G32[(0 * W + k) * ne + i], G1 = C.G32[(1 * W + k) * ne + i], G2 = C.G32[(2 * W + k) * ne + i];
+        const int j = k < W ? C.hf_nb[k * ne + i] : -1;
+#pragma unroll
+        for (int m = 0; m < 3; m++) G[m][k] = k < W ? C.G32[(m * W + k) * ne + i] : 0.f;
+        on = on && j >= 0;
+        live[k] = on;
+        nb[k] = on ? j : i;
+    }
+    double pn[3][kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) pn[q][k] = phi[q][nb[k]];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        if (!live[k]) continue;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const float d = narrow_f32(phi[q][nb] - pe[q]);
-            g[q][0] += G0 * d; g[q][1] += G1 * d; g[q][2] += G2 * d;
+            const float d = narrow_f32(pn[q][k] - pe[q]);
+            g[q][0] += G[0][k] * d; g[q][1] += G[1][k] * d; g[q][2] += G[2][k] * d;
         }
     }
 #pragma unroll

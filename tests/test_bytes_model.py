@@ -25,6 +25,7 @@ def test_mesh_level_jacobi_sweep_is_104_bytes_per_hex_cell():
     # the FP32 form of the mixed solve halves the values, not the indices
     assert amg_kernel_bytes("k_v_jac_f", levels, 4) == (16 + 24 + 24) * ne
     assert amg_kernel_bytes("k_v_jac0_f", levels, 8) == 24 * ne
+    assert amg_kernel_bytes("k_v_jacr_f", levels, 4) == (12 + 24 + 24) * ne   # t = w/D r formed in the sweep
     assert 218103808 == amg_kernel_bytes("k_v_jac_f", levels, 8)   # the 128^3 bench figure
 
 

@@ -302,13 +302,21 @@ __global__ void __launch_bounds__(kTile) k_amg_prep0(const CaseDev *__restrict__
     const int i = t.first + (int)threadIdx.x;
     if (i >= t.last || C.sc->halted) return;
     const double ap = C.ap_p[i];
-    C.rap_p[i] = kOmega / ap;
-    if (C.precision >= 1) {
+    const bool mixed = C.precision >= 1;
+    // the row's loads before its stores (a store holds back the loads after it)
+    double a[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) a[k] = mixed && k < C.W ? C.anb_p[k * C.ne + i] : 0.0;
+    const double rd = kOmega / ap;
+    C.rap_p[i] = rd;
+    if (mixed) {
         // the FP32 copies converted in the integer pipe (GB300 runs the hardware
         // conversions at its FP64 rate)
         C.fdiag_p[i] = narrow_f32(ap);
-        C.frap_p[i] = narrow_f32(kOmega / ap);
-        for (int k = 0; k < C.W; k++) C.fanb_p[k * C.ne + i] = narrow_f32(C.anb_p[k * C.ne + i]);
+        C.frap_p[i] = narrow_f32(rd);
+#pragma unroll
+        for (int k = 0; k < kMaxW; k++)
+            if (k < C.W) C.fanb_p[k * C.ne + i] = narrow_f32(a[k]);
     }
 }
 
@@ -1372,12 +1380,16 @@ __global__ void __launch_bounds__(kTile) k_mx_res(const CaseDev *__restrict__ ca
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
+    // two rows per step, both rows' loads before either store
     double v[1] = {0};
-    FOR_CELLS(t) {
-        const LP<double> P = level<double>(C, 0);
-        const double r = (C.b[i] - S->mean_b) - amul<double>(P, C.phic, i);
-        C.kr[i] = r;
-        v[0] += r * r;
+    const LP<double> P = level<double>(C, 0);
+    const double mb = S->mean_b;
+    FOR_ROW_PAIRS(t) {
+        double r0 = 0.0, r1 = 0.0;
+        if (ok0) r0 = (C.b[i0] - mb) - amul<double>(P, C.phic, i0);
+        if (ok1) r1 = (C.b[i1] - mb) - amul<double>(P, C.phic, i1);
+        if (ok0) { C.kr[i0] = r0; v[0] += r0 * r0; }
+        if (ok1) { C.kr[i1] = r1; v[0] += r1 * r1; }
     }
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_M0], cnt[t.c])) {

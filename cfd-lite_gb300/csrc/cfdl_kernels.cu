@@ -503,55 +503,70 @@ __global__ void __launch_bounds__(kTile) k_coef_p_face(const CaseDev *__restrict
 }
 
 // the matrix: anb = the face coefficient on interior slots (0 on walls,
-// mod_uvwp.f90:354-363), ap = their sum
+// mod_uvwp.f90:354-363), ap = their sum.  Every slot's index loads, then
+// every coefficient gather, are issued before the stores (a store in the
+// slot loop held back the next slot's loads: three dependent trips to
+// memory a slot).
 __global__ void __launch_bounds__(kTile) k_coef_p_mat(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
-    double ap = 0.0;
+    int nb[kMaxW], fc[kMaxW];
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
-        if (k >= W) continue;
-        const int nb = C.hf_nb[k * ne + i];
-        double a = 0.0;
-        if (nb >= 0 && nb < ne) {
-            a = C.fdiff[face_of(C.hf_fc[k * ne + i])];
-            ap += a;
-        }
-        C.anb_p[k * ne + i] = a;
+        nb[k] = k < W ? C.hf_nb[k * ne + i] : -1;
+        fc[k] = k < W ? C.hf_fc[k * ne + i] : 0;
     }
+    double a[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) a[k] = nb[k] >= 0 && nb[k] < ne ? C.fdiff[face_of(fc[k])] : 0.0;
+    double ap = 0.0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++)
+        if (nb[k] >= 0 && nb[k] < ne) ap += a[k];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++)
+        if (k < W) C.anb_p[k * ne + i] = a[k];
     C.ap_p[i] = ap;
 }
 
 // the right-hand side: b = net inflow over the interior faces, minus the
-// boundary mass fluxes in BC-loop order
+// boundary mass fluxes in BC-loop order (ascending halo index).  The slots'
+// loads are issued together; the boundary slots are then taken in halo
+// order by selection over the row's registers.
 __global__ void __launch_bounds__(kTile) k_coef_p_rhs(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles) {
     CFDL_PDL_WAIT();
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
-    double sumf = 0.0;
-    int bslot[kMaxW], nb_cnt = 0;
+    int nb[kMaxW], fc[kMaxW];
 #pragma unroll
     for (int k = 0; k < kMaxW; k++) {
-        if (k >= W) continue;
-        const int nb = C.hf_nb[k * ne + i];
-        if (nb >= ne) bslot[nb_cnt++] = k;
-        else if (nb >= 0) {
-            const int fc = C.hf_fc[k * ne + i];
-            sumf += flip_sign(C.mip[face_of(fc)], fc >= 0);   // -sg * mip
-        }
+        nb[k] = k < W ? C.hf_nb[k * ne + i] : -1;
+        fc[k] = k < W ? C.hf_fc[k * ne + i] : 0;
     }
-    for (int q = 1; q < nb_cnt; q++) {
-        int s = bslot[q], j = q - 1;
-        while (j >= 0 && C.hf_nb[bslot[j] * ne + i] > C.hf_nb[s * ne + i]) { bslot[j + 1] = bslot[j]; j--; }
-        bslot[j + 1] = s;
+    double m[kMaxW];
+    int kind[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) {
+        m[k] = nb[k] >= 0 ? C.mip[face_of(fc[k])] : 0.0;
+        kind[k] = nb[k] >= ne ? C.h_kind[nb[k] - ne] : 0;
     }
-    for (int q = 0; q < nb_cnt; q++) {
-        const int k = bslot[q];
-        if (C.h_kind[C.hf_nb[k * ne + i] - ne] == 0) continue;
-        sumf = sumf - C.mip[face_of(C.hf_fc[k * ne + i])];
+    double sumf = 0.0;
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++)
+        if (nb[k] >= 0 && nb[k] < ne) sumf += flip_sign(m[k], fc[k] >= 0);   // -sg * mip
+    int prev = ne - 1;
+    for (int q = 0; q < kMaxW; q++) {       // the boundary slot of the next larger halo index
+        int best = 0x7fffffff, bkind = 0;
+        double bm = 0.0;
+#pragma unroll
+        for (int k = 0; k < kMaxW; k++)
+            if (nb[k] > prev && nb[k] < best) { best = nb[k]; bm = m[k]; bkind = kind[k]; }
+        if (best == 0x7fffffff) break;
+        prev = best;
+        if (bkind != 0) sumf = sumf - bm;
     }
     C.b[i] = sumf;
 }
@@ -570,14 +585,15 @@ __global__ void __launch_bounds__(kTile) k_adjust_pc(const CaseDev *__restrict__
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const int ne = C.ne, W = C.W;
+    // the row's loads before its stores (a store holds back the loads after it)
+    int nb[kMaxW];
+#pragma unroll
+    for (int k = 0; k < kMaxW; k++) nb[k] = k < W ? C.hf_nb[k * ne + i] : -1;
     const double v = C.phic[i] - C.sc->pref;
     C.phic[i] = v;
 #pragma unroll
-    for (int k = 0; k < kMaxW; k++) {
-        if (k >= W) break;
-        const int nb = C.hf_nb[k * ne + i];
-        if (nb >= ne) C.phic[nb] = v;
-    }
+    for (int k = 0; k < kMaxW; k++)
+        if (nb[k] >= ne) C.phic[nb[k]] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -589,18 +605,19 @@ __global__ void __launch_bounds__(kTile) k_update_cells(const CaseDev *__restric
     TILE_PROLOGUE(cells)
     if (i >= t.last) return;
     const double a = C.alpha_p;
+    double g[3];
     if (a == 1.0) {
         C.p[i] = C.p[i] + C.phic[i];
 #pragma unroll
-        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = C.gp[3 * i + q] + C.gpc[3 * i + q];
+        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = g[q] = C.gp[3 * i + q] + C.gpc[3 * i + q];
     } else {
         C.p[i] = C.p[i] + a * C.phic[i];
 #pragma unroll
-        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = C.gp[3 * i + q] + a * C.gpc[3 * i + q];
+        for (int q = 0; q < 3; q++) C.gp[3 * i + q] = g[q] = C.gp[3 * i + q] + a * C.gpc[3 * i + q];
     }
-    if (C.gp32) {   // precision 3: the FP32 copy the Rhie-Chow term reads
+    if (C.gp32) {   // precision 3: the FP32 copy the Rhie-Chow term reads, from the new values in registers
 #pragma unroll
-        for (int q = 0; q < 3; q++) C.gp32[3 * i + q] = narrow_f32(C.gp[3 * i + q]);
+        for (int q = 0; q < 3; q++) C.gp32[3 * i + q] = narrow_f32(g[q]);
     }
 }
 

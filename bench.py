@@ -184,10 +184,11 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def ncu_traffic(kernel, n):
+def ncu_traffic(kernel, n, precision=0):
     """DRAM bytes per launch from a committed ncu summary (profiles/ncu_traffic.txt:
-    lines 'kernel n_cells bytes_per_launch'), scaled to n^3 cells when the
-    capture was taken on a smaller mesh; None when absent."""
+    lines 'kernel n_cells bytes_per_launch [precision]', precision 0 when
+    absent), scaled to n^3 cells when the capture was taken on a smaller mesh;
+    None when there is no capture of that kernel at that precision."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
@@ -195,7 +196,9 @@ def ncu_traffic(kernel, n):
     with open(path) as fh:
         for line in fh:
             f = line.split()
-            if len(f) >= 3 and f[0] == kernel and not line.startswith("#"):
+            if line.startswith("#") or len(f) < 3 or f[0] != kernel:
+                continue
+            if (int(f[3]) if len(f) >= 4 else 0) == precision:
                 best = (int(f[1]), float(f[2]))
     if not best:
         return None
@@ -272,9 +275,11 @@ def run_ours(a, dist):
         cfdl._check(cfdl.lib().cfdl_amg_info(g._h, 15, C.byref(nl), ns, ws), "amg_info")
         levels = [(ns[l], ws[l]) for l in range(nl.value + 1)]
         val = 4 if (a.precision >= 1 and (dominant.startswith("k_v_") or dominant.startswith("k_mx_"))) else 8
-        nbytes = amg_kernel_bytes(dominant, levels, val)
+        # bytes per mesh-level neighbour index (16-bit offsets in the FP32 kernels when they fit)
+        ib = cfdl.lib().cfdl_amg_index_bytes(g._h) if val == 4 else 4
+        nbytes = amg_kernel_bytes(dominant, levels, val, ib=ib)
     achieved = nbytes / avg_s / 1e9 if nbytes else None
-    traffic = ncu_traffic(dominant, a.n)
+    traffic = ncu_traffic(dominant, a.n, a.precision)
     # the FP64 pipe's ceiling: the probe's DFMA rate on this device, and each
     # FP64-bound kernel's FP64 instructions per launch (flops_model) over its
     # average launch time from the profile pass above
@@ -930,7 +935,7 @@ def run_energy(a, dist):
                           "solve_uvwp_without_energy_setup": ms_plain / a.steps},
         "temperature_range": [float(t_range.min()), float(t_range.max())],
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peaks["hbm_gbs"],
-                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": ncu_traffic(dominant, a.n),
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": ncu_traffic(dominant, a.n, a.precision),
                      "algorithmic_bytes": nbytes, "avg_launch_us": avg_s * 1e6, "launches": dp[0],
                      "peak_source": peak_kind},
         "kernel_shares": shares,

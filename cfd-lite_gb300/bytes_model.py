@@ -76,9 +76,10 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
     return table.get(name)
 
 
-def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
-    """One V-cycle kernel at one level of n cells and ELL width W."""
-    ell_i = 4 * W * n
+def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0, ib=4):
+    """One V-cycle kernel at one level of n cells and ELL width W; ib = bytes
+    per neighbour index (2 for the mesh level's 16-bit offsets)."""
+    ell_i = ib * W * n
     return {
         "jac0": 3 * s * n,                                  # r, w/D in; t out
         "jac": 4 * s * n + W * s * n + ell_i,               # t, r, w/D in; z out; ELL values and indices
@@ -90,14 +91,16 @@ def _vcycle_level_bytes(kind, n, W, s, n_prev=0, n_next=0):
     }[kind]
 
 
-def amg_kernel_bytes(name, levels, s, tail_rows=2048):
+def amg_kernel_bytes(name, levels, s, tail_rows=2048, ib=4):
     """Multigrid and CG-around-multigrid kernels.  levels = [(n_l, W_l)] for
     l = 0 (mesh) .. L (coarsest); s = value size (8 for the FP64 form, 4 for
-    the FP32 inner solve of the mixed form).  Kernels suffixed _f run on the
-    mesh level; _c kernels are averaged over the coarse levels they run on."""
+    the FP32 inner solve of the mixed form); ib = bytes per mesh-level
+    neighbour index (cfdl_amg_index_bytes: 2 for 16-bit offsets, else 4).
+    Kernels suffixed _f run on the mesh level; _c kernels are averaged over
+    the coarse levels they run on."""
     ne, W = levels[0]
     L = len(levels) - 1
-    ell_i = 4 * W * ne
+    ell_i = ib * W * ne
     fixed = {
         "k_apc_rz": 16 * ne, "k_apc_p": 24 * ne, "k_apc_x": 48 * ne,
         "k_apc_q": ne * 24 + 8 * W * ne + ell_i,
@@ -125,7 +128,7 @@ def amg_kernel_bytes(name, levels, s, tail_rows=2048):
     if where == "f":
         if kind == "restrict":
             return _vcycle_level_bytes(kind, levels[1][0], levels[1][1], s, n_prev=ne)
-        return _vcycle_level_bytes(kind, ne, W, s, n_next=levels[1][0])
+        return _vcycle_level_bytes(kind, ne, W, s, n_next=levels[1][0], ib=ib)
     if kind == "restrict":
         ls = list(range(2, L + 1))
         vals = [_vcycle_level_bytes(kind, levels[l][0], levels[l][1], s, n_prev=levels[l - 1][0]) for l in ls]

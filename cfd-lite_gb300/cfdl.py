@@ -166,6 +166,7 @@ def lib():
     L.cfdl_solve_pc_noalloc.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, C.c_double, C.c_int,
                                         ip, dp]
     L.cfdl_amg_info.argtypes = [vp, C.c_int, ip, vp, vp]
+    L.cfdl_amg_index_bytes.argtypes = [vp]
     L.cfdl_set_graph_mode.argtypes = [vp, C.c_int]
     L.cfdl_batch_create.argtypes = [C.c_int, vp, vp, C.POINTER(vp)]
     L.cfdl_case_add.argtypes = [vp, C.POINTER(Mesh), C.POINTER(Config), ip]

@@ -56,18 +56,19 @@ template <class T> struct LP {
     const T *a, *dg, *rd;   // rd = omega / diagonal (the damped Jacobi scaling)
     T *r, *z, *t;
     const int *len;         // coarse levels: valid slots of each row, packed first (null on the mesh level)
+    const short *nb16;      // mesh level: the neighbours as 16-bit offsets (CaseDev::nb16), or null
 };
 
 template <class T> __device__ __forceinline__ LP<T> level(const CaseDev &C, int l);
 template <> __device__ __forceinline__ LP<double> level<double>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb_p, C.ap_p, C.rap_p, C.kr, C.ks, C.ksh, nullptr};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.anb_p, C.ap_p, C.rap_p, C.kr, C.ks, C.ksh, nullptr, C.nb16};
     const AmgLevelDev &L = C.lev[l - 1];
-    return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t, L.len};
+    return {L.n, L.W, L.nb, L.a, L.dg, L.rd, L.r, L.z, L.t, L.len, nullptr};
 }
 template <> __device__ __forceinline__ LP<float> level<float>(const CaseDev &C, int l) {
-    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb_p, C.fdiag_p, C.frap_p, C.fr, C.fz, C.ft, nullptr};
+    if (l == 0) return {C.ne, C.W, C.hf_nb, C.fanb_p, C.fdiag_p, C.frap_p, C.fr, C.fz, C.ft, nullptr, C.nb16};
     const AmgLevelDev &L = C.lev[l - 1];
-    return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32, L.len};
+    return {L.n, L.W, L.nb, L.a32, L.dg32, L.rd32, L.r32, L.z32, L.t32, L.len, nullptr};
 }
 
 // (A x)_i at a level; neighbours outside [0, n) (halos, padding) are skipped
@@ -86,15 +87,19 @@ template <class T> __device__ __forceinline__ T amul(const LP<T> &P, const T *x,
         if (const int i1 = i0 + kTile, ok0 = i0 < (t).last, ok1 = j_ + 1 < (t).pad && i1 < (t).last; \
             true)
 
+template <class T, bool k16> __device__ __forceinline__ T amul_mesh(const LP<T> &P, const T *x, int i);
+
 // CG's q = A p over a thread's rows of a wide tile, returning its share of
 // (p, q), two rows per step
-template <class T>
+template <class T, bool k16>
 __device__ __forceinline__ T cg_aq_rows(const LP<T> &P, const T *p, T *q, const Tile &t) {
     T v = 0;
     FOR_ROW_PAIRS(t) {
         T q0 = 0, q1 = 0, p0 = 0, p1 = 0;
-        if (ok0) { q0 = amul<T>(P, p, i0); p0 = p[i0]; }
-        if (ok1) { q1 = amul<T>(P, p, i1); p1 = p[i1]; }
+        // the int32 form keeps amul's guarded coefficient loads (measured
+        // faster in these multi-row tiles than the mesh sweeps' eager ones)
+        if (ok0) { q0 = k16 ? amul_mesh<T, true>(P, p, i0) : amul<T>(P, p, i0); p0 = p[i0]; }
+        if (ok1) { q1 = k16 ? amul_mesh<T, true>(P, p, i1) : amul<T>(P, p, i1); p1 = p[i1]; }
         if (ok0) { q[i0] = q0; v += p0 * q0; }
         if (ok1) { q[i1] = q1; v += p1 * q1; }
     }
@@ -176,12 +181,18 @@ template <class T> __device__ __forceinline__ T amul_coarse(const LP<T> &P, cons
 // kGuard: the row has P.W <= W slots (the mesh level, W = kMaxW); slots past
 // P.W are not read.  kEager false: the coefficient load waits for the index
 // (the coarse levels' kernels, where that form measured faster).
-template <int W, class T, bool kGuard, bool kEager = true>
+template <int W, class T, bool kGuard, bool kEager = true, bool k16 = false>
 __device__ __forceinline__ void row_slots(const LP<T> &P, int i, int (&j)[W], T (&c)[W]) {
 #pragma unroll
     for (int k = 0; k < W; k++) {
         const bool in = !kGuard || k < P.W;
-        const int jj = in ? P.nb[k * P.n + i] : -1;
+        int jj;
+        if (k16) {      // the mesh level's 16-bit offsets: half the index bytes
+            const int d = in ? (int)P.nb16[k * P.n + i] : (int)kNb16None;
+            jj = d == (int)kNb16None ? -1 : i + d;
+        } else {
+            jj = in ? P.nb[k * P.n + i] : -1;
+        }
         const bool ok = (unsigned)jj < (unsigned)P.n;
         j[k] = ok ? jj : i;
         if (kEager) {
@@ -207,11 +218,11 @@ template <class T> struct VecRdR {
 
 // sum_j a_ij x_j over the row's couplings inside the level (the ELL values
 // are the off-diagonal magnitudes: A = D - offdiag)
-template <int W, class T, bool kGuard = false, bool kEager = true, class X>
+template <int W, class T, bool kGuard = false, bool kEager = true, bool k16 = false, class X>
 __device__ __forceinline__ T offsum_w(const LP<T> &P, const X &xv, int i) {
     int j[W];
     T c[W];
-    row_slots<W, T, kGuard, kEager>(P, i, j, c);
+    row_slots<W, T, kGuard, kEager, k16>(P, i, j, c);
     T xj[W];
 #pragma unroll
     for (int k = 0; k < W; k++) xj[k] = xv(j[k]);
@@ -223,24 +234,25 @@ __device__ __forceinline__ T offsum_w(const LP<T> &P, const X &xv, int i) {
 
 // The mesh level (level 0): at most kMaxW slots a row, every width on the
 // short fixed-width paths (no wide-row code in the kernels that use these)
-template <class T, class X> __device__ __forceinline__ T offsum_mesh(const LP<T> &P, const X &x, int i) {
-    if (P.W == 6) return offsum_w<6, T>(P, x, i);
-    if (P.W == 4) return offsum_w<4, T>(P, x, i);
-    return offsum_w<kMaxW, T, true>(P, x, i);
+// k16: the level's neighbours are read from P.nb16 (every case of the launch has them)
+template <class T, bool k16, class X> __device__ __forceinline__ T offsum_mesh(const LP<T> &P, const X &x, int i) {
+    if (P.W == 6) return offsum_w<6, T, false, true, k16>(P, x, i);
+    if (P.W == 4) return offsum_w<4, T, false, true, k16>(P, x, i);
+    return offsum_w<kMaxW, T, true, true, k16>(P, x, i);
 }
-template <int W, class T, bool kGuard = false> __device__ __forceinline__ T amul_w(const LP<T> &P, const T *x, int i) {
+template <int W, class T, bool kGuard = false, bool k16 = false> __device__ __forceinline__ T amul_w(const LP<T> &P, const T *x, int i) {
     int j[W];
     T c[W];
-    row_slots<W, T, kGuard>(P, i, j, c);
+    row_slots<W, T, kGuard, true, k16>(P, i, j, c);
     T s = P.dg[i] * x[i];
 #pragma unroll
     for (int k = 0; k < W; k++) s -= c[k] * x[j[k]];
     return s;
 }
-template <class T> __device__ __forceinline__ T amul_mesh(const LP<T> &P, const T *x, int i) {
-    if (P.W == 6) return amul_w<6, T>(P, x, i);
-    if (P.W == 4) return amul_w<4, T>(P, x, i);
-    return amul_w<kMaxW, T, true>(P, x, i);
+template <class T, bool k16> __device__ __forceinline__ T amul_mesh(const LP<T> &P, const T *x, int i) {
+    if (P.W == 6) return amul_w<6, T, false, k16>(P, x, i);
+    if (P.W == 4) return amul_w<4, T, false, k16>(P, x, i);
+    return amul_w<kMaxW, T, true, k16>(P, x, i);
 }
 // Valid slots of row i: a coarse row's couplings are packed in its first
 // len[i] slots (the rest is padding up to the level's widest row, W).
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(kTile) k_v_jac0(const CaseDev *__restrict__ ca
 // kFromR: the first pre-smoothing sweep, from t = w D^-1 r formed on the fly
 // for the row and its neighbours instead of read from k_v_jac0's pass (the
 // same products, so the same z; one pass over the level fewer)
-template <class T, bool kMesh, bool kToT, bool kFromR = false>
+template <class T, bool kMesh, bool kToT, bool kFromR = false, bool k16 = false>
 __device__ __forceinline__ void v_jac_row(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
@@ -419,14 +431,14 @@ __device__ __forceinline__ void v_jac_row(const CaseDev *__restrict__ cases, con
     if (kFromR) {
         const VecRdR<T> tv{P.rd, P.r};
         const T ri = P.r[i], rdi = P.rd[i];
-        const T off = kMesh ? offsum_mesh<T>(P, tv, i) : offsum_x<T>(P, tv, i);
+        const T off = kMesh ? offsum_mesh<T, k16>(P, tv, i) : offsum_x<T>(P, tv, i);
         P.z[i] = jacobi_step<T, 2>(rdi * ri, ri, rdi, off);
         return;
     }
     const T *x = kToT ? P.z : P.t;
     T *y = kToT ? P.t : P.z;
     if (kMesh) {
-        const T off = offsum_mesh<T>(P, VecIn<T>{x}, i);
+        const T off = offsum_mesh<T, k16>(P, VecIn<T>{x}, i);
         y[i] = jacobi_step<T, kToT ? 1 : 2>(x[i], P.r[i], P.rd[i], off);
     } else {
         // the row's own values first: measured faster on the coarse levels
@@ -445,10 +457,10 @@ __global__ void __launch_bounds__(kTile) k_v_jac(const CaseDev *__restrict__ cas
 // 8-byte spill slot), measured 2-4% faster at 128^3 than the 40 registers
 // and 6 CTAs the compiler picks unbounded; the coarse sweeps would spill
 // 100+ bytes under the same cap.
-template <class T, bool kToT = false, bool kFromR = false>
+template <class T, bool k16, bool kToT = false, bool kFromR = false>
 __global__ void __launch_bounds__(kTile, 8) k_v_jac_mesh(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
-    v_jac_row<T, true, kToT, kFromR>(cases, tiles, l);
+    v_jac_row<T, true, kToT, kFromR, k16>(cases, tiles, l);
 }
 
 // z = z + s P z_{l+1}: the prolongated coarse correction, added in place.
@@ -470,7 +482,7 @@ __global__ void __launch_bounds__(kTile) k_v_lift(const CaseDev *__restrict__ ca
 }
 
 // t = r - A z (the smoothed residual, one thread per cell, coalesced)
-template <class T, bool kMesh>
+template <class T, bool kMesh, bool k16 = false>
 __device__ __forceinline__ void v_resid_row(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     const Tile tl = tiles[blockIdx.x];
     const CaseDev &C = cases[tl.c];
@@ -478,7 +490,7 @@ __device__ __forceinline__ void v_resid_row(const CaseDev *__restrict__ cases, c
     const int i = tl.first + (int)threadIdx.x;
     if (i >= tl.last) return;
     const LP<T> P = level<T>(C, l);
-    P.t[i] = P.r[i] - (kMesh ? amul_mesh<T>(P, P.z, i) : amul_coarse<T>(P, P.z, i));
+    P.t[i] = P.r[i] - (kMesh ? amul_mesh<T, k16>(P, P.z, i) : amul_coarse<T>(P, P.z, i));
 }
 template <class T>
 __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
@@ -486,10 +498,10 @@ __global__ void __launch_bounds__(kTile) k_v_resid(const CaseDev *__restrict__ c
     v_resid_row<T, false>(cases, tiles, l);
 }
 // the mesh level's residual, with the mesh sweeps' register cap
-template <class T>
+template <class T, bool k16>
 __global__ void __launch_bounds__(kTile, 8) k_v_resid_mesh(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles, int l) {
     CFDL_PDL_WAIT();
-    v_resid_row<T, true>(cases, tiles, l);
+    v_resid_row<T, true, k16>(cases, tiles, l);
 }
 
 // sum of t over the members of aggregate I of the level below L: four
@@ -831,7 +843,7 @@ __global__ void __launch_bounds__(kTile) k_apc_q(const CaseDev *__restrict__ cas
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active_p) return;
-    double v[1] = {cg_aq_rows<double>(level<double>(C, 0), C.kp, C.kv, t)};
+    double v[1] = {cg_aq_rows<double, false>(level<double>(C, 0), C.kp, C.kv, t)};
     block_reduce<1>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A2], cnt[t.c])) {
         __shared__ double s[1];
@@ -880,6 +892,22 @@ __global__ void __launch_bounds__(kTile) k_apc_x(const CaseDev *__restrict__ cas
             S->active_p = act;
         }
     }
+}
+
+// the mesh level's neighbour offsets for CaseDev::nb16; overflow is set when
+// an offset does not fit in 16 bits
+__global__ void k_nb16(const int *__restrict__ nb, short *__restrict__ out, int ne, int W, unsigned *overflow) {
+    const size_t s = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (s >= (size_t)W * ne) return;
+    const int i = (int)(s % (size_t)ne);
+    const int j = nb[s];
+    short v = kNb16None;
+    if (j >= 0 && j < ne) {
+        const int d = j - i;
+        if (d < -32767 || d > 32767) atomicOr(overflow, 1u);
+        else v = (short)d;
+    }
+    out[s] = v;
 }
 
 }  // namespace
@@ -997,6 +1025,16 @@ int upload_case_amg(HostCase *hc, AmgHierarchy *H) {
     if (ncoarse > kAmgCoarsest) return CFDL_ERR_MESH;
     if ((st = dzeros(hc, &d.cinv, (size_t)ncoarse * ncoarse))) return st;
     if ((st = dzeros(hc, &d.cinv32, (size_t)ncoarse * ncoarse))) return st;
+    if (hc->cfg.precision >= 1) {   // the FP32 mesh kernels' 16-bit neighbour offsets, used when every one fits
+        const size_t nslot = (size_t)hc->W * ne;
+        short *nb16 = nullptr;
+        unsigned *flag = nullptr, over = 0;
+        if ((st = dzeros(hc, &nb16, nslot)) || (st = dzeros(hc, &flag, 1))) return st;
+        k_nb16<<<(unsigned)((nslot + kTile - 1) / kTile), kTile>>>(d.hf_nb, nb16, ne, hc->W, flag);
+        if ((st = cuda_status(cudaGetLastError()))) return st;
+        if ((st = cuda_status(cudaMemcpy(&over, flag, sizeof(unsigned), cudaMemcpyDeviceToHost)))) return st;
+        d.nb16 = over ? nullptr : nb16;
+    }
     d.nlev = nlev;
     d.ncoarse = ncoarse;
     d.lev = dlev;
@@ -1013,6 +1051,9 @@ int ensure_amg(cfdl_ctx *ctx) {
             changed = true;
         }
     }
+    bool all16 = true;
+    for (HostCase *hc : ctx->cases) all16 = all16 && hc->dev.nb16 != nullptr;
+    if (all16 != ctx->amg_nb16) { ctx->amg_nb16 = all16; destroy_graph(ctx); }
     if (!changed && ctx->amg_lmax >= 0) return CFDL_OK;
     int lmax = 0;
     for (HostCase *hc : ctx->cases) lmax = std::max(lmax, hc->dev.nlev);
@@ -1116,6 +1157,10 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
     // (the autotuned cgroup); small levels run 8 lanes per row, which
     // shortens each thread's chain of loads (amg_grouped[l] = G).
     const int L = ctx->amg_lmax;
+    // the FP32 mesh-level kernels read 16-bit neighbour offsets when every
+    // case has them: 52 B a row instead of 64, 8% faster at 128^3; the FP64
+    // sweeps gained 3% for 12% fewer bytes (latency-bound) and keep int32
+    const bool n16 = sizeof(T) == 4 && ctx->amg_nb16;
     for (int l = 0; l < L; l++) {
         int G = ctx->amg_grouped[l];
         if (G > 1) {
@@ -1127,13 +1172,21 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
             // pass (46.6 -> 33.2 us at 128^3).  The FP64 form keeps the two
             // passes: there the fused sweep measured slower (65.0 -> 74.7 us),
             // and so did the coarse levels' in both forms.
-            ALAUNCH("k_v_jacr_f", (k_v_jac_mesh<T, false, true>), ctx->amg_smooth[l], l);
-            ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T>), ctx->amg_smooth[l], l);
+            if (n16) {
+                ALAUNCH("k_v_jacr_f", (k_v_jac_mesh<T, true, false, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T, true>), ctx->amg_smooth[l], l);
+            } else {
+                ALAUNCH("k_v_jacr_f", (k_v_jac_mesh<T, false, false, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T, false>), ctx->amg_smooth[l], l);
+            }
         } else {
             ALAUNCH(l ? "k_v_jac0_c" : "k_v_jac0_f", k_v_jac0<T>, ctx->amg_smooth[l], l);
-            if (l == 0) {
-                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T>), ctx->amg_smooth[l], l);
+            if (l == 0 && n16) {
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T, true>), ctx->amg_smooth[l], l);
+            } else if (l == 0) {
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, false>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_resid_f", (k_v_resid_mesh<T, false>), ctx->amg_smooth[l], l);
             } else {
                 ALAUNCH("k_v_jac_c", (k_v_jac<T>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_resid_c", (k_v_resid<T>), ctx->amg_smooth[l], l);
@@ -1153,9 +1206,12 @@ template <class T> static void vcycle(cfdl_ctx *ctx) {
         } else {
             // z += s P z_{l+1}; t = J(z); z = J(t)
             ALAUNCH(l ? "k_v_lift_c" : "k_v_lift_f", k_v_lift<T>, ctx->amg_smooth[l], l);
-            if (l == 0) {
+            if (l == 0 && n16) {
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, true, true>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, true>), ctx->amg_smooth[l], l);
-                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T>), ctx->amg_smooth[l], l);
+            } else if (l == 0) {
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, false, true>), ctx->amg_smooth[l], l);
+                ALAUNCH("k_v_jac_f", (k_v_jac_mesh<T, false>), ctx->amg_smooth[l], l);
             } else {
                 ALAUNCH("k_v_jac_c", (k_v_jac<T, true>), ctx->amg_smooth[l], l);
                 ALAUNCH("k_v_jac_c", (k_v_jac<T>), ctx->amg_smooth[l], l);
@@ -1322,6 +1378,7 @@ __global__ void __launch_bounds__(kTile) k_mx_p(const CaseDev *__restrict__ case
     cg_p_rows<float>(C.fz, C.fp, S->iters32 == 0, S->beta32, t);
 }
 
+template <bool k16>
 __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ cases, const Tile *__restrict__ tiles,
                                                 const int *__restrict__ cfirst, const int *__restrict__ cnt, float *partials) {
     CFDL_PDL_WAIT();
@@ -1329,7 +1386,7 @@ __global__ void __launch_bounds__(kTile) k_mx_q(const CaseDev *__restrict__ case
     const CaseDev &C = cases[t.c];
     SolveScalars *S = C.sc;
     if (!S->active32) return;
-    float v[1] = {cg_aq_rows<float>(level<float>(C, 0), C.fp, C.fq, t)};
+    float v[1] = {cg_aq_rows<float, k16>(level<float>(C, 0), C.fp, C.fq, t)};
     block_reduce<1, float>(v, &partials[(size_t)blockIdx.x * kNPart]);
     if (last_tile_of_case(&C.counters[CNT_A3], cnt[t.c])) {
         __shared__ float s[1];
@@ -1421,7 +1478,8 @@ void mx_inner_iter(cfdl_ctx *ctx) {
     else ALAUNCH("k_mx_jacobi", k_mx_jacobi, ctx->cellsv);
     ALAUNCH("k_mx_rz", k_mx_rz, ctx->cellsv, RED32);
     ALAUNCH("k_mx_p", k_mx_p, ctx->cellsv);
-    ALAUNCH("k_mx_q", k_mx_q, ctx->cellsv, RED32);
+    if (ctx->amg_nb16) ALAUNCH("k_mx_q", k_mx_q<true>, ctx->cellsv, RED32);
+    else ALAUNCH("k_mx_q", k_mx_q<false>, ctx->cellsv, RED32);
     ALAUNCH("k_mx_x", k_mx_x, ctx->cellsv, RED32);
 }
 void mx_finish(cfdl_ctx *ctx) {
@@ -1457,6 +1515,10 @@ int solve_pressure_mixed(cfdl_ctx *ctx) {
 #undef RED32
 
 }  // namespace cfdl
+
+extern "C" int cfdl_amg_index_bytes(const cfdl_ctx *ctx) {
+    return ctx ? (ctx->amg_nb16 && !ctx->cases.empty() && ctx->cases[0]->cfg.precision >= 1 ? 2 : 4) : -1;
+}
 
 extern "C" int cfdl_amg_info(cfdl_ctx *ctx, int maxlev, int *nlev, int *n, int *W) {
     using namespace cfdl;

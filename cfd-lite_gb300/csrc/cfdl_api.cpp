@@ -656,7 +656,7 @@ size_t cfdl_case_bytes_estimate(int ne, int nf, int nbf, int W) {
     bytes += 9 * c * 8 + w * c * 8 + 4 * f * 8;      // coefficients, face intermediates
     bytes += 10 * f * 8;                              // property planes
     bytes += 24 * c * 8 + 8 * c * 4 + w * c * 4 + c * 8;   // Krylov and FP32 vectors
-    bytes += 160 * c;                                 // multigrid hierarchy (bound)
+    bytes += 160 * c + w * c * 2;                     // multigrid hierarchy (bound), 16-bit mesh offsets
     bytes += 9 * c * 4 + 3 * w * c * 4 + 7 * f * 4;   // precision 3 FP32 gradients, stencil, face planes
     bytes += w * c * 12 + c * 24;                     // the pressure matrix's own storage and FP32 copies
     return bytes;

@@ -31,6 +31,7 @@ namespace cfdl {
 
 constexpr int kTile = 256;        // cells / faces / halos per CTA
 constexpr int kMaxW = 6;          // max faces per cell supported (HEXA_8)
+constexpr short kNb16None = -32768; // CaseDev::nb16: the slot has no interior neighbour
 constexpr int kNPart = 16;        // partial slots per tile
 constexpr int kVec = 4;           // default cells per thread in the solver kernels
 constexpr int kFaceVec = 8;       // faces per thread in the face reductions (their FP64 tree amortised)
@@ -151,6 +152,10 @@ struct CaseDev {
     int nlev, ncoarse;                    // coarse levels; cells of the coarsest level
     int amg_tail;                         // first level the one-CTA V-cycle tail runs (k_v_tail)
     const AmgLevelDev *lev;               // [nlev] device array
+    // [W][ne] the mesh level's interior neighbours as 16-bit offsets j - i
+    // (kNb16None: no interior neighbour) for the mixed pressure solve's FP32
+    // mesh-level kernels; null when an offset does not fit, or in FP64
+    const short *nb16;
     double *cinv;                         // [ncoarse^2] dense inverse of the coarsest operator
     float *cinv32;
     SolveScalars *sc;
@@ -249,6 +254,7 @@ struct cfdl_ctx {
     std::vector<int> amg_grouped;                           // lanes per row of each level (1: one thread per row)
     int cgroup = 1;                                          // lanes per row on the large coarse levels (autotuned)
     int amg_lmax = -1;
+    bool amg_nb16 = false;                                   // every case has CaseDev::nb16 (the mesh kernels read it)
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;
     bool graph_branches = true;          // the outer-iteration graph's parallel branches (off: one chain)

@@ -350,6 +350,13 @@ int cfdl_set_pdl(cfdl_ctx *ctx, int on);
  * (level 0 = the mesh); at most maxlev+1 entries are written. */
 int cfdl_amg_info(cfdl_ctx *ctx, int maxlev, int *nlev, int *n, int *W);
 
+/* Bytes per neighbour index that the mixed (precision >= 1) AMG pressure
+ * solve's FP32 mesh-level kernels read: 2 when every case's mesh neighbours
+ * fit in 16-bit offsets from their cell (checked when the multigrid
+ * hierarchy is set up), else 4; 4 for the FP64 form (its kernels read int32
+ * indices) and before the first AMG pressure solve.  -1 for a null context. */
+int cfdl_amg_index_bytes(const cfdl_ctx *ctx);
+
 /* ---- batches: many independent cases in one context ---------------------
  * No counterpart in the reference, which holds one case per process.  Every
  * case of a context is advanced by the same launches (each kernel's work list

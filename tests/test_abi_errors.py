@@ -17,7 +17,8 @@ CFDL_ERR_INVALID = 1
 # server reads 0
 NULL_OK = {"cfdl_setup_destroy": 0, "cfdl_server_now": 0.0}
 # getters that return a value, not a status: -1 for no context
-GETTERS = {"cfdl_get_tile", "cfdl_get_coarse_group", "cfdl_get_energy_tile", "cfdl_case_count", "cfdl_launch_count"}
+GETTERS = {"cfdl_get_tile", "cfdl_get_coarse_group", "cfdl_get_energy_tile", "cfdl_case_count", "cfdl_launch_count",
+           "cfdl_amg_index_bytes"}
 
 
 def handle_entry_points():

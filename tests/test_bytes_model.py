@@ -27,6 +27,10 @@ def test_mesh_level_jacobi_sweep_is_104_bytes_per_hex_cell():
     assert amg_kernel_bytes("k_v_jac0_f", levels, 8) == 24 * ne
     assert amg_kernel_bytes("k_v_jacr_f", levels, 4) == (12 + 24 + 24) * ne   # t = w/D r formed in the sweep
     assert 218103808 == amg_kernel_bytes("k_v_jac_f", levels, 8)   # the 128^3 bench figure
+    # 16-bit neighbour offsets on the mesh level: 12 index bytes a row, not 24
+    assert amg_kernel_bytes("k_v_jac_f", levels, 8, ib=2) == 92 * ne
+    assert amg_kernel_bytes("k_apc_q", levels, 8, ib=2) == (24 + 48 + 12) * ne
+    assert amg_kernel_bytes("k_v_jac_c", levels, 8, ib=2) == amg_kernel_bytes("k_v_jac_c", levels, 8)
 
 
 def test_cg_and_bicgstab_spmv_counts():

@@ -169,6 +169,9 @@ def test_amg_default_mode_reaches_steady_state(need_gpu, precond, precision):
     g.step(400)
     for f in ("u", "v", "w"):
         assert rel_l2(g.get(f)[:o.ne], o.get(f)[:o.ne]) < 1e-6, f
+    # this mesh's neighbours fit in 16-bit offsets, so the mixed form's FP32
+    # mesh-level kernels ran on them; the FP64 form reads int32 indices
+    assert cfdl.lib().cfdl_amg_index_bytes(g._h) == (2 if precision >= 1 else 4)
 
 
 def test_default_mode_reaches_oracle_steady_state(need_gpu):

@@ -129,10 +129,15 @@ def amg_kernel_bytes(name, levels, s, tail_rows=2048, ib=4):
         if kind == "restrict":
             return _vcycle_level_bytes(kind, levels[1][0], levels[1][1], s, n_prev=ne)
         return _vcycle_level_bytes(kind, ne, W, s, n_next=levels[1][0], ib=ib)
+    # the coarse levels that run per-level kernels: those above the tail level
+    # (the first of at most tail_rows rows, which k_v_tail runs with the rest);
+    # each of them gets the same launches per V-cycle, so the mean over them
+    # is the mean per launch
+    lt = next((l for l in range(1, L + 1) if levels[l][0] <= tail_rows), L)
     if kind == "restrict":
-        ls = list(range(2, L + 1))
+        ls = list(range(2, lt + 1))
         vals = [_vcycle_level_bytes(kind, levels[l][0], levels[l][1], s, n_prev=levels[l - 1][0]) for l in ls]
     else:
-        ls = list(range(1, L))
+        ls = list(range(1, lt))
         vals = [_vcycle_level_bytes(kind, levels[l][0], levels[l][1], s, n_next=levels[l + 1][0]) for l in ls]
     return sum(vals) / len(vals) if vals else None

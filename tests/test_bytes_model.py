@@ -52,6 +52,16 @@ def test_counts_grow_linearly_with_the_mesh():
     assert kernel_bytes("no_such_kernel", *hex_sizes(8), 6) is None
 
 
+def test_coarse_kernels_average_over_the_levels_they_run_on():
+    """_c kernels run on the coarse levels above the tail level (the first of
+    at most 2048 rows); the levels the tail kernel runs are not in the mean."""
+    levels = [(2097152, 6), (262144, 26), (32768, 26), (4096, 26), (512, 20), (64, 12)]
+    jac = [4 * 8 * n + w * 8 * n + 4 * w * n for n, w in levels[1:4]]
+    assert amg_kernel_bytes("k_v_jac_c", levels, 8) == sum(jac) / 3
+    rst = [n_prev * (8 + 4) + n * (4 + 8) for (n_prev, _), (n, _) in zip(levels[1:4], levels[2:5])]
+    assert amg_kernel_bytes("k_v_restrict_c", levels, 8) == sum(rst) / 3
+
+
 def test_lift_and_tail_counts():
     """k_v_lift reads and writes z and reads the aggregate map (plus the coarse
     vector); the tail sums its levels' passes and the dense coarsest solve."""

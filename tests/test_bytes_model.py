@@ -86,3 +86,17 @@ def test_flops_model_matches_the_counted_instructions():
     for k, c in counted.items():
         m = fp64_inst(k, ne, nf, nbf, 6)
         assert abs(m - c) <= 0.02 * c, (k, m, c)
+
+
+def test_ncu_traffic_is_looked_up_per_precision():
+    """bench.py's roofline traffic comes from profiles/ncu_traffic.txt, per
+    kernel and precision (FP64 and FP32 sweeps move different bytes), scaled
+    from the capture's cell count; a kernel or precision without a capture
+    has none."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.ncu_traffic("k_v_jac_f", 112, 0) == 141687168
+    assert bench.ncu_traffic("k_v_jac_f", 112, 3) == 67869696
+    assert abs(bench.ncu_traffic("k_v_jac_f", 128, 3) - 67869696 * 128 ** 3 / 112 ** 3) < 1
+    assert bench.ncu_traffic("k_v_jac_f", 128, 1) is None
+    assert bench.ncu_traffic("k_v_jac_c", 128, 0) is None

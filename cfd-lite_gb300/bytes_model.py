@@ -31,7 +31,10 @@ def kernel_bytes(name, ne, nf, nbf, W, ncomp_active=3):
         # Rhie-Chow: own/nb, 8 geometry planes, mip0 in, mip out; 12 cell doubles
         "k_calc_mip": nfi * (8 + 72 + 16) + ne * 80,
         "k_coef_p_face": nfi * (8 + 16 + 8) + nbf * 8 + ne * 8,
-        "k_coef_p_cell": 2 * ell_i + nf * 16 + ell_d + ne * 16,
+        # matrix: ELL nb/fc, the face coefficient of every face; anb ELL and ap out
+        "k_coef_p_mat": 2 * ell_i + nf * 8 + ell_d + ne * 8,
+        # right-hand side: ELL nb/fc, the flux of every face, halo kinds; b out
+        "k_coef_p_rhs": 2 * ell_i + nf * 8 + nbf * 4 + ne * 8,
         "k_adjust_pc": ell_i + ne * 16 + nbf * 8,
         "k_update_cells": ne * (8 + 8 + 8 + 24 + 24 + 24),
         "k_update_faces": nfi * (8 + 16 + 16) + ne * 32,

@@ -146,6 +146,7 @@ def lib():
     L.cfdl_check_conversions.argtypes = [C.c_int, vp]
     L.cfdl_probe_fp64.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cfdl_set_pdl.argtypes = [vp, C.c_int]
+    L.cfdl_set_index16.argtypes = [vp, C.c_int]
     L.cfdl_set_energy_tile.argtypes = [vp, C.c_int]
     L.cfdl_get_energy_tile.argtypes = [vp]
     L.cfdl_calc_coef_energy.argtypes = [vp]
@@ -459,6 +460,14 @@ class Solver:
 
     def set_pdl(self, on):
         _check(lib().cfdl_set_pdl(self._h, int(bool(on))), "set_pdl")
+
+    def set_index16(self, on):
+        """16-bit neighbour offsets in the FP32 mesh-level kernels (default on)."""
+        _check(lib().cfdl_set_index16(self._h, int(bool(on))), "set_index16")
+
+    def index_bytes(self):
+        """Bytes per neighbour index of the FP32 mesh-level kernels (2 or 4)."""
+        return lib().cfdl_amg_index_bytes(self._h)
 
     def set_graph_mode(self, on):
         """solve_uvwp as one CUDA graph (True or 1, default), as individual

@@ -1051,7 +1051,7 @@ int ensure_amg(cfdl_ctx *ctx) {
             changed = true;
         }
     }
-    bool all16 = true;
+    bool all16 = ctx->index16;
     for (HostCase *hc : ctx->cases) all16 = all16 && hc->dev.nb16 != nullptr;
     if (all16 != ctx->amg_nb16) { ctx->amg_nb16 = all16; destroy_graph(ctx); }
     if (!changed && ctx->amg_lmax >= 0) return CFDL_OK;

@@ -696,6 +696,16 @@ int cfdl_set_pdl(cfdl_ctx *ctx, int on) {
     return CFDL_OK;
 }
 
+int cfdl_set_index16(cfdl_ctx *ctx, int on) {
+    int st = check_ctx(ctx);
+    if (st) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(ctx->stream)))) return st;
+    ctx->index16 = on != 0;
+    ctx->amg_lmax = -1;   // the choice is made when the multigrid work lists are built
+    destroy_graph(ctx);   // captured launches carry the kernel form
+    return CFDL_OK;
+}
+
 int cfdl_set_graph_mode(cfdl_ctx *ctx, int on) {
     if (!ctx || on < 0 || on > 2) return CFDL_ERR_INVALID;
     const bool branches = on != 2;

@@ -255,6 +255,7 @@ struct cfdl_ctx {
     int cgroup = 1;                                          // lanes per row on the large coarse levels (autotuned)
     int amg_lmax = -1;
     bool amg_nb16 = false;                                   // every case has CaseDev::nb16 (the mesh kernels read it)
+    bool index16 = true;                                     // cfdl_set_index16: allow amg_nb16
     // solve_uvwp as one CUDA graph with device-side loops (cfdl_graph.cu)
     bool use_graph = true, capturing = false;
     bool graph_branches = true;          // the outer-iteration graph's parallel branches (off: one chain)

@@ -344,6 +344,11 @@ int cfdl_set_graph_mode(cfdl_ctx *ctx, int on);
  * kernel may be scheduled while the one before it drains, and waits for it
  * on the device.  Results do not depend on it. */
 int cfdl_set_pdl(cfdl_ctx *ctx, int on);
+/* 16-bit neighbour offsets in the mixed form's FP32 mesh-level kernels
+ * (default on; used only where every case's offsets fit, see
+ * cfdl_amg_index_bytes).  Off, those kernels read the int32 indices; the
+ * results are the same either way. */
+int cfdl_set_index16(cfdl_ctx *ctx, int on);
 
 /* Multigrid hierarchy of case 0 (built on the first AMG pressure solve):
  * *nlev coarse levels; n[0..nlev] cells and W[0..nlev] ELL widths per level

@@ -363,3 +363,20 @@ def test_programmatic_launch_does_not_change_results(need_gpu, precision):
     for f in out[0]:
         for o in out[1:]:
             assert np.array_equal(out[0][f], o[f]), f
+
+
+def test_sixteen_bit_offsets_do_not_change_results(need_gpu):
+    """The mixed form's FP32 mesh-level kernels read the neighbours as 16-bit
+    offsets where they fit: the same neighbours and coefficients in the same
+    order as the int32 indices, so the fields are the same bit for bit."""
+    s = cfdl.Setup(cfdl.Zone(12, False, 0.2, seed=3))
+    out = []
+    for on in (True, False):
+        g = cfdl.Solver(s, cfdl.steady(precision=3))
+        g.set_index16(on)
+        g.step(20, 3)
+        assert g.index_bytes() == (2 if on else 4)
+        out.append({f: g.get(f) for f in ("u", "v", "w", "p", "mip")})
+        g.close()
+    for f in out[0]:
+        assert np.array_equal(out[0][f], out[1][f]), f

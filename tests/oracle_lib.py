@@ -1,7 +1,7 @@
 """ctypes access to the CPU oracle (oracle/liboracle.so) for the tests.
 
-Test infrastructure only: the oracle is the checker, never the code under
-test.  It restates the reference Fortran line by line (see oracle/*.c).
+Test infrastructure only: the oracle checks the results of the code under
+test and is never part of it.  It restates the reference Fortran line by line (see oracle/*.c).
 """
 import ctypes as C
 import hashlib
